@@ -1,0 +1,104 @@
+// qg_internal.h -- internal interface between the QuEST-ABI front-end
+// (api.cpp) and the sm_103a engines (*.cu).  Not installed, not part of the ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "QuEST.h"
+
+namespace qg {
+
+typedef long long idx_t;
+
+// ---- runtime -------------------------------------------------------------
+// All device work of the library is queued on one stream created with the
+// default (blocking) flags, so it also orders against legacy-stream work that
+// callers issue on the same device.
+cudaStream_t stream();
+// Report a CUDA failure through invalidQuESTInputError; returns true on error.
+bool cudaFailed(cudaError_t e, const char* what, const char* caller);
+#define QG_CUDA(call, caller) ::qg::cudaFailed((call), #call, caller)
+// Check the last launch; returns true on error.
+bool launchFailed(const char* caller);
+
+int numSMs();
+
+// Per-register reduction workspace held in Qureg.firstLevelReduction.
+// Layout (doubles): [partials: 2*kMaxReduceBlocks][result: 64][counter word]
+constexpr int kMaxReduceBlocks = 2048;
+constexpr size_t kScratchDoubles = 2 * kMaxReduceBlocks + 64 + 8;
+struct Scratch {
+    double* partials;          // 2*kMaxReduceBlocks doubles (double2 per block)
+    double* result;            // device result slots
+    unsigned int* counter;     // last-block-done ticket, kept at 0 between calls
+    double* host;              // pinned host slots (Qureg.secondLevelReduction)
+};
+Scratch scratchOf(const Qureg& q);
+
+// ---- state-vector gates (sv_gates.cu) ------------------------------------
+// Every launcher acts on the FP64 SoA arrays (re, im) of 2^n amplitudes.
+struct SV {
+    double* re;
+    double* im;
+    int n;                      // qubits in the state vector (2N for a density matrix)
+};
+inline SV svOf(const Qureg& q) { return SV{q.deviceStateVec.real, q.deviceStateVec.imag, q.numQubitsInStateVec}; }
+
+struct Mat2 { double r[2][2], i[2][2]; };
+
+// U on target for amplitudes whose control bits match: ((idx ^ flip) & ctrl) == ctrl.
+void gateMatrix2(SV s, int target, uint64_t ctrl, uint64_t flip, const Mat2& u);
+// [alpha, -conj(beta); beta, conj(alpha)] (QuEST compactUnitary form).
+void gateCompact(SV s, int target, uint64_t ctrl, double ar, double ai, double br, double bi);
+void gateHadamard(SV s, int target);
+// amp <-> amp ^ targMask where ctrl bits are set (X, CNOT, multi-qubit NOT).
+void gateNot(SV s, uint64_t ctrl, uint64_t targMask);
+// Y (conjFac=+1) or conj(Y) (conjFac=-1) on target, where ctrl bits are set.
+void gatePauliY(SV s, int target, uint64_t ctrl, double conjFac);
+// amp *= (tr + i ti) where all bits of mask are 1.
+void gatePhase(SV s, uint64_t mask, double tr, double ti);
+// amp *= exp(-i angle/2 * (+1 even parity of idx&targ, -1 odd)), where ctrl bits set.
+void gateRotateZ(SV s, uint64_t ctrl, uint64_t targ, double angle);
+// exp(-i angle/2 P) with P a Pauli string given by x/y/z masks, where ctrl bits set;
+// conj!=0 applies the elementwise conjugate operator.
+void gatePauliRotation(SV s, uint64_t ctrl, uint64_t xmask, uint64_t ymask, uint64_t zmask, double angle, int conj);
+void gateSwap(SV s, int q1, int q2);
+// Dense 2^k x 2^k (k <= 6) on targets (targs[0] = least significant matrix bit).
+// mr/mi row-major host arrays.
+void gateMatrixN(SV s, uint64_t ctrl, const int* targs, int k, const double* mr, const double* mi);
+
+// ---- initialisation / elementwise (state_ops.cu) --------------------------
+void stateFill(SV s, double re, double im);
+void stateSetOne(SV s, idx_t index, double re, double im);   // one element, others untouched
+void stateDebug(SV s);
+void statePlusDM(SV s, int nRep);
+void statePureDM(SV rho, const double* psiRe, const double* psiIm, int nRep);
+void stateWeighted(SV out, double f1r, double f1i, SV a, double f2r, double f2i, SV b, double for_, double foi);
+void stateMixDM(SV a, double p, SV b);
+void collapseSV(SV s, int target, int outcome, double renorm);
+void collapseDM(SV s, int target, int nRep, int outcome, double renorm);
+// density-matrix channels (QuEST.c:1259-1298 semantics)
+void dmDephase(SV s, int target, int nRep, double retain);
+void dmDepolarise(SV s, int target, int nRep, double level);
+void dmDamp(SV s, int target, int nRep, double prob);
+
+// ---- reductions (reduce.cu) -------------------------------------------------
+// All return their value through the pinned host slot after a stream sync.
+double reduceTotalProbSV(SV s, const Scratch& w);
+double reduceTotalProbDM(SV s, int nRep, const Scratch& w);
+double reduceProbZeroSV(SV s, int target, const Scratch& w);
+double reduceProbZeroDM(SV s, int target, int nRep, const Scratch& w);
+void reduceInnerProduct(SV bra, SV ket, const Scratch& w, double* outRe, double* outIm);
+double reduceDotReal(SV a, SV b, const Scratch& w);          // sum re*re' + im*im'
+double reduceNormSq(SV s, const Scratch& w);                 // sum |amp|^2 (no Kahan split)
+double reduceDistSq(SV a, SV b, const Scratch& w);
+double reduceFidelityDM(SV rho, SV psi, int nRep, const Scratch& w);
+// Expectation sum_t coeff_t <psi|P_t|psi> of Pauli strings that share one
+// X/Y mask (SV), or Tr(P_t rho) (DM).  yz/nY per term.
+struct PauliTerm { uint64_t yz; int nY; double coeff; };
+double reduceExpecPauliGroup(SV s, int isDM, int nRep, uint64_t xmask, const PauliTerm* terms, int numTerms, const Scratch& w);
+void reduceProbAllOutcomes(SV s, int isDM, int nRep, const int* qubits, int numQubits, double* hostOut, const Scratch& w);
+
+}  // namespace qg

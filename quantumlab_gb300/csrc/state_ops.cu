@@ -1,0 +1,257 @@
+// state_ops.cu -- initialisation, elementwise combinations, measurement
+// collapse and the single-qubit density-matrix channels (FP64, sm_103a).
+//
+// Channel semantics follow Code/QuEST340/QuEST/src/QuEST.c:1259-1298 and the
+// GPU kernels of QuEST_gpu.cu:2868-3078: the reference runs depolarising and
+// damping as two launches (an off-diagonal pass, then a diagonal pass); here
+// each channel is one pass over groups of the four entries
+// {rho[.0..0.], rho[.0..1.], rho[.1..0.], rho[.1..1.]} (row bit t, column bit
+// t+N), with the same per-entry arithmetic.
+#include "qg_internal.h"
+
+namespace qg {
+namespace {
+
+constexpr int kThreads = 256;
+inline unsigned blocksFor(uint64_t threads) { return (unsigned)((threads + kThreads - 1) / kThreads); }
+
+__device__ __forceinline__ double2 ld2(const double* p) { return *reinterpret_cast<const double2*>(p); }
+__device__ __forceinline__ void st2(double* p, double2 v) { *reinterpret_cast<double2*>(p) = v; }
+__device__ __forceinline__ uint64_t ins2(uint64_t k, int lo, int hi) {     // insert zeros at lo < hi
+    k = ((k >> lo) << (lo + 1)) | (k & ((1ull << lo) - 1ull));
+    k = ((k >> hi) << (hi + 1)) | (k & ((1ull << hi) - 1ull));
+    return k;
+}
+
+// ---------------------------------------------------------------- fills
+__global__ void kFill(double* __restrict__ re, double* __restrict__ im, uint64_t n2, double vr, double vi) {
+    const uint64_t t = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (t >= n2) return;
+    st2(re + 2 * t, make_double2(vr, vr));
+    st2(im + 2 * t, make_double2(vi, vi));
+}
+
+// QuEST_gpu.cu:659-684 (initDebugState): amp_k = (2k + i(2k+1)) / 10
+__global__ void kDebug(double* __restrict__ re, double* __restrict__ im, uint64_t n) {
+    const uint64_t t = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (t >= n) return;
+    re[t] = (t * 2.0) / 10.0;
+    im[t] = (t * 2.0 + 1.0) / 10.0;
+}
+
+// rho[r + c D] = psi_r conj(psi_c)  (QuEST_gpu.cu:188-228)
+__global__ void kPureDM(double* __restrict__ re, double* __restrict__ im, const double* __restrict__ pr,
+                        const double* __restrict__ pi, int nRep, uint64_t n) {
+    const uint64_t t = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (t >= n) return;
+    const uint64_t D = 1ull << nRep;
+    const uint64_t r = t & (D - 1), c = t >> nRep;
+    const double ar = pr[r], ai = pi[r], br = pr[c], bi = -pi[c];
+    re[t] = ar * br - ai * bi;
+    im[t] = ar * bi + ai * br;
+}
+
+// out = f1 a + f2 b + fo out  (QuEST_gpu.cu:3148-3190)
+__global__ void kWeighted(double* __restrict__ oR, double* __restrict__ oI, const double* __restrict__ aR,
+                          const double* __restrict__ aI, const double* __restrict__ bR, const double* __restrict__ bI,
+                          double f1r, double f1i, double f2r, double f2i, double for_, double foi, uint64_t n) {
+    const uint64_t t = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (t >= n) return;
+    const double ar = aR[t], ai = aI[t], br = bR[t], bi = bI[t], xr = oR[t], xi = oI[t];
+    oR[t] = f1r * ar - f1i * ai + f2r * br - f2i * bi + for_ * xr - foi * xi;
+    oI[t] = f1r * ai + f1i * ar + f2r * bi + f2i * br + for_ * xi + foi * xr;
+}
+
+// a = (1-p) a + p b  (QuEST_gpu.cu:2839-2866)
+__global__ void kMixDM(double* __restrict__ aR, double* __restrict__ aI, const double* __restrict__ bR,
+                       const double* __restrict__ bI, double p, uint64_t n2) {
+    const uint64_t t = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (t >= n2) return;
+    double2 ar = ld2(aR + 2 * t), ai = ld2(aI + 2 * t);
+    const double2 br = ld2(bR + 2 * t), bi = ld2(bI + 2 * t);
+    const double q = 1 - p;
+    ar.x = ar.x * q + p * br.x; ar.y = ar.y * q + p * br.y;
+    ai.x = ai.x * q + p * bi.x; ai.y = ai.y * q + p * bi.y;
+    st2(aR + 2 * t, ar); st2(aI + 2 * t, ai);
+}
+
+// ---------------------------------------------------------------- collapse
+// keep amps whose bit t == outcome (scaled), zero the rest (QuEST_gpu.cu:2718-2781)
+__global__ void kCollapseSV(double* __restrict__ re, double* __restrict__ im, uint64_t n2, uint64_t tbit,
+                            int outcome, double renorm) {
+    const uint64_t t = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (t >= n2) return;
+    const uint64_t i = 2 * t;
+    double2 r = ld2(re + i), m = ld2(im + i);
+    const double f0 = (((i & tbit) != 0) == (outcome != 0)) ? renorm : 0.0;
+    const double f1 = ((((i + 1) & tbit) != 0) == (outcome != 0)) ? renorm : 0.0;
+    r.x *= f0; m.x *= f0; r.y *= f1; m.y *= f1;
+    st2(re + i, r); st2(im + i, m);
+}
+
+// DM: keep entries whose row and column bits both equal outcome, / prob
+// (QuEST_gpu.cu:2784-2837; 64-bit bit tests here, the reference uses int)
+__global__ void kCollapseDM(double* __restrict__ re, double* __restrict__ im, uint64_t n2, uint64_t rbit,
+                            uint64_t cbit, int outcome, double renorm) {
+    const uint64_t t = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (t >= n2) return;
+    const uint64_t i = 2 * t;
+    double2 r = ld2(re + i), m = ld2(im + i);
+    const uint64_t want = outcome ? (rbit | cbit) : 0;
+    const double f0 = ((i & (rbit | cbit)) == want) ? renorm : 0.0;
+    const double f1 = (((i + 1) & (rbit | cbit)) == want) ? renorm : 0.0;
+    r.x *= f0; m.x *= f0; r.y *= f1; m.y *= f1;
+    st2(re + i, r); st2(im + i, m);
+}
+
+// ---------------------------------------------------------------- channels
+// The four entries of one group: e00 = base, e01 = base|row, e10 = base|col,
+// e11 = base|row|col.  Off-diagonal-in-t entries are e01, e10.
+struct Dephase {
+    double retain;
+    __device__ __forceinline__ void operator()(double&, double&, double& r01, double& i01, double& r10, double& i10,
+                                               double&, double&) const {
+        r01 *= retain; i01 *= retain; r10 *= retain; i10 *= retain;
+    }
+};
+// QuEST_gpu.cu:2980-3004 (after the 1-level dephase): both diagonal entries
+// become (1-l) x + l (x+y)/2
+struct Depolarise {
+    double level;
+    __device__ __forceinline__ void operator()(double& r00, double& i00, double& r01, double& i01, double& r10,
+                                               double& i10, double& r11, double& i11) const {
+        const double retain = 1 - level;
+        r01 *= retain; i01 *= retain; r10 *= retain; i10 *= retain;
+        const double avr = level * 0.5 * (r00 + r11), avi = level * 0.5 * (i00 + i11);
+        r00 = r00 * retain + avr; i00 = i00 * retain + avi;
+        r11 = r11 * retain + avr; i11 = i11 * retain + avi;
+    }
+};
+// QuEST_gpu.cu:3006-3078: off-diagonals * sqrt(1-p); rho00 += p rho11; rho11 *= 1-p
+struct Damp {
+    double p, dephase;
+    __device__ __forceinline__ void operator()(double& r00, double& i00, double& r01, double& i01, double& r10,
+                                               double& i10, double& r11, double& i11) const {
+        r01 *= dephase; i01 *= dephase; r10 *= dephase; i10 *= dephase;
+        const double tr = p * r11, ti = p * i11;
+        r11 *= 1 - p; i11 *= 1 - p;
+        r00 += tr; i00 += ti;
+    }
+};
+
+// row bit t >= 1: two consecutive groups per thread with double2 loads
+template <class Op>
+__global__ void __launch_bounds__(kThreads) kChannelVec(double* __restrict__ re, double* __restrict__ im, int t, int N,
+                                                        uint64_t nThreads, Op op) {
+    const uint64_t k = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (k >= nThreads) return;
+    const uint64_t rb = 1ull << t, cb = 1ull << (t + N);
+    const uint64_t b = ins2(k << 1, t, t + N);
+    double2 r00 = ld2(re + b), i00 = ld2(im + b);
+    double2 r01 = ld2(re + (b | rb)), i01 = ld2(im + (b | rb));
+    double2 r10 = ld2(re + (b | cb)), i10 = ld2(im + (b | cb));
+    double2 r11 = ld2(re + (b | rb | cb)), i11 = ld2(im + (b | rb | cb));
+    op(r00.x, i00.x, r01.x, i01.x, r10.x, i10.x, r11.x, i11.x);
+    op(r00.y, i00.y, r01.y, i01.y, r10.y, i10.y, r11.y, i11.y);
+    st2(re + b, r00); st2(im + b, i00);
+    st2(re + (b | rb), r01); st2(im + (b | rb), i01);
+    st2(re + (b | cb), r10); st2(im + (b | cb), i10);
+    st2(re + (b | rb | cb), r11); st2(im + (b | rb | cb), i11);
+}
+
+// row bit t == 0: (e00, e01) and (e10, e11) are adjacent pairs
+template <class Op>
+__global__ void __launch_bounds__(kThreads) kChannelT0(double* __restrict__ re, double* __restrict__ im, int N,
+                                                       uint64_t nGroups, Op op) {
+    const uint64_t k = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (k >= nGroups) return;
+    const uint64_t cb = 1ull << N;
+    const uint64_t b = ins2(k, 0, N);
+    double2 rA = ld2(re + b), iA = ld2(im + b), rB = ld2(re + (b | cb)), iB = ld2(im + (b | cb));
+    op(rA.x, iA.x, rA.y, iA.y, rB.x, iB.x, rB.y, iB.y);
+    st2(re + b, rA); st2(im + b, iA); st2(re + (b | cb), rB); st2(im + (b | cb), iB);
+}
+
+template <class Op>
+void launchChannel(SV s, int t, int N, const Op& op, const char* caller) {
+    const uint64_t nGroups = 1ull << (s.n - 2);
+    if (t >= 1 && nGroups >= 2)
+        kChannelVec<Op><<<blocksFor(nGroups / 2), kThreads, 0, stream()>>>(s.re, s.im, t, N, nGroups / 2, op);
+    else
+        kChannelT0<Op><<<blocksFor(nGroups), kThreads, 0, stream()>>>(s.re, s.im, N, nGroups, op);
+    launchFailed(caller);
+}
+
+}  // namespace
+
+void stateFill(SV s, double vr, double vi) {
+    const uint64_t n = 1ull << s.n;
+    cudaStream_t st = stream();
+    if (vr == 0.0 && vi == 0.0) {
+        if (QG_CUDA(cudaMemsetAsync(s.re, 0, n * sizeof(double), st), "initBlankState")) return;
+        QG_CUDA(cudaMemsetAsync(s.im, 0, n * sizeof(double), st), "initBlankState");
+        return;
+    }
+    if (n < 2) {
+        double v[2] = {vr, vi};
+        QG_CUDA(cudaMemcpyAsync(s.re, &v[0], sizeof(double), cudaMemcpyHostToDevice, st), "initPlusState");
+        QG_CUDA(cudaMemcpyAsync(s.im, &v[1], sizeof(double), cudaMemcpyHostToDevice, st), "initPlusState");
+        QG_CUDA(cudaStreamSynchronize(st), "initPlusState");
+        return;
+    }
+    kFill<<<blocksFor(n / 2), kThreads, 0, st>>>(s.re, s.im, n / 2, vr, vi);
+    launchFailed("initPlusState");
+}
+
+void stateSetOne(SV s, idx_t index, double vr, double vi) {
+    cudaStream_t st = stream();
+    // pageable source: the copy stages the values before returning
+    double v[2] = {vr, vi};
+    if (QG_CUDA(cudaMemcpyAsync(s.re + index, &v[0], sizeof(double), cudaMemcpyHostToDevice, st), "initClassicalState")) return;
+    QG_CUDA(cudaMemcpyAsync(s.im + index, &v[1], sizeof(double), cudaMemcpyHostToDevice, st), "initClassicalState");
+}
+
+void stateDebug(SV s) {
+    const uint64_t n = 1ull << s.n;
+    kDebug<<<blocksFor(n), kThreads, 0, stream()>>>(s.re, s.im, n);
+    launchFailed("initDebugState");
+}
+
+void statePlusDM(SV s, int nRep) { stateFill(s, 1.0 / (double)(1ull << nRep), 0.0); }
+
+void statePureDM(SV rho, const double* pr, const double* pi, int nRep) {
+    const uint64_t n = 1ull << rho.n;
+    kPureDM<<<blocksFor(n), kThreads, 0, stream()>>>(rho.re, rho.im, pr, pi, nRep, n);
+    launchFailed("initPureState");
+}
+
+void stateWeighted(SV out, double f1r, double f1i, SV a, double f2r, double f2i, SV b, double for_, double foi) {
+    const uint64_t n = 1ull << out.n;
+    kWeighted<<<blocksFor(n), kThreads, 0, stream()>>>(out.re, out.im, a.re, a.im, b.re, b.im, f1r, f1i, f2r, f2i, for_, foi, n);
+    launchFailed("setWeightedQureg");
+}
+
+void stateMixDM(SV a, double p, SV b) {
+    const uint64_t n = 1ull << a.n;
+    kMixDM<<<blocksFor(n / 2), kThreads, 0, stream()>>>(a.re, a.im, b.re, b.im, p, n / 2);
+    launchFailed("mixDensityMatrix");
+}
+
+void collapseSV(SV s, int target, int outcome, double renorm) {
+    const uint64_t n = 1ull << s.n;
+    kCollapseSV<<<blocksFor(n / 2), kThreads, 0, stream()>>>(s.re, s.im, n / 2, 1ull << target, outcome, renorm);
+    launchFailed("collapseToOutcome");
+}
+
+void collapseDM(SV s, int target, int nRep, int outcome, double renorm) {
+    const uint64_t n = 1ull << s.n;
+    kCollapseDM<<<blocksFor(n / 2), kThreads, 0, stream()>>>(s.re, s.im, n / 2, 1ull << target, 1ull << (target + nRep),
+                                                             outcome, renorm);
+    launchFailed("collapseToOutcome");
+}
+
+void dmDephase(SV s, int t, int N, double retain) { launchChannel(s, t, N, Dephase{retain}, "mixDephasing"); }
+void dmDepolarise(SV s, int t, int N, double level) { launchChannel(s, t, N, Depolarise{level}, "mixDepolarising"); }
+void dmDamp(SV s, int t, int N, double p) { launchChannel(s, t, N, Damp{p, sqrt(1 - p)}, "mixDamping"); }
+
+}  // namespace qg

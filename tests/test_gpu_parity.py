@@ -1,0 +1,106 @@
+"""GPU library vs the reference's outputs (golden fixtures) and vs the oracle.
+
+Every API case of the catalogue is replayed through the C ABI of
+libquest_gb300.so on cuda:0 and compared amplitude by amplitude (FP64 plain
+path: |d amp| <= 1e-12 x the case's largest amplitude)."""
+import numpy as np
+import pytest
+
+import quest_cases as QC
+from parity import check_case
+from quantumlab_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def test_catalogue_against_reference(gpulib, golden):
+    cases, amps, _ = golden
+    failures = []
+    for i, case in enumerate(cases):
+        a, results, probes = QC.run_case(gpulib, case)
+        try:
+            check_case(case, a, results, probes, amps[f"case{i}"])
+        except AssertionError as e:
+            failures.append(str(e))
+    assert not failures, f"{len(failures)} failing cases:\n" + "\n".join(failures[:40])
+
+
+def test_circuits_against_reference(gpulib, golden):
+    _, _, circ = golden
+    L = gpulib
+    q = L.create(12)
+    W.run_ops(L, q, W.c1_circuit(n=12, layers=8, seed=11))
+    assert np.max(np.abs(L.amps(q) - circ["c1_amps"])) < 1e-12
+    assert abs(L.lib.calcTotalProb(q) - circ["c1_total"][0]) < 1e-13
+    p1 = [L.lib.calcProbOfOutcome(q, t, 1) for t in range(12)]
+    assert np.max(np.abs(np.array(p1) - circ["c1_p1"])) < 1e-13
+    L.destroy(q)
+    q = L.create(10)
+    W.run_ops(L, q, W.c2_circuit(n=10, layers=6, seed=12))
+    assert np.max(np.abs(L.amps(q) - circ["c2_amps"])) < 1e-12
+    L.destroy(q)
+    d = L.create(5, True)
+    W.run_ops(L, d, W.c3_circuit(nq=5, layers=4, seed=13))
+    assert np.max(np.abs(L.amps(d) - circ["c3_amps"])) < 1e-12
+    assert abs(L.lib.calcPurity(d) - circ["c3_purity"][0]) < 1e-12
+    assert abs(L.lib.calcTotalProb(d) - circ["c3_trace"][0]) < 1e-12
+    L.destroy(d)
+
+
+def test_hubbard_trotter_against_reference(gpulib, golden):
+    _, _, circ = golden
+    L = gpulib
+    for k, (U, dt, order) in enumerate([(2.0, 0.1, 1), (4.0, 0.05, 2), (8.0, 0.1, 2)]):
+        codes, coeffs, const = W.hubbard_terms(4, U)
+        q = L.create(8)
+        L.lib.initClassicalState(q, W.neel_index(4))
+        h = L.pauli_hamil(codes, coeffs)
+        L.lib.applyTrotterCircuit(q, h, 1.0, order, int(round(1.0 / dt)))
+        ws = L.create(8)
+        e = L.calcExpecPauliSum(q, codes, coeffs, ws) + const
+        assert abs(e - circ["c4_energy"][k]) < 1e-11
+        occ = [L.lib.calcProbOfOutcome(q, t, 1) for t in range(8)]
+        assert np.max(np.abs(np.array(occ) - circ["c4_occ"][k])) < 1e-12
+        L.destroy(ws)
+        L.lib.destroyPauliHamil(h)
+        L.destroy(q)
+
+
+@pytest.mark.parametrize("n", [16, 20])
+def test_plain_random_circuit_vs_oracle(gpulib, oracle, n):
+    """Config-1 structure at full size (20 qubits, 40 layers): every amplitude,
+    total probability and P(q=1) for every qubit against the oracle."""
+    ops = W.c1_circuit(n=n, layers=40 if n == 20 else 10, seed=1)
+    res = []
+    for L in (gpulib, oracle):
+        q = L.create(n)
+        W.run_ops(L, q, ops)
+        res.append((L.amps(q).copy(), L.lib.calcTotalProb(q), [L.lib.calcProbOfOutcome(q, t, 1) for t in range(n)]))
+        L.destroy(q)
+    (ag, tg, pg), (ao, to, po) = res
+    assert np.max(np.abs(ag - ao)) < 1e-12
+    assert abs(tg - to) < 1e-13 and abs(tg - 1) < 1e-10
+    assert np.max(np.abs(np.array(pg) - np.array(po))) < 1e-13
+
+
+def test_validation_messages_match_reference(gpulib):
+    """Invalid input reaches invalidQuESTInputError with the reference's
+    message; the call returns without touching the state."""
+    L = gpulib
+    assert L.capture_errors()
+    q = L.create(3)
+    before = L.amps(q).copy()
+    L.errors.clear()
+    L.lib.hadamard(q, 3)
+    L.lib.controlledNot(q, 1, 1)
+    L.lib.compactUnitary(q, 0, QC.Complex(1, 0), QC.Complex(1, 0))
+    L.lib.mixDephasing(q, 0, 0.1)
+    L.lib.calcProbOfOutcome(q, 0, 2)
+    msgs = [m for _, m in L.errors]
+    assert msgs == ["Invalid target qubit. Must be >=0 and <numQubits.",
+                    "Control qubit cannot equal target qubit.",
+                    "Compact matrix formed by given complex numbers is not unitary.",
+                    "Operation valid only for density matrices.",
+                    "Invalid measurement outcome -- must be either 0 or 1."]
+    assert np.array_equal(L.amps(q), before)
+    L.destroy(q)
