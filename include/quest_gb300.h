@@ -25,6 +25,50 @@ int quest_gb300_eventRecord(int slot);
 /* Milliseconds between two recorded events (waits for `slotB`); -1 on error. */
 double quest_gb300_eventElapsedMs(int slotA, int slotB);
 
+/* ---- gate-fusion plans ---------------------------------------------------
+ * A plan records a gate stream on numQubits qubits and compiles it into
+ * passes: dense 2^k x 2^k complex matrices on k <= maxFusedQubits (<= 6)
+ * qubits, formed as FP64 products of the absorbed gates.  Matrices are
+ * row-major with matrix bit b on targets[b]; compactUnitary and friends keep
+ * the QuEST conventions.  Add functions return 0, or -1 on invalid input.   */
+void* quest_gb300_planCreate(int numQubits, int maxFusedQubits);
+void quest_gb300_planDestroy(void* plan);
+int quest_gb300_planAddGate(void* plan, const int* targets, int numTargets, const double* re, const double* im);
+int quest_gb300_planAddCompactUnitary(void* plan, int target, double alphaRe, double alphaIm, double betaRe, double betaIm);
+int quest_gb300_planAddUnitary(void* plan, int target, const double* re4, const double* im4);
+int quest_gb300_planAddHadamard(void* plan, int target);
+int quest_gb300_planAddControlledNot(void* plan, int control, int target);
+int quest_gb300_planAddControlledPhaseShift(void* plan, int qubit1, int qubit2, double angle);
+/* Compile; returns the number of passes. */
+int quest_gb300_planCompile(void* plan);
+int quest_gb300_planNumGates(void* plan);
+/* Copy pass i (targets ascending, FP64 matrix); returns k or -1. */
+int quest_gb300_planPass(void* plan, int i, int* targets, double* re, double* im);
+
+/* ---- FP32 registers of the fused engine ----------------------------------
+ * A state vector of 2^numQubits FP32 complex amplitudes (SoA) on the
+ * device.  Reductions accumulate in FP64.                                    */
+void* quest_gb300_createQuregF32(int numQubits);
+void quest_gb300_destroyQuregF32(void* qureg32);
+void quest_gb300_initZeroStateF32(void* qureg32);
+/* host FP64 amplitudes (like initStateFromAmps), rounded to FP32 on the device */
+void quest_gb300_initStateFromAmpsF32(void* qureg32, const double* reals, const double* imags);
+/* all amplitudes to host FP64 arrays */
+void quest_gb300_copyStateToHostF32(void* qureg32, double* reals, double* imags);
+/* device-side conversion from / to an FP64 state-vector Qureg of equal size */
+void quest_gb300_copyFromQureg(void* qureg32, Qureg source);
+void quest_gb300_copyToQureg(void* qureg32, Qureg destination);
+/* apply every pass of the plan (compiling it first if needed); 0 on success */
+int quest_gb300_applyPlanF32(void* qureg32, void* plan);
+/* passes on 4..6 qubits run on the tensor cores (split-TF32) unless disabled
+ * here (1 = enabled, the default; 0 = FP32 SIMT applier for k <= 5) */
+void quest_gb300_setTensorCores(int enabled);
+double quest_gb300_calcTotalProbF32(void* qureg32);
+double quest_gb300_calcProbOfOutcomeF32(void* qureg32, int measureQubit, int outcome);
+/* 1 - |<ref|q>|^2 / (<ref|ref><q|q>) against an FP64 state vector; writes the
+ * largest |amplitude difference| to *maxAmpErr when it is not NULL */
+double quest_gb300_compareF32(void* qureg32, Qureg reference, double* maxAmpErr);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,7 +19,7 @@ _lib = None
 
 
 def build(verbose: bool = False) -> str:
-    from .build import build as _build
+    from .builder import build as _build
     return _build(verbose=verbose)
 
 

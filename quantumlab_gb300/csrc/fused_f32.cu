@@ -1,0 +1,398 @@
+// fused_f32.cu -- the FP32 fused engine: an FP32 SoA register, the pass
+// applier, and FP64-accumulated reductions over it (sm_103a).
+//
+// No counterpart in the reference.  A compiled plan (fused_plan.cpp) is a
+// list of dense 2^k x 2^k complex matrices formed in FP64; each is applied to
+// the FP32 state in one streaming pass.  This file holds the SIMT applier
+// (FP32 FFMA, matrix rounded to FP32 and held in the kernel's constant
+// parameter bank) used for k <= 5; the tensor-core split-TF32 applier lives
+// in fused_tc.cu.  Norms, probabilities and the comparison against an FP64
+// register accumulate in FP64.
+#include "fused_plan.h"
+#include "quest_gb300.h"
+#include "reduce_kernel.cuh"
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace qg {
+
+struct QuregF32 {
+    int n = 0;
+    float* re = nullptr;
+    float* im = nullptr;
+    double* scratch = nullptr;     // kScratchDoubles, counter kept at 0
+    double* host = nullptr;        // pinned result slots
+    double* staging = nullptr;     // FP64 device staging for host transfers
+    size_t stagingAmps = 0;
+    Scratch w() const {
+        Scratch s;
+        s.partials = scratch;
+        s.result = scratch + 2 * kMaxReduceBlocks;
+        s.counter = reinterpret_cast<unsigned int*>(scratch + 2 * kMaxReduceBlocks + 64);
+        s.host = host;
+        return s;
+    }
+};
+
+// tensor-core applier (fused_tc.cu); returns false if it does not take the pass
+bool applyPassTCIndexed(QuregF32& q, const FusedPass& p, const void* devPlan, size_t index, cudaStream_t st);
+void* uploadPlanTC(const FusedPlan& plan);
+void freePlanTC(void* d);
+int tcErrorFlag(const void* devPlan);
+void setTensorCoresEnabled(bool on);
+bool tensorCoresEnabled();
+float* f32re(QuregF32& q) { return q.re; }
+float* f32im(QuregF32& q) { return q.im; }
+int f32n(const QuregF32& q) { return q.n; }
+
+namespace {
+
+constexpr int kApplyThreads = 128;
+
+template <int K>
+struct PassParams {
+    float mr[1 << K][1 << K];
+    float mi[1 << K][1 << K];
+    uint64_t off[1 << K];     // address offset of matrix index j (bits on the targets)
+    int ins[K];               // ascending target positions (zeros inserted into the group index)
+};
+
+// One thread per group of 2^K amplitudes (the non-target bits fixed): load
+// the group, multiply by the matrix (constant-bank operands), store.
+template <int K>
+__global__ void __launch_bounds__(kApplyThreads, (K <= 4 ? 4 : 2)) kApplySimt(float* __restrict__ re, float* __restrict__ im,
+                                                           uint64_t nGroups, const __grid_constant__ PassParams<K> p) {
+    constexpr int D = 1 << K;
+    const uint64_t g = (uint64_t)blockIdx.x * kApplyThreads + threadIdx.x;
+    if (g >= nGroups) return;
+    uint64_t base = g;
+#pragma unroll
+    for (int b = 0; b < K; ++b) {
+        const int s = p.ins[b];
+        base = ((base >> s) << (s + 1)) | (base & ((1ull << s) - 1ull));
+    }
+    float xr[D], xi[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+        xr[j] = re[base + p.off[j]];
+        xi[j] = im[base + p.off[j]];
+    }
+    // rows rolled (uniform index: matrix entries come from the constant bank
+    // through the uniform datapath), columns unrolled
+#pragma unroll 1
+    for (int r = 0; r < D; ++r) {
+        float ar = 0.f, ai = 0.f;
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+            ar = fmaf(p.mr[r][j], xr[j], ar);
+            ar = fmaf(-p.mi[r][j], xi[j], ar);
+            ai = fmaf(p.mr[r][j], xi[j], ai);
+            ai = fmaf(p.mi[r][j], xr[j], ai);
+        }
+        re[base + p.off[r]] = ar;
+        im[base + p.off[r]] = ai;
+    }
+}
+
+template <int K>
+bool launchSimt(QuregF32& q, const FusedPass& pass, cudaStream_t st) {
+    constexpr int D = 1 << K;
+    PassParams<K> p;
+    for (int r = 0; r < D; ++r)
+        for (int c = 0; c < D; ++c) {
+            p.mr[r][c] = (float)pass.m[(size_t)r * D + c].real();
+            p.mi[r][c] = (float)pass.m[(size_t)r * D + c].imag();
+        }
+    for (int j = 0; j < D; ++j) {
+        uint64_t o = 0;
+        for (int b = 0; b < K; ++b)
+            if (j >> b & 1) o |= 1ull << pass.targets[b];
+        p.off[j] = o;
+    }
+    for (int b = 0; b < K; ++b) p.ins[b] = pass.targets[b];
+    const uint64_t nGroups = 1ull << (q.n - K);
+    const unsigned blocks = (unsigned)((nGroups + kApplyThreads - 1) / kApplyThreads);
+    kApplySimt<K><<<blocks, kApplyThreads, 0, st>>>(q.re, q.im, nGroups, p);
+    return !launchFailed("applyPlanF32");
+}
+
+bool applyPassSimt(QuregF32& q, const FusedPass& pass, cudaStream_t st) {
+    switch (pass.targets.size()) {
+        case 1: return launchSimt<1>(q, pass, st);
+        case 2: return launchSimt<2>(q, pass, st);
+        case 3: return launchSimt<3>(q, pass, st);
+        case 4: return launchSimt<4>(q, pass, st);
+        case 5: return launchSimt<5>(q, pass, st);
+        default: return false;
+    }
+}
+
+// ------------------------------------------------------------ elementwise
+__global__ void kZeroF32(float* __restrict__ re, float* __restrict__ im) {
+    re[0] = 1.f;
+    (void)im;
+}
+__global__ void kF64toF32(const double* __restrict__ sr, const double* __restrict__ si, float* __restrict__ dr,
+                          float* __restrict__ di, uint64_t n) {
+    const uint64_t t = (uint64_t)blockIdx.x * 256 + threadIdx.x;
+    if (t >= n) return;
+    dr[t] = (float)sr[t];
+    di[t] = (float)si[t];
+}
+__global__ void kF32toF64(const float* __restrict__ sr, const float* __restrict__ si, double* __restrict__ dr,
+                          double* __restrict__ di, uint64_t n) {
+    const uint64_t t = (uint64_t)blockIdx.x * 256 + threadIdx.x;
+    if (t >= n) return;
+    dr[t] = (double)sr[t];
+    di[t] = (double)si[t];
+}
+
+// ------------------------------------------------------------ reductions
+struct NormF32 {
+    const float *re, *im;
+    __device__ __forceinline__ double2 operator()(uint64_t i) const {
+        const float2 r = *reinterpret_cast<const float2*>(re + 2 * i), m = *reinterpret_cast<const float2*>(im + 2 * i);
+        return make_double2((double)r.x * r.x + (double)m.x * m.x + (double)r.y * r.y + (double)m.y * m.y, 0.0);
+    }
+};
+struct ProbZeroF32 {
+    const float *re, *im;
+    int t;
+    __device__ __forceinline__ double2 operator()(uint64_t k) const {
+        const uint64_t i = ((k >> t) << (t + 1)) | (k & ((1ull << t) - 1ull));
+        const double r = re[i], m = im[i];
+        return make_double2(r * r + m * m, 0.0);
+    }
+};
+// <psi64 | psi32> (complex), accumulated in FP64
+struct OverlapF32 {
+    const double *ar, *ai;
+    const float *br, *bi;
+    __device__ __forceinline__ double2 operator()(uint64_t i) const {
+        const double xr = ar[i], xi = ai[i], yr = br[i], yi = bi[i];
+        return make_double2(xr * yr + xi * yi, xr * yi - xi * yr);
+    }
+};
+__global__ void kMaxAbsDiff(const double* __restrict__ ar, const double* __restrict__ ai, const float* __restrict__ br,
+                            const float* __restrict__ bi, uint64_t n, unsigned long long* __restrict__ out) {
+    double m = 0.0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const double dr = ar[i] - (double)br[i], di = ai[i] - (double)bi[i];
+        m = fmax(m, sqrt(dr * dr + di * di));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+bool ensureStaging(QuregF32& q, size_t amps) {
+    if (q.stagingAmps >= amps) return true;
+    if (q.staging) cudaFree(q.staging);
+    q.staging = nullptr;
+    q.stagingAmps = 0;
+    if (QG_CUDA(cudaMalloc(&q.staging, 2 * amps * sizeof(double)), "createQuregF32")) return false;
+    q.stagingAmps = amps;
+    return true;
+}
+
+QuregF32* Q(void* h) { return reinterpret_cast<QuregF32*>(h); }
+}  // namespace
+// read the tensor-core error flag after every plan application (one sync)
+bool g_checkTC = true;
+namespace {
+
+}  // namespace
+}  // namespace qg
+
+using qg::QuregF32;
+
+extern "C" {
+
+void* quest_gb300_createQuregF32(int numQubits) {
+    if (numQubits < 1 || numQubits > 36) return nullptr;
+    QuregF32* q = new QuregF32();
+    q->n = numQubits;
+    const size_t n = 1ull << numQubits;
+    float* base = nullptr;
+    if (QG_CUDA(cudaMalloc(&base, 2 * n * sizeof(float)), "createQuregF32")) {
+        delete q;
+        return nullptr;
+    }
+    q->re = base;
+    q->im = base + n;
+    if (QG_CUDA(cudaMalloc(&q->scratch, qg::kScratchDoubles * sizeof(double)), "createQuregF32") ||
+        QG_CUDA(cudaMallocHost(&q->host, 64 * sizeof(double)), "createQuregF32")) {
+        cudaFree(base);
+        delete q;
+        return nullptr;
+    }
+    cudaMemsetAsync(q->scratch, 0, qg::kScratchDoubles * sizeof(double), qg::stream());
+    quest_gb300_initZeroStateF32(q);
+    return q;
+}
+
+void quest_gb300_destroyQuregF32(void* h) {
+    QuregF32* q = qg::Q(h);
+    if (!q) return;
+    cudaStreamSynchronize(qg::stream());
+    cudaFree(q->re);
+    cudaFree(q->scratch);
+    cudaFreeHost(q->host);
+    if (q->staging) cudaFree(q->staging);
+    delete q;
+}
+
+void quest_gb300_initZeroStateF32(void* h) {
+    QuregF32* q = qg::Q(h);
+    const size_t n = 1ull << q->n;
+    cudaStream_t st = qg::stream();
+    if (QG_CUDA(cudaMemsetAsync(q->re, 0, 2 * n * sizeof(float), st), "initZeroStateF32")) return;
+    qg::kZeroF32<<<1, 1, 0, st>>>(q->re, q->im);
+    qg::launchFailed("initZeroStateF32");
+}
+
+void quest_gb300_copyFromQureg(void* h, Qureg src) {
+    QuregF32* q = qg::Q(h);
+    const uint64_t n = 1ull << q->n;
+    if (src.numAmpsTotal != (long long)n) {
+        invalidQuESTInputError("Dimensions of the qubit registers don't match.", "copyFromQureg");
+        return;
+    }
+    qg::kF64toF32<<<(unsigned)((n + 255) / 256), 256, 0, qg::stream()>>>(src.deviceStateVec.real, src.deviceStateVec.imag,
+                                                                        q->re, q->im, n);
+    qg::launchFailed("copyFromQureg");
+}
+
+void quest_gb300_copyToQureg(void* h, Qureg dst) {
+    QuregF32* q = qg::Q(h);
+    const uint64_t n = 1ull << q->n;
+    if (dst.numAmpsTotal != (long long)n) {
+        invalidQuESTInputError("Dimensions of the qubit registers don't match.", "copyToQureg");
+        return;
+    }
+    qg::kF32toF64<<<(unsigned)((n + 255) / 256), 256, 0, qg::stream()>>>(q->re, q->im, dst.deviceStateVec.real,
+                                                                        dst.deviceStateVec.imag, n);
+    qg::launchFailed("copyToQureg");
+}
+
+// host FP64 amplitudes -> FP32 register, through a bounded FP64 staging
+// buffer on the device (chunks of at most 2^26 amplitudes)
+void quest_gb300_initStateFromAmpsF32(void* h, const double* re, const double* im) {
+    QuregF32* q = qg::Q(h);
+    const uint64_t n = 1ull << q->n;
+    const uint64_t chunk = std::min<uint64_t>(n, 1ull << 26);
+    if (!qg::ensureStaging(*q, chunk)) return;
+    cudaStream_t st = qg::stream();
+    for (uint64_t s = 0; s < n; s += chunk) {
+        const uint64_t c = std::min(chunk, n - s);
+        if (QG_CUDA(cudaMemcpyAsync(q->staging, re + s, c * sizeof(double), cudaMemcpyHostToDevice, st), "initStateFromAmpsF32")) return;
+        if (QG_CUDA(cudaMemcpyAsync(q->staging + chunk, im + s, c * sizeof(double), cudaMemcpyHostToDevice, st), "initStateFromAmpsF32")) return;
+        qg::kF64toF32<<<(unsigned)((c + 255) / 256), 256, 0, st>>>(q->staging, q->staging + chunk, q->re + s, q->im + s, c);
+        if (qg::launchFailed("initStateFromAmpsF32")) return;
+    }
+    QG_CUDA(cudaStreamSynchronize(st), "initStateFromAmpsF32");
+}
+
+void quest_gb300_copyStateToHostF32(void* h, double* re, double* im) {
+    QuregF32* q = qg::Q(h);
+    const uint64_t n = 1ull << q->n;
+    const uint64_t chunk = std::min<uint64_t>(n, 1ull << 26);
+    if (!qg::ensureStaging(*q, chunk)) return;
+    cudaStream_t st = qg::stream();
+    for (uint64_t s = 0; s < n; s += chunk) {
+        const uint64_t c = std::min(chunk, n - s);
+        qg::kF32toF64<<<(unsigned)((c + 255) / 256), 256, 0, st>>>(q->re + s, q->im + s, q->staging, q->staging + chunk, c);
+        if (qg::launchFailed("copyStateToHostF32")) return;
+        if (QG_CUDA(cudaMemcpyAsync(re + s, q->staging, c * sizeof(double), cudaMemcpyDeviceToHost, st), "copyStateToHostF32")) return;
+        if (QG_CUDA(cudaMemcpyAsync(im + s, q->staging + chunk, c * sizeof(double), cudaMemcpyDeviceToHost, st), "copyStateToHostF32")) return;
+    }
+    QG_CUDA(cudaStreamSynchronize(st), "copyStateToHostF32");
+}
+
+int quest_gb300_applyPlanF32(void* h, void* plan) {
+    QuregF32* q = qg::Q(h);
+    qg::FusedPlan* p = reinterpret_cast<qg::FusedPlan*>(plan);
+    if (!q || !p || p->numQubits != q->n) {
+        invalidQuESTInputError("Dimensions of the qubit registers don't match.", "applyPlanF32");
+        return -1;
+    }
+    if (!p->compiled) qg::compilePlan(*p);
+    if (!p->device) {
+        p->device = qg::uploadPlanTC(*p);
+        p->deviceFree = qg::freePlanTC;
+    }
+    cudaStream_t st = qg::stream();
+    bool usedTC = false;
+    for (size_t i = 0; i < p->passes.size(); ++i) {
+        const qg::FusedPass& pass = p->passes[i];
+        if (qg::applyPassTCIndexed(*q, pass, p->device, i, st)) {
+            usedTC = true;
+            continue;
+        }
+        if (!qg::applyPassSimt(*q, pass, st)) {
+            invalidQuESTInputError("fused pass on more than 5 qubits needs the tensor-core applier", "applyPlanF32");
+            return -1;
+        }
+    }
+    if (usedTC && qg::g_checkTC) {
+        const int e = qg::tcErrorFlag(p->device);
+        if (e) {
+            invalidQuESTInputError(e == 1 ? "tensor-core applier: operand staging timed out"
+                                          : "tensor-core applier: MMA completion timed out",
+                                   "applyPlanF32");
+            return -1;
+        }
+    }
+    return 0;
+}
+
+void quest_gb300_setTensorCores(int enabled) { qg::setTensorCoresEnabled(enabled != 0); }
+
+double quest_gb300_calcTotalProbF32(void* h) {
+    QuregF32* q = qg::Q(h);
+    double v = 0;
+    qg::red::runReduce(qg::NormF32{q->re, q->im}, (1ull << q->n) / 2, q->w(), &v, nullptr, "calcTotalProbF32");
+    return v;
+}
+
+double quest_gb300_calcProbOfOutcomeF32(void* h, int t, int outcome) {
+    QuregF32* q = qg::Q(h);
+    if (t < 0 || t >= q->n) {
+        invalidQuESTInputError("Invalid target qubit. Must be >=0 and <numQubits.", "calcProbOfOutcomeF32");
+        return 0;
+    }
+    double v = 0;
+    qg::red::runReduce(qg::ProbZeroF32{q->re, q->im, t}, (1ull << q->n) / 2, q->w(), &v, nullptr, "calcProbOfOutcomeF32");
+    return outcome == 0 ? v : 1 - v;
+}
+
+// 1 - |<psi64|psi32>|^2 / (<psi64|psi64> <psi32|psi32>) and max |d amp|
+double quest_gb300_compareF32(void* h, Qureg ref, double* maxAmpErr) {
+    QuregF32* q = qg::Q(h);
+    const uint64_t n = 1ull << q->n;
+    if (ref.numAmpsTotal != (long long)n || ref.isDensityMatrix) {
+        invalidQuESTInputError("Dimensions of the qubit registers don't match.", "compareF32");
+        return -1;
+    }
+    double orr = 0, oi = 0;
+    qg::red::runReduce(qg::OverlapF32{ref.deviceStateVec.real, ref.deviceStateVec.imag, q->re, q->im}, n, q->w(), &orr, &oi,
+                       "compareF32");
+    const double n32 = quest_gb300_calcTotalProbF32(h);
+    const double n64 = calcTotalProb(ref);
+    if (maxAmpErr) {
+        unsigned long long* d = reinterpret_cast<unsigned long long*>(q->scratch + 2 * qg::kMaxReduceBlocks + 32);
+        cudaStream_t st = qg::stream();
+        cudaMemsetAsync(d, 0, sizeof(unsigned long long), st);
+        qg::kMaxAbsDiff<<<qg::numSMs() * 8, 256, 0, st>>>(ref.deviceStateVec.real, ref.deviceStateVec.imag, q->re, q->im, n, d);
+        qg::launchFailed("compareF32");
+        cudaMemcpyAsync(q->host + 16, d, sizeof(double), cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        memcpy(maxAmpErr, q->host + 16, sizeof(double));
+    }
+    const double f = (orr * orr + oi * oi) / (n32 * n64);
+    return 1.0 - f;
+}
+
+}  // extern "C"

@@ -1,0 +1,44 @@
+// fused_plan.h -- gate-fusion planner of the FP32 fused engine (host C++).
+//
+// No counterpart in the reference (QuEST applies one kernel per gate).  A
+// plan records a gate stream and groups it into "passes": dense
+// 2^k x 2^k complex matrices on k <= kmax qubits, each formed as the FP64
+// product of the gates it absorbs.  Each pass is one streaming sweep of the
+// FP32 state on the device.
+#pragma once
+
+#include <complex>
+#include <cstdint>
+#include <vector>
+
+namespace qg {
+
+using cplx = std::complex<double>;
+
+struct FusedGate {
+    std::vector<int> qubits;   // matrix bit b <-> qubits[b]
+    std::vector<cplx> m;       // row-major 2^q x 2^q
+};
+
+struct FusedPass {
+    std::vector<int> targets;  // ascending; matrix bit b <-> targets[b]
+    std::vector<cplx> m;       // row-major D x D, D = 2^targets.size()
+    int numGates = 0;
+};
+
+struct FusedPlan {
+    int numQubits = 0;
+    int maxFused = 4;
+    std::vector<FusedGate> gates;
+    std::vector<FusedPass> passes;
+    bool compiled = false;
+    // device copy of the per-pass FP32 (and split-TF32) operands, built on
+    // first use by the FP32 engine; owned by the engine
+    void* device = nullptr;
+    void (*deviceFree)(void*) = nullptr;
+};
+
+// Greedy fusion over blocks with disjoint qubit sets (see fused_plan.cpp).
+void compilePlan(FusedPlan& plan);
+
+}  // namespace qg

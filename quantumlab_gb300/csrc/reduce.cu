@@ -10,112 +10,15 @@
 // ticket counter in the register's scratch) adds the per-block partials in a
 // fixed order.  The partial layout depends only on the problem size, so
 // results are deterministic run to run.  One scalar pair is copied back.
-#include "qg_internal.h"
+#include "reduce_kernel.cuh"
 
 #include <algorithm>
 
 namespace qg {
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kWarps = kThreads / 32;
-
-__device__ __forceinline__ double2 ld2(const double* p) { return *reinterpret_cast<const double2*>(p); }
-__device__ __forceinline__ uint64_t ins0(uint64_t k, int b) { return ((k >> b) << (b + 1)) | (k & ((1ull << b) - 1ull)); }
-
-struct Acc {
-    double s = 0.0, c = 0.0;
-    __device__ __forceinline__ void add(double x) {       // Neumaier
-        const double t = s + x;
-        if (fabs(s) >= fabs(x)) c += (s - t) + x;
-        else c += (x - t) + s;
-        s = t;
-    }
-    __device__ __forceinline__ double value() const { return s + c; }
-};
-
-__device__ __forceinline__ double warpSum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// f(i) -> double2 contribution of item i.  4 items are loaded per iteration
-// so every thread keeps several loads in flight.
-template <class F>
-__global__ void __launch_bounds__(kThreads) kReduce(F f, uint64_t nItems, double* __restrict__ partials,
-                                                    unsigned int* __restrict__ counter, double* __restrict__ result) {
-    __shared__ double sx[kWarps], sy[kWarps];
-    __shared__ bool amLast;
-    Acc ax, ay;
-    const uint64_t stride = (uint64_t)gridDim.x * kThreads;
-    uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
-    for (; i + 3 * stride < nItems; i += 4 * stride) {
-        const double2 v0 = f(i), v1 = f(i + stride), v2 = f(i + 2 * stride), v3 = f(i + 3 * stride);
-        ax.add(v0.x); ay.add(v0.y);
-        ax.add(v1.x); ay.add(v1.y);
-        ax.add(v2.x); ay.add(v2.y);
-        ax.add(v3.x); ay.add(v3.y);
-    }
-    for (; i < nItems; i += stride) {
-        const double2 v = f(i);
-        ax.add(v.x); ay.add(v.y);
-    }
-    double x = warpSum(ax.value()), y = warpSum(ay.value());
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) { sx[w] = x; sy[w] = y; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double bx = 0, by = 0;
-        for (int k = 0; k < kWarps; ++k) { bx += sx[k]; by += sy[k]; }
-        partials[2 * blockIdx.x] = bx;
-        partials[2 * blockIdx.x + 1] = by;
-        __threadfence();
-        const unsigned ticket = atomicAdd(counter, 1u);
-        amLast = (ticket == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!amLast) return;
-    __threadfence();
-    // last block: fixed-order sum of the partials
-    Acc fx, fy;
-    for (unsigned b = threadIdx.x; b < gridDim.x; b += kThreads) {
-        fx.add(__ldcg(partials + 2 * b));
-        fy.add(__ldcg(partials + 2 * b + 1));
-    }
-    x = warpSum(fx.value());
-    y = warpSum(fy.value());
-    if (lane == 0) { sx[w] = x; sy[w] = y; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double bx = 0, by = 0;
-        for (int k = 0; k < kWarps; ++k) { bx += sx[k]; by += sy[k]; }
-        result[0] = bx;
-        result[1] = by;
-        *counter = 0u;
-    }
-}
-
-int reduceGrid(uint64_t nItems) {
-    // one full wave: 256-thread blocks, 8 resident per SM (the kernel needs
-    // well under 32 registers per thread)
-    const uint64_t resident = 8ull * (uint64_t)numSMs();
-    const uint64_t want = (nItems + kThreads - 1) / kThreads;
-    return (int)std::max<uint64_t>(1, std::min<uint64_t>(want, std::min<uint64_t>(resident, kMaxReduceBlocks)));
-}
-
-template <class F>
-bool runReduce(const F& f, uint64_t nItems, const Scratch& w, double* out0, double* out1, const char* caller) {
-    cudaStream_t st = stream();
-    const int grid = reduceGrid(nItems);
-    kReduce<F><<<grid, kThreads, 0, st>>>(f, nItems, w.partials, w.counter, w.result);
-    if (launchFailed(caller)) return false;
-    if (QG_CUDA(cudaMemcpyAsync(w.host, w.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), caller)) return false;
-    if (QG_CUDA(cudaStreamSynchronize(st), caller)) return false;
-    if (out0) *out0 = w.host[0];
-    if (out1) *out1 = w.host[1];
-    return true;
-}
+using namespace red;
+constexpr int kThreads = red::kThreads;
 
 // ------------------------------------------------------------------ functors
 struct NormSq2 {          // two consecutive amplitudes per item

@@ -171,6 +171,29 @@ SIGNATURES = {
     "quest_gb300_launchCount": (c_ll, []),
     "quest_gb300_eventRecord": (_I, [_I]),
     "quest_gb300_eventElapsedMs": (qreal, [_I, _I]),
+    "quest_gb300_planCreate": (C.c_void_p, [_I, _I]),
+    "quest_gb300_planDestroy": (None, [C.c_void_p]),
+    "quest_gb300_planAddGate": (_I, [C.c_void_p, _P(_I), _I, _P(qreal), _P(qreal)]),
+    "quest_gb300_planAddCompactUnitary": (_I, [C.c_void_p, _I, _D, _D, _D, _D]),
+    "quest_gb300_planAddUnitary": (_I, [C.c_void_p, _I, _P(qreal), _P(qreal)]),
+    "quest_gb300_planAddHadamard": (_I, [C.c_void_p, _I]),
+    "quest_gb300_planAddControlledNot": (_I, [C.c_void_p, _I, _I]),
+    "quest_gb300_planAddControlledPhaseShift": (_I, [C.c_void_p, _I, _I, _D]),
+    "quest_gb300_planCompile": (_I, [C.c_void_p]),
+    "quest_gb300_planNumGates": (_I, [C.c_void_p]),
+    "quest_gb300_planPass": (_I, [C.c_void_p, _I, _P(_I), _P(qreal), _P(qreal)]),
+    "quest_gb300_createQuregF32": (C.c_void_p, [_I]),
+    "quest_gb300_destroyQuregF32": (None, [C.c_void_p]),
+    "quest_gb300_initZeroStateF32": (None, [C.c_void_p]),
+    "quest_gb300_initStateFromAmpsF32": (None, [C.c_void_p, _P(qreal), _P(qreal)]),
+    "quest_gb300_copyStateToHostF32": (None, [C.c_void_p, _P(qreal), _P(qreal)]),
+    "quest_gb300_copyFromQureg": (None, [C.c_void_p, _Q]),
+    "quest_gb300_copyToQureg": (None, [C.c_void_p, _Q]),
+    "quest_gb300_applyPlanF32": (_I, [C.c_void_p, C.c_void_p]),
+    "quest_gb300_setTensorCores": (None, [_I]),
+    "quest_gb300_calcTotalProbF32": (qreal, [C.c_void_p]),
+    "quest_gb300_calcProbOfOutcomeF32": (qreal, [C.c_void_p, _I, _I]),
+    "quest_gb300_compareF32": (qreal, [C.c_void_p, _Q, _P(qreal)]),
 }
 
 
@@ -351,6 +374,35 @@ class QuESTLibrary:
 
     def calcExpecPauliProd(self, q, ts, ps, ws):
         return self.lib.calcExpecPauliProd(q, _ints(ts), _ints(ps), len(ts), ws)
+
+    # ---- fused FP32 engine (include/quest_gb300.h) ----------------------------
+    def plan(self, n: int, kmax: int, ops) -> int:
+        """Record workloads-style ops into a fusion plan and compile it."""
+        p = self.lib.quest_gb300_planCreate(n, kmax)
+        if not p:
+            raise ValueError("invalid plan parameters")
+        for op in ops:
+            k = op[0]
+            if k == "cu":
+                rc = self.lib.quest_gb300_planAddCompactUnitary(p, *op[1:])
+            elif k == "cx":
+                rc = self.lib.quest_gb300_planAddControlledNot(p, op[1], op[2])
+            elif k == "cp":
+                rc = self.lib.quest_gb300_planAddControlledPhaseShift(p, op[1], op[2], op[3])
+            elif k == "h":
+                rc = self.lib.quest_gb300_planAddHadamard(p, op[1])
+            else:
+                raise ValueError(f"op {k} cannot be fused")
+            if rc != 0:
+                raise ValueError(f"rejected op {op}")
+        self.lib.quest_gb300_planCompile(p)
+        return p
+
+    def amps_f32(self, q32, n: int) -> np.ndarray:
+        re = np.empty(1 << n)
+        im = np.empty(1 << n)
+        self.lib.quest_gb300_copyStateToHostF32(q32, re.ctypes.data_as(C.POINTER(qreal)), im.ctypes.data_as(C.POINTER(qreal)))
+        return re + 1j * im
 
     def pauli_hamil(self, codes, coeffs):
         codes = np.asarray(codes, dtype=np.int32)

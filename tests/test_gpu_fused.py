@@ -1,0 +1,100 @@
+"""FP32 fused engine against the FP64 plain engine (GPU).
+
+Tolerances: 1 - fidelity <= 1e-6 (the fused path's stated bound) and
+max |d amp| <= 1e-5; observed errors are printed."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from quantumlab_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def run_both(L, n, kmax, ops):
+    q64 = L.create(n)
+    W.run_ops(L, q64, ops)
+    q32 = L.lib.quest_gb300_createQuregF32(n)
+    plan = L.plan(n, kmax, ops)
+    assert L.lib.quest_gb300_applyPlanF32(q32, plan) == 0
+    err = C.c_double(0)
+    one_minus_f = L.lib.quest_gb300_compareF32(q32, q64, C.byref(err))
+    return q64, q32, plan, one_minus_f, err.value
+
+
+@pytest.mark.parametrize("kmax", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("n", [7, 16, 22])
+def test_fused_matches_plain(gpulib, n, kmax):
+    L = gpulib
+    L.lib.quest_gb300_setTensorCores(0)
+    ops = W.c2_circuit(n=n, layers=6, seed=21 + n)
+    if kmax == 1:
+        ops = [o for o in ops if o[0] == "cu"]
+    q64, q32, plan, omf, err = run_both(L, n, kmax, ops)
+    L.lib.quest_gb300_setTensorCores(1)
+    print(f"n={n} k={kmax}: 1-F={omf:.2e} max|d amp|={err:.2e}")
+    assert omf <= 1e-6 and err <= 1e-5
+    p32 = L.lib.quest_gb300_calcTotalProbF32(q32)
+    assert abs(p32 - 1) < 1e-5
+    for t in (0, n // 2, n - 1):
+        assert abs(L.lib.quest_gb300_calcProbOfOutcomeF32(q32, t, 1) - L.lib.calcProbOfOutcome(q64, t, 1)) < 1e-6
+    L.lib.quest_gb300_planDestroy(plan)
+    L.lib.quest_gb300_destroyQuregF32(q32)
+    L.destroy(q64)
+
+
+def test_fused_host_roundtrip(gpulib):
+    L = gpulib
+    n = 12
+    rng = np.random.default_rng(5)
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    psi /= np.linalg.norm(psi)
+    q32 = L.lib.quest_gb300_createQuregF32(n)
+    re, im = np.ascontiguousarray(psi.real), np.ascontiguousarray(psi.imag)
+    L.lib.quest_gb300_initStateFromAmpsF32(q32, re.ctypes.data_as(C.POINTER(C.c_double)), im.ctypes.data_as(C.POINTER(C.c_double)))
+    back = L.amps_f32(q32, n)
+    assert np.max(np.abs(back - psi)) < 1e-7
+    q64 = L.create(n)
+    L.set_amps(q64, psi)
+    L.lib.quest_gb300_copyToQureg(q32, q64)
+    assert np.max(np.abs(L.amps(q64) - back)) == 0
+    L.lib.quest_gb300_destroyQuregF32(q32)
+    L.destroy(q64)
+
+
+@pytest.mark.parametrize("kmax", [4, 5, 6])
+@pytest.mark.parametrize("n", [13, 18])
+def test_tensor_core_applier(gpulib, n, kmax):
+    """tcgen05 split-TF32 passes (k = 4..6) against the FP64 plain engine and
+    against the FP32 SIMT applier."""
+    L = gpulib
+    ops = W.c2_circuit(n=n, layers=4, seed=31 + n)
+    L.lib.quest_gb300_setTensorCores(1)
+    q64, q32, plan, omf, err = run_both(L, n, kmax, ops)
+    print(f"TC n={n} k={kmax}: 1-F={omf:.2e} max|d amp|={err:.2e}")
+    assert omf <= 1e-6 and err <= 1e-5
+    if kmax <= 5:
+        L.lib.quest_gb300_setTensorCores(0)
+        s32 = L.lib.quest_gb300_createQuregF32(n)
+        assert L.lib.quest_gb300_applyPlanF32(s32, plan) == 0
+        L.lib.quest_gb300_setTensorCores(1)
+        a, b = L.amps_f32(q32, n), L.amps_f32(s32, n)
+        assert np.max(np.abs(a - b)) < 1e-5
+        L.lib.quest_gb300_destroyQuregF32(s32)
+    L.lib.quest_gb300_planDestroy(plan)
+    L.lib.quest_gb300_destroyQuregF32(q32)
+    L.destroy(q64)
+
+
+@pytest.mark.parametrize("kmax", [4, 6])
+def test_fused_30q_headline_accuracy(gpulib, kmax):
+    """The 30-qubit, 20-layer circuit: fused FP32 vs plain FP64."""
+    L = gpulib
+    ops = W.c2_circuit(n=30, layers=20, seed=2)
+    q64, q32, plan, omf, err = run_both(L, 30, kmax, ops)
+    print(f"30q: 1-F={omf:.3e} max|d amp|={err:.3e}")
+    assert omf <= 1e-6
+    L.lib.quest_gb300_planDestroy(plan)
+    L.lib.quest_gb300_destroyQuregF32(q32)
+    L.destroy(q64)
