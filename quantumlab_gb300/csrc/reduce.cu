@@ -5,7 +5,7 @@
 // cudaDeviceSynchronize per level, runs complex inner products twice (real,
 // imaginary), and computes calcTotalProb by copying the whole state to the
 // host (:1626-1679).  Here every reduction is a single pass: each thread keeps
-// Neumaier-compensated FP64 sums of two components, warps combine with
+// FP64 partial sums of two components, warps combine with
 // shuffles, blocks through shared memory, and the last block to finish (a
 // ticket counter in the register's scratch) adds the per-block partials in a
 // fixed order.  The partial layout depends only on the problem size, so

@@ -1,6 +1,6 @@
 // reduce_kernel.cuh -- single-pass FP64 reduction machinery shared by the
 // FP64 engine (reduce.cu) and the FP32 fused engine (fused_f32.cu).
-// Each thread keeps Neumaier-compensated sums of two components; warps
+// Each thread keeps FP64 partial sums of two components; warps
 // combine with shuffles, blocks through shared memory; the last block to
 // finish (ticket counter in the register's scratch) adds the per-block
 // partials in a fixed order, so results are deterministic.
@@ -18,15 +18,20 @@ constexpr int kWarps = kThreads / 32;
 __device__ __forceinline__ double2 ld2(const double* p) { return *reinterpret_cast<const double2*>(p); }
 __device__ __forceinline__ uint64_t ins0(uint64_t k, int b) { return ((k >> b) << (b + 1)) | (k & ((1ull << b) - 1ull)); }
 
+// Per-thread accumulation: FP64 adds into two independent partial sums.
+// GB300 executes FP64 at a small fraction of its FP32 rate, so the sums use
+// no compensation terms (a Neumaier step costs ~4 extra FP64 operations per
+// addition and made these kernels FP64-bound); accuracy comes from the short
+// per-thread chains (about 2^n / (2 * 256 * resident blocks) terms each) and
+// the pairwise block / grid combination.
 struct Acc {
-    double s = 0.0, c = 0.0;
-    __device__ __forceinline__ void add(double x) {       // Neumaier
-        const double t = s + x;
-        if (fabs(s) >= fabs(x)) c += (s - t) + x;
-        else c += (x - t) + s;
-        s = t;
+    double s0 = 0.0, s1 = 0.0;
+    __device__ __forceinline__ void add(double x) { s0 += x; }
+    __device__ __forceinline__ void add2(double x, double y) {
+        s0 += x;
+        s1 += y;
     }
-    __device__ __forceinline__ double value() const { return s + c; }
+    __device__ __forceinline__ double value() const { return s0 + s1; }
 };
 
 __device__ __forceinline__ double warpSum(double v) {
@@ -47,10 +52,8 @@ __global__ void __launch_bounds__(kThreads) kReduce(F f, uint64_t nItems, double
     uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
     for (; i + 3 * stride < nItems; i += 4 * stride) {
         const double2 v0 = f(i), v1 = f(i + stride), v2 = f(i + 2 * stride), v3 = f(i + 3 * stride);
-        ax.add(v0.x); ay.add(v0.y);
-        ax.add(v1.x); ay.add(v1.y);
-        ax.add(v2.x); ay.add(v2.y);
-        ax.add(v3.x); ay.add(v3.y);
+        ax.add2(v0.x + v2.x, v1.x + v3.x);
+        ay.add2(v0.y + v2.y, v1.y + v3.y);
     }
     for (; i < nItems; i += stride) {
         const double2 v = f(i);
