@@ -69,6 +69,24 @@ double quest_gb300_calcProbOfOutcomeF32(void* qureg32, int measureQubit, int out
  * largest |amplitude difference| to *maxAmpErr when it is not NULL */
 double quest_gb300_compareF32(void* qureg32, Qureg reference, double* maxAmpErr);
 
+/* ---- total probability without allocating ---------------------------------
+ * No counterpart in the reference.  For callers that hold their own FP64
+ * state arrays and must not allocate while they run (a host callback or
+ * real-time worker kept out of the CUDA allocator, a process whose device
+ * memory is reserved by another framework's pool, a library that only borrows
+ * device pointers): sum |amp|^2 of deviceReal/deviceImag[numAmps] with no
+ * cudaMalloc, cudaFree or allocating library call.  Scratch is a fixed
+ * __device__ array of about 16.5 KB per GPU, so numAmps must be a power of two
+ * in [2, 2^27]; larger states are rejected with an error (use calcTotalProb).
+ * The result is written to *result (host or device memory) and the call
+ * returns after `stream` (a cudaStream_t; NULL = legacy default stream) has
+ * finished it.  The first call on a device looks up the scratch address and
+ * should come before any stream capture.  All calls share the scratch: calls
+ * that overlap on the GPU race.  Returns 0 on success, nonzero after
+ * reporting the error through invalidQuESTInputError.                       */
+int quest_gb300_calcTotalProbNoAlloc(const double* deviceReal, const double* deviceImag, long long numAmps,
+                                     double* result, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

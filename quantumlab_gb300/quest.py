@@ -191,6 +191,7 @@ SIGNATURES = {
     "quest_gb300_copyToQureg": (None, [C.c_void_p, _Q]),
     "quest_gb300_applyPlanF32": (_I, [C.c_void_p, C.c_void_p]),
     "quest_gb300_setTensorCores": (None, [_I]),
+    "quest_gb300_calcTotalProbNoAlloc": (_I, [C.c_void_p, C.c_void_p, c_ll, _P(qreal), C.c_void_p]),
     "quest_gb300_calcTotalProbF32": (qreal, [C.c_void_p]),
     "quest_gb300_calcProbOfOutcomeF32": (qreal, [C.c_void_p, _I, _I]),
     "quest_gb300_compareF32": (qreal, [C.c_void_p, _Q, _P(qreal)]),
