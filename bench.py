@@ -4,8 +4,10 @@ through the GB300 library, plus the QuEST-CPU baseline.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-One step = the whole circuit once (initZeroState, all gates, calcTotalProb)
-on one register.  `value` is the per-gate FP64 algorithmic throughput: the
+One step = the whole circuit once on one register through the fused FP32
+engine (initZeroState, every fused pass, FP64 total probability); the plain
+FP64 per-gate engine runs the same circuit once for the comparison and the
+1 - fidelity check.  `value` is the per-gate FP64 algorithmic throughput: the
 bytes a per-gate FP64 simulator must stream for this circuit (1q gate
 2*2^n*16 B, CNOT 2^n*16 B, CPhase 2^(n-1)*16 B; 28.2 TB at 30 qubits, 20
 layers) divided by the time per circuit.  The same definition is used for
@@ -24,6 +26,8 @@ import statistics
 import subprocess
 import sys
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -113,114 +117,216 @@ def barrier(world: int):
 
 
 # ----------------------------------------------------------------- GB300 arm
+def run_plain_step(L, q, ops):
+    from quantumlab_gb300.quest import Complex
+    lib = L.lib
+    for op in ops:
+        kind = op[0]
+        if kind == "cu":
+            lib.compactUnitary(q, op[1], Complex(op[2], op[3]), Complex(op[4], op[5]))
+        elif kind == "cx":
+            lib.controlledNot(q, op[1], op[2])
+        else:
+            lib.controlledPhaseShift(q, op[1], op[2], op[3])
+
+
 def run_gpu(args, rank, world):
+    import ctypes as C
     import quantumlab_gb300 as qg
     from quantumlab_gb300 import workloads as W
-    from quantumlab_gb300.quest import Complex
 
     L = qg.load()
     lib = L.lib
-    n = args.qubits
+    n, k = args.qubits, args.fusion
     ops = W.c2_circuit(n=n, layers=args.layers, seed=2)
     alg_bytes = W.algorithmic_bytes(ops, n)
-    q = L.create(n)
+    pass_bytes = 2 * (1 << n) * 8                   # one fused pass: read + write the FP32 state
 
-    def step(time_kernels=False, slot_base=100):
-        lib.initZeroState(q)
-        k = 0
-        for op in ops:
-            kind = op[0]
-            if kind == "cu":
-                if time_kernels:
-                    lib.quest_gb300_eventRecord(slot_base + 2 * k)
-                lib.compactUnitary(q, op[1], Complex(op[2], op[3]), Complex(op[4], op[5]))
-                if time_kernels:
-                    lib.quest_gb300_eventRecord(slot_base + 2 * k + 1)
-                k += 1
-            elif kind == "cx":
-                lib.controlledNot(q, op[1], op[2])
-            else:
-                lib.controlledPhaseShift(q, op[1], op[2], op[3])
-        total = lib.calcTotalProb(q)
-        kern = []
-        if time_kernels:
-            kern = [lib.quest_gb300_eventElapsedMs(slot_base + 2 * i, slot_base + 2 * i + 1) for i in range(k)]
-        return total, kern
+    # ---- fused FP32 engine (the headline) --------------------------------
+    t0 = time.perf_counter()
+    plan = L.plan(n, k, ops)
+    plan_s = time.perf_counter() - t0
+    npass = lib.quest_gb300_planCompile(plan)
+    tc = [lib.quest_gb300_planPassUsesTensorCores(plan, i) for i in range(npass)]
+    kk = [lib.quest_gb300_planPass(plan, i, None, None, None) for i in range(npass)]
+    q32 = lib.quest_gb300_createQuregF32(n)
+
+    def fused_step(per_pass=False):
+        lib.quest_gb300_initZeroStateF32(q32)
+        if not per_pass:
+            lib.quest_gb300_applyPlanF32(q32, plan)
+        else:
+            for i in range(npass):
+                lib.quest_gb300_eventRecord(100 + 2 * i)
+                lib.quest_gb300_applyPlanF32Range(q32, plan, i, 1)
+                lib.quest_gb300_eventRecord(101 + 2 * i)
+        total = lib.quest_gb300_calcTotalProbF32(q32)
+        return total, ([lib.quest_gb300_eventElapsedMs(100 + 2 * i, 101 + 2 * i) for i in range(npass)] if per_pass else [])
 
     for _ in range(args.warmup):
-        step()
+        fused_step()
     barrier(world)
     launches0 = lib.quest_gb300_launchCount()
-    kern_ms = []
+    pass_ms = [0.0] * npass
     with Clocks(int(os.environ.get("LOCAL_RANK", 0))) as clk:
         lib.quest_gb300_eventRecord(0)
         t0 = time.perf_counter()
-        for s in range(args.steps):
-            total, kern = step(time_kernels=True)
-            kern_ms += kern
+        for _ in range(args.steps):
+            total32, pm = fused_step(per_pass=True)
+            pass_ms = [a + b for a, b in zip(pass_ms, pm)]
         lib.quest_gb300_eventRecord(1)
         ms = lib.quest_gb300_eventElapsedMs(0, 1)
         wall = time.perf_counter() - t0
     launches = lib.quest_gb300_launchCount() - launches0
     ms_step = barrier_max(ms / args.steps, world)
     value = world * alg_bytes / (ms_step / 1e3) / 1e9
+    pass_ms = [x / args.steps for x in pass_ms]
 
-    # end to end through the C ABI with host buffers: the pinned host mirror
-    # holds |0..0>; each step copies it in, runs the circuit, reads the total
-    # probability and copies the whole state back (QLSimulatorVector pattern)
-    lib.initZeroState(q)
-    lib.copyStateFromGPU(q)
+    # dominant kernel: group passes by applier and k
+    groups = {}
+    for i in range(npass):
+        key = (f"kApplyTC<{kk[i]}> (tcgen05 split-TF32)" if tc[i] else f"kApplySimt<{kk[i]}> (FP32 FFMA)")
+        g = groups.setdefault(key, [0, 0.0])
+        g[0] += 1
+        g[1] += pass_ms[i]
+    dom_name, (dom_count, dom_ms) = max(groups.items(), key=lambda kv: kv[1][1])
+    dom_avg = dom_ms / dom_count
+
+    # ---- plain FP64 engine on the same circuit (per-gate, QuEST API) ------
+    q64 = L.create(n)
+    plain_ms = None
+    if not args.skip_plain:
+        lib.initZeroState(q64)
+        run_plain_step(L, q64, ops)
+        lib.calcTotalProb(q64)
+        lib.initZeroState(q64)
+        lib.quest_gb300_eventRecord(2)
+        run_plain_step(L, q64, ops)
+        lib.calcTotalProb(q64)
+        lib.quest_gb300_eventRecord(3)
+        plain_ms = lib.quest_gb300_eventElapsedMs(2, 3)
+        err = C.c_double(0)
+        one_minus_f = lib.quest_gb300_compareF32(q32, q64, C.byref(err))
+        max_amp_err = err.value
+    else:
+        one_minus_f = max_amp_err = None
+
+    # ---- end to end through the C ABI with host buffers ------------------
+    # input: the |0..0> amplitudes in pinned host FP64 arrays (the plain
+    # register's host mirror); output: total probability + every amplitude
+    # back to host FP64 arrays (the QLSimulatorVector pattern)
+    lib.initZeroState(q64)
+    lib.copyStateFromGPU(q64)
+    hre, him = q64.stateVec.real, q64.stateVec.imag
     e2e_steps = max(1, min(args.steps, 2))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        lib.copyStateToGPU(q)
-        for op in ops:
-            kind = op[0]
-            if kind == "cu":
-                lib.compactUnitary(q, op[1], Complex(op[2], op[3]), Complex(op[4], op[5]))
-            elif kind == "cx":
-                lib.controlledNot(q, op[1], op[2])
-            else:
-                lib.controlledPhaseShift(q, op[1], op[2], op[3])
-        lib.calcTotalProb(q)
-        lib.copyStateFromGPU(q)
+        lib.quest_gb300_initStateFromAmpsF32(q32, hre, him)
+        lib.quest_gb300_applyPlanF32(q32, plan)
+        lib.quest_gb300_calcTotalProbF32(q32)
+        lib.quest_gb300_copyStateToHostF32(q32, hre, him)
     e2e_s = barrier_max((time.perf_counter() - t0) / e2e_steps, world)
     state_bytes = (1 << n) * 16
-    L.destroy(q)
+    L.destroy(q64)
+    lib.quest_gb300_destroyQuregF32(q32)
+    lib.quest_gb300_planDestroy(plan)
 
     peak, peak_kind = peaks()
-    one_q_bytes = 2 * (1 << n) * 16
-    avg_kernel_ms = statistics.mean(kern_ms) if kern_ms else float("nan")
-    achieved = one_q_bytes / (avg_kernel_ms / 1e3) / 1e9
+    achieved = pass_bytes / (dom_avg / 1e3) / 1e9
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
-        t = json.load(open(tp)).get("plain_compactUnitary_per_amp_bytes")
+        t = json.load(open(tp)).get(dom_name.split(" ")[0])
         if t:
             traffic = t * (1 << n)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s (per-gate FP64 algorithmic bytes)",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (split-TF32 tensor cores; FP64 fusion products and reductions)",
         "data": "synthetic (seeded Haar/CPhase-matching/CNOT-brickwork circuit)",
-        "config": {"workload": f"{n}-qubit random circuit, {args.layers} layers, plain FP64 per-gate engine",
-                   "qubits": n, "layers": args.layers, "gates_per_circuit": len(ops),
-                   "algorithmic_bytes_per_circuit": alg_bytes, "engine": "plain-fp64",
-                   "l2": "state 16 GiB >> 129 MB L2, no flush needed", "parallelism": "replicas" if world > 1 else "1 GPU"},
-        "roofline": {"bound": "hbm", "kernel": "compactUnitary (kPairVec<OpCompact>)",
-                     "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "avg_launch_ms": round(avg_kernel_ms, 4), "launches_timed": len(kern_ms)},
+        "config": {"workload": f"{n}-qubit random circuit, {args.layers} layers: fused FP32 engine (k<={k}) vs plain FP64 per-gate engine",
+                   "qubits": n, "layers": args.layers, "gates_per_circuit": len(ops), "fusion_max_qubits": k,
+                   "fused_passes": npass, "algorithmic_bytes_per_circuit": alg_bytes,
+                   "value_definition": "per-gate FP64 algorithmic bytes of the circuit / time per circuit",
+                   "l2": "state 8 GiB (FP32) / 16 GiB (FP64) >> 129 MB L2, no flush needed",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "fused_fp32": {"ms_per_circuit": round(ms_step, 2), "gbs": round(value, 1), "passes": npass,
+                       "plan_compile_s": round(plan_s, 3), "one_minus_fidelity": one_minus_f,
+                       "max_amp_err": max_amp_err,
+                       "kernels": {name: {"passes": c, "ms_per_circuit": round(t, 2)} for name, (c, t) in groups.items()}},
+        "plain_fp64": ({"ms_per_circuit": round(plain_ms, 1), "gbs": round(alg_bytes / (plain_ms / 1e3) / 1e9, 1),
+                        "launches": len(ops)} if plain_ms else None),
+        "speedup_fused_vs_plain": round(plain_ms / ms_step, 2) if plain_ms else None,
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "avg_launch_ms": round(dom_avg, 4), "launches_per_circuit": dom_count,
+                     "bytes_per_launch": pass_bytes},
         "e2e": {"value": round(world * alg_bytes / e2e_s / 1e9, 2), "unit": "GB/s (per-gate FP64 algorithmic bytes)",
-                "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes + 16},
-        "gpu_launches": int(launches),
-        "total_prob": total,
+                "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes + 8,
+                "ms_per_step": round(e2e_s * 1e3, 2)},
+        "gpu_launches": int(launches // max(1, args.steps)),
+        "gpu_launches_timed_region": int(launches),
+        "total_prob_fp32": total32,
         "wall_s": round(wall, 3),
     }
     clk_sum = clk.summary()
     if clk_sum:
         out["clocks"] = clk_sum
     return out
+
+
+# ------------------------------------------------------- batched swap tests
+def run_swaps(args):
+    """65,536 QKMeans swap tests (4096 vectors x 16 centroids, 9..21 qubits):
+    the batched engine (one persistent kernel, CUDA-graph replay) against one
+    circuit at a time through the QuEST API (the reference pattern, per-gate
+    FP64 kernels) on a per-size subsample, extrapolated over the size mix."""
+    import ctypes as C
+    import quantumlab_gb300 as qg
+    from quantumlab_gb300 import workloads as W
+
+    L = qg.load()
+    lib = L.lib
+    ds, comps, vecs, cents = W.gaussian_mixture_vectors(count=args.swap_vectors, seed=5)
+    pool, offsets, dims, ia, ib = W.swap_test_pool(vecs, cents)
+    P = lambda a, t: a.ctypes.data_as(C.POINTER(t))
+    t0 = time.perf_counter()
+    h = lib.quest_gb300_swapTestBatchCreate(P(pool, C.c_double), P(offsets, C.c_longlong), P(dims, C.c_int),
+                                            len(offsets), P(ia, C.c_int), P(ib, C.c_int), len(ia))
+    create_s = time.perf_counter() - t0
+    out = np.zeros(len(ia))
+    for _ in range(3):
+        lib.quest_gb300_swapTestBatchRun(h, P(out, C.c_double))
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        lib.quest_gb300_swapTestBatchRun(h, P(out, C.c_double))
+    batch_s = (time.perf_counter() - t0) / reps
+    lib.quest_gb300_swapTestBatchDestroy(h)
+    items = list(vecs) + [m for d in range(4, 11) for m in cents[d]]
+    want = np.array([(1 + np.dot(items[a], items[b]) ** 2) / 2 for a, b in zip(ia, ib)])
+    err = float(np.max(np.abs(out - want)))
+    # one circuit at a time through the QuEST API, per size class
+    per_size = {}
+    counts = {d: int(np.sum(dims[ia] == d)) for d in range(4, 11)}
+    for d in range(4, 11):
+        pick = [k for k in range(len(ia)) if dims[ia[k]] == d][: args.swap_sample]
+        q = L.create(2 * d + 1)
+        W.swap_test_plain(L, q, items[ia[pick[0]]], items[ib[pick[0]]], d)     # warm-up
+        t0 = time.perf_counter()
+        for k in pick:
+            p = W.swap_test_plain(L, q, items[ia[k]], items[ib[k]], d)
+        per_size[d] = (time.perf_counter() - t0) / len(pick)
+        L.destroy(q)
+    plain_total = sum(counts[d] * per_size[d] for d in counts)
+    return {
+        "tests": int(len(ia)), "qubits": "9..21", "tests_per_s": round(len(ia) / batch_s, 1),
+        "batch_ms": round(batch_s * 1e3, 3), "create_s": round(create_s, 3),
+        "max_abs_err_vs_fp64_closed_form": err,
+        "per_gate_tests_per_s": round(len(ia) / plain_total, 1),
+        "per_gate_sample": f"{args.swap_sample} circuits per size d=4..10, extrapolated over the size mix",
+        "speedup_batched_vs_per_gate": round(plain_total / batch_s, 1),
+    }
 
 
 # --------------------------------------------------------- CPU (QuEST) side
@@ -295,6 +401,11 @@ def main():
     ap.add_argument("--layers", type=int, default=20)
     ap.add_argument("--cpu-sample-ops", type=int, default=30)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fusion", type=int, default=5, help="max qubits per fused pass (1..6)")
+    ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--no-swap", action="store_true")
+    ap.add_argument("--swap-vectors", type=int, default=4096)
+    ap.add_argument("--swap-sample", type=int, default=6)
     args = ap.parse_args()
     rank, world, local = dist_info()
     os.environ.setdefault("QUEST_GB300_DEVICE", str(local))
@@ -304,6 +415,8 @@ def main():
             print(json.dumps(out), flush=True)
         return
     out = run_gpu(args, rank, world)
+    if not args.no_swap:
+        out["swap_tests"] = run_swaps(args)
     if rank == 0:
         if not args.no_cpu_baseline:
             gbs, dt, kind, nops = cpu_sample(args.qubits, args.layers, args.cpu_sample_ops)

@@ -60,6 +60,10 @@ void quest_gb300_copyFromQureg(void* qureg32, Qureg source);
 void quest_gb300_copyToQureg(void* qureg32, Qureg destination);
 /* apply every pass of the plan (compiling it first if needed); 0 on success */
 int quest_gb300_applyPlanF32(void* qureg32, void* plan);
+/* apply passes [firstPass, firstPass + numPasses) only (timing, stepping) */
+int quest_gb300_applyPlanF32Range(void* qureg32, void* plan, int firstPass, int numPasses);
+/* 1 if pass i runs on the tensor cores, 0 if on the SIMT applier, -1 if invalid */
+int quest_gb300_planPassUsesTensorCores(void* plan, int i);
 /* passes on 4..6 qubits run on the tensor cores (split-TF32) unless disabled
  * here (1 = enabled, the default; 0 = FP32 SIMT applier for k <= 5) */
 void quest_gb300_setTensorCores(int enabled);
@@ -68,6 +72,20 @@ double quest_gb300_calcProbOfOutcomeF32(void* qureg32, int measureQubit, int out
 /* 1 - |<ref|q>|^2 / (<ref|ref><q|q>) against an FP64 state vector; writes the
  * largest |amplitude difference| to *maxAmpErr when it is not NULL */
 double quest_gb300_compareF32(void* qureg32, Qureg reference, double* maxAmpErr);
+
+/* ---- batched swap tests (QKMeans distances) --------------------------------
+ * For each test t, P(ancilla = 0) of the (2d+1)-qubit swap-test circuit
+ * |0>|v>|u> -> H(anc) -> CSWAP(anc; u_i, v_i) for i < d -> H(anc), with
+ * u = vector idxA[t], v = vector idxB[t] (real, length 2^d, 1 <= d <= 10).
+ * The distance estimate is 2 P0 - 1 = |<u|v>|^2.  Vectors are concatenated
+ * in `vectors` (host, FP64) at offsets[i] with length 2^dimLog2[i].  Create
+ * uploads the data and captures one persistent kernel into a CUDA graph;
+ * Run replays it (FP32 state vectors, FP64-combined probabilities) and writes
+ * numTests values to p0Out (host) in the caller's order.                    */
+void* quest_gb300_swapTestBatchCreate(const double* vectors, const long long* offsets, const int* dimLog2,
+                                      int numVectors, const int* idxA, const int* idxB, int numTests);
+int quest_gb300_swapTestBatchRun(void* batch, double* p0Out);
+void quest_gb300_swapTestBatchDestroy(void* batch);
 
 /* ---- total probability without allocating ---------------------------------
  * No counterpart in the reference.  For callers that hold their own FP64

@@ -461,7 +461,6 @@ bool cudaFailed(cudaError_t e, const char* what, const char* caller) {
     invalidQuESTInputError(buf, caller);
     return true;
 }
-extern std::atomic<long long> g_launches;
 bool launchFailed(const char* caller) {
     g_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaFailed(cudaGetLastError(), "kernel launch", caller);

@@ -12,6 +12,7 @@
 #include "quest_gb300.h"
 #include "reduce_kernel.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -311,7 +312,7 @@ void quest_gb300_copyStateToHostF32(void* h, double* re, double* im) {
     QG_CUDA(cudaStreamSynchronize(st), "copyStateToHostF32");
 }
 
-int quest_gb300_applyPlanF32(void* h, void* plan) {
+int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPasses) {
     QuregF32* q = qg::Q(h);
     qg::FusedPlan* p = reinterpret_cast<qg::FusedPlan*>(plan);
     if (!q || !p || p->numQubits != q->n) {
@@ -323,11 +324,17 @@ int quest_gb300_applyPlanF32(void* h, void* plan) {
         p->device = qg::uploadPlanTC(*p);
         p->deviceFree = qg::freePlanTC;
     }
+    const int total = (int)p->passes.size();
+    if (firstPass < 0 || numPasses < 0 || firstPass > total) {
+        invalidQuESTInputError("Pass range outside the plan.", "applyPlanF32");
+        return -1;
+    }
+    const int last = std::min(total, firstPass + numPasses);
     cudaStream_t st = qg::stream();
     bool usedTC = false;
-    for (size_t i = 0; i < p->passes.size(); ++i) {
+    for (int i = firstPass; i < last; ++i) {
         const qg::FusedPass& pass = p->passes[i];
-        if (qg::applyPassTCIndexed(*q, pass, p->device, i, st)) {
+        if (qg::applyPassTCIndexed(*q, pass, p->device, (size_t)i, st)) {
             usedTC = true;
             continue;
         }
@@ -336,7 +343,7 @@ int quest_gb300_applyPlanF32(void* h, void* plan) {
             return -1;
         }
     }
-    if (usedTC && qg::g_checkTC) {
+    if (usedTC && qg::g_checkTC && last == total) {
         const int e = qg::tcErrorFlag(p->device);
         if (e) {
             invalidQuESTInputError(e == 1 ? "tensor-core applier: operand staging timed out"
@@ -346,6 +353,16 @@ int quest_gb300_applyPlanF32(void* h, void* plan) {
         }
     }
     return 0;
+}
+
+int quest_gb300_applyPlanF32(void* h, void* plan) { return quest_gb300_applyPlanF32Range(h, plan, 0, 1 << 30); }
+
+/* 1 if pass i of the plan runs on the tensor cores for registers of its size */
+int quest_gb300_planPassUsesTensorCores(void* plan, int i) {
+    qg::FusedPlan* p = reinterpret_cast<qg::FusedPlan*>(plan);
+    if (!p || !p->compiled || i < 0 || i >= (int)p->passes.size()) return -1;
+    const int k = (int)p->passes[i].targets.size();
+    return (qg::tensorCoresEnabled() && k >= 4 && k <= 6 && p->numQubits >= k + 7) ? 1 : 0;
 }
 
 void quest_gb300_setTensorCores(int enabled) { qg::setTensorCoresEnabled(enabled != 0); }

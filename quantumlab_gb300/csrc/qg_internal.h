@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <atomic>
 #include <stddef.h>
 
 #include "QuEST.h"
@@ -24,6 +25,8 @@ bool cudaFailed(cudaError_t e, const char* what, const char* caller);
 bool launchFailed(const char* caller);
 
 int numSMs();
+// kernels launched by the library (quest_gb300_launchCount)
+extern std::atomic<long long> g_launches;
 
 // Per-register reduction workspace held in Qureg.firstLevelReduction.
 // Layout (doubles): [partials: 2*kMaxReduceBlocks][result: 64][counter word]

@@ -244,22 +244,69 @@ def hubbard_instances(count: int = 64):
 def gaussian_mixture_vectors(count: int = 4096, components: int = 16, dmin: int = 4, dmax: int = 10, seed: int = 5):
     """QKMeans inputs: per vector a dimension exponent d ~ U{dmin..dmax}, a
     mixture component, and a unit-normalised real vector of length 2^d drawn
-    around that component's mean.  Returns (d[], comp[], vectors[], centroids)
-    with centroids[d][c] the normalised component means."""
-    rng = Xoshiro(seed)
-    ds = [dmin + rng.randint(dmax - dmin + 1) for _ in range(count)]
-    comps = [rng.randint(components) for _ in range(count)]
+    around that component's mean.  Returns (d[], comp[], vectors[],
+    centroids) with centroids[d][c] the normalised component means.  Seeded
+    through xoshiro256** into numpy's PCG64 (vectorised draws)."""
+    x = Xoshiro(seed)
+    rng = np.random.Generator(np.random.PCG64(x.next()))
+    ds = rng.integers(dmin, dmax + 1, size=count)
+    comps = rng.integers(0, components, size=count)
     centroids = {}
     for d in range(dmin, dmax + 1):
-        dim = 1 << d
-        cs = []
-        for _ in range(components):
-            v = np.array([rng.gauss() for _ in range(dim)])
-            cs.append(v / np.linalg.norm(v))
-        centroids[d] = cs
+        m = rng.standard_normal((components, 1 << d))
+        centroids[d] = m / np.linalg.norm(m, axis=1, keepdims=True)
     vecs = []
     for d, c in zip(ds, comps):
-        dim = 1 << d
-        v = centroids[d][c] + 0.3 / math.sqrt(dim) * np.array([rng.gauss() for _ in range(dim)])
+        dim = 1 << int(d)
+        v = centroids[int(d)][c] + 0.3 / math.sqrt(dim) * rng.standard_normal(dim)
         vecs.append(v / np.linalg.norm(v))
-    return ds, comps, vecs, centroids
+    return [int(d) for d in ds], [int(c) for c in comps], vecs, centroids
+
+
+def swap_test_pool(vecs, centroids, dmin: int = 4, dmax: int = 10):
+    """Concatenate data vectors and centroids into one pool and list the
+    (vector, centroid) pairs of equal dimension: every vector against every
+    centroid of its dimension.  Returns (pool, offsets, dimLog2, idxA, idxB)."""
+    items = list(vecs)
+    dims = [int(round(math.log2(len(v)))) for v in vecs]
+    cent_index = {}
+    for d in range(dmin, dmax + 1):
+        for c, m in enumerate(centroids[d]):
+            cent_index[(d, c)] = len(items)
+            items.append(m)
+            dims.append(d)
+    offsets = np.zeros(len(items), dtype=np.int64)
+    pos = 0
+    for i, v in enumerate(items):
+        offsets[i] = pos
+        pos += len(v)
+    pool = np.concatenate(items).astype(np.float64)
+    ncent = len(centroids[dmin])
+    idx_a, idx_b = [], []
+    for i, v in enumerate(vecs):
+        d = dims[i]
+        for c in range(ncent):
+            idx_a.append(i)
+            idx_b.append(cent_index[(d, c)])
+    return pool, offsets, np.array(dims, dtype=np.int32), np.array(idx_a, dtype=np.int32), np.array(idx_b, dtype=np.int32)
+
+
+def swap_test_plain(L, q, u, v, d: int) -> float:
+    """One swap test through the QuEST API, one kernel per gate (the
+    reference pattern): initStateFromAmps(|0>|v>|u>) with u on qubits 0..d-1,
+    v on d..2d-1, ancilla 2d; H; d controlled swaps as CNOT(v_i -> u_i),
+    Toffoli(anc, u_i -> v_i), CNOT(v_i -> u_i); H; P(anc = 0).  `q` is a
+    (2d+1)-qubit register that is reused between calls."""
+    n = 2 * d + 1
+    psi = np.zeros(1 << n, dtype=np.complex128)
+    psi[: 1 << (2 * d)] = np.kron(v, u)
+    L.set_amps(q, psi)
+    anc = 2 * d
+    L.lib.hadamard(q, anc)
+    for i in range(d):
+        a, b = i, d + i
+        L.lib.controlledNot(q, b, a)
+        L.multiControlledMultiQubitNot(q, [anc, a], [b])
+        L.lib.controlledNot(q, b, a)
+    L.lib.hadamard(q, anc)
+    return L.lib.calcProbOfOutcome(q, anc, 0)
