@@ -43,6 +43,7 @@ void* uploadPlanTC(const FusedPlan& plan);
 void freePlanTC(void* d);
 int tcErrorFlag(const void* devPlan);
 void setTensorCoresEnabled(bool on);
+void setTensorCoreKernel(int version);
 bool tensorCoresEnabled();
 float* f32re(QuregF32& q) { return q.re; }
 float* f32im(QuregF32& q) { return q.im; }
@@ -366,6 +367,7 @@ int quest_gb300_planPassUsesTensorCores(void* plan, int i) {
 }
 
 void quest_gb300_setTensorCores(int enabled) { qg::setTensorCoresEnabled(enabled != 0); }
+void quest_gb300_setTensorCoreKernel(int version) { qg::setTensorCoreKernel(version); }
 
 double quest_gb300_calcTotalProbF32(void* h) {
     QuregF32* q = qg::Q(h);

@@ -139,7 +139,21 @@ __host__ __device__ constexpr uint32_t idescTF32(int M, int N) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-__device__ __forceinline__ uint32_t tf32Hi(float x) { return __float_as_uint(x) & 0xFFFFE000u; }
+// Round to the nearest TF32 value (ties away from zero).  Both split parts are
+// rounded to nearest: the MMA reads operands by dropping their low 13 bits,
+// and a truncated split (hi = x with the low bits cleared) leaves lo with the
+// sign of x, so the dropped bits of lo would bias every product toward zero
+// (a norm loss of ~1e-6 per pass); with hi rounded to nearest lo takes both
+// signs and is itself rounded to nearest, so the residual error is unbiased.
+__device__ __forceinline__ uint32_t tf32RN(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ void splitTF32(float x, uint32_t& hi, uint32_t& lo) {
+    hi = tf32RN(x);
+    lo = tf32RN(x - __uint_as_float(hi));
+}
 
 // ------------------------------------------------------------ the kernel
 // TMEM columns: [0, K) Xh, [K, 2K) Xl, [2K, 2K+N) Out, with K = N = 2D.
@@ -224,10 +238,7 @@ __global__ void __launch_bounds__(kThreadsTC) kApplyTC(float* __restrict__ re, f
             for (int c0 = 0; c0 < CH; c0 += 16) {
                 uint32_t hi[16], lo[16];
 #pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                    hi[e] = tf32Hi(x[c0 + e]);
-                    lo[e] = __float_as_uint(x[c0 + e] - __uint_as_float(hi[e]));
-                }
+                for (int e = 0; e < 16; ++e) splitTF32(x[c0 + e], hi[e], lo[e]);
                 tmemSt16(tXh + laneBase + h + c0, hi);
                 tmemSt16(tXl + laneBase + h + c0, lo);
             }
@@ -286,6 +297,312 @@ __global__ void __launch_bounds__(kThreadsTC) kApplyTC(float* __restrict__ re, f
     if (warp == 0) tmemDealloc(tbase, kCols);
 }
 
+// ------------------------------------------------------------ pipelined kernel
+// Warp-specialised version used for every tensor-core pass:
+//   warps 0-3  loaders:  global -> shared (coalesced 16-byte loads of the
+//              whole tile, stored with a 4-byte XOR swizzle), then each thread
+//              reads its tile column, splits it and writes Xh/Xl to a TMEM
+//              stage with tcgen05.st;
+//   warp 8     TMEM allocation, the one-time TMA bulk copy of Gh/Gl, and the
+//              MMA issue loop (one thread);
+//   warps 4-7  epilogue: tcgen05.ld of a finished accumulator, swizzled
+//              shared-memory staging, coalesced 16-byte stores.
+// TMEM holds two operand stages and two accumulators, so loading tile t+1,
+// multiplying tile t and storing tile t-1 overlap.  A tile is 128 groups
+// over the qubit set I = targets + the 7 lowest other qubits; I always
+// contains qubits [0, r) with r >= 7, so the tile is made of contiguous runs
+// of >= 128 amplitudes and every global access is coalesced whatever the
+// targets are.  The swizzle p ^ ((p >> 5) & 31) makes both the row-order
+// writes and the column-order reads of the staging buffers conflict-free.
+// For k = 6 a tile's K = 128 is split into two stages (real rows, imaginary
+// rows) so the operand stages and both accumulators fit the 512 columns.
+constexpr int kTileBitsC = 7;
+constexpr int kThreadsTC2 = 9 * 32;
+
+template <int KQ>
+struct TC2Params {
+    uint64_t scatterHigh[1 << KQ];   // address bits of the tile-index bits above the low run
+    uint32_t pj[1 << KQ];            // tile-index bits of matrix index j
+    int pcPos[kTileBitsC];           // tile-index positions of the column bits
+    int insI[KQ + kTileBitsC];       // ascending qubits of I
+    int runBits;                     // I contains qubits [0, runBits)
+};
+
+__device__ __forceinline__ void namedBar(int id, int count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ uint32_t swz(uint32_t q) { return q ^ ((q >> 5) & 31u); }
+__device__ __forceinline__ void mbarArrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smemAddr(bar)) : "memory");
+}
+// bounded wait that also gives up when another role has aborted
+__device__ __forceinline__ bool mbarWaitOrAbort(uint64_t* bar, uint32_t parity, volatile int* abortF) {
+    const uint32_t a = smemAddr(bar);
+    for (long long i = 0; i < kSpinLimit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((i & 255) == 255 && *abortF) return false;
+    }
+    return false;
+}
+
+template <int KQ>
+__device__ __forceinline__ uint64_t tileAddr(const TC2Params<KQ>& p, uint32_t q) {
+    return (uint64_t)(q & ((1u << p.runBits) - 1u)) | p.scatterHigh[q >> p.runBits];
+}
+
+template <int KQ>
+__global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ re, float* __restrict__ im,
+                                                            const float* __restrict__ gImage, uint64_t numTiles,
+                                                            int* __restrict__ errFlag,
+                                                            const __grid_constant__ TC2Params<KQ> p) {
+    constexpr int D = 1 << KQ;
+    constexpr int K = 2 * D, N = 2 * D;
+    constexpr int TILE = 1 << (KQ + kTileBitsC);         // amplitudes per plane per tile
+    constexpr int NCH = (KQ == 6) ? 2 : 1;               // K stages per tile
+    constexpr int KC = K / NCH;                          // K columns per stage (<= 64)
+    constexpr int PLS = (NCH == 2) ? 1 : 2;              // planes per stage
+    constexpr int EPASS = (NCH == 2) ? 2 : 1;            // epilogue passes (one plane each for k = 6)
+    constexpr uint32_t kGFloats = (uint32_t)N * K;
+    constexpr uint32_t kXFloats = (uint32_t)TILE * PLS;
+    constexpr uint32_t kStageCols = 2 * KC;
+    constexpr uint32_t kDCol0 = 2 * kStageCols;
+    constexpr uint32_t kUsed = kDCol0 + 2 * N;
+    constexpr uint32_t kCols = kUsed <= 64 ? 64 : (kUsed <= 128 ? 128 : (kUsed <= 256 ? 256 : 512));
+    constexpr uint32_t kLBO = 128, kSBO = (K / 4) * 128;
+    constexpr uint32_t idesc = idescTF32(kTile, N);
+    constexpr int V4 = TILE / 4 / 128;                   // 16-byte loads per loader thread per plane
+
+    extern __shared__ __align__(128) uint8_t smem[];
+    float* gh = reinterpret_cast<float*>(smem);
+    float* gl = gh + kGFloats;
+    float* xs = gl + kGFloats;                           // 2 stage buffers
+    float* es = xs + 2 * kXFloats;                       // epilogue staging
+    __shared__ __align__(8) uint64_t barG, fullB[2], emptyB[2], dFullB[2], dEmptyB[2];
+    __shared__ uint32_t tmemBase;
+    __shared__ volatile int abortF;
+    __shared__ int roleOk[2];
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 8) {
+        if (lane == 0) {
+            abortF = 0;
+            mbarInit(&barG, 1);
+            for (int b = 0; b < 2; ++b) {
+                mbarInit(&fullB[b], 128);
+                mbarInit(&emptyB[b], 1);
+                mbarInit(&dFullB[b], 1);
+                mbarInit(&dEmptyB[b], 128);
+            }
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        tmemAlloc(&tmemBase, kCols);
+    }
+    fenceBefore();
+    __syncthreads();
+    fenceAfter();
+    const uint32_t tmem = tmemBase;
+
+    if (warp < 4) {
+        // ------------------------------------------------ loaders
+        const int lt = threadIdx.x;
+        uint32_t pc = 0;
+#pragma unroll
+        for (int b = 0; b < kTileBitsC; ++b)
+            if (lt >> b & 1) pc |= 1u << p.pcPos[b];
+        const uint32_t laneSel = (uint32_t)(32 * warp) << 16;
+        uint32_t sq = 0;
+        bool ok = true;
+        for (uint64_t tile = blockIdx.x; tile < numTiles && ok; tile += gridDim.x) {
+            uint64_t tb = tile;
+#pragma unroll
+            for (int b = 0; b < KQ + kTileBitsC; ++b) {
+                const int s = p.insI[b];
+                tb = ((tb >> s) << (s + 1)) | (tb & ((1ull << s) - 1ull));
+            }
+            for (int ch = 0; ch < NCH; ++ch, ++sq) {
+                const int b = sq & 1;
+                const uint32_t u = sq >> 1;
+                if (lt == 0) roleOk[0] = (u == 0) || mbarWaitOrAbort(&emptyB[b], (u - 1) & 1, &abortF);
+                namedBar(1, 128);
+                if (!roleOk[0]) {
+                    ok = false;
+                    break;
+                }
+                float* xb = xs + b * kXFloats;
+#pragma unroll
+                for (int pl = 0; pl < PLS; ++pl) {
+                    const float* src = ((NCH == 2 ? ch : pl) == 0) ? re : im;
+                    float4 v[V4];
+#pragma unroll
+                    for (int m = 0; m < V4; ++m)
+                        v[m] = __ldcs(reinterpret_cast<const float4*>(src + tb + tileAddr(p, 4u * lt + 512u * m)));
+                    float* dst = xb + pl * TILE;
+#pragma unroll
+                    for (int m = 0; m < V4; ++m) {
+                        const uint32_t q = 4u * lt + 512u * m;
+                        dst[swz(q)] = v[m].x;
+                        dst[swz(q + 1)] = v[m].y;
+                        dst[swz(q + 2)] = v[m].z;
+                        dst[swz(q + 3)] = v[m].w;
+                    }
+                }
+                namedBar(1, 128);
+                const uint32_t aH = tmem + laneSel + b * kStageCols;
+#pragma unroll
+                for (int c0 = 0; c0 < KC; c0 += 16) {
+                    uint32_t hi[16], lo[16];
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) {
+                        const int kl = c0 + e;
+                        const int pl = (NCH == 2) ? 0 : kl / D;
+                        const int j = (NCH == 2) ? kl : kl % D;
+                        splitTF32(xb[pl * TILE + swz(pc | p.pj[j])], hi[e], lo[e]);
+                    }
+                    tmemSt16(aH + c0, hi);
+                    tmemSt16(aH + KC + c0, lo);
+                }
+                tmemWaitSt();
+                fenceBefore();
+                mbarArrive(&fullB[b]);
+            }
+        }
+        if (!ok) {
+            if (lt == 0) atomicExch(errFlag, 3);
+            abortF = 1;
+        }
+    } else if (warp < 8) {
+        // ------------------------------------------------ epilogue
+        const int et = threadIdx.x - 128;
+        const int ew = warp - 4;
+        uint32_t pc = 0;
+#pragma unroll
+        for (int b = 0; b < kTileBitsC; ++b)
+            if (et >> b & 1) pc |= 1u << p.pcPos[b];
+        const uint32_t laneSel = (uint32_t)(32 * ew) << 16;
+        uint32_t tl = 0;
+        bool ok = true;
+        for (uint64_t tile = blockIdx.x; tile < numTiles && ok; tile += gridDim.x, ++tl) {
+            uint64_t tb = tile;
+#pragma unroll
+            for (int b = 0; b < KQ + kTileBitsC; ++b) {
+                const int s = p.insI[b];
+                tb = ((tb >> s) << (s + 1)) | (tb & ((1ull << s) - 1ull));
+            }
+            const int bd = tl & 1;
+            if (et == 0) roleOk[1] = mbarWaitOrAbort(&dFullB[bd], (tl >> 1) & 1, &abortF);
+            namedBar(2, 128);
+            if (!roleOk[1]) {
+                ok = false;
+                break;
+            }
+            fenceAfter();
+            const uint32_t dA = tmem + laneSel + kDCol0 + bd * N;
+#pragma unroll
+            for (int pe = 0; pe < EPASS; ++pe) {
+                constexpr int COLS = N / EPASS;
+#pragma unroll
+                for (int c0 = 0; c0 < COLS; c0 += 16) {
+                    uint32_t v[16];
+                    tmemLd16(dA + pe * COLS + c0, v);
+                    tmemWaitLd();
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) {
+                        const int col = pe * COLS + c0 + e;           // output row index r in [0, 2D)
+                        const int plLocal = (EPASS == 2) ? 0 : col / D;
+                        es[plLocal * TILE + swz(pc | p.pj[col % D])] = __uint_as_float(v[e]);
+                    }
+                }
+                if (pe == EPASS - 1) {                                // accumulator drained
+                    fenceBefore();
+                    mbarArrive(&dEmptyB[bd]);
+                }
+                namedBar(2, 128);
+#pragma unroll
+                for (int pl = 0; pl < 2 / EPASS; ++pl) {
+                    float* dstPlane = ((EPASS == 2 ? pe : pl) == 0) ? re : im;
+                    const float* sb = es + pl * TILE;
+#pragma unroll
+                    for (int m = 0; m < V4; ++m) {
+                        const uint32_t q = 4u * et + 512u * m;
+                        float4 w;
+                        w.x = sb[swz(q)];
+                        w.y = sb[swz(q + 1)];
+                        w.z = sb[swz(q + 2)];
+                        w.w = sb[swz(q + 3)];
+                        __stcs(reinterpret_cast<float4*>(dstPlane + tb + tileAddr(p, q)), w);
+                    }
+                }
+                namedBar(2, 128);
+            }
+        }
+        if (!ok) {
+            if (et == 0) atomicExch(errFlag, 4);
+            abortF = 1;
+        }
+    } else if (lane == 0) {
+        // ------------------------------------------------ TMA of G, then MMAs
+        mbarExpectTx(&barG, 2 * kGFloats * 4);
+        bulkG2S(gh, gImage, kGFloats * 4, &barG);
+        bulkG2S(gl, gImage + kGFloats, kGFloats * 4, &barG);
+        bool ok = mbarWaitOrAbort(&barG, 0, &abortF);
+        if (!ok) mbarWaitOrAbort(&barG, 0, &abortF);                // once more for the copies in flight
+        const uint32_t ghA = smemAddr(gh), glA = smemAddr(gl);
+        uint32_t sq = 0, tl = 0;
+        for (uint64_t tile = blockIdx.x; tile < numTiles && ok; tile += gridDim.x, ++tl) {
+            const int bd = tl & 1;
+            if (tl >= 2 && !mbarWaitOrAbort(&dEmptyB[bd], ((tl >> 1) - 1) & 1, &abortF)) {
+                ok = false;
+                break;
+            }
+            fenceAfter();
+            const uint32_t dT = tmem + kDCol0 + bd * N;
+            for (int ch = 0; ch < NCH; ++ch, ++sq) {
+                const int b = sq & 1;
+                if (!mbarWaitOrAbort(&fullB[b], (sq >> 1) & 1, &abortF)) {
+                    ok = false;
+                    break;
+                }
+                fenceAfter();
+                const uint32_t aH = tmem + b * kStageCols, aL = aH + KC;
+#pragma unroll
+                for (int ks = 0; ks < KC / 8; ++ks) {
+                    const uint32_t sg = ch * (KC / 8) + ks;
+                    mmaTF32(dT, aH + 8 * ks, smemDesc(ghA + 256u * sg, kLBO, kSBO), idesc, (ch | ks) != 0);
+                }
+#pragma unroll
+                for (int ks = 0; ks < KC / 8; ++ks) {
+                    const uint32_t sg = ch * (KC / 8) + ks;
+                    mmaTF32(dT, aL + 8 * ks, smemDesc(ghA + 256u * sg, kLBO, kSBO), idesc, 1);
+                }
+#pragma unroll
+                for (int ks = 0; ks < KC / 8; ++ks) {
+                    const uint32_t sg = ch * (KC / 8) + ks;
+                    mmaTF32(dT, aH + 8 * ks, smemDesc(glA + 256u * sg, kLBO, kSBO), idesc, 1);
+                }
+                mmaCommit(&emptyB[b]);
+            }
+            if (!ok) break;
+            mmaCommit(&dFullB[bd]);
+        }
+        if (!ok) {
+            atomicExch(errFlag, 5);
+            abortF = 1;
+        }
+        // drain: wait (bounded) for the last accumulator to finish before TMEM is freed
+        if (tl > 0) mbarWaitOrAbort(&dFullB[(tl - 1) & 1], ((tl - 1) >> 1) & 1, &abortF);
+    }
+    fenceBefore();
+    __syncthreads();
+    fenceAfter();
+    if (warp == 8) tmemDealloc(tmem, kCols);
+}
+
 // ------------------------------------------------------------ host side
 struct DevicePlan {
     std::vector<float*> images;      // per pass: Gh image then Gl image (or nullptr)
@@ -302,10 +619,11 @@ void packKMajor(const std::vector<float>& rowMajor, int N, int K, float* out) {
         }
 }
 
-float hostTf32Hi(float x) {
+// nearest TF32 value of x (ties away from zero), as cvt.rna.tf32.f32
+float hostTf32RN(float x) {
     uint32_t u;
     std::memcpy(&u, &x, 4);
-    u &= 0xFFFFE000u;
+    if ((u & 0x7F800000u) != 0x7F800000u) u = (u + 0x1000u) & 0xFFFFE000u;   // finite values
     float y;
     std::memcpy(&y, &u, 4);
     return y;
@@ -343,7 +661,64 @@ bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* i
     return !launchFailed("applyPlanF32");
 }
 
+
+template <int KQ>
+bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, cudaStream_t st) {
+    constexpr int D = 1 << KQ;
+    constexpr int K = 2 * D, N = 2 * D;
+    constexpr int TILE = 1 << (KQ + kTileBitsC);
+    constexpr int PLS = (KQ == 6) ? 1 : 2;
+    constexpr int EPASS = (KQ == 6) ? 2 : 1;
+    const size_t smem = ((size_t)2 * N * K + 2 * (size_t)TILE * PLS + (size_t)TILE * (2 / EPASS)) * 4 + 128;
+    TC2Params<KQ> p{};
+    // I = targets + the 7 lowest other qubits (ascending)
+    uint64_t tmask = 0;
+    for (int b = 0; b < KQ; ++b) tmask |= 1ull << pass.targets[b];
+    uint64_t imask = tmask;
+    for (int q = 0, added = 0; q < n && added < kTileBitsC; ++q)
+        if (!(tmask >> q & 1ull)) {
+            imask |= 1ull << q;
+            ++added;
+        }
+    int I[64], ni = 0;
+    for (int q = 0; q < n; ++q)
+        if (imask >> q & 1ull) I[ni++] = q;
+    if (ni != KQ + kTileBitsC) return false;
+    int run = 0;
+    while (run < ni && I[run] == run) ++run;
+    p.runBits = run;
+    for (int b = 0; b < ni; ++b) p.insI[b] = I[b];
+    for (uint32_t h = 0; h < (1u << (ni - run)); ++h) {
+        uint64_t a = 0;
+        for (int i = 0; i < ni - run; ++i)
+            if (h >> i & 1u) a |= 1ull << I[run + i];
+        p.scatterHigh[h] = a;
+    }
+    int posOf[64];
+    for (int b = 0; b < ni; ++b) posOf[I[b]] = b;
+    for (int j = 0; j < D; ++j) {
+        uint32_t v = 0;
+        for (int b = 0; b < KQ; ++b)
+            if (j >> b & 1) v |= 1u << posOf[pass.targets[b]];
+        p.pj[j] = v;
+    }
+    for (int b = 0, m = 0; b < ni; ++b)
+        if (!(tmask >> I[b] & 1ull)) p.pcPos[m++] = b;
+    const uint64_t numTiles = 1ull << (n - KQ - kTileBitsC);
+    static bool configured[8] = {};
+    if (!configured[KQ]) {
+        if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "applyPlanF32"))
+            return false;
+        configured[KQ] = true;
+    }
+    const uint64_t grid = std::min<uint64_t>(numTiles, (uint64_t)numSMs());
+    kApplyTC2<KQ><<<(unsigned)grid, kThreadsTC2, smem, st>>>(re, im, img, numTiles, errFlag, p);
+    return !launchFailed("applyPlanF32");
+}
+
 bool g_tcEnabled = true;
+int g_tcVersion = 2;
 bool g_tcChecked = false;
 
 }  // namespace
@@ -371,9 +746,9 @@ void* uploadPlanTC(const FusedPlan& plan) {
                 double v;
                 if (r < D) v = (j < D) ? g.real() : -g.imag();
                 else v = (j < D) ? g.imag() : g.real();
-                const float h = hostTf32Hi((float)v);
+                const float h = hostTf32RN((float)v);
                 hi[(size_t)r * K + j] = h;
-                lo[(size_t)r * K + j] = (float)(v - (double)h);
+                lo[(size_t)r * K + j] = hostTf32RN((float)(v - (double)h));
             }
         std::vector<float> img(2 * (size_t)N * K);
         packKMajor(hi, N, K, img.data());
@@ -408,6 +783,14 @@ bool applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan,
     float* re = f32re(q);
     float* im = f32im(q);
     const int n = f32n(q);
+    if (g_tcVersion == 2) {
+        switch (k) {
+            case 4: return launchTC2<4>(re, im, n, pass, dp->images[index], dp->errFlag, st);
+            case 5: return launchTC2<5>(re, im, n, pass, dp->images[index], dp->errFlag, st);
+            case 6: return launchTC2<6>(re, im, n, pass, dp->images[index], dp->errFlag, st);
+            default: return false;
+        }
+    }
     switch (k) {
         case 4: return launchTC<4>(re, im, n, pass, dp->images[index], dp->errFlag, st);
         case 5: return launchTC<5>(re, im, n, pass, dp->images[index], dp->errFlag, st);
@@ -426,6 +809,7 @@ int tcErrorFlag(const void* devPlan) {
 }
 
 void setTensorCoresEnabled(bool on) { g_tcEnabled = on; }
+void setTensorCoreKernel(int version) { g_tcVersion = version == 1 ? 1 : 2; }
 bool tensorCoresEnabled() { return g_tcEnabled; }
 
 }  // namespace qg

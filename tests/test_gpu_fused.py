@@ -87,14 +87,58 @@ def test_tensor_core_applier(gpulib, n, kmax):
     L.destroy(q64)
 
 
+def _single_gate_plan(L, n, targets, seed):
+    rng = np.random.default_rng(seed)
+    k = len(targets)
+    z = rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k))
+    u, _ = np.linalg.qr(z)
+    p = L.lib.quest_gb300_planCreate(n, k)
+    re, im = np.ascontiguousarray(u.real.ravel()), np.ascontiguousarray(u.imag.ravel())
+    ts = (C.c_int * k)(*targets)
+    assert L.lib.quest_gb300_planAddGate(p, ts, k, re.ctypes.data_as(C.POINTER(C.c_double)),
+                                         im.ctypes.data_as(C.POINTER(C.c_double))) == 0
+    L.lib.quest_gb300_planCompile(p)
+    return p, u
+
+
+@pytest.mark.parametrize("targets", [[0, 1, 2, 3], [0, 2, 4, 6, 8], [0, 1, 2, 3, 4, 5], [1, 3, 5, 7, 9, 11],
+                                     [2, 9, 10, 14], [4, 5, 6, 7, 15, 16], [12, 13, 14, 15, 16, 17]])
+@pytest.mark.parametrize("version", [1, 2])
+def test_tensor_core_target_layouts(gpulib, targets, version):
+    """One dense gate on low, interleaved and high target sets, both tensor-core
+    kernels, against the FP32 SIMT applier (k <= 5) or the FP64 engine."""
+    L = gpulib
+    n = 18
+    rng = np.random.default_rng(3)
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    psi /= np.linalg.norm(psi)
+    q64 = L.create(n)
+    L.set_amps(q64, psi)
+    q32 = L.lib.quest_gb300_createQuregF32(n)
+    L.lib.quest_gb300_copyFromQureg(q32, q64)
+    plan, u = _single_gate_plan(L, n, targets, 11)
+    L.lib.quest_gb300_setTensorCoreKernel(version)
+    assert L.lib.quest_gb300_applyPlanF32(q32, plan) == 0
+    L.lib.quest_gb300_setTensorCoreKernel(2)
+    L.multiQubitUnitary(q64, targets, u)
+    err = C.c_double(0)
+    omf = L.lib.quest_gb300_compareF32(q32, q64, C.byref(err))
+    print(f"TC v{version} targets={targets}: 1-F={omf:.2e} max|d amp|={err.value:.2e}")
+    assert omf < 1e-9 and err.value < 1e-5
+    L.lib.quest_gb300_planDestroy(plan)
+    L.lib.quest_gb300_destroyQuregF32(q32)
+    L.destroy(q64)
+
+
 @pytest.mark.parametrize("kmax", [4, 6])
 def test_fused_30q_headline_accuracy(gpulib, kmax):
     """The 30-qubit, 20-layer circuit: fused FP32 vs plain FP64."""
     L = gpulib
     ops = W.c2_circuit(n=30, layers=20, seed=2)
     q64, q32, plan, omf, err = run_both(L, 30, kmax, ops)
-    print(f"30q: 1-F={omf:.3e} max|d amp|={err:.3e}")
-    assert omf <= 1e-6
+    norm = L.lib.quest_gb300_calcTotalProbF32(q32)
+    print(f"30q k={kmax}: 1-F={omf:.3e} max|d amp|={err:.3e} norm-1={norm - 1:.2e}")
+    assert omf <= 1e-6 and abs(norm - 1) < 1e-5
     L.lib.quest_gb300_planDestroy(plan)
     L.lib.quest_gb300_destroyQuregF32(q32)
     L.destroy(q64)
