@@ -67,8 +67,9 @@ int quest_gb300_planPassUsesTensorCores(void* plan, int i);
 /* passes on 4..6 qubits run on the tensor cores (split-TF32) unless disabled
  * here (1 = enabled, the default; 0 = FP32 SIMT applier for k <= 5) */
 void quest_gb300_setTensorCores(int enabled);
-/* tensor-core kernel variant: 2 = warp-specialised pipelined (default),
- * 1 = the single-role kernel (kept for comparison) */
+/* tensor-core kernel: 0 = chosen per pass (default: direct-load kernel when
+ * every target is >= qubit 5, pipelined staging kernel otherwise),
+ * 1 = always the direct-load kernel, 2 = always the pipelined kernel */
 void quest_gb300_setTensorCoreKernel(int version);
 double quest_gb300_calcTotalProbF32(void* qureg32);
 double quest_gb300_calcProbOfOutcomeF32(void* qureg32, int measureQubit, int outcome);

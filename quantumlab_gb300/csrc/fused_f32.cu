@@ -42,6 +42,7 @@ bool applyPassTCIndexed(QuregF32& q, const FusedPass& p, const void* devPlan, si
 void* uploadPlanTC(const FusedPlan& plan);
 void freePlanTC(void* d);
 int tcErrorFlag(const void* devPlan);
+void tcBeginPlan(void* devPlan, size_t numPasses);
 void setTensorCoresEnabled(bool on);
 void setTensorCoreKernel(int version);
 bool tensorCoresEnabled();
@@ -332,6 +333,7 @@ int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPas
     }
     const int last = std::min(total, firstPass + numPasses);
     cudaStream_t st = qg::stream();
+    if (firstPass == 0) qg::tcBeginPlan(p->device, p->passes.size());
     bool usedTC = false;
     for (int i = firstPass; i < last; ++i) {
         const qg::FusedPass& pass = p->passes[i];

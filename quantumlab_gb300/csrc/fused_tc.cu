@@ -52,7 +52,14 @@ namespace {
 
 constexpr int kTile = 128;              // groups per tile = MMA M = TMEM lanes
 constexpr int kThreadsTC = 128;         // 4 warps: one TMEM lane quarter each
-constexpr long long kSpinLimit = 1ll << 26;
+// every wait gives up after this much wall-clock time (read from %globaltimer)
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;   // 1 s
+
+__device__ __forceinline__ unsigned long long globalTimerNs() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
 
 // ------------------------------------------------------------ PTX wrappers
 __device__ __forceinline__ uint32_t smemAddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -66,7 +73,8 @@ __device__ __forceinline__ void mbarExpectTx(uint64_t* bar, uint32_t bytes) {
 // bounded wait for the phase with the given parity to complete; false on timeout
 __device__ __forceinline__ bool mbarWait(uint64_t* bar, uint32_t parity) {
     const uint32_t a = smemAddr(bar);
-    for (long long i = 0; i < kSpinLimit; ++i) {
+    const unsigned long long t0 = globalTimerNs();
+    for (;;) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
@@ -74,8 +82,8 @@ __device__ __forceinline__ bool mbarWait(uint64_t* bar, uint32_t parity) {
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
+        if (globalTimerNs() - t0 > kWaitLimitNs) return false;
     }
-    return false;
 }
 __device__ __forceinline__ void bulkG2S(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -155,6 +163,12 @@ __device__ __forceinline__ void splitTF32(float x, uint32_t& hi, uint32_t& lo) {
     lo = tf32RN(x - __uint_as_float(hi));
 }
 
+__device__ __forceinline__ double warpSumD(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
 // ------------------------------------------------------------ the kernel
 // TMEM columns: [0, K) Xh, [K, 2K) Xl, [2K, 2K+N) Out, with K = N = 2D.
 template <int KQ>
@@ -166,7 +180,8 @@ struct TCParams {
 template <int KQ>
 __global__ void __launch_bounds__(kThreadsTC) kApplyTC(float* __restrict__ re, float* __restrict__ im,
                                                        const float* __restrict__ gImage, uint64_t numTiles,
-                                                       int* __restrict__ errFlag,
+                                                       int* __restrict__ errFlag, double* __restrict__ norms,
+                                                       const double* __restrict__ prevNorms,
                                                        const __grid_constant__ TCParams<KQ> p) {
     constexpr int D = 1 << KQ;
     constexpr int K = 2 * D;                    // GEMM K = N
@@ -215,6 +230,9 @@ __global__ void __launch_bounds__(kThreadsTC) kApplyTC(float* __restrict__ re, f
     const uint32_t ghAddr = smemAddr(gh), glAddr = smemAddr(gl);
 
     const bool aborted = abortFlag != 0;                   // read after the barrier above: uniform
+    float scale = 1.f;
+    if (prevNorms && prevNorms[1] > 0.0) scale = (float)sqrt(prevNorms[0] / prevNorms[1]);
+    double normIn = 0.0, normOut = 0.0;
     for (uint64_t tile = blockIdx.x; tile < numTiles && !aborted; tile += gridDim.x) {
         // ---- load this lane's group, split, write Xh / Xl rows to TMEM
         uint64_t base = tile * kTile + (uint64_t)threadIdx.x;
@@ -234,6 +252,13 @@ __global__ void __launch_bounds__(kThreadsTC) kApplyTC(float* __restrict__ re, f
                 const int j = h + e;
                 x[e] = (j < D) ? re[base + p.off[j]] : im[base + p.off[j - D]];
             }
+            float nrm = 0.f;
+#pragma unroll
+            for (int e = 0; e < CH; ++e) {
+                x[e] *= scale;
+                nrm = fmaf(x[e], x[e], nrm);
+            }
+            normIn += (double)nrm;
 #pragma unroll
             for (int c0 = 0; c0 < CH; c0 += 16) {
                 uint32_t hi[16], lo[16];
@@ -277,6 +302,7 @@ __global__ void __launch_bounds__(kThreadsTC) kApplyTC(float* __restrict__ re, f
             break;
         }
         fenceAfter();
+        float nrmOut = 0.f;
 #pragma unroll
         for (int c0 = 0; c0 < N; c0 += 16) {
             uint32_t v[16];
@@ -285,13 +311,22 @@ __global__ void __launch_bounds__(kThreadsTC) kApplyTC(float* __restrict__ re, f
 #pragma unroll
             for (int e = 0; e < 16; ++e) {
                 const int r = c0 + e;
-                if (r < D) re[base + p.off[r]] = __uint_as_float(v[e]);
-                else im[base + p.off[r - D]] = __uint_as_float(v[e]);
+                const float y = __uint_as_float(v[e]);
+                nrmOut = fmaf(y, y, nrmOut);
+                if (r < D) re[base + p.off[r]] = y;
+                else im[base + p.off[r - D]] = y;
             }
         }
+        normOut += (double)nrmOut;
         fenceBefore();
         __syncthreads();
         fenceAfter();
+    }
+    normIn = warpSumD(normIn);
+    normOut = warpSumD(normOut);
+    if (lane == 0 && norms) {
+        atomicAdd(norms, normIn);
+        atomicAdd(norms + 1, normOut);
     }
     __syncthreads();
     if (warp == 0) tmemDealloc(tbase, kCols);
@@ -338,7 +373,8 @@ __device__ __forceinline__ void mbarArrive(uint64_t* bar) {
 // bounded wait that also gives up when another role has aborted
 __device__ __forceinline__ bool mbarWaitOrAbort(uint64_t* bar, uint32_t parity, volatile int* abortF) {
     const uint32_t a = smemAddr(bar);
-    for (long long i = 0; i < kSpinLimit; ++i) {
+    const unsigned long long t0 = globalTimerNs();
+    for (unsigned i = 1;; ++i) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
@@ -346,9 +382,8 @@ __device__ __forceinline__ bool mbarWaitOrAbort(uint64_t* bar, uint32_t parity, 
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
-        if ((i & 255) == 255 && *abortF) return false;
+        if ((i & 15) == 0 && (*abortF || globalTimerNs() - t0 > kWaitLimitNs)) return false;
     }
-    return false;
 }
 
 template <int KQ>
@@ -359,7 +394,8 @@ __device__ __forceinline__ uint64_t tileAddr(const TC2Params<KQ>& p, uint32_t q)
 template <int KQ>
 __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ re, float* __restrict__ im,
                                                             const float* __restrict__ gImage, uint64_t numTiles,
-                                                            int* __restrict__ errFlag,
+                                                            int* __restrict__ errFlag, double* __restrict__ norms,
+                                                            const double* __restrict__ prevNorms,
                                                             const __grid_constant__ TC2Params<KQ> p) {
     constexpr int D = 1 << KQ;
     constexpr int K = 2 * D, N = 2 * D;
@@ -416,66 +452,85 @@ __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ 
         for (int b = 0; b < kTileBitsC; ++b)
             if (lt >> b & 1) pc |= 1u << p.pcPos[b];
         const uint32_t laneSel = (uint32_t)(32 * warp) << 16;
-        uint32_t sq = 0;
-        bool ok = true;
-        for (uint64_t tile = blockIdx.x; tile < numTiles && ok; tile += gridDim.x) {
+        // this CTA's chunks, in order: chunk s = (tile blockIdx.x + (s / NCH) * gridDim.x, K stage s % NCH)
+        const uint32_t nMy = blockIdx.x < numTiles ? (uint32_t)((numTiles - 1 - blockIdx.x) / gridDim.x + 1) * NCH : 0u;
+        // norm correction for the drift of the previous tensor-core pass
+        float scale = 1.f;
+        if (prevNorms && prevNorms[1] > 0.0) scale = (float)sqrt(prevNorms[0] / prevNorms[1]);
+        double normIn = 0.0;
+        float4 v[PLS][V4];
+        auto issue = [&](uint32_t sc) {
+            const uint64_t tile = blockIdx.x + (uint64_t)(sc / NCH) * gridDim.x;
+            const int ch = sc % NCH;
             uint64_t tb = tile;
 #pragma unroll
             for (int b = 0; b < KQ + kTileBitsC; ++b) {
-                const int s = p.insI[b];
-                tb = ((tb >> s) << (s + 1)) | (tb & ((1ull << s) - 1ull));
+                const int sh = p.insI[b];
+                tb = ((tb >> sh) << (sh + 1)) | (tb & ((1ull << sh) - 1ull));
             }
-            for (int ch = 0; ch < NCH; ++ch, ++sq) {
-                const int b = sq & 1;
-                const uint32_t u = sq >> 1;
-                if (lt == 0) roleOk[0] = (u == 0) || mbarWaitOrAbort(&emptyB[b], (u - 1) & 1, &abortF);
-                namedBar(1, 128);
-                if (!roleOk[0]) {
-                    ok = false;
-                    break;
-                }
-                float* xb = xs + b * kXFloats;
 #pragma unroll
-                for (int pl = 0; pl < PLS; ++pl) {
-                    const float* src = ((NCH == 2 ? ch : pl) == 0) ? re : im;
-                    float4 v[V4];
+            for (int pl = 0; pl < PLS; ++pl) {
+                const float* src = ((NCH == 2 ? ch : pl) == 0) ? re : im;
 #pragma unroll
-                    for (int m = 0; m < V4; ++m)
-                        v[m] = __ldcs(reinterpret_cast<const float4*>(src + tb + tileAddr(p, 4u * lt + 512u * m)));
-                    float* dst = xb + pl * TILE;
-#pragma unroll
-                    for (int m = 0; m < V4; ++m) {
-                        const uint32_t q = 4u * lt + 512u * m;
-                        dst[swz(q)] = v[m].x;
-                        dst[swz(q + 1)] = v[m].y;
-                        dst[swz(q + 2)] = v[m].z;
-                        dst[swz(q + 3)] = v[m].w;
-                    }
-                }
-                namedBar(1, 128);
-                const uint32_t aH = tmem + laneSel + b * kStageCols;
-#pragma unroll
-                for (int c0 = 0; c0 < KC; c0 += 16) {
-                    uint32_t hi[16], lo[16];
-#pragma unroll
-                    for (int e = 0; e < 16; ++e) {
-                        const int kl = c0 + e;
-                        const int pl = (NCH == 2) ? 0 : kl / D;
-                        const int j = (NCH == 2) ? kl : kl % D;
-                        splitTF32(xb[pl * TILE + swz(pc | p.pj[j])], hi[e], lo[e]);
-                    }
-                    tmemSt16(aH + c0, hi);
-                    tmemSt16(aH + KC + c0, lo);
-                }
-                tmemWaitSt();
-                fenceBefore();
-                mbarArrive(&fullB[b]);
+                for (int m = 0; m < V4; ++m)
+                    v[pl][m] = __ldcs(reinterpret_cast<const float4*>(src + tb + tileAddr(p, 4u * lt + 512u * m)));
             }
+        };
+        if (nMy) issue(0);
+        bool ok = true;
+        for (uint32_t sq = 0; sq < nMy; ++sq) {
+            const int b = sq & 1;
+            const uint32_t u = sq >> 1;
+            if (lt == 0) roleOk[0] = (u == 0) || mbarWaitOrAbort(&emptyB[b], (u - 1) & 1, &abortF);
+            namedBar(1, 128);
+            if (!roleOk[0]) {
+                ok = false;
+                break;
+            }
+            float* xb = xs + b * kXFloats;
+            float nrm = 0.f;
+#pragma unroll
+            for (int pl = 0; pl < PLS; ++pl) {
+                float* dst = xb + pl * TILE;
+#pragma unroll
+                for (int m = 0; m < V4; ++m) {
+                    const uint32_t q = 4u * lt + 512u * m;
+                    const float x0 = v[pl][m].x * scale, x1 = v[pl][m].y * scale;
+                    const float x2 = v[pl][m].z * scale, x3 = v[pl][m].w * scale;
+                    nrm = fmaf(x0, x0, fmaf(x1, x1, fmaf(x2, x2, fmaf(x3, x3, nrm))));
+                    dst[swz(q)] = x0;
+                    dst[swz(q + 1)] = x1;
+                    dst[swz(q + 2)] = x2;
+                    dst[swz(q + 3)] = x3;
+                }
+            }
+            normIn += (double)nrm;
+            namedBar(1, 128);
+            if (sq + 1 < nMy) issue(sq + 1);                 // next chunk's loads fly during the split below
+            const uint32_t aH = tmem + laneSel + b * kStageCols;
+#pragma unroll
+            for (int c0 = 0; c0 < KC; c0 += 16) {
+                uint32_t hi[16], lo[16];
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    const int kl = c0 + e;
+                    const int pl = (NCH == 2) ? 0 : kl / D;
+                    const int j = (NCH == 2) ? kl : kl % D;
+                    splitTF32(xb[pl * TILE + swz(pc | p.pj[j])], hi[e], lo[e]);
+                }
+                tmemSt16(aH + c0, hi);
+                tmemSt16(aH + KC + c0, lo);
+            }
+            tmemWaitSt();
+            fenceBefore();
+            mbarArrive(&fullB[b]);
         }
         if (!ok) {
             if (lt == 0) atomicExch(errFlag, 3);
             abortF = 1;
         }
+        normIn = warpSumD(normIn);
+        if (lane == 0 && norms) atomicAdd(norms, normIn);
     } else if (warp < 8) {
         // ------------------------------------------------ epilogue
         const int et = threadIdx.x - 128;
@@ -487,6 +542,7 @@ __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ 
         const uint32_t laneSel = (uint32_t)(32 * ew) << 16;
         uint32_t tl = 0;
         bool ok = true;
+        double normOut = 0.0;
         for (uint64_t tile = blockIdx.x; tile < numTiles && ok; tile += gridDim.x, ++tl) {
             uint64_t tb = tile;
 #pragma unroll
@@ -503,6 +559,7 @@ __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ 
             }
             fenceAfter();
             const uint32_t dA = tmem + laneSel + kDCol0 + bd * N;
+            float nrmTile = 0.f;
 #pragma unroll
             for (int pe = 0; pe < EPASS; ++pe) {
                 constexpr int COLS = N / EPASS;
@@ -515,7 +572,9 @@ __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ 
                     for (int e = 0; e < 16; ++e) {
                         const int col = pe * COLS + c0 + e;           // output row index r in [0, 2D)
                         const int plLocal = (EPASS == 2) ? 0 : col / D;
-                        es[plLocal * TILE + swz(pc | p.pj[col % D])] = __uint_as_float(v[e]);
+                        const float y = __uint_as_float(v[e]);
+                        nrmTile = fmaf(y, y, nrmTile);
+                        es[plLocal * TILE + swz(pc | p.pj[col % D])] = y;
                     }
                 }
                 if (pe == EPASS - 1) {                                // accumulator drained
@@ -540,11 +599,14 @@ __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ 
                 }
                 namedBar(2, 128);
             }
+            normOut += (double)nrmTile;
         }
         if (!ok) {
             if (et == 0) atomicExch(errFlag, 4);
             abortF = 1;
         }
+        normOut = warpSumD(normOut);
+        if (lane == 0 && norms) atomicAdd(norms + 1, normOut);
     } else if (lane == 0) {
         // ------------------------------------------------ TMA of G, then MMAs
         mbarExpectTx(&barG, 2 * kGFloats * 4);
@@ -607,6 +669,12 @@ __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ 
 struct DevicePlan {
     std::vector<float*> images;      // per pass: Gh image then Gl image (or nullptr)
     int* errFlag = nullptr;
+    // per pass: (sum |x|^2 of its scaled input, sum |y|^2 of its output) in
+    // FP64, accumulated by the tensor-core kernels.  The next tensor-core
+    // pass rescales its input by sqrt(in / out) of the previous one, which
+    // removes the slow norm loss of the tensor cores' FP32 accumulation.
+    double* norms = nullptr;
+    int lastTC = -1;
 };
 
 // Canonical no-swizzle K-major image of an N x K operand (rows r, K index j):
@@ -630,7 +698,8 @@ float hostTf32RN(float x) {
 }
 
 template <int KQ>
-bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, cudaStream_t st) {
+bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, double* norms,
+              const double* prevNorms, cudaStream_t st) {
     constexpr int D = 1 << KQ;
     constexpr int K = 2 * D;
     const size_t smem = 2 * (size_t)K * K * 4;
@@ -657,13 +726,14 @@ bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* i
         configured[KQ] = true;
     }
     const uint64_t grid = std::min<uint64_t>(numTiles, (uint64_t)perSM * numSMs());
-    kApplyTC<KQ><<<(unsigned)grid, kThreadsTC, smemReq, st>>>(re, im, img, numTiles, errFlag, p);
+    kApplyTC<KQ><<<(unsigned)grid, kThreadsTC, smemReq, st>>>(re, im, img, numTiles, errFlag, norms, prevNorms, p);
     return !launchFailed("applyPlanF32");
 }
 
 
 template <int KQ>
-bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, cudaStream_t st) {
+bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, double* norms,
+               const double* prevNorms, cudaStream_t st) {
     constexpr int D = 1 << KQ;
     constexpr int K = 2 * D, N = 2 * D;
     constexpr int TILE = 1 << (KQ + kTileBitsC);
@@ -713,12 +783,12 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
         configured[KQ] = true;
     }
     const uint64_t grid = std::min<uint64_t>(numTiles, (uint64_t)numSMs());
-    kApplyTC2<KQ><<<(unsigned)grid, kThreadsTC2, smem, st>>>(re, im, img, numTiles, errFlag, p);
+    kApplyTC2<KQ><<<(unsigned)grid, kThreadsTC2, smem, st>>>(re, im, img, numTiles, errFlag, norms, prevNorms, p);
     return !launchFailed("applyPlanF32");
 }
 
 bool g_tcEnabled = true;
-int g_tcVersion = 2;
+int g_tcVersion = 0;      // 0: per pass by target layout, 1 / 2: force one kernel
 bool g_tcChecked = false;
 
 }  // namespace
@@ -731,6 +801,10 @@ void* uploadPlanTC(const FusedPlan& plan) {
         return nullptr;
     }
     cudaMemsetAsync(dp->errFlag, 0, sizeof(int), stream());
+    if (cudaMalloc(&dp->norms, 2 * std::max<size_t>(1, plan.passes.size()) * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        dp->norms = nullptr;
+    }
     for (const FusedPass& pass : plan.passes) {
         const int k = (int)pass.targets.size();
         if (k < 4 || k > 6 || plan.numQubits < k + 7) {
@@ -772,31 +846,52 @@ void freePlanTC(void* h) {
     for (float* f : dp->images)
         if (f) cudaFree(f);
     if (dp->errFlag) cudaFree(dp->errFlag);
+    if (dp->norms) cudaFree(dp->norms);
     delete dp;
 }
 
-// explicit entry used by the FP32 engine with the pass index
+// start of a plan application: clear the norm accumulators
+void tcBeginPlan(void* devPlan, size_t numPasses) {
+    DevicePlan* dp = reinterpret_cast<DevicePlan*>(devPlan);
+    if (!dp) return;
+    dp->lastTC = -1;
+    if (dp->norms) cudaMemsetAsync(dp->norms, 0, 2 * std::max<size_t>(1, numPasses) * sizeof(double), stream());
+}
+
+// explicit entry used by the FP32 engine with the pass index.  Passes whose
+// targets are all at or above qubit 5 run on the direct-load kernel (each
+// lane's group is then 32 consecutive amplitudes of a warp line); passes with
+// a low target run on the pipelined kernel, whose shared-memory staging keeps
+// them coalesced.
 bool applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, size_t index, cudaStream_t st) {
-    const DevicePlan* dp = reinterpret_cast<const DevicePlan*>(devPlan);
+    DevicePlan* dp = const_cast<DevicePlan*>(reinterpret_cast<const DevicePlan*>(devPlan));
     if (!dp || !g_tcEnabled || index >= dp->images.size() || !dp->images[index]) return false;
     const int k = (int)pass.targets.size();
     float* re = f32re(q);
     float* im = f32im(q);
     const int n = f32n(q);
-    if (g_tcVersion == 2) {
+    double* norms = dp->norms ? dp->norms + 2 * index : nullptr;
+    const double* prev = (dp->norms && dp->lastTC >= 0) ? dp->norms + 2 * dp->lastTC : nullptr;
+    int version = g_tcVersion;
+    if (version == 0) version = pass.targets[0] >= 5 ? 1 : 2;
+    bool ok = false;
+    if (version == 2) {
         switch (k) {
-            case 4: return launchTC2<4>(re, im, n, pass, dp->images[index], dp->errFlag, st);
-            case 5: return launchTC2<5>(re, im, n, pass, dp->images[index], dp->errFlag, st);
-            case 6: return launchTC2<6>(re, im, n, pass, dp->images[index], dp->errFlag, st);
+            case 4: ok = launchTC2<4>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
+            case 5: ok = launchTC2<5>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
+            case 6: ok = launchTC2<6>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
+            default: return false;
+        }
+    } else {
+        switch (k) {
+            case 4: ok = launchTC<4>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
+            case 5: ok = launchTC<5>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
+            case 6: ok = launchTC<6>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
             default: return false;
         }
     }
-    switch (k) {
-        case 4: return launchTC<4>(re, im, n, pass, dp->images[index], dp->errFlag, st);
-        case 5: return launchTC<5>(re, im, n, pass, dp->images[index], dp->errFlag, st);
-        case 6: return launchTC<6>(re, im, n, pass, dp->images[index], dp->errFlag, st);
-        default: return false;
-    }
+    if (ok) dp->lastTC = (int)index;
+    return ok;
 }
 
 int tcErrorFlag(const void* devPlan) {
@@ -809,7 +904,7 @@ int tcErrorFlag(const void* devPlan) {
 }
 
 void setTensorCoresEnabled(bool on) { g_tcEnabled = on; }
-void setTensorCoreKernel(int version) { g_tcVersion = version == 1 ? 1 : 2; }
+void setTensorCoreKernel(int version) { g_tcVersion = (version == 1 || version == 2) ? version : 0; }
 bool tensorCoresEnabled() { return g_tcEnabled; }
 
 }  // namespace qg
