@@ -45,6 +45,16 @@ int quest_gb300_planNumGates(void* plan);
 /* Copy pass i (targets ascending, FP64 matrix); returns k or -1. */
 int quest_gb300_planPass(void* plan, int i, int* targets, double* re, double* im);
 
+/* ---- autotuner -------------------------------------------------------------
+ * Per-pass cost table (ms) by width k and target layout (a target below qubit
+ * 5 or not) for registers of numQubits qubits, measured on a scratch FP32
+ * register and cached as JSON ($QUEST_GB300_TUNE_CACHE, default
+ * ~/.cache/quest_gb300_tune.json).  planCompileTuned compiles the plan at
+ * every width in [minK, maxK] and keeps the fastest predicted one.          */
+int quest_gb300_autotune(int numQubits);
+double quest_gb300_planPredictMs(void* plan);
+int quest_gb300_planCompileTuned(void* plan, int minK, int maxK);
+
 /* ---- FP32 registers of the fused engine ----------------------------------
  * A state vector of 2^numQubits FP32 complex amplitudes (SoA) on the
  * device.  Reductions accumulate in FP64.                                    */
@@ -67,8 +77,8 @@ int quest_gb300_planPassUsesTensorCores(void* plan, int i);
 /* passes on 4..6 qubits run on the tensor cores (split-TF32) unless disabled
  * here (1 = enabled, the default; 0 = FP32 SIMT applier for k <= 5) */
 void quest_gb300_setTensorCores(int enabled);
-/* tensor-core kernel: 0 = chosen per pass (default: direct-load kernel when
- * every target is >= qubit 5, pipelined staging kernel otherwise),
+/* tensor-core kernel: 0 = chosen per pass (default: direct-load kernel for
+ * 4-qubit passes with every target >= qubit 5, pipelined kernel otherwise),
  * 1 = always the direct-load kernel, 2 = always the pipelined kernel */
 void quest_gb300_setTensorCoreKernel(int version);
 double quest_gb300_calcTotalProbF32(void* qureg32);

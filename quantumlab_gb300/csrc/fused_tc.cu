@@ -178,7 +178,7 @@ struct TCParams {
 };
 
 template <int KQ>
-__global__ void __launch_bounds__(kThreadsTC) kApplyTC(float* __restrict__ re, float* __restrict__ im,
+__global__ void __launch_bounds__(kThreadsTC, (KQ == 4 ? 4 : 1)) kApplyTC(float* __restrict__ re, float* __restrict__ im,
                                                        const float* __restrict__ gImage, uint64_t numTiles,
                                                        int* __restrict__ errFlag, double* __restrict__ norms,
                                                        const double* __restrict__ prevNorms,
@@ -858,11 +858,12 @@ void tcBeginPlan(void* devPlan, size_t numPasses) {
     if (dp->norms) cudaMemsetAsync(dp->norms, 0, 2 * std::max<size_t>(1, numPasses) * sizeof(double), stream());
 }
 
-// explicit entry used by the FP32 engine with the pass index.  Passes whose
-// targets are all at or above qubit 5 run on the direct-load kernel (each
-// lane's group is then 32 consecutive amplitudes of a warp line); passes with
-// a low target run on the pipelined kernel, whose shared-memory staging keeps
-// them coalesced.
+// explicit entry used by the FP32 engine with the pass index.  Kernel choice
+// (measured at 30 qubits): 5- and 6-qubit passes always run on the pipelined
+// kernel; 4-qubit passes whose targets are all at or above qubit 5 run on the
+// direct-load kernel (four CTAs per SM; each lane's group is then part of a
+// coalesced warp line), the others on the pipelined kernel, whose
+// shared-memory staging keeps them coalesced.
 bool applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, size_t index, cudaStream_t st) {
     DevicePlan* dp = const_cast<DevicePlan*>(reinterpret_cast<const DevicePlan*>(devPlan));
     if (!dp || !g_tcEnabled || index >= dp->images.size() || !dp->images[index]) return false;
@@ -873,7 +874,7 @@ bool applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan,
     double* norms = dp->norms ? dp->norms + 2 * index : nullptr;
     const double* prev = (dp->norms && dp->lastTC >= 0) ? dp->norms + 2 * dp->lastTC : nullptr;
     int version = g_tcVersion;
-    if (version == 0) version = pass.targets[0] >= 5 ? 1 : 2;
+    if (version == 0) version = (k == 4 && pass.targets[0] >= 5) ? 1 : 2;
     bool ok = false;
     if (version == 2) {
         switch (k) {

@@ -182,6 +182,9 @@ SIGNATURES = {
     "quest_gb300_planCompile": (_I, [C.c_void_p]),
     "quest_gb300_planNumGates": (_I, [C.c_void_p]),
     "quest_gb300_planPass": (_I, [C.c_void_p, _I, _P(_I), _P(qreal), _P(qreal)]),
+    "quest_gb300_autotune": (_I, [_I]),
+    "quest_gb300_planPredictMs": (qreal, [C.c_void_p]),
+    "quest_gb300_planCompileTuned": (_I, [C.c_void_p, _I, _I]),
     "quest_gb300_createQuregF32": (C.c_void_p, [_I]),
     "quest_gb300_destroyQuregF32": (None, [C.c_void_p]),
     "quest_gb300_initZeroStateF32": (None, [C.c_void_p]),

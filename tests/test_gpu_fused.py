@@ -142,3 +142,25 @@ def test_fused_30q_headline_accuracy(gpulib, kmax):
     L.lib.quest_gb300_planDestroy(plan)
     L.lib.quest_gb300_destroyQuregF32(q32)
     L.destroy(q64)
+
+
+def test_autotuned_plan_matches_and_predicts(gpulib, tmp_path, monkeypatch):
+    """planCompileTuned picks a width in [4, 6], the tuned plan is still the
+    circuit, and its predicted time is positive."""
+    L = gpulib
+    monkeypatch.setenv("QUEST_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+    n = 16
+    ops = W.c2_circuit(n=n, layers=4, seed=77)
+    p = L.plan(n, 4, ops)
+    k = L.lib.quest_gb300_planCompileTuned(p, 4, 6)
+    assert 4 <= k <= 6
+    assert L.lib.quest_gb300_planPredictMs(p) > 0
+    q32 = L.lib.quest_gb300_createQuregF32(n)
+    assert L.lib.quest_gb300_applyPlanF32(q32, p) == 0
+    q64 = L.create(n)
+    W.run_ops(L, q64, ops)
+    omf = L.lib.quest_gb300_compareF32(q32, q64, None)
+    assert omf < 1e-9
+    L.lib.quest_gb300_planDestroy(p)
+    L.lib.quest_gb300_destroyQuregF32(q32)
+    L.destroy(q64)
