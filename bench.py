@@ -185,7 +185,9 @@ def run_gpu(args, rank, world):
     # dominant kernel: group passes by applier and k
     groups = {}
     for i in range(npass):
-        key = (f"kApplyTC<{kk[i]}> (tcgen05 split-TF32)" if tc[i] else f"kApplySimt<{kk[i]}> (FP32 FFMA)")
+        key = {0: f"kApplySimt<{kk[i]}> (FP32 FFMA)", 1: f"kApplyTC<{kk[i]}> (tcgen05 split-TF32, direct loads)",
+               2: f"kApplyTC2<{kk[i]},2> (tcgen05 split-TF32, pipelined)",
+               3: f"kApplyTC2<{kk[i]},1> (tcgen05 split-TF32, pipelined)"}[tc[i]]
         g = groups.setdefault(key, [0, 0.0])
         g[0] += 1
         g[1] += pass_ms[i]
@@ -400,7 +402,7 @@ def main():
     ap.add_argument("--layers", type=int, default=20)
     ap.add_argument("--cpu-sample-ops", type=int, default=60)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--fusion", type=int, default=5, help="max qubits per fused pass (1..6)")
+    ap.add_argument("--fusion", type=int, default=6, help="max qubits per fused pass (1..6)")
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--no-swap", action="store_true")
     ap.add_argument("--swap-vectors", type=int, default=4096)

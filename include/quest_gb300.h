@@ -72,14 +72,17 @@ void quest_gb300_copyToQureg(void* qureg32, Qureg destination);
 int quest_gb300_applyPlanF32(void* qureg32, void* plan);
 /* apply passes [firstPass, firstPass + numPasses) only (timing, stepping) */
 int quest_gb300_applyPlanF32Range(void* qureg32, void* plan, int firstPass, int numPasses);
-/* 1 if pass i runs on the tensor cores, 0 if on the SIMT applier, -1 if invalid */
+/* applier of pass i: 0 = SIMT, 1 = direct-load tensor-core kernel, 2 or 3 =
+ * pipelined tensor-core kernel (two / one loader groups); -1 if invalid */
 int quest_gb300_planPassUsesTensorCores(void* plan, int i);
 /* passes on 4..6 qubits run on the tensor cores (split-TF32) unless disabled
  * here (1 = enabled, the default; 0 = FP32 SIMT applier for k <= 5) */
 void quest_gb300_setTensorCores(int enabled);
-/* tensor-core kernel: 0 = chosen per pass (default: direct-load kernel for
- * 4-qubit passes with every target >= qubit 5, pipelined kernel otherwise),
- * 1 = always the direct-load kernel, 2 = always the pipelined kernel */
+/* tensor-core kernel: 0 = chosen per pass (default: 4-qubit passes with every
+ * target >= qubit 5 on the SIMT applier, every other 4..6-qubit pass on the
+ * pipelined kernel with two loader groups), 1 = always the direct-load
+ * kernel, 2 = always the pipelined kernel with two loader groups, 3 = always
+ * the pipelined kernel with one loader group */
 void quest_gb300_setTensorCoreKernel(int version);
 double quest_gb300_calcTotalProbF32(void* qureg32);
 double quest_gb300_calcProbOfOutcomeF32(void* qureg32, int measureQubit, int outcome);

@@ -37,8 +37,8 @@ struct QuregF32 {
     }
 };
 
-// tensor-core applier (fused_tc.cu); returns false if it does not take the pass
-bool applyPassTCIndexed(QuregF32& q, const FusedPass& p, const void* devPlan, size_t index, cudaStream_t st);
+// tensor-core applier (fused_tc.cu): 1 applied, 0 not a tensor-core pass, -1 launch failed
+int applyPassTCIndexed(QuregF32& q, const FusedPass& p, const void* devPlan, size_t index, cudaStream_t st);
 void* uploadPlanTC(const FusedPlan& plan);
 void freePlanTC(void* d);
 int tcErrorFlag(const void* devPlan);
@@ -46,6 +46,7 @@ void tcBeginPlan(void* devPlan, size_t numPasses);
 void setTensorCoresEnabled(bool on);
 void setTensorCoreKernel(int version);
 bool tensorCoresEnabled();
+int tcKernelFor(const FusedPass& pass, int n);
 float* f32re(QuregF32& q) { return q.re; }
 float* f32im(QuregF32& q) { return q.im; }
 int f32n(const QuregF32& q) { return q.n; }
@@ -337,7 +338,9 @@ int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPas
     bool usedTC = false;
     for (int i = firstPass; i < last; ++i) {
         const qg::FusedPass& pass = p->passes[i];
-        if (qg::applyPassTCIndexed(*q, pass, p->device, (size_t)i, st)) {
+        const int tc = qg::applyPassTCIndexed(*q, pass, p->device, (size_t)i, st);
+        if (tc < 0) return -1;
+        if (tc > 0) {
             usedTC = true;
             continue;
         }
@@ -349,9 +352,15 @@ int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPas
     if (usedTC && qg::g_checkTC && last == total) {
         const int e = qg::tcErrorFlag(p->device);
         if (e) {
-            invalidQuESTInputError(e == 1 ? "tensor-core applier: operand staging timed out"
-                                          : "tensor-core applier: MMA completion timed out",
-                                   "applyPlanF32");
+            // codes: 1 copy of G (direct-load kernel), 2 its MMAs; pipelined
+            // kernel: 3 loaders waiting for a free stage, 4 epilogue waiting for
+            // an accumulator, 5 MMA issuer waiting for operands or a free accumulator
+            static const char* const what[] = {
+                "", "tensor-core applier: operand staging timed out", "tensor-core applier: MMA completion timed out",
+                "tensor-core applier: loaders timed out waiting for a free operand stage",
+                "tensor-core applier: epilogue timed out waiting for an accumulator",
+                "tensor-core applier: MMA issue timed out waiting for operands or an accumulator"};
+            invalidQuESTInputError(e >= 1 && e <= 5 ? what[e] : "tensor-core applier: timed out", "applyPlanF32");
             return -1;
         }
     }
@@ -360,12 +369,11 @@ int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPas
 
 int quest_gb300_applyPlanF32(void* h, void* plan) { return quest_gb300_applyPlanF32Range(h, plan, 0, 1 << 30); }
 
-/* 1 if pass i of the plan runs on the tensor cores for registers of its size */
+/* applier of pass i of the plan for registers of its size (tcKernelFor) */
 int quest_gb300_planPassUsesTensorCores(void* plan, int i) {
     qg::FusedPlan* p = reinterpret_cast<qg::FusedPlan*>(plan);
     if (!p || !p->compiled || i < 0 || i >= (int)p->passes.size()) return -1;
-    const int k = (int)p->passes[i].targets.size();
-    return (qg::tensorCoresEnabled() && k >= 4 && k <= 6 && p->numQubits >= k + 7) ? 1 : 0;
+    return qg::tcKernelFor(p->passes[i], p->numQubits);
 }
 
 void quest_gb300_setTensorCores(int enabled) { qg::setTensorCoresEnabled(enabled != 0); }

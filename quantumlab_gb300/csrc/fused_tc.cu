@@ -333,31 +333,38 @@ __global__ void __launch_bounds__(kThreadsTC, (KQ == 4 ? 4 : 1)) kApplyTC(float*
 }
 
 // ------------------------------------------------------------ pipelined kernel
-// Warp-specialised version used for every tensor-core pass:
-//   warps 0-3  loaders:  global -> shared (coalesced 16-byte loads of the
-//              whole tile, stored with a 4-byte XOR swizzle), then each thread
-//              reads its tile column, splits it and writes Xh/Xl to a TMEM
-//              stage with tcgen05.st;
-//   warp 8     TMEM allocation, the one-time TMA bulk copy of Gh/Gl, and the
-//              MMA issue loop (one thread);
-//   warps 4-7  epilogue: tcgen05.ld of a finished accumulator, swizzled
-//              shared-memory staging, coalesced 16-byte stores.
+// Warp-specialised kernel used for every tensor-core pass by default:
+//   LG loader groups of 4 warps: global -> registers (coalesced 16-byte
+//              loads of a whole chunk, issued one chunk ahead), registers ->
+//              shared memory (XOR swizzle), then each thread reads its tile
+//              column, splits it and writes Xh/Xl to the group's TMEM stage
+//              with tcgen05.st.  With LG = 2 the groups take alternate chunks,
+//              so two chunks of loads are in flight per SM;
+//   4 epilogue warps: tcgen05.ld of a finished accumulator, scale, swizzled
+//              shared-memory staging, coalesced 16-byte stores;
+//   1 warp:    TMEM allocation, the one-time TMA bulk copy of Gh/Gl, and the
+//              MMA issue loop (one thread).
 // TMEM holds two operand stages and two accumulators, so loading tile t+1,
 // multiplying tile t and storing tile t-1 overlap.  A tile is 128 groups
 // over the qubit set I = targets + the 7 lowest other qubits; I always
 // contains qubits [0, r) with r >= 7, so the tile is made of contiguous runs
 // of >= 128 amplitudes and every global access is coalesced whatever the
-// targets are.  The swizzle p ^ ((p >> 5) & 31) makes both the row-order
-// writes and the column-order reads of the staging buffers conflict-free.
-// For k = 6 a tile's K = 128 is split into two stages (real rows, imaginary
-// rows) so the operand stages and both accumulators fit the 512 columns.
+// targets are.  The swizzle swz(p) = p ^ ((p >> 5) & 31) makes the row-order
+// writes conflict-free and the column-order reads conflict-free or 2-way.
+// It is linear over disjoint bit sets (swz(a | b) = swz(a) ^ swz(b)), so a
+// column address is swz(column bits) ^ swz(matrix-index bits): one XOR with
+// a per-pass constant.  For k = 6 a tile's K = 128 is split into two stages
+// (real rows, imaginary rows) so the operand stages and both accumulators
+// fit the 512 TMEM columns.
+// Instruction budget per amplitude (the kernel is issue-bound, not DRAM-
+// bound, when these loops are loose): load 1/4, store to staging 1, norm 1,
+// column read 2, split 2, epilogue scale + norm 2, staging 2, store 1/4.
 constexpr int kTileBitsC = 7;
-constexpr int kThreadsTC2 = 9 * 32;
 
 template <int KQ>
 struct TC2Params {
     uint64_t scatterHigh[1 << KQ];   // address bits of the tile-index bits above the low run
-    uint32_t pj[1 << KQ];            // tile-index bits of matrix index j
+    uint32_t sj[1 << KQ];            // swz(tile-index bits of matrix index j)
     int pcPos[kTileBitsC];           // tile-index positions of the column bits
     int insI[KQ + kTileBitsC];       // ascending qubits of I
     int runBits;                     // I contains qubits [0, runBits)
@@ -386,17 +393,35 @@ __device__ __forceinline__ bool mbarWaitOrAbort(uint64_t* bar, uint32_t parity, 
     }
 }
 
+// amplitude offset of the first amplitude of a tile: the tile index bits go,
+// in order, to the qubits outside I
 template <int KQ>
-__device__ __forceinline__ uint64_t tileAddr(const TC2Params<KQ>& p, uint32_t q) {
-    return (uint64_t)(q & ((1u << p.runBits) - 1u)) | p.scatterHigh[q >> p.runBits];
+__device__ __forceinline__ uint64_t tileBase(const TC2Params<KQ>& p, uint64_t tile) {
+    uint64_t tb = tile << p.runBits;
+#pragma unroll 1
+    for (int b = p.runBits; b < KQ + kTileBitsC; ++b) {
+        const int s = p.insI[b];
+        tb = ((tb >> s) << (s + 1)) | (tb & ((1ull << s) - 1ull));
+    }
+    return tb;
 }
 
+// swz of the column bits of tile column c (thread c of a role)
 template <int KQ>
-__global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ re, float* __restrict__ im,
-                                                            const float* __restrict__ gImage, uint64_t numTiles,
-                                                            int* __restrict__ errFlag, double* __restrict__ norms,
-                                                            const double* __restrict__ prevNorms,
-                                                            const __grid_constant__ TC2Params<KQ> p) {
+__device__ __forceinline__ uint32_t swzColumn(const TC2Params<KQ>& p, int c) {
+    uint32_t pc = 0;
+#pragma unroll
+    for (int b = 0; b < kTileBitsC; ++b)
+        if (c >> b & 1) pc |= 1u << p.pcPos[b];
+    return swz(pc);
+}
+
+template <int KQ, int LG>
+__global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restrict__ re, float* __restrict__ im,
+                                                                  const float* __restrict__ gImage, uint64_t numTiles,
+                                                                  int* __restrict__ errFlag, double* __restrict__ norms,
+                                                                  const double* __restrict__ prevNorms,
+                                                                  const __grid_constant__ TC2Params<KQ> p) {
     constexpr int D = 1 << KQ;
     constexpr int K = 2 * D, N = 2 * D;
     constexpr int TILE = 1 << (KQ + kTileBitsC);         // amplitudes per plane per tile
@@ -412,7 +437,9 @@ __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ 
     constexpr uint32_t kCols = kUsed <= 64 ? 64 : (kUsed <= 128 ? 128 : (kUsed <= 256 ? 256 : 512));
     constexpr uint32_t kLBO = 128, kSBO = (K / 4) * 128;
     constexpr uint32_t idesc = idescTF32(kTile, N);
-    constexpr int V4 = TILE / 4 / 128;                   // 16-byte loads per loader thread per plane
+    constexpr int V4 = TILE / 4 / 128;                   // 16-byte accesses per thread per plane
+    constexpr int kEpiWarp0 = 4 * LG, kMmaWarp = 4 * LG + 4;
+    constexpr int kEpiBar = 1 + LG;                      // named barrier ids: loaders 1..LG, epilogue LG + 1
 
     extern __shared__ __align__(128) uint8_t smem[];
     float* gh = reinterpret_cast<float*>(smem);
@@ -420,12 +447,15 @@ __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ 
     float* xs = gl + kGFloats;                           // 2 stage buffers
     float* es = xs + 2 * kXFloats;                       // epilogue staging
     __shared__ __align__(8) uint64_t barG, fullB[2], emptyB[2], dFullB[2], dEmptyB[2];
+    // offTab[w][m]: amplitude offset of tile position 128 w + 512 m (the
+    // 16-byte access m of warp w of a role; its lanes add 4 * lane)
+    __shared__ uint64_t offTab[4][V4];
     __shared__ uint32_t tmemBase;
     __shared__ volatile int abortF;
-    __shared__ int roleOk[2];
+    __shared__ int roleOk[LG + 1];
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (warp == 8) {
+    if (warp == kMmaWarp) {
         if (lane == 0) {
             abortF = 0;
             mbarInit(&barG, 1);
@@ -437,53 +467,53 @@ __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ 
             }
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
+        for (int i = lane; i < 4 * V4; i += 32) {
+            const uint32_t q = 128u * (i / V4) + 512u * (i % V4);
+            offTab[i / V4][i % V4] = (uint64_t)(q & ((1u << p.runBits) - 1u)) | p.scatterHigh[q >> p.runBits];
+        }
         tmemAlloc(&tmemBase, kCols);
     }
     fenceBefore();
     __syncthreads();
     fenceAfter();
     const uint32_t tmem = tmemBase;
+    // norm correction for the drift of the previous tensor-core pass, applied
+    // to this pass's output (Out = scale * G X)
+    float scale = 1.f;
+    if (prevNorms && prevNorms[1] > 0.0) scale = (float)sqrt(prevNorms[0] / prevNorms[1]);
 
-    if (warp < 4) {
+    if (warp < kEpiWarp0) {
         // ------------------------------------------------ loaders
-        const int lt = threadIdx.x;
-        uint32_t pc = 0;
-#pragma unroll
-        for (int b = 0; b < kTileBitsC; ++b)
-            if (lt >> b & 1) pc |= 1u << p.pcPos[b];
-        const uint32_t laneSel = (uint32_t)(32 * warp) << 16;
-        // this CTA's chunks, in order: chunk s = (tile blockIdx.x + (s / NCH) * gridDim.x, K stage s % NCH)
+        const int g = warp >> 2;
+        const int lt = threadIdx.x - 128 * g;            // tile column = TMEM lane
+        const int lw = lt >> 5;
+        const uint32_t colSw = swzColumn(p, lt);
+        const uint32_t sb0 = (4u * lt) ^ (uint32_t)(lt >> 3), sb1 = sb0 ^ 16u;   // swz(4 lt + 512 m + i) = (sb ^ i) + 512 m
+        const uint32_t laneSel = (uint32_t)(32 * lw) << 16;
+        // this CTA's chunks, in order: chunk s = (tile blockIdx.x + (s / NCH) * gridDim.x, K stage s % NCH);
+        // group g takes s = g, g + LG, ...
         const uint32_t nMy = blockIdx.x < numTiles ? (uint32_t)((numTiles - 1 - blockIdx.x) / gridDim.x + 1) * NCH : 0u;
-        // norm correction for the drift of the previous tensor-core pass
-        float scale = 1.f;
-        if (prevNorms && prevNorms[1] > 0.0) scale = (float)sqrt(prevNorms[0] / prevNorms[1]);
         double normIn = 0.0;
         float4 v[PLS][V4];
         auto issue = [&](uint32_t sc) {
             const uint64_t tile = blockIdx.x + (uint64_t)(sc / NCH) * gridDim.x;
             const int ch = sc % NCH;
-            uint64_t tb = tile;
-#pragma unroll
-            for (int b = 0; b < KQ + kTileBitsC; ++b) {
-                const int sh = p.insI[b];
-                tb = ((tb >> sh) << (sh + 1)) | (tb & ((1ull << sh) - 1ull));
-            }
+            const uint64_t tb = tileBase(p, tile) + 4u * lane;
 #pragma unroll
             for (int pl = 0; pl < PLS; ++pl) {
-                const float* src = ((NCH == 2 ? ch : pl) == 0) ? re : im;
+                const float* src = (((NCH == 2) ? ch : pl) == 0 ? re : im) + tb;
 #pragma unroll
-                for (int m = 0; m < V4; ++m)
-                    v[pl][m] = __ldcs(reinterpret_cast<const float4*>(src + tb + tileAddr(p, 4u * lt + 512u * m)));
+                for (int m = 0; m < V4; ++m) v[pl][m] = __ldcs(reinterpret_cast<const float4*>(src + offTab[lw][m]));
             }
         };
-        if (nMy) issue(0);
+        if (nMy > (uint32_t)g) issue(g);
         bool ok = true;
-        for (uint32_t sq = 0; sq < nMy; ++sq) {
+        for (uint32_t sq = g; sq < nMy; sq += LG) {
             const int b = sq & 1;
             const uint32_t u = sq >> 1;
-            if (lt == 0) roleOk[0] = (u == 0) || mbarWaitOrAbort(&emptyB[b], (u - 1) & 1, &abortF);
-            namedBar(1, 128);
-            if (!roleOk[0]) {
+            if (lt == 0) roleOk[g] = (u == 0) || mbarWaitOrAbort(&emptyB[b], (u - 1) & 1, &abortF);
+            namedBar(1 + g, 128);
+            if (!roleOk[g]) {
                 ok = false;
                 break;
             }
@@ -494,19 +524,18 @@ __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ 
                 float* dst = xb + pl * TILE;
 #pragma unroll
                 for (int m = 0; m < V4; ++m) {
-                    const uint32_t q = 4u * lt + 512u * m;
-                    const float x0 = v[pl][m].x * scale, x1 = v[pl][m].y * scale;
-                    const float x2 = v[pl][m].z * scale, x3 = v[pl][m].w * scale;
-                    nrm = fmaf(x0, x0, fmaf(x1, x1, fmaf(x2, x2, fmaf(x3, x3, nrm))));
-                    dst[swz(q)] = x0;
-                    dst[swz(q + 1)] = x1;
-                    dst[swz(q + 2)] = x2;
-                    dst[swz(q + 3)] = x3;
+                    const uint32_t s = (m & 1) ? sb1 : sb0;
+                    const float4 x = v[pl][m];
+                    nrm = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, nrm))));
+                    dst[(s ^ 0u) + 512 * m] = x.x;
+                    dst[(s ^ 1u) + 512 * m] = x.y;
+                    dst[(s ^ 2u) + 512 * m] = x.z;
+                    dst[(s ^ 3u) + 512 * m] = x.w;
                 }
             }
             normIn += (double)nrm;
-            namedBar(1, 128);
-            if (sq + 1 < nMy) issue(sq + 1);                 // next chunk's loads fly during the split below
+            namedBar(1 + g, 128);
+            if (sq + LG < nMy) issue(sq + LG);               // next chunk's loads fly during the split below
             const uint32_t aH = tmem + laneSel + b * kStageCols;
 #pragma unroll
             for (int c0 = 0; c0 < KC; c0 += 16) {
@@ -516,7 +545,12 @@ __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ 
                     const int kl = c0 + e;
                     const int pl = (NCH == 2) ? 0 : kl / D;
                     const int j = (NCH == 2) ? kl : kl % D;
-                    splitTF32(xb[pl * TILE + swz(pc | p.pj[j])], hi[e], lo[e]);
+                    // hi = x rounded to TF32; lo = x - hi (exact), which the
+                    // MMA reads as its leading TF32 bits; lo takes both signs,
+                    // so that truncation is unbiased
+                    const float x = xb[pl * TILE + (colSw ^ p.sj[j])];
+                    hi[e] = tf32RN(x);
+                    lo[e] = __float_as_uint(x - __uint_as_float(hi[e]));
                 }
                 tmemSt16(aH + c0, hi);
                 tmemSt16(aH + KC + c0, lo);
@@ -529,31 +563,24 @@ __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ 
             if (lt == 0) atomicExch(errFlag, 3);
             abortF = 1;
         }
-        normIn = warpSumD(normIn);
+        normIn = warpSumD(normIn) * (double)scale * (double)scale;
         if (lane == 0 && norms) atomicAdd(norms, normIn);
-    } else if (warp < 8) {
+    } else if (warp < kMmaWarp) {
         // ------------------------------------------------ epilogue
-        const int et = threadIdx.x - 128;
-        const int ew = warp - 4;
-        uint32_t pc = 0;
-#pragma unroll
-        for (int b = 0; b < kTileBitsC; ++b)
-            if (et >> b & 1) pc |= 1u << p.pcPos[b];
+        const int et = threadIdx.x - 32 * kEpiWarp0;
+        const int ew = et >> 5;
+        const uint32_t colSw = swzColumn(p, et);
+        const uint32_t sb0 = (4u * et) ^ (uint32_t)(et >> 3), sb1 = sb0 ^ 16u;
         const uint32_t laneSel = (uint32_t)(32 * ew) << 16;
         uint32_t tl = 0;
         bool ok = true;
         double normOut = 0.0;
         for (uint64_t tile = blockIdx.x; tile < numTiles && ok; tile += gridDim.x, ++tl) {
-            uint64_t tb = tile;
-#pragma unroll
-            for (int b = 0; b < KQ + kTileBitsC; ++b) {
-                const int s = p.insI[b];
-                tb = ((tb >> s) << (s + 1)) | (tb & ((1ull << s) - 1ull));
-            }
+            const uint64_t tb = tileBase(p, tile) + 4u * lane;
             const int bd = tl & 1;
-            if (et == 0) roleOk[1] = mbarWaitOrAbort(&dFullB[bd], (tl >> 1) & 1, &abortF);
-            namedBar(2, 128);
-            if (!roleOk[1]) {
+            if (et == 0) roleOk[LG] = mbarWaitOrAbort(&dFullB[bd], (tl >> 1) & 1, &abortF);
+            namedBar(kEpiBar, 128);
+            if (!roleOk[LG]) {
                 ok = false;
                 break;
             }
@@ -564,40 +591,41 @@ __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ 
             for (int pe = 0; pe < EPASS; ++pe) {
                 constexpr int COLS = N / EPASS;
 #pragma unroll
-                for (int c0 = 0; c0 < COLS; c0 += 16) {
-                    uint32_t v[16];
-                    tmemLd16(dA + pe * COLS + c0, v);
+                for (int c0 = 0; c0 < COLS; c0 += 32) {
+                    uint32_t va[16], vb[16];
+                    tmemLd16(dA + pe * COLS + c0, va);
+                    tmemLd16(dA + pe * COLS + c0 + 16, vb);
                     tmemWaitLd();
 #pragma unroll
-                    for (int e = 0; e < 16; ++e) {
+                    for (int e = 0; e < 32; ++e) {
                         const int col = pe * COLS + c0 + e;           // output row index r in [0, 2D)
                         const int plLocal = (EPASS == 2) ? 0 : col / D;
-                        const float y = __uint_as_float(v[e]);
+                        const float y = __uint_as_float(e < 16 ? va[e] : vb[e - 16]) * scale;
                         nrmTile = fmaf(y, y, nrmTile);
-                        es[plLocal * TILE + swz(pc | p.pj[col % D])] = y;
+                        es[plLocal * TILE + (colSw ^ p.sj[col % D])] = y;
                     }
                 }
                 if (pe == EPASS - 1) {                                // accumulator drained
                     fenceBefore();
                     mbarArrive(&dEmptyB[bd]);
                 }
-                namedBar(2, 128);
+                namedBar(kEpiBar, 128);
 #pragma unroll
                 for (int pl = 0; pl < 2 / EPASS; ++pl) {
-                    float* dstPlane = ((EPASS == 2 ? pe : pl) == 0) ? re : im;
-                    const float* sb = es + pl * TILE;
+                    float* dstPlane = (((EPASS == 2) ? pe : pl) == 0 ? re : im) + tb;
+                    const float* sbuf = es + pl * TILE;
 #pragma unroll
                     for (int m = 0; m < V4; ++m) {
-                        const uint32_t q = 4u * et + 512u * m;
+                        const uint32_t s = (m & 1) ? sb1 : sb0;
                         float4 w;
-                        w.x = sb[swz(q)];
-                        w.y = sb[swz(q + 1)];
-                        w.z = sb[swz(q + 2)];
-                        w.w = sb[swz(q + 3)];
-                        __stcs(reinterpret_cast<float4*>(dstPlane + tb + tileAddr(p, q)), w);
+                        w.x = sbuf[(s ^ 0u) + 512 * m];
+                        w.y = sbuf[(s ^ 1u) + 512 * m];
+                        w.z = sbuf[(s ^ 2u) + 512 * m];
+                        w.w = sbuf[(s ^ 3u) + 512 * m];
+                        __stcs(reinterpret_cast<float4*>(dstPlane + offTab[ew][m]), w);
                     }
                 }
-                namedBar(2, 128);
+                namedBar(kEpiBar, 128);
             }
             normOut += (double)nrmTile;
         }
@@ -662,7 +690,7 @@ __global__ void __launch_bounds__(kThreadsTC2, 1) kApplyTC2(float* __restrict__ 
     fenceBefore();
     __syncthreads();
     fenceAfter();
-    if (warp == 8) tmemDealloc(tmem, kCols);
+    if (warp == kMmaWarp) tmemDealloc(tmem, kCols);
 }
 
 // ------------------------------------------------------------ host side
@@ -675,7 +703,21 @@ struct DevicePlan {
     // removes the slow norm loss of the tensor cores' FP32 accumulation.
     double* norms = nullptr;
     int lastTC = -1;
+    // per pass: 1 if its matrix is unitary to 1e-10.  Only the drift of a
+    // unitary pass is corrected; a non-unitary pass changes the norm on purpose.
+    std::vector<char> unitary;
 };
+
+bool isUnitary(const FusedPass& pass) {
+    const int D = 1 << (int)pass.targets.size();
+    for (int r = 0; r < D; ++r)
+        for (int c = 0; c < D; ++c) {
+            cplx acc = 0;
+            for (int j = 0; j < D; ++j) acc += pass.m[(size_t)r * D + j] * std::conj(pass.m[(size_t)c * D + j]);
+            if (std::abs(acc - cplx(r == c ? 1.0 : 0.0, 0.0)) > 1e-10) return false;
+        }
+    return true;
+}
 
 // Canonical no-swizzle K-major image of an N x K operand (rows r, K index j):
 // byte (r/8)*SBO + (j/4)*128 + (r%8)*16 + (j%4)*4 with SBO = (K/4)*128.
@@ -731,7 +773,9 @@ bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* i
 }
 
 
-template <int KQ>
+uint32_t hostSwz(uint32_t q) { return q ^ ((q >> 5) & 31u); }
+
+template <int KQ, int LG>
 bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, double* norms,
                const double* prevNorms, cudaStream_t st) {
     constexpr int D = 1 << KQ;
@@ -770,25 +814,26 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
         uint32_t v = 0;
         for (int b = 0; b < KQ; ++b)
             if (j >> b & 1) v |= 1u << posOf[pass.targets[b]];
-        p.pj[j] = v;
+        p.sj[j] = hostSwz(v);
     }
     for (int b = 0, m = 0; b < ni; ++b)
         if (!(tmask >> I[b] & 1ull)) p.pcPos[m++] = b;
     const uint64_t numTiles = 1ull << (n - KQ - kTileBitsC);
-    static bool configured[8] = {};
-    if (!configured[KQ]) {
-        if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+    static bool configured[8][3] = {};
+    if (!configured[KQ][LG]) {
+        if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ, LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "applyPlanF32"))
             return false;
-        configured[KQ] = true;
+        configured[KQ][LG] = true;
     }
     const uint64_t grid = std::min<uint64_t>(numTiles, (uint64_t)numSMs());
-    kApplyTC2<KQ><<<(unsigned)grid, kThreadsTC2, smem, st>>>(re, im, img, numTiles, errFlag, norms, prevNorms, p);
+    kApplyTC2<KQ, LG><<<(unsigned)grid, (4 * LG + 5) * 32, smem, st>>>(re, im, img, numTiles, errFlag, norms,
+                                                                      prevNorms, p);
     return !launchFailed("applyPlanF32");
 }
 
 bool g_tcEnabled = true;
-int g_tcVersion = 0;      // 0: per pass by target layout, 1 / 2: force one kernel
+int g_tcVersion = 0;      // 0: per pass by target layout; 1, 2, 3: force one kernel
 bool g_tcChecked = false;
 
 }  // namespace
@@ -807,6 +852,7 @@ void* uploadPlanTC(const FusedPlan& plan) {
     }
     for (const FusedPass& pass : plan.passes) {
         const int k = (int)pass.targets.size();
+        dp->unitary.push_back(isUnitary(pass) ? 1 : 0);
         if (k < 4 || k > 6 || plan.numQubits < k + 7) {
             dp->images.push_back(nullptr);
             continue;
@@ -858,41 +904,60 @@ void tcBeginPlan(void* devPlan, size_t numPasses) {
     if (dp->norms) cudaMemsetAsync(dp->norms, 0, 2 * std::max<size_t>(1, numPasses) * sizeof(double), stream());
 }
 
-// explicit entry used by the FP32 engine with the pass index.  Kernel choice
-// (measured at 30 qubits): 5- and 6-qubit passes always run on the pipelined
-// kernel; 4-qubit passes whose targets are all at or above qubit 5 run on the
-// direct-load kernel (four CTAs per SM; each lane's group is then part of a
-// coalesced warp line), the others on the pipelined kernel, whose
-// shared-memory staging keeps them coalesced.
-bool applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, size_t index, cudaStream_t st) {
+// Which applier runs a pass on registers of n qubits: 0 = the FP32 SIMT
+// applier, 1 = the direct-load tensor-core kernel, 2 / 3 = the pipelined one
+// with two / one loader groups.  Default choice (measured at 30 qubits, ms
+// per pass): passes on 1..3 qubits and 4-qubit passes whose targets are all
+// at or above qubit 5 run on the SIMT applier (3.2 ms against 3.7 ms for the
+// direct-load kernel: every lane's group is part of a coalesced warp line and
+// the multiply is cheap); the other 4-qubit passes (SIMT 9.0 ms) and all 5-
+// and 6-qubit passes run on the pipelined kernel, whose shared-memory staging
+// keeps them coalesced.
+int tcKernelFor(const FusedPass& pass, int n) {
+    const int k = (int)pass.targets.size();
+    if (!g_tcEnabled || k < 4 || k > 6 || n < k + 7) return 0;
+    if (g_tcVersion != 0) return g_tcVersion;
+    return (k == 4 && pass.targets[0] >= 5) ? 0 : 2;
+}
+
+// explicit entry used by the FP32 engine with the pass index: 1 = applied on
+// the tensor cores, 0 = not a tensor-core pass (the caller runs it on SIMT),
+// -1 = the launch failed (already reported)
+int applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, size_t index, cudaStream_t st) {
     DevicePlan* dp = const_cast<DevicePlan*>(reinterpret_cast<const DevicePlan*>(devPlan));
-    if (!dp || !g_tcEnabled || index >= dp->images.size() || !dp->images[index]) return false;
+    if (!dp || index >= dp->images.size() || !dp->images[index]) return 0;
     const int k = (int)pass.targets.size();
     float* re = f32re(q);
     float* im = f32im(q);
     const int n = f32n(q);
+    const int version = tcKernelFor(pass, n);
+    if (version == 0) return 0;
     double* norms = dp->norms ? dp->norms + 2 * index : nullptr;
-    const double* prev = (dp->norms && dp->lastTC >= 0) ? dp->norms + 2 * dp->lastTC : nullptr;
-    int version = g_tcVersion;
-    if (version == 0) version = (k == 4 && pass.targets[0] >= 5) ? 1 : 2;
+    const double* prev =
+        (dp->norms && dp->lastTC >= 0 && dp->unitary[dp->lastTC]) ? dp->norms + 2 * dp->lastTC : nullptr;
     bool ok = false;
-    if (version == 2) {
+    if (version >= 2) {
+        const bool two = version == 2;       // 2: two loader groups, 3: one
         switch (k) {
-            case 4: ok = launchTC2<4>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
-            case 5: ok = launchTC2<5>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
-            case 6: ok = launchTC2<6>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
-            default: return false;
+            case 4: ok = two ? launchTC2<4, 2>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st)
+                             : launchTC2<4, 1>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
+            case 5: ok = two ? launchTC2<5, 2>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st)
+                             : launchTC2<5, 1>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
+            case 6: ok = two ? launchTC2<6, 2>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st)
+                             : launchTC2<6, 1>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
+            default: return 0;
         }
     } else {
         switch (k) {
             case 4: ok = launchTC<4>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
             case 5: ok = launchTC<5>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
             case 6: ok = launchTC<6>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
-            default: return false;
+            default: return 0;
         }
     }
-    if (ok) dp->lastTC = (int)index;
-    return ok;
+    if (!ok) return -1;
+    dp->lastTC = (int)index;
+    return 1;
 }
 
 int tcErrorFlag(const void* devPlan) {
@@ -905,7 +970,7 @@ int tcErrorFlag(const void* devPlan) {
 }
 
 void setTensorCoresEnabled(bool on) { g_tcEnabled = on; }
-void setTensorCoreKernel(int version) { g_tcVersion = (version == 1 || version == 2) ? version : 0; }
+void setTensorCoreKernel(int version) { g_tcVersion = (version >= 1 && version <= 3) ? version : 0; }
 bool tensorCoresEnabled() { return g_tcEnabled; }
 
 }  // namespace qg

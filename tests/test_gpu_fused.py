@@ -12,6 +12,18 @@ from quantumlab_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(autouse=True)
+def no_library_errors(gpulib):
+    """Every error the library reports through invalidQuESTInputError fails
+    the test (instead of the default handler's exit)."""
+    gpulib.capture_errors()
+    gpulib.errors.clear()
+    yield
+    errors = list(gpulib.errors)
+    gpulib.errors.clear()
+    assert not errors, errors
+
+
 def run_both(L, n, kmax, ops):
     q64 = L.create(n)
     W.run_ops(L, q64, ops)
@@ -103,10 +115,11 @@ def _single_gate_plan(L, n, targets, seed):
 
 @pytest.mark.parametrize("targets", [[0, 1, 2, 3], [0, 2, 4, 6, 8], [0, 1, 2, 3, 4, 5], [1, 3, 5, 7, 9, 11],
                                      [2, 9, 10, 14], [4, 5, 6, 7, 15, 16], [12, 13, 14, 15, 16, 17]])
-@pytest.mark.parametrize("version", [0, 1, 2])
+@pytest.mark.parametrize("version", [0, 1, 2, 3])
 def test_tensor_core_target_layouts(gpulib, targets, version):
-    """One dense gate on low, interleaved and high target sets, both tensor-core
-    kernels, against the FP32 SIMT applier (k <= 5) or the FP64 engine."""
+    """One dense gate on low, interleaved and high target sets, every
+    tensor-core kernel (direct-load; pipelined with two or one loader groups),
+    against the FP64 engine."""
     L = gpulib
     n = 18
     rng = np.random.default_rng(3)
@@ -126,6 +139,49 @@ def test_tensor_core_target_layouts(gpulib, targets, version):
     print(f"TC v{version} targets={targets}: 1-F={omf:.2e} max|d amp|={err.value:.2e}")
     assert omf < 1e-9 and err.value < 1e-5
     L.lib.quest_gb300_planDestroy(plan)
+    L.lib.quest_gb300_destroyQuregF32(q32)
+    L.destroy(q64)
+
+
+@pytest.mark.parametrize("version", [0, 1, 3])
+def test_non_unitary_passes_keep_their_norm(gpulib, version):
+    """A plan mixing non-unitary and unitary dense gates on the tensor cores:
+    the drift correction must not undo a pass that changes the norm on
+    purpose (only unitary passes are corrected)."""
+    L = gpulib
+    n = 18
+    rng = np.random.default_rng(8)
+    gates = []
+    for i, ts in enumerate([[0, 3, 5, 9, 12], [1, 2, 6, 7, 8, 13], [4, 10, 11, 14, 15, 16], [0, 1, 2, 3, 17]]):
+        k = len(ts)
+        z = rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k))
+        m = np.linalg.qr(z)[0] if i % 2 else 0.3 * z / np.sqrt(1 << k)
+        gates.append((ts, m))
+    p = L.lib.quest_gb300_planCreate(n, 6)
+    for ts, m in gates:
+        re, im = np.ascontiguousarray(m.real.ravel()), np.ascontiguousarray(m.imag.ravel())
+        assert L.lib.quest_gb300_planAddGate(p, (C.c_int * len(ts))(*ts), len(ts),
+                                             re.ctypes.data_as(C.POINTER(C.c_double)),
+                                             im.ctypes.data_as(C.POINTER(C.c_double))) == 0
+    assert L.lib.quest_gb300_planCompile(p) == 4
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    psi /= np.linalg.norm(psi)
+    q64 = L.create(n)
+    L.set_amps(q64, psi)
+    q32 = L.lib.quest_gb300_createQuregF32(n)
+    L.lib.quest_gb300_copyFromQureg(q32, q64)
+    L.lib.quest_gb300_setTensorCoreKernel(version)
+    assert L.lib.quest_gb300_applyPlanF32(q32, p) == 0
+    L.lib.quest_gb300_setTensorCoreKernel(0)
+    for ts, m in gates:
+        L.applyMatrixN(q64, ts, m)
+    err = C.c_double(0)
+    omf = L.lib.quest_gb300_compareF32(q32, q64, C.byref(err))
+    p64 = L.lib.calcTotalProb(q64)
+    p32 = L.lib.quest_gb300_calcTotalProbF32(q32)
+    print(f"non-unitary v{version}: norm {p64:.6e} vs {p32:.6e}, 1-F={omf:.2e}")
+    assert abs(p32 / p64 - 1) < 1e-5 and omf < 1e-9
+    L.lib.quest_gb300_planDestroy(p)
     L.lib.quest_gb300_destroyQuregF32(q32)
     L.destroy(q64)
 
