@@ -43,6 +43,8 @@ void* uploadPlanTC(const FusedPlan& plan);
 void freePlanTC(void* d);
 int tcErrorFlag(const void* devPlan);
 void tcBeginPlan(void* devPlan, size_t numPasses);
+void tcBeginRange(void* devPlan);
+void tcNoteSimtPass(void* devPlan, size_t index);
 void setTensorCoresEnabled(bool on);
 void setTensorCoreKernel(int version);
 bool tensorCoresEnabled();
@@ -335,6 +337,7 @@ int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPas
     const int last = std::min(total, firstPass + numPasses);
     cudaStream_t st = qg::stream();
     if (firstPass == 0) qg::tcBeginPlan(p->device, p->passes.size());
+    qg::tcBeginRange(p->device);
     bool usedTC = false;
     for (int i = firstPass; i < last; ++i) {
         const qg::FusedPass& pass = p->passes[i];
@@ -348,6 +351,7 @@ int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPas
             invalidQuESTInputError("fused pass on more than 5 qubits needs the tensor-core applier", "applyPlanF32");
             return -1;
         }
+        qg::tcNoteSimtPass(p->device, (size_t)i);
     }
     if (usedTC && qg::g_checkTC && last == total) {
         const int e = qg::tcErrorFlag(p->device);

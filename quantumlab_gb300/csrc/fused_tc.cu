@@ -163,6 +163,36 @@ __device__ __forceinline__ void splitTF32(float x, uint32_t& hi, uint32_t& lo) {
     lo = tf32RN(x - __uint_as_float(hi));
 }
 
+// nearest TF32 value of a finite x (ties away from zero), as cvt.rna.tf32.f32,
+// in two integer operations
+__device__ __forceinline__ uint32_t tf32Bits(float x) { return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u; }
+
+// Norm bookkeeping of one tensor-core pass (FP64 sums, accumulated with atomics):
+//   out      sum |y|^2 of this pass's output;
+//   in       sum |x|^2 of its input, or null when the host takes it from the
+//            previous pass's output (nothing changed the state in between);
+//   scaleSq  where this pass writes the square of the scale it applied;
+//   corrIn, corrOut, corrScaleSq  the same three numbers of the previous
+//            unitary tensor-core pass, or null.  That pass's own drift is
+//            out / (in * scale^2); this pass scales by its inverse square root.
+struct NormLinks {
+    double* out;
+    double* in;
+    double* scaleSq;
+    const double* corrIn;
+    const double* corrOut;
+    const double* corrScaleSq;
+};
+// the scale minus one (kept exact to FP32 relative precision)
+__device__ __forceinline__ float driftCorrection(const NormLinks& nl) {
+    if (!nl.corrIn || !nl.corrOut || !nl.corrScaleSq || !(*nl.corrOut > 0.0)) return 0.f;
+    return (float)(sqrt(*nl.corrIn * *nl.corrScaleSq / *nl.corrOut) - 1.0);
+}
+// written once per launch, by the calling thread when `writer`
+__device__ __forceinline__ void recordScale(const NormLinks& nl, float sm1, bool writer) {
+    if (nl.scaleSq && writer) *nl.scaleSq = (1.0 + (double)sm1) * (1.0 + (double)sm1);
+}
+
 __device__ __forceinline__ double warpSumD(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -180,8 +210,7 @@ struct TCParams {
 template <int KQ>
 __global__ void __launch_bounds__(kThreadsTC, (KQ == 4 ? 4 : 1)) kApplyTC(float* __restrict__ re, float* __restrict__ im,
                                                        const float* __restrict__ gImage, uint64_t numTiles,
-                                                       int* __restrict__ errFlag, double* __restrict__ norms,
-                                                       const double* __restrict__ prevNorms,
+                                                       int* __restrict__ errFlag, const NormLinks nl,
                                                        const __grid_constant__ TCParams<KQ> p) {
     constexpr int D = 1 << KQ;
     constexpr int K = 2 * D;                    // GEMM K = N
@@ -230,8 +259,8 @@ __global__ void __launch_bounds__(kThreadsTC, (KQ == 4 ? 4 : 1)) kApplyTC(float*
     const uint32_t ghAddr = smemAddr(gh), glAddr = smemAddr(gl);
 
     const bool aborted = abortFlag != 0;                   // read after the barrier above: uniform
-    float scale = 1.f;
-    if (prevNorms && prevNorms[1] > 0.0) scale = (float)sqrt(prevNorms[0] / prevNorms[1]);
+    const float sm1 = driftCorrection(nl);               // input scaled by 1 + sm1
+    recordScale(nl, sm1, blockIdx.x == 0 && threadIdx.x == 0);
     double normIn = 0.0, normOut = 0.0;
     for (uint64_t tile = blockIdx.x; tile < numTiles && !aborted; tile += gridDim.x) {
         // ---- load this lane's group, split, write Xh / Xl rows to TMEM
@@ -255,8 +284,8 @@ __global__ void __launch_bounds__(kThreadsTC, (KQ == 4 ? 4 : 1)) kApplyTC(float*
             float nrm = 0.f;
 #pragma unroll
             for (int e = 0; e < CH; ++e) {
-                x[e] *= scale;
                 nrm = fmaf(x[e], x[e], nrm);
+                x[e] = fmaf(x[e], sm1, x[e]);
             }
             normIn += (double)nrm;
 #pragma unroll
@@ -324,9 +353,9 @@ __global__ void __launch_bounds__(kThreadsTC, (KQ == 4 ? 4 : 1)) kApplyTC(float*
     }
     normIn = warpSumD(normIn);
     normOut = warpSumD(normOut);
-    if (lane == 0 && norms) {
-        atomicAdd(norms, normIn);
-        atomicAdd(norms + 1, normOut);
+    if (lane == 0) {
+        if (nl.in) atomicAdd(nl.in, normIn);
+        if (nl.out) atomicAdd(nl.out, normOut);
     }
     __syncthreads();
     if (warp == 0) tmemDealloc(tbase, kCols);
@@ -419,8 +448,7 @@ __device__ __forceinline__ uint32_t swzColumn(const TC2Params<KQ>& p, int c) {
 template <int KQ, int LG>
 __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restrict__ re, float* __restrict__ im,
                                                                   const float* __restrict__ gImage, uint64_t numTiles,
-                                                                  int* __restrict__ errFlag, double* __restrict__ norms,
-                                                                  const double* __restrict__ prevNorms,
+                                                                  int* __restrict__ errFlag, const NormLinks nl,
                                                                   const __grid_constant__ TC2Params<KQ> p) {
     constexpr int D = 1 << KQ;
     constexpr int K = 2 * D, N = 2 * D;
@@ -446,7 +474,7 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
     float* gl = gh + kGFloats;
     float* xs = gl + kGFloats;                           // 2 stage buffers
     float* es = xs + 2 * kXFloats;                       // epilogue staging
-    __shared__ __align__(8) uint64_t barG, fullB[2], emptyB[2], dFullB[2], dEmptyB[2];
+    __shared__ __align__(8) uint64_t barG, gReady, fullB[2], emptyB[2], dFullB[2], dEmptyB[2];
     // offTab[w][m]: amplitude offset of tile position 128 w + 512 m (the
     // 16-byte access m of warp w of a role; its lanes add 4 * lane)
     __shared__ uint64_t offTab[4][V4];
@@ -459,6 +487,7 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
         if (lane == 0) {
             abortF = 0;
             mbarInit(&barG, 1);
+            mbarInit(&gReady, 128);
             for (int b = 0; b < 2; ++b) {
                 mbarInit(&fullB[b], 128);
                 mbarInit(&emptyB[b], 1);
@@ -477,10 +506,6 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
     __syncthreads();
     fenceAfter();
     const uint32_t tmem = tmemBase;
-    // norm correction for the drift of the previous tensor-core pass, applied
-    // to this pass's output (Out = scale * G X)
-    float scale = 1.f;
-    if (prevNorms && prevNorms[1] > 0.0) scale = (float)sqrt(prevNorms[0] / prevNorms[1]);
 
     if (warp < kEpiWarp0) {
         // ------------------------------------------------ loaders
@@ -494,6 +519,7 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
         // group g takes s = g, g + LG, ...
         const uint32_t nMy = blockIdx.x < numTiles ? (uint32_t)((numTiles - 1 - blockIdx.x) / gridDim.x + 1) * NCH : 0u;
         double normIn = 0.0;
+        const bool measure = nl.in != nullptr;             // input norm wanted (uniform)
         float4 v[PLS][V4];
         auto issue = [&](uint32_t sc) {
             const uint64_t tile = blockIdx.x + (uint64_t)(sc / NCH) * gridDim.x;
@@ -509,7 +535,7 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
         if (nMy > (uint32_t)g) issue(g);
         bool ok = true;
         for (uint32_t sq = g; sq < nMy; sq += LG) {
-            const int b = sq & 1;
+            const int b = (LG == 2) ? g : (int)(sq & 1);      // the stage (group g owns stage g when LG = 2)
             const uint32_t u = sq >> 1;
             if (lt == 0) roleOk[g] = (u == 0) || mbarWaitOrAbort(&emptyB[b], (u - 1) & 1, &abortF);
             namedBar(1 + g, 128);
@@ -518,22 +544,40 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
                 break;
             }
             float* xb = xs + b * kXFloats;
-            float nrm = 0.f;
+            {
+                // pointer bases, so that the plane and 512 m strides become
+                // immediate offsets of the shared stores
+                float* const e0 = xb + (sb0 ^ 0u);
+                float* const e1 = xb + (sb0 ^ 1u);
+                float* const e2 = xb + (sb0 ^ 2u);
+                float* const e3 = xb + (sb0 ^ 3u);
+                float* const o0 = xb + (sb1 ^ 0u);
+                float* const o1 = xb + (sb1 ^ 1u);
+                float* const o2 = xb + (sb1 ^ 2u);
+                float* const o3 = xb + (sb1 ^ 3u);
 #pragma unroll
-            for (int pl = 0; pl < PLS; ++pl) {
-                float* dst = xb + pl * TILE;
+                for (int pl = 0; pl < PLS; ++pl)
 #pragma unroll
-                for (int m = 0; m < V4; ++m) {
-                    const uint32_t s = (m & 1) ? sb1 : sb0;
-                    const float4 x = v[pl][m];
-                    nrm = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, nrm))));
-                    dst[(s ^ 0u) + 512 * m] = x.x;
-                    dst[(s ^ 1u) + 512 * m] = x.y;
-                    dst[(s ^ 2u) + 512 * m] = x.z;
-                    dst[(s ^ 3u) + 512 * m] = x.w;
-                }
+                    for (int m = 0; m < V4; ++m) {
+                        const int off = pl * TILE + 512 * m;
+                        const float4 x = v[pl][m];
+                        (m & 1 ? o0 : e0)[off] = x.x;
+                        (m & 1 ? o1 : e1)[off] = x.y;
+                        (m & 1 ? o2 : e2)[off] = x.z;
+                        (m & 1 ? o3 : e3)[off] = x.w;
+                    }
             }
-            normIn += (double)nrm;
+            if (measure) {
+                float nrm = 0.f;
+#pragma unroll
+                for (int pl = 0; pl < PLS; ++pl)
+#pragma unroll
+                    for (int m = 0; m < V4; ++m) {
+                        const float4 x = v[pl][m];
+                        nrm = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, nrm))));
+                    }
+                normIn += (double)nrm;
+            }
             namedBar(1 + g, 128);
             if (sq + LG < nMy) issue(sq + LG);               // next chunk's loads fly during the split below
             const uint32_t aH = tmem + laneSel + b * kStageCols;
@@ -548,8 +592,8 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
                     // hi = x rounded to TF32; lo = x - hi (exact), which the
                     // MMA reads as its leading TF32 bits; lo takes both signs,
                     // so that truncation is unbiased
-                    const float x = xb[pl * TILE + (colSw ^ p.sj[j])];
-                    hi[e] = tf32RN(x);
+                    const float x = (xb + pl * TILE)[colSw ^ p.sj[j]];
+                    hi[e] = tf32Bits(x);
                     lo[e] = __float_as_uint(x - __uint_as_float(hi[e]));
                 }
                 tmemSt16(aH + c0, hi);
@@ -563,17 +607,41 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
             if (lt == 0) atomicExch(errFlag, 3);
             abortF = 1;
         }
-        normIn = warpSumD(normIn) * (double)scale * (double)scale;
-        if (lane == 0 && norms) atomicAdd(norms, normIn);
+        normIn = warpSumD(normIn);
+        if (lane == 0 && measure) atomicAdd(nl.in, normIn);
     } else if (warp < kMmaWarp) {
         // ------------------------------------------------ epilogue
         const int et = threadIdx.x - 32 * kEpiWarp0;
         const int ew = et >> 5;
         const uint32_t colSw = swzColumn(p, et);
         const uint32_t sb0 = (4u * et) ^ (uint32_t)(et >> 3), sb1 = sb0 ^ 16u;
+        const float* const ee0 = es + (sb0 ^ 0u);
+        const float* const ee1 = es + (sb0 ^ 1u);
+        const float* const ee2 = es + (sb0 ^ 2u);
+        const float* const ee3 = es + (sb0 ^ 3u);
+        const float* const eo0 = es + (sb1 ^ 0u);
+        const float* const eo1 = es + (sb1 ^ 1u);
+        const float* const eo2 = es + (sb1 ^ 2u);
+        const float* const eo3 = es + (sb1 ^ 3u);
         const uint32_t laneSel = (uint32_t)(32 * ew) << 16;
+        // the previous pass's drift correction, folded into this pass's G:
+        // G' = (1 + sm1) (Gh + Gl), split again into TF32 parts (the sum of
+        // the two parts is exact in FP32)
+        bool ok = mbarWaitOrAbort(&barG, 0, &abortF);
+        const float sm1 = driftCorrection(nl);
+        recordScale(nl, sm1, blockIdx.x == 0 && et == 0);
+        if (ok && sm1 != 0.f) {
+            for (uint32_t i = et; i < kGFloats; i += 128) {
+                const float g0 = gh[i] + gl[i];
+                const float g = fmaf(g0, sm1, g0);
+                const uint32_t h = tf32Bits(g);
+                gh[i] = __uint_as_float(h);
+                gl[i] = __uint_as_float(tf32Bits(g - __uint_as_float(h)));
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // visible to the MMAs
+        }
+        mbarArrive(&gReady);
         uint32_t tl = 0;
-        bool ok = true;
         double normOut = 0.0;
         for (uint64_t tile = blockIdx.x; tile < numTiles && ok; tile += gridDim.x, ++tl) {
             const uint64_t tb = tileBase(p, tile) + 4u * lane;
@@ -600,9 +668,9 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
                     for (int e = 0; e < 32; ++e) {
                         const int col = pe * COLS + c0 + e;           // output row index r in [0, 2D)
                         const int plLocal = (EPASS == 2) ? 0 : col / D;
-                        const float y = __uint_as_float(e < 16 ? va[e] : vb[e - 16]) * scale;
+                        const float y = __uint_as_float(e < 16 ? va[e] : vb[e - 16]);
                         nrmTile = fmaf(y, y, nrmTile);
-                        es[plLocal * TILE + (colSw ^ p.sj[col % D])] = y;
+                        (es + plLocal * TILE)[colSw ^ p.sj[col % D]] = y;
                     }
                 }
                 if (pe == EPASS - 1) {                                // accumulator drained
@@ -613,15 +681,14 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
 #pragma unroll
                 for (int pl = 0; pl < 2 / EPASS; ++pl) {
                     float* dstPlane = (((EPASS == 2) ? pe : pl) == 0 ? re : im) + tb;
-                    const float* sbuf = es + pl * TILE;
 #pragma unroll
                     for (int m = 0; m < V4; ++m) {
-                        const uint32_t s = (m & 1) ? sb1 : sb0;
+                        const int off = pl * TILE + 512 * m;
                         float4 w;
-                        w.x = sbuf[(s ^ 0u) + 512 * m];
-                        w.y = sbuf[(s ^ 1u) + 512 * m];
-                        w.z = sbuf[(s ^ 2u) + 512 * m];
-                        w.w = sbuf[(s ^ 3u) + 512 * m];
+                        w.x = (m & 1 ? eo0 : ee0)[off];
+                        w.y = (m & 1 ? eo1 : ee1)[off];
+                        w.z = (m & 1 ? eo2 : ee2)[off];
+                        w.w = (m & 1 ? eo3 : ee3)[off];
                         __stcs(reinterpret_cast<float4*>(dstPlane + offTab[ew][m]), w);
                     }
                 }
@@ -634,7 +701,7 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
             abortF = 1;
         }
         normOut = warpSumD(normOut);
-        if (lane == 0 && norms) atomicAdd(norms + 1, normOut);
+        if (lane == 0 && nl.out) atomicAdd(nl.out, normOut);
     } else if (lane == 0) {
         // ------------------------------------------------ TMA of G, then MMAs
         mbarExpectTx(&barG, 2 * kGFloats * 4);
@@ -642,6 +709,7 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
         bulkG2S(gl, gImage + kGFloats, kGFloats * 4, &barG);
         bool ok = mbarWaitOrAbort(&barG, 0, &abortF);
         if (!ok) mbarWaitOrAbort(&barG, 0, &abortF);                // once more for the copies in flight
+        ok = ok && mbarWaitOrAbort(&gReady, 0, &abortF);            // G rescaled by the epilogue warps
         const uint32_t ghA = smemAddr(gh), glA = smemAddr(gl);
         uint32_t sq = 0, tl = 0;
         for (uint64_t tile = blockIdx.x; tile < numTiles && ok; tile += gridDim.x, ++tl) {
@@ -697,12 +765,16 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
 struct DevicePlan {
     std::vector<float*> images;      // per pass: Gh image then Gl image (or nullptr)
     int* errFlag = nullptr;
-    // per pass: (sum |x|^2 of its scaled input, sum |y|^2 of its output) in
-    // FP64, accumulated by the tensor-core kernels.  The next tensor-core
-    // pass rescales its input by sqrt(in / out) of the previous one, which
-    // removes the slow norm loss of the tensor cores' FP32 accumulation.
+    // per pass: (sum |x|^2 of its input, sum |y|^2 of its output, square of
+    // the scale it applied) in FP64, written by the tensor-core kernels.  The
+    // next tensor-core pass scales by sqrt(in * scale^2 / out) of the previous
+    // one, which removes the norm drift of the tensor cores' FP32 accumulation.
     double* norms = nullptr;
-    int lastTC = -1;
+    // per pass: where its input norm lives (its own slot, or the output slot
+    // of the previous tensor-core pass when nothing changed the state between)
+    std::vector<const double*> inNorm;
+    int lastTC = -1;        // last tensor-core pass applied (its drift is corrected next)
+    bool chain = false;     // the state is still lastTC's output up to unitary SIMT passes
     // per pass: 1 if its matrix is unitary to 1e-10.  Only the drift of a
     // unitary pass is corrected; a non-unitary pass changes the norm on purpose.
     std::vector<char> unitary;
@@ -740,8 +812,8 @@ float hostTf32RN(float x) {
 }
 
 template <int KQ>
-bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, double* norms,
-              const double* prevNorms, cudaStream_t st) {
+bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, const NormLinks& nl,
+              cudaStream_t st) {
     constexpr int D = 1 << KQ;
     constexpr int K = 2 * D;
     const size_t smem = 2 * (size_t)K * K * 4;
@@ -768,7 +840,7 @@ bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* i
         configured[KQ] = true;
     }
     const uint64_t grid = std::min<uint64_t>(numTiles, (uint64_t)perSM * numSMs());
-    kApplyTC<KQ><<<(unsigned)grid, kThreadsTC, smemReq, st>>>(re, im, img, numTiles, errFlag, norms, prevNorms, p);
+    kApplyTC<KQ><<<(unsigned)grid, kThreadsTC, smemReq, st>>>(re, im, img, numTiles, errFlag, nl, p);
     return !launchFailed("applyPlanF32");
 }
 
@@ -776,8 +848,8 @@ bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* i
 uint32_t hostSwz(uint32_t q) { return q ^ ((q >> 5) & 31u); }
 
 template <int KQ, int LG>
-bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, double* norms,
-               const double* prevNorms, cudaStream_t st) {
+bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, const NormLinks& nl,
+               cudaStream_t st) {
     constexpr int D = 1 << KQ;
     constexpr int K = 2 * D, N = 2 * D;
     constexpr int TILE = 1 << (KQ + kTileBitsC);
@@ -827,8 +899,7 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
         configured[KQ][LG] = true;
     }
     const uint64_t grid = std::min<uint64_t>(numTiles, (uint64_t)numSMs());
-    kApplyTC2<KQ, LG><<<(unsigned)grid, (4 * LG + 5) * 32, smem, st>>>(re, im, img, numTiles, errFlag, norms,
-                                                                      prevNorms, p);
+    kApplyTC2<KQ, LG><<<(unsigned)grid, (4 * LG + 5) * 32, smem, st>>>(re, im, img, numTiles, errFlag, nl, p);
     return !launchFailed("applyPlanF32");
 }
 
@@ -846,7 +917,7 @@ void* uploadPlanTC(const FusedPlan& plan) {
         return nullptr;
     }
     cudaMemsetAsync(dp->errFlag, 0, sizeof(int), stream());
-    if (cudaMalloc(&dp->norms, 2 * std::max<size_t>(1, plan.passes.size()) * sizeof(double)) != cudaSuccess) {
+    if (cudaMalloc(&dp->norms, 3 * std::max<size_t>(1, plan.passes.size()) * sizeof(double)) != cudaSuccess) {
         cudaGetLastError();
         dp->norms = nullptr;
     }
@@ -896,12 +967,26 @@ void freePlanTC(void* h) {
     delete dp;
 }
 
-// start of a plan application: clear the norm accumulators
+// start of a plan application (pass 0): no previous tensor-core pass
 void tcBeginPlan(void* devPlan, size_t numPasses) {
     DevicePlan* dp = reinterpret_cast<DevicePlan*>(devPlan);
     if (!dp) return;
     dp->lastTC = -1;
-    if (dp->norms) cudaMemsetAsync(dp->norms, 0, 2 * std::max<size_t>(1, numPasses) * sizeof(double), stream());
+    dp->chain = false;
+    dp->inNorm.assign(numPasses, nullptr);
+}
+
+// start of every applyPlanF32Range call: the caller may have changed the
+// state since the last call, so the next tensor-core pass measures its input
+void tcBeginRange(void* devPlan) {
+    DevicePlan* dp = reinterpret_cast<DevicePlan*>(devPlan);
+    if (dp) dp->chain = false;
+}
+
+// a pass ran on the SIMT applier: a non-unitary one changes the norm
+void tcNoteSimtPass(void* devPlan, size_t index) {
+    DevicePlan* dp = reinterpret_cast<DevicePlan*>(devPlan);
+    if (dp && (index >= dp->unitary.size() || !dp->unitary[index])) dp->chain = false;
 }
 
 // Which applier runs a pass on registers of n qubits: 0 = the FP32 SIMT
@@ -932,31 +1017,45 @@ int applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, 
     const int n = f32n(q);
     const int version = tcKernelFor(pass, n);
     if (version == 0) return 0;
-    double* norms = dp->norms ? dp->norms + 2 * index : nullptr;
-    const double* prev =
-        (dp->norms && dp->lastTC >= 0 && dp->unitary[dp->lastTC]) ? dp->norms + 2 * dp->lastTC : nullptr;
+    NormLinks nl{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    if (dp->norms) {
+        if (dp->inNorm.size() != dp->images.size()) dp->inNorm.assign(dp->images.size(), nullptr);
+        double* mine = dp->norms + 3 * index;            // in, out, scale^2
+        cudaMemsetAsync(mine, 0, 3 * sizeof(double), st);
+        nl.out = mine + 1;
+        nl.scaleSq = mine + 2;
+        const bool chained = dp->chain && dp->lastTC >= 0;
+        nl.in = chained ? nullptr : mine;
+        dp->inNorm[index] = chained ? dp->norms + 3 * dp->lastTC + 1 : mine;
+        if (dp->lastTC >= 0 && dp->unitary[dp->lastTC]) {
+            nl.corrIn = dp->inNorm[dp->lastTC];
+            nl.corrOut = dp->norms + 3 * dp->lastTC + 1;
+            nl.corrScaleSq = dp->norms + 3 * dp->lastTC + 2;
+        }
+    }
     bool ok = false;
     if (version >= 2) {
         const bool two = version == 2;       // 2: two loader groups, 3: one
         switch (k) {
-            case 4: ok = two ? launchTC2<4, 2>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st)
-                             : launchTC2<4, 1>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
-            case 5: ok = two ? launchTC2<5, 2>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st)
-                             : launchTC2<5, 1>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
-            case 6: ok = two ? launchTC2<6, 2>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st)
-                             : launchTC2<6, 1>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
+            case 4: ok = two ? launchTC2<4, 2>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)
+                             : launchTC2<4, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st); break;
+            case 5: ok = two ? launchTC2<5, 2>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)
+                             : launchTC2<5, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st); break;
+            case 6: ok = two ? launchTC2<6, 2>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)
+                             : launchTC2<6, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st); break;
             default: return 0;
         }
     } else {
         switch (k) {
-            case 4: ok = launchTC<4>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
-            case 5: ok = launchTC<5>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
-            case 6: ok = launchTC<6>(re, im, n, pass, dp->images[index], dp->errFlag, norms, prev, st); break;
+            case 4: ok = launchTC<4>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st); break;
+            case 5: ok = launchTC<5>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st); break;
+            case 6: ok = launchTC<6>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st); break;
             default: return 0;
         }
     }
     if (!ok) return -1;
     dp->lastTC = (int)index;
+    dp->chain = true;
     return 1;
 }
 
