@@ -186,8 +186,9 @@ def run_gpu(args, rank, world):
     groups = {}
     for i in range(npass):
         key = {0: f"kApplySimt<{kk[i]}> (FP32 FFMA)", 1: f"kApplyTC<{kk[i]}> (tcgen05 split-TF32, direct loads)",
-               2: f"kApplyTC2<{kk[i]},2> (tcgen05 split-TF32, pipelined)",
-               3: f"kApplyTC2<{kk[i]},1> (tcgen05 split-TF32, pipelined)"}[tc[i]]
+               2: f"kApplyTC2<{kk[i]},2,1> (tcgen05 split-TF32, pipelined)",
+               3: f"kApplyTC2<{kk[i]},1,1> (tcgen05 split-TF32, pipelined)",
+               4: f"kApplyTC2<{kk[i]},1,2> (tcgen05 split-TF32, pipelined)"}[tc[i]]
         g = groups.setdefault(key, [0, 0.0])
         g[0] += 1
         g[1] += pass_ms[i]

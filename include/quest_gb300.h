@@ -72,17 +72,15 @@ void quest_gb300_copyToQureg(void* qureg32, Qureg destination);
 int quest_gb300_applyPlanF32(void* qureg32, void* plan);
 /* apply passes [firstPass, firstPass + numPasses) only (timing, stepping) */
 int quest_gb300_applyPlanF32Range(void* qureg32, void* plan, int firstPass, int numPasses);
-/* applier of pass i: 0 = SIMT, 1 = direct-load tensor-core kernel, 2 or 3 =
- * pipelined tensor-core kernel (two / one loader groups); -1 if invalid */
+/* applier of pass i: 0 = SIMT, 1 = direct-load tensor-core kernel, 2..4 =
+ * pipelined tensor-core kernel (as setTensorCoreKernel); -1 if invalid */
 int quest_gb300_planPassUsesTensorCores(void* plan, int i);
 /* passes on 4..6 qubits run on the tensor cores (split-TF32) unless disabled
  * here (1 = enabled, the default; 0 = FP32 SIMT applier for k <= 5) */
 void quest_gb300_setTensorCores(int enabled);
-/* tensor-core kernel: 0 = chosen per pass (default: 4-qubit passes with every
- * target >= qubit 5 on the SIMT applier, every other 4..6-qubit pass on the
- * pipelined kernel with two loader groups), 1 = always the direct-load
- * kernel, 2 = always the pipelined kernel with two loader groups, 3 = always
- * the pipelined kernel with one loader group */
+/* tensor-core kernel: 0 = chosen per pass (default), 1 = always the
+ * direct-load kernel, 2..4 = always the pipelined kernel with 2 loader + 1
+ * epilogue warp groups (2), 1 + 1 (3) or 1 + 2 (4) */
 void quest_gb300_setTensorCoreKernel(int version);
 double quest_gb300_calcTotalProbF32(void* qureg32);
 double quest_gb300_calcProbOfOutcomeF32(void* qureg32, int measureQubit, int outcome);
@@ -103,6 +101,25 @@ void* quest_gb300_swapTestBatchCreate(const double* vectors, const long long* of
                                       int numVectors, const int* idxA, const int* idxB, int numTests);
 int quest_gb300_swapTestBatchRun(void* batch, double* p0Out);
 void quest_gb300_swapTestBatchDestroy(void* batch);
+
+/* ---- op-stream capture ------------------------------------------------------
+ * No counterpart in the reference.  With capture on for a register, its gate
+ * calls (every unitary/matrix/rotation/phase/NOT/swap/Pauli-rotation call and
+ * applyTrotterCircuit) are queued as dense FP64 matrices on the <= 6 qubits
+ * they touch instead of running; the first other call on the register (a
+ * reduction, measurement, copy, amplitude read, channel, ...) applies the
+ * queue through the fusion planner and the FP32 fused engine; calls that
+ * overwrite the whole state (init*, initStateFromAmps, copyStateToGPU, a
+ * cloneQureg target) drop it.  Results then carry the FP32 engine's precision.
+ * QUEST_GB300_CAPTURE=fp32 turns capture on for registers created afterwards. */
+/* mode 1: capture with FP32 fused flushes; 0: off (flushes what is queued).
+ * Returns 0, or -1 for an unallocated register. */
+int quest_gb300_setCapture(Qureg qureg, int mode);
+void quest_gb300_flushCapture(Qureg qureg);
+/* gates queued and not yet applied */
+int quest_gb300_capturedGates(Qureg qureg);
+/* widest fused pass of the flushes, 1..6 (default 6) */
+void quest_gb300_setCaptureFusion(int maxFusedQubits);
 
 /* ---- total probability without allocating ---------------------------------
  * No counterpart in the reference.  For callers that hold their own FP64

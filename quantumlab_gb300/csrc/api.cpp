@@ -295,7 +295,25 @@ struct MT19937 {
     double real1() { return (double)next() * (1.0 / 4294967295.0); }
 } g_mt;
 
-inline qg::SV sv(const Qureg& q) { return qg::svOf(q); }
+// State access of every call but the gates: the register's captured gates
+// (capture.cpp) are applied first.
+inline qg::SV sv(const Qureg& q) {
+    qg::captureFlush(q.deviceStateVec.real, q.deviceStateVec.imag);
+    return qg::svOf(q);
+}
+// State access of the gate calls: with capture on, the launchers queue the gate.
+inline qg::SV svg(const Qureg& q) {
+    qg::SV s = qg::svOf(q);
+    s.cap = qg::captureHandle(q.deviceStateVec.real);
+    return s;
+}
+// A call that overwrites the whole state: queued gates are dropped unapplied.
+inline qg::SV svOverwrite(const Qureg& q) {
+    qg::captureDiscard(q.deviceStateVec.real);
+    return qg::svOf(q);
+}
+inline void flushQ(const Qureg& q) { qg::captureFlush(q.deviceStateVec.real, q.deviceStateVec.imag); }
+inline void discardQ(const Qureg& q) { qg::captureDiscard(q.deviceStateVec.real); }
 inline bool syncStream(const char* caller) { return !QG_CUDA(cudaStreamSynchronize(qg::stream()), caller); }
 
 qg::Mat2 toMat(const ComplexMatrix2& u, bool conj) {
@@ -310,22 +328,22 @@ qg::Mat2 toMat(const ComplexMatrix2& u, bool conj) {
 
 // ---- gate helpers applying the density-matrix doubling -----------------------
 void applyCompact(const Qureg& q, int t, uint64_t ctrl, Complex a, Complex b) {
-    qg::gateCompact(sv(q), t, ctrl, a.real, a.imag, b.real, b.imag);
+    qg::gateCompact(svg(q), t, ctrl, a.real, a.imag, b.real, b.imag);
     if (q.isDensityMatrix) {
         const int s = q.numQubitsRepresented;
-        qg::gateCompact(sv(q), t + s, ctrl << s, a.real, -a.imag, b.real, -b.imag);
+        qg::gateCompact(svg(q), t + s, ctrl << s, a.real, -a.imag, b.real, -b.imag);
     }
 }
 void applyMatrix2Doubled(const Qureg& q, int t, uint64_t ctrl, uint64_t flip, const ComplexMatrix2& u) {
-    qg::gateMatrix2(sv(q), t, ctrl, flip, toMat(u, false));
+    qg::gateMatrix2(svg(q), t, ctrl, flip, toMat(u, false));
     if (q.isDensityMatrix) {
         const int s = q.numQubitsRepresented;
-        qg::gateMatrix2(sv(q), t + s, ctrl << s, flip << s, toMat(u, true));
+        qg::gateMatrix2(svg(q), t + s, ctrl << s, flip << s, toMat(u, true));
     }
 }
 void applyPhaseDoubled(const Qureg& q, uint64_t mask, double tr, double ti) {
-    qg::gatePhase(sv(q), mask, tr, ti);
-    if (q.isDensityMatrix) qg::gatePhase(sv(q), mask << q.numQubitsRepresented, tr, -ti);
+    qg::gatePhase(svg(q), mask, tr, ti);
+    if (q.isDensityMatrix) qg::gatePhase(svg(q), mask << q.numQubitsRepresented, tr, -ti);
 }
 void rotationPair(double angle, Vector axis, Complex* a, Complex* b) {  // QuEST_common.c:117-124
     const double mag = sqrt(axis.x * axis.x + axis.y * axis.y + axis.z * axis.z);
@@ -349,10 +367,10 @@ void applyPauliRotation(const Qureg& q, uint64_t ctrl, const int* ts, const enum
     uint64_t x, y, z;
     pauliMasks(ts, ps, n, &x, &y, &z);
     if ((x | z) == 0) return;                 // all identity: QuEST applies nothing (QuEST_common.c:430-431)
-    qg::gatePauliRotation(sv(q), ctrl, x, y, z, angle, 0);
+    qg::gatePauliRotation(svg(q), ctrl, x, y, z, angle, 0);
     if (q.isDensityMatrix) {
         const int s = q.numQubitsRepresented;
-        qg::gatePauliRotation(sv(q), ctrl << s, x << s, y << s, z << s, angle, 1);
+        qg::gatePauliRotation(svg(q), ctrl << s, x << s, y << s, z << s, angle, 1);
     }
 }
 void applyMatrixNDoubled(const Qureg& q, uint64_t ctrl, const int* ts, int k, qreal** ur, qreal** ui, bool doubled) {
@@ -363,13 +381,13 @@ void applyMatrixNDoubled(const Qureg& q, uint64_t ctrl, const int* ts, int k, qr
             mr[(size_t)r * D + c] = ur[r][c];
             mi[(size_t)r * D + c] = ui[r][c];
         }
-    qg::gateMatrixN(sv(q), ctrl, ts, k, mr.data(), mi.data());
+    qg::gateMatrixN(svg(q), ctrl, ts, k, mr.data(), mi.data());
     if (doubled && q.isDensityMatrix) {
         const int s = q.numQubitsRepresented;
         int sh[64];
         for (int i = 0; i < k; ++i) sh[i] = ts[i] + s;
         for (auto& v : mi) v = -v;
-        qg::gateMatrixN(sv(q), ctrl << s, sh, k, mr.data(), mi.data());
+        qg::gateMatrixN(svg(q), ctrl << s, sh, k, mr.data(), mi.data());
     }
 }
 
@@ -418,6 +436,7 @@ Qureg allocQureg(int nsv, int isDM, int nrep, const char* caller) {
     cudaMemsetAsync(scratch, 0, qg::kScratchDoubles * sizeof(double), qg::stream());
     q.deviceStateVec.real = dev;
     q.deviceStateVec.imag = dev + n;
+    qg::captureRegister(dev, nsv);
     q.stateVec.real = host;
     q.stateVec.imag = host + n;
     q.pairStateVec.real = nullptr;
@@ -557,6 +576,7 @@ Qureg createCloneQureg(Qureg src, QuESTEnv env) {
 void destroyQureg(Qureg q, QuESTEnv env) {
     (void)env;
     if (!q.deviceStateVec.real) return;
+    qg::captureDrop(q.deviceStateVec.real);
     cudaStreamSynchronize(qg::stream());
     bool pinned = true;
     {
@@ -574,6 +594,7 @@ void destroyQureg(Qureg q, QuESTEnv env) {
     cudaFreeHost(q.secondLevelReduction);
 }
 void copyStateToGPU(Qureg q) {
+    discardQ(q);
     cudaStream_t st = qg::stream();
     const size_t b = (size_t)q.numAmpsTotal * sizeof(double);
     if (QG_CUDA(cudaMemcpyAsync(q.deviceStateVec.real, q.stateVec.real, b, cudaMemcpyHostToDevice, st), "copyStateToGPU")) return;
@@ -581,6 +602,7 @@ void copyStateToGPU(Qureg q) {
     syncStream("copyStateToGPU");
 }
 void copyStateFromGPU(Qureg q) {
+    flushQ(q);
     cudaStream_t st = qg::stream();
     const size_t b = (size_t)q.numAmpsTotal * sizeof(double);
     if (QG_CUDA(cudaMemcpyAsync(q.stateVec.real, q.deviceStateVec.real, b, cudaMemcpyDeviceToHost, st), "copyStateFromGPU")) return;
@@ -590,6 +612,7 @@ void copyStateFromGPU(Qureg q) {
 void copySubstateToGPU(Qureg q, idx_t start, idx_t n) {
     const char* caller = "copySubstateToGPU";
     if (!vNumAmps(q, start, n, caller)) return;
+    flushQ(q);
     cudaStream_t st = qg::stream();
     const size_t b = (size_t)n * sizeof(double);
     if (QG_CUDA(cudaMemcpyAsync(q.deviceStateVec.real + start, q.stateVec.real + start, b, cudaMemcpyHostToDevice, st), caller)) return;
@@ -599,6 +622,7 @@ void copySubstateToGPU(Qureg q, idx_t start, idx_t n) {
 void copySubstateFromGPU(Qureg q, idx_t start, idx_t n) {
     const char* caller = "copySubstateFromGPU";
     if (!vNumAmps(q, start, n, caller)) return;
+    flushQ(q);
     cudaStream_t st = qg::stream();
     const size_t b = (size_t)n * sizeof(double);
     if (QG_CUDA(cudaMemcpyAsync(q.stateVec.real + start, q.deviceStateVec.real + start, b, cudaMemcpyDeviceToHost, st), caller)) return;
@@ -661,32 +685,34 @@ void initPauliHamil(PauliHamil h, qreal* coeffs, enum pauliOpType* codes) {
 }
 
 // ---- initialisation (QuEST.c:119-176) ----
-void initBlankState(Qureg q) { qg::stateFill(sv(q), 0.0, 0.0); }
+void initBlankState(Qureg q) { qg::stateFill(svOverwrite(q), 0.0, 0.0); }
 void initZeroState(Qureg q) {
-    qg::stateFill(sv(q), 0.0, 0.0);
+    qg::stateFill(svOverwrite(q), 0.0, 0.0);
     qg::stateSetOne(sv(q), 0, 1.0, 0.0);
 }
 void initPlusState(Qureg q) {
-    if (q.isDensityMatrix) qg::statePlusDM(sv(q), q.numQubitsRepresented);
-    else qg::stateFill(sv(q), 1.0 / sqrt((double)q.numAmpsTotal), 0.0);
+    if (q.isDensityMatrix) qg::statePlusDM(svOverwrite(q), q.numQubitsRepresented);
+    else qg::stateFill(svOverwrite(q), 1.0 / sqrt((double)q.numAmpsTotal), 0.0);
 }
 void initClassicalState(Qureg q, idx_t ind) {
     const char* caller = "initClassicalState";
     if (!REQUIRE(ind >= 0 && ind < (1LL << q.numQubitsRepresented), E_INVALID_STATE_INDEX)) return;
-    qg::stateFill(sv(q), 0.0, 0.0);
+    qg::stateFill(svOverwrite(q), 0.0, 0.0);
     const idx_t at = q.isDensityMatrix ? ind * ((1LL << q.numQubitsRepresented) + 1) : ind;
     qg::stateSetOne(sv(q), at, 1.0, 0.0);
 }
 void initPureState(Qureg q, Qureg pure) {
     const char* caller = "initPureState";
     if (!vSecondStateVec(pure, caller) || !vMatchDims(q, pure, caller)) return;
-    if (q.isDensityMatrix) qg::statePureDM(sv(q), pure.deviceStateVec.real, pure.deviceStateVec.imag, q.numQubitsRepresented);
+    flushQ(pure);
+    if (q.isDensityMatrix) qg::statePureDM(svOverwrite(q), pure.deviceStateVec.real, pure.deviceStateVec.imag, q.numQubitsRepresented);
     else cloneQureg(q, pure);
 }
-void initDebugState(Qureg q) { qg::stateDebug(sv(q)); }
+void initDebugState(Qureg q) { qg::stateDebug(svOverwrite(q)); }
 void setAmps(Qureg q, idx_t start, qreal* re, qreal* im, idx_t n) {
     const char* caller = "setAmps";
     if (!vStateVec(q, caller) || !vNumAmps(q, start, n, caller)) return;
+    flushQ(q);
     cudaStream_t st = qg::stream();
     if (QG_CUDA(cudaMemcpyAsync(q.deviceStateVec.real + start, re, n * sizeof(double), cudaMemcpyHostToDevice, st), caller)) return;
     if (QG_CUDA(cudaMemcpyAsync(q.deviceStateVec.imag + start, im, n * sizeof(double), cudaMemcpyHostToDevice, st), caller)) return;
@@ -694,6 +720,7 @@ void setAmps(Qureg q, idx_t start, qreal* re, qreal* im, idx_t n) {
 }
 void initStateFromAmps(Qureg q, qreal* re, qreal* im) {                 // QuEST.c:163 (no validation there either)
     const char* caller = "initStateFromAmps";
+    discardQ(q);
     cudaStream_t st = qg::stream();
     const size_t b = (size_t)q.numAmpsTotal * sizeof(double);
     if (QG_CUDA(cudaMemcpyAsync(q.deviceStateVec.real, re, b, cudaMemcpyHostToDevice, st), caller)) return;
@@ -706,6 +733,7 @@ void setDensityAmps(Qureg q, idx_t row, idx_t col, qreal* re, qreal* im, idx_t n
     if (!REQUIRE(n >= 0 && n <= q.numAmpsTotal, E_INVALID_NUM_AMPS)) return;
     const idx_t start = row + col * (1LL << q.numQubitsRepresented);
     if (!REQUIRE(n + start <= q.numAmpsTotal, E_INVALID_OFFSET_NUM_AMPS_QUREG)) return;
+    flushQ(q);
     cudaStream_t st = qg::stream();
     if (QG_CUDA(cudaMemcpyAsync(q.deviceStateVec.real + start, re, n * sizeof(double), cudaMemcpyHostToDevice, st), caller)) return;
     if (QG_CUDA(cudaMemcpyAsync(q.deviceStateVec.imag + start, im, n * sizeof(double), cudaMemcpyHostToDevice, st), caller)) return;
@@ -714,6 +742,8 @@ void setDensityAmps(Qureg q, idx_t row, idx_t col, qreal* re, qreal* im, idx_t n
 void cloneQureg(Qureg t, Qureg s) {
     const char* caller = "cloneQureg";
     if (!vMatchTypes(t, s, caller) || !vMatchDims(t, s, caller)) return;
+    flushQ(s);
+    if (t.deviceStateVec.real != s.deviceStateVec.real) discardQ(t);
     cudaStream_t st = qg::stream();
     const size_t b = (size_t)t.numAmpsTotal * sizeof(double);
     if (QG_CUDA(cudaMemcpyAsync(t.deviceStateVec.real, s.deviceStateVec.real, b, cudaMemcpyDeviceToDevice, st), caller)) return;
@@ -728,6 +758,7 @@ void setWeightedQureg(Complex f1, Qureg a, Complex f2, Qureg b, Complex fo, Qure
 // ---- amplitude access (QuEST.c:940-970, QuEST_gpu.cu:526-582) ----
 static Complex readAmp(const Qureg& q, idx_t i, const char* caller) {
     Complex c = {0, 0};
+    flushQ(q);
     cudaStream_t st = qg::stream();
     double* slot = q.secondLevelReduction + 8;
     if (QG_CUDA(cudaMemcpyAsync(slot, q.deviceStateVec.real + i, sizeof(double), cudaMemcpyDeviceToHost, st), caller)) return c;
@@ -770,20 +801,20 @@ Complex getDensityAmp(Qureg q, idx_t r, idx_t c) {
 void hadamard(Qureg q, int t) {                                           // QuEST.c:178
     const char* caller = "hadamard";
     if (!vTarget(q, t, caller)) return;
-    qg::gateHadamard(sv(q), t);
-    if (q.isDensityMatrix) qg::gateHadamard(sv(q), t + q.numQubitsRepresented);
+    qg::gateHadamard(svg(q), t);
+    if (q.isDensityMatrix) qg::gateHadamard(svg(q), t + q.numQubitsRepresented);
 }
 void pauliX(Qureg q, int t) {                                             // QuEST.c:438
     const char* caller = "pauliX";
     if (!vTarget(q, t, caller)) return;
-    qg::gateNot(sv(q), 0, 1ull << t);
-    if (q.isDensityMatrix) qg::gateNot(sv(q), 0, 1ull << (t + q.numQubitsRepresented));
+    qg::gateNot(svg(q), 0, 1ull << t);
+    if (q.isDensityMatrix) qg::gateNot(svg(q), 0, 1ull << (t + q.numQubitsRepresented));
 }
 void pauliY(Qureg q, int t) {                                             // QuEST.c:449
     const char* caller = "pauliY";
     if (!vTarget(q, t, caller)) return;
-    qg::gatePauliY(sv(q), t, 0, 1.0);
-    if (q.isDensityMatrix) qg::gatePauliY(sv(q), t + q.numQubitsRepresented, 0, -1.0);
+    qg::gatePauliY(svg(q), t, 0, 1.0);
+    if (q.isDensityMatrix) qg::gatePauliY(svg(q), t + q.numQubitsRepresented, 0, -1.0);
 }
 void pauliZ(Qureg q, int t) {
     const char* caller = "pauliZ";
@@ -849,26 +880,26 @@ void unitary(Qureg q, int t, ComplexMatrix2 u) {                          // QuE
 void applyMatrix2(Qureg q, int t, ComplexMatrix2 u) {                     // QuEST.c:1107 (no DM doubling)
     const char* caller = "applyMatrix2";
     if (!vTarget(q, t, caller)) return;
-    qg::gateMatrix2(sv(q), t, 0, 0, toMat(u, false));
+    qg::gateMatrix2(svg(q), t, 0, 0, toMat(u, false));
 }
 
 // ---- controlled gates ----
 void controlledNot(Qureg q, int c, int t) {                               // QuEST.c:530
     const char* caller = "controlledNot";
     if (!vControlTarget(q, c, t, caller)) return;
-    qg::gateNot(sv(q), 1ull << c, 1ull << t);
+    qg::gateNot(svg(q), 1ull << c, 1ull << t);
     if (q.isDensityMatrix) {
         const int s = q.numQubitsRepresented;
-        qg::gateNot(sv(q), 1ull << (c + s), 1ull << (t + s));
+        qg::gateNot(svg(q), 1ull << (c + s), 1ull << (t + s));
     }
 }
 void controlledPauliY(Qureg q, int c, int t) {                            // QuEST.c:568
     const char* caller = "controlledPauliY";
     if (!vControlTarget(q, c, t, caller)) return;
-    qg::gatePauliY(sv(q), t, 1ull << c, 1.0);
+    qg::gatePauliY(svg(q), t, 1ull << c, 1.0);
     if (q.isDensityMatrix) {
         const int s = q.numQubitsRepresented;
-        qg::gatePauliY(sv(q), t + s, 1ull << (c + s), -1.0);
+        qg::gatePauliY(svg(q), t + s, 1ull << (c + s), -1.0);
     }
 }
 void controlledPhaseShift(Qureg q, int a, int b, qreal angle) {           // QuEST.c:504
@@ -933,23 +964,23 @@ void multiControlledPhaseFlip(Qureg q, int* cs, int nc) {                 // QuE
 void multiQubitNot(Qureg q, int* ts, int nt) {                            // QuEST.c:542
     const char* caller = "multiQubitNot";
     if (!vMultiTargets(q, ts, nt, caller)) return;
-    qg::gateNot(sv(q), 0, maskOf(ts, nt));
-    if (q.isDensityMatrix) qg::gateNot(sv(q), 0, maskOf(ts, nt) << q.numQubitsRepresented);
+    qg::gateNot(svg(q), 0, maskOf(ts, nt));
+    if (q.isDensityMatrix) qg::gateNot(svg(q), 0, maskOf(ts, nt) << q.numQubitsRepresented);
 }
 void multiControlledMultiQubitNot(Qureg q, int* cs, int nc, int* ts, int nt) {   // QuEST.c:555
     const char* caller = "multiControlledMultiQubitNot";
     if (!vMultiControlsMultiTargets(q, cs, nc, ts, nt, caller)) return;
-    qg::gateNot(sv(q), maskOf(cs, nc), maskOf(ts, nt));
+    qg::gateNot(svg(q), maskOf(cs, nc), maskOf(ts, nt));
     if (q.isDensityMatrix) {
         const int s = q.numQubitsRepresented;
-        qg::gateNot(sv(q), maskOf(cs, nc) << s, maskOf(ts, nt) << s);
+        qg::gateNot(svg(q), maskOf(cs, nc) << s, maskOf(ts, nt) << s);
     }
 }
 void swapGate(Qureg q, int a, int b) {                                    // QuEST.c:629
     const char* caller = "swapGate";
     if (!vUniqueTargets(q, a, b, caller)) return;
-    qg::gateSwap(sv(q), a, b);
-    if (q.isDensityMatrix) qg::gateSwap(sv(q), a + q.numQubitsRepresented, b + q.numQubitsRepresented);
+    qg::gateSwap(svg(q), a, b);
+    if (q.isDensityMatrix) qg::gateSwap(svg(q), a + q.numQubitsRepresented, b + q.numQubitsRepresented);
 }
 void sqrtSwapGate(Qureg q, int a, int b) {                                // QuEST.c:641, QuEST_common.c:386
     const char* caller = "sqrtSwapGate";
@@ -1020,17 +1051,17 @@ void multiRotateZ(Qureg q, int* qs, int n, qreal angle) {                 // QuE
     const char* caller = "multiRotateZ";
     if (!vMultiTargets(q, qs, n, caller)) return;
     const uint64_t m = maskOf(qs, n);
-    qg::gateRotateZ(sv(q), 0, m, angle);
-    if (q.isDensityMatrix) qg::gateRotateZ(sv(q), 0, m << q.numQubitsRepresented, -angle);
+    qg::gateRotateZ(svg(q), 0, m, angle);
+    if (q.isDensityMatrix) qg::gateRotateZ(svg(q), 0, m << q.numQubitsRepresented, -angle);
 }
 void multiControlledMultiRotateZ(Qureg q, int* cs, int nc, int* ts, int nt, qreal angle) {   // QuEST.c:673
     const char* caller = "multiControlledMultiRotateZ";
     if (!vMultiControlsMultiTargets(q, cs, nc, ts, nt, caller)) return;
     const uint64_t c = maskOf(cs, nc), m = maskOf(ts, nt);
-    qg::gateRotateZ(sv(q), c, m, angle);
+    qg::gateRotateZ(svg(q), c, m, angle);
     if (q.isDensityMatrix) {
         const int s = q.numQubitsRepresented;
-        qg::gateRotateZ(sv(q), c << s, m << s, -angle);
+        qg::gateRotateZ(svg(q), c << s, m << s, -angle);
     }
 }
 void multiRotatePauli(Qureg q, int* ts, enum pauliOpType* ps, int n, qreal angle) {   // QuEST.c:691

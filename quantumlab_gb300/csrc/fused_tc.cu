@@ -110,6 +110,11 @@ __device__ __forceinline__ void tmemSt16(uint32_t taddr, const uint32_t (&v)[16]
         "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
         : "memory");
 }
+__device__ __forceinline__ void tmemSt8(uint32_t taddr, const uint32_t (&v)[8]) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr), "r"(v[0]),
+                 "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+                 : "memory");
+}
 __device__ __forceinline__ void tmemWaitSt() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tmemLd16(uint32_t taddr, uint32_t (&v)[16]) {
     asm volatile(
@@ -365,44 +370,53 @@ __global__ void __launch_bounds__(kThreadsTC, (KQ == 4 ? 4 : 1)) kApplyTC(float*
 // Warp-specialised kernel used for every tensor-core pass by default:
 //   LG loader groups of 4 warps: global -> registers (coalesced 16-byte
 //              loads of a whole chunk, issued one chunk ahead), registers ->
-//              shared memory (XOR swizzle), then each thread reads its tile
-//              column, splits it and writes Xh/Xl to the group's TMEM stage
-//              with tcgen05.st.  With LG = 2 the groups take alternate chunks,
-//              so two chunks of loads are in flight per SM;
-//   4 epilogue warps: tcgen05.ld of a finished accumulator, scale, swizzled
-//              shared-memory staging, coalesced 16-byte stores;
+//              shared memory in row order, then each thread reads its tile
+//              column back, splits it and writes Xh/Xl to the group's TMEM
+//              stage with tcgen05.st.  With LG = 2 the groups take alternate
+//              chunks, so two chunks of loads are in flight per SM;
+//   4 epilogue warps: tcgen05.ld of a finished accumulator, column-order
+//              stores to shared memory, row-order reads, coalesced 16-byte
+//              stores;
 //   1 warp:    TMEM allocation, the one-time TMA bulk copy of Gh/Gl, and the
 //              MMA issue loop (one thread).
 // TMEM holds two operand stages and two accumulators, so loading tile t+1,
 // multiplying tile t and storing tile t-1 overlap.  A tile is 128 groups
-// over the qubit set I = targets + the 7 lowest other qubits; I always
-// contains qubits [0, r) with r >= 7, so the tile is made of contiguous runs
-// of >= 128 amplitudes and every global access is coalesced whatever the
-// targets are.  The swizzle swz(p) = p ^ ((p >> 5) & 31) makes the row-order
-// writes conflict-free and the column-order reads conflict-free or 2-way.
-// It is linear over disjoint bit sets (swz(a | b) = swz(a) ^ swz(b)), so a
-// column address is swz(column bits) ^ swz(matrix-index bits): one XOR with
-// a per-pass constant.  For k = 6 a tile's K = 128 is split into two stages
-// (real rows, imaginary rows) so the operand stages and both accumulators
-// fit the 512 TMEM columns.
-// Instruction budget per amplitude (the kernel is issue-bound, not DRAM-
-// bound, when these loops are loose): load 1/4, store to staging 1, norm 1,
-// column read 2, split 2, epilogue scale + norm 2, staging 2, store 1/4.
+// (TMEM lanes) over the qubit set I = targets + the 7 lowest other qubits; I
+// always contains qubits [0, r) with r >= 7, so the tile is made of
+// contiguous runs of >= 128 amplitudes and every global access is coalesced
+// whatever the targets are.  For k = 6 a tile's K = 128 is split into two
+// stages (real rows, imaginary rows) so the operand stages and both
+// accumulators fit the 512 TMEM columns.
+//
+// Warp-local staging.  Warp w of a role owns TMEM lanes (groups) 32w..32w+31,
+// whose tile positions have the 6th and 7th column bits equal to w.  Each
+// warp stages, and reads back, only those positions, in its own buffers, so
+// the row <-> column transposition needs __syncwarp and no barrier across
+// warps.  A warp's positions are split into two parts of at most 1024
+// (k <= 5: the two planes; k = 6: the two halves by the top target bit, which
+// the region index puts in its top bit).  Inside a part, index q lives at
+// pad(q) = q + (q >> 5).  pad is additive over disjoint bit sets, so
+//   * a row access (q = 4 lane + i + 128 m) is pad(4 lane) + i + pad(128 m):
+//     a per-thread base plus an immediate offset, conflict-free;
+//   * a column access (group bits of the lane | bits of matrix index j) is
+//     pad(lane bits) + pad(j bits): one add of a per-pass constant, and
+//     conflict-free whenever the lane bits' positions differ mod 5 (2-way at
+//     worst otherwise).
 constexpr int kTileBitsC = 7;
+
+__host__ __device__ constexpr uint32_t padIdx(uint32_t q) { return q + (q >> 5); }
 
 template <int KQ>
 struct TC2Params {
-    uint64_t scatterHigh[1 << KQ];   // address bits of the tile-index bits above the low run
-    uint32_t sj[1 << KQ];            // swz(tile-index bits of matrix index j)
-    int pcPos[kTileBitsC];           // tile-index positions of the column bits
-    int insI[KQ + kTileBitsC];       // ascending qubits of I
-    int runBits;                     // I contains qubits [0, runBits)
+    uint64_t scatterHigh[1 << KQ];        // address bits of the tile-position bits above the low run
+    uint64_t warpOff[4][1 << (KQ - 2)];   // amplitude offset of region index 128 m of warp w
+    uint64_t laneOff[32];                 // amplitude offset of region index 4 lane
+    uint32_t colLane[32];                 // pad(in-part index of the group bits of lane l)
+    uint32_t colJ[1 << KQ];               // pad(in-part index of the position bits of matrix index j)
+    int insI[KQ + kTileBitsC];            // ascending qubits of I
+    int runBits;                          // I contains qubits [0, runBits)
 };
 
-__device__ __forceinline__ void namedBar(int id, int count) {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
-__device__ __forceinline__ uint32_t swz(uint32_t q) { return q ^ ((q >> 5) & 31u); }
 __device__ __forceinline__ void mbarArrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smemAddr(bar)) : "memory");
 }
@@ -421,6 +435,12 @@ __device__ __forceinline__ bool mbarWaitOrAbort(uint64_t* bar, uint32_t parity, 
         if ((i & 15) == 0 && (*abortF || globalTimerNs() - t0 > kWaitLimitNs)) return false;
     }
 }
+// the same wait for a whole warp: lane 0 polls, the result goes to every lane
+__device__ __forceinline__ bool warpWaitOrAbort(uint64_t* bar, uint32_t parity, volatile int* abortF, int lane) {
+    int ok = 1;
+    if (lane == 0) ok = mbarWaitOrAbort(bar, parity, abortF) ? 1 : 0;
+    return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
 
 // amplitude offset of the first amplitude of a tile: the tile index bits go,
 // in order, to the qubits outside I
@@ -435,18 +455,8 @@ __device__ __forceinline__ uint64_t tileBase(const TC2Params<KQ>& p, uint64_t ti
     return tb;
 }
 
-// swz of the column bits of tile column c (thread c of a role)
-template <int KQ>
-__device__ __forceinline__ uint32_t swzColumn(const TC2Params<KQ>& p, int c) {
-    uint32_t pc = 0;
-#pragma unroll
-    for (int b = 0; b < kTileBitsC; ++b)
-        if (c >> b & 1) pc |= 1u << p.pcPos[b];
-    return swz(pc);
-}
-
-template <int KQ, int LG>
-__global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restrict__ re, float* __restrict__ im,
+template <int KQ, int LG, int EG>
+__global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* __restrict__ re, float* __restrict__ im,
                                                                   const float* __restrict__ gImage, uint64_t numTiles,
                                                                   int* __restrict__ errFlag, const NormLinks nl,
                                                                   const __grid_constant__ TC2Params<KQ> p) {
@@ -455,39 +465,35 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
     constexpr int TILE = 1 << (KQ + kTileBitsC);         // amplitudes per plane per tile
     constexpr int NCH = (KQ == 6) ? 2 : 1;               // K stages per tile
     constexpr int KC = K / NCH;                          // K columns per stage (<= 64)
-    constexpr int PLS = (NCH == 2) ? 1 : 2;              // planes per stage
-    constexpr int EPASS = (NCH == 2) ? 2 : 1;            // epilogue passes (one plane each for k = 6)
     constexpr uint32_t kGFloats = (uint32_t)N * K;
-    constexpr uint32_t kXFloats = (uint32_t)TILE * PLS;
+    constexpr int PART = (KQ == 6) ? TILE / 8 : TILE / 4;   // positions per warp per part (<= 1024)
+    constexpr int V4P = PART / 128;                      // 16-byte accesses per lane per part
+    constexpr int JP = (KQ == 6) ? 32 : D;               // matrix indices per part
+    constexpr int EPARTS = (KQ == 6) ? 4 : 2;            // epilogue parts per tile (plane x half)
+    constexpr int R = (int)((padIdx(PART - 1) + 1 + 3) & ~3u);   // floats per part buffer
     constexpr uint32_t kStageCols = 2 * KC;
     constexpr uint32_t kDCol0 = 2 * kStageCols;
     constexpr uint32_t kUsed = kDCol0 + 2 * N;
     constexpr uint32_t kCols = kUsed <= 64 ? 64 : (kUsed <= 128 ? 128 : (kUsed <= 256 ? 256 : 512));
     constexpr uint32_t kLBO = 128, kSBO = (K / 4) * 128;
     constexpr uint32_t idesc = idescTF32(kTile, N);
-    constexpr int V4 = TILE / 4 / 128;                   // 16-byte accesses per thread per plane
-    constexpr int kEpiWarp0 = 4 * LG, kMmaWarp = 4 * LG + 4;
-    constexpr int kEpiBar = 1 + LG;                      // named barrier ids: loaders 1..LG, epilogue LG + 1
+    constexpr int kEpiWarp0 = 4 * LG, kMmaWarp = 4 * (LG + EG);
 
-    extern __shared__ __align__(128) uint8_t smem[];
+    extern __shared__ __align__(1024) uint8_t smem[];
     float* gh = reinterpret_cast<float*>(smem);
     float* gl = gh + kGFloats;
-    float* xs = gl + kGFloats;                           // 2 stage buffers
-    float* es = xs + 2 * kXFloats;                       // epilogue staging
+    float* xs = gl + kGFloats;                           // [loader group][warp][part][R]
+    float* es = xs + LG * 4 * 2 * R;                     // [epilogue group][warp][R]
     __shared__ __align__(8) uint64_t barG, gReady, fullB[2], emptyB[2], dFullB[2], dEmptyB[2];
-    // offTab[w][m]: amplitude offset of tile position 128 w + 512 m (the
-    // 16-byte access m of warp w of a role; its lanes add 4 * lane)
-    __shared__ uint64_t offTab[4][V4];
     __shared__ uint32_t tmemBase;
     __shared__ volatile int abortF;
-    __shared__ int roleOk[LG + 1];
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == kMmaWarp) {
         if (lane == 0) {
             abortF = 0;
             mbarInit(&barG, 1);
-            mbarInit(&gReady, 128);
+            mbarInit(&gReady, 128 * EG);
             for (int b = 0; b < 2; ++b) {
                 mbarInit(&fullB[b], 128);
                 mbarInit(&emptyB[b], 1);
@@ -496,40 +502,41 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
             }
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
-        for (int i = lane; i < 4 * V4; i += 32) {
-            const uint32_t q = 128u * (i / V4) + 512u * (i % V4);
-            offTab[i / V4][i % V4] = (uint64_t)(q & ((1u << p.runBits) - 1u)) | p.scatterHigh[q >> p.runBits];
-        }
         tmemAlloc(&tmemBase, kCols);
     }
     fenceBefore();
     __syncthreads();
     fenceAfter();
     const uint32_t tmem = tmemBase;
+    const int rw = warp & 3;                             // warp within its role = TMEM lane quarter
+    const uint32_t laneSel = (uint32_t)(32 * rw) << 16;
+    const uint32_t rowBase = 4u * lane + (uint32_t)(lane >> 3);      // pad(4 lane)
 
     if (warp < kEpiWarp0) {
         // ------------------------------------------------ loaders
         const int g = warp >> 2;
-        const int lt = threadIdx.x - 128 * g;            // tile column = TMEM lane
-        const int lw = lt >> 5;
-        const uint32_t colSw = swzColumn(p, lt);
-        const uint32_t sb0 = (4u * lt) ^ (uint32_t)(lt >> 3), sb1 = sb0 ^ 16u;   // swz(4 lt + 512 m + i) = (sb ^ i) + 512 m
-        const uint32_t laneSel = (uint32_t)(32 * lw) << 16;
+        const uint64_t laneA = p.laneOff[lane];
+        const uint32_t colBase = p.colLane[lane];
         // this CTA's chunks, in order: chunk s = (tile blockIdx.x + (s / NCH) * gridDim.x, K stage s % NCH);
         // group g takes s = g, g + LG, ...
         const uint32_t nMy = blockIdx.x < numTiles ? (uint32_t)((numTiles - 1 - blockIdx.x) / gridDim.x + 1) * NCH : 0u;
         double normIn = 0.0;
         const bool measure = nl.in != nullptr;             // input norm wanted (uniform)
-        float4 v[PLS][V4];
+        // a chunk's two parts: k <= 5 the real and imaginary planes, k = 6 the
+        // two halves (region indices 128 m, m < 8 and m >= 8) of one plane
+        float4 v[2][V4P];
         auto issue = [&](uint32_t sc) {
             const uint64_t tile = blockIdx.x + (uint64_t)(sc / NCH) * gridDim.x;
             const int ch = sc % NCH;
-            const uint64_t tb = tileBase(p, tile) + 4u * lane;
+            const uint64_t tb = tileBase(p, tile) + laneA;
 #pragma unroll
-            for (int pl = 0; pl < PLS; ++pl) {
-                const float* src = (((NCH == 2) ? ch : pl) == 0 ? re : im) + tb;
+            for (int pt = 0; pt < 2; ++pt) {
+                const float* src = (((NCH == 2) ? ch : pt) == 0 ? re : im) + tb;
 #pragma unroll
-                for (int m = 0; m < V4; ++m) v[pl][m] = __ldcs(reinterpret_cast<const float4*>(src + offTab[lw][m]));
+                for (int mm = 0; mm < V4P; ++mm) {
+                    const int m = (KQ == 6) ? V4P * pt + mm : mm;
+                    v[pt][mm] = __ldcs(reinterpret_cast<const float4*>(src + p.warpOff[rw][m]));
+                }
             }
         };
         if (nMy > (uint32_t)g) issue(g);
@@ -537,93 +544,77 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
         for (uint32_t sq = g; sq < nMy; sq += LG) {
             const int b = (LG == 2) ? g : (int)(sq & 1);      // the stage (group g owns stage g when LG = 2)
             const uint32_t u = sq >> 1;
-            if (lt == 0) roleOk[g] = (u == 0) || mbarWaitOrAbort(&emptyB[b], (u - 1) & 1, &abortF);
-            namedBar(1 + g, 128);
-            if (!roleOk[g]) {
+            if (u > 0 && !warpWaitOrAbort(&emptyB[b], (u - 1) & 1, &abortF, lane)) {
                 ok = false;
                 break;
             }
-            float* xb = xs + b * kXFloats;
+            float* const xr = xs + (size_t)(g * 4 + rw) * 2 * R;   // the group's warp buffer (one chunk at a time)
             {
-                // pointer bases, so that the plane and 512 m strides become
-                // immediate offsets of the shared stores
-                float* const e0 = xb + (sb0 ^ 0u);
-                float* const e1 = xb + (sb0 ^ 1u);
-                float* const e2 = xb + (sb0 ^ 2u);
-                float* const e3 = xb + (sb0 ^ 3u);
-                float* const o0 = xb + (sb1 ^ 0u);
-                float* const o1 = xb + (sb1 ^ 1u);
-                float* const o2 = xb + (sb1 ^ 2u);
-                float* const o3 = xb + (sb1 ^ 3u);
+                float* const rb = xr + rowBase;
 #pragma unroll
-                for (int pl = 0; pl < PLS; ++pl)
+                for (int pt = 0; pt < 2; ++pt)
 #pragma unroll
-                    for (int m = 0; m < V4; ++m) {
-                        const int off = pl * TILE + 512 * m;
-                        const float4 x = v[pl][m];
-                        (m & 1 ? o0 : e0)[off] = x.x;
-                        (m & 1 ? o1 : e1)[off] = x.y;
-                        (m & 1 ? o2 : e2)[off] = x.z;
-                        (m & 1 ? o3 : e3)[off] = x.w;
+                    for (int m = 0; m < V4P; ++m) {
+                        const int off = pt * R + (int)padIdx(128u * m);
+                        const float4 x = v[pt][m];
+                        rb[off + 0] = x.x;
+                        rb[off + 1] = x.y;
+                        rb[off + 2] = x.z;
+                        rb[off + 3] = x.w;
                     }
             }
             if (measure) {
                 float nrm = 0.f;
 #pragma unroll
-                for (int pl = 0; pl < PLS; ++pl)
+                for (int pt = 0; pt < 2; ++pt)
 #pragma unroll
-                    for (int m = 0; m < V4; ++m) {
-                        const float4 x = v[pl][m];
+                    for (int m = 0; m < V4P; ++m) {
+                        const float4 x = v[pt][m];
                         nrm = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, nrm))));
                     }
                 normIn += (double)nrm;
             }
-            namedBar(1 + g, 128);
+            __syncwarp();
             if (sq + LG < nMy) issue(sq + LG);               // next chunk's loads fly during the split below
             const uint32_t aH = tmem + laneSel + b * kStageCols;
+            const float* const cb = xr + colBase;
 #pragma unroll
-            for (int c0 = 0; c0 < KC; c0 += 16) {
-                uint32_t hi[16], lo[16];
+            for (int c0 = 0; c0 < KC; c0 += 8) {
+                uint32_t hi[8], lo[8];
 #pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                    const int kl = c0 + e;
-                    const int pl = (NCH == 2) ? 0 : kl / D;
+                for (int e = 0; e < 8; ++e) {
+                    const int kl = c0 + e;                   // stage column: part kl / JP
+                    const int pl = kl / JP;
                     const int j = (NCH == 2) ? kl : kl % D;
                     // hi = x rounded to TF32; lo = x - hi (exact), which the
                     // MMA reads as its leading TF32 bits; lo takes both signs,
                     // so that truncation is unbiased
-                    const float x = (xb + pl * TILE)[colSw ^ p.sj[j]];
+                    const float x = (cb + pl * R)[p.colJ[j]];
                     hi[e] = tf32Bits(x);
                     lo[e] = __float_as_uint(x - __uint_as_float(hi[e]));
                 }
-                tmemSt16(aH + c0, hi);
-                tmemSt16(aH + KC + c0, lo);
+                tmemSt8(aH + c0, hi);
+                tmemSt8(aH + KC + c0, lo);
             }
             tmemWaitSt();
             fenceBefore();
             mbarArrive(&fullB[b]);
+            __syncwarp();                                    // column reads done before the region is rewritten
         }
         if (!ok) {
-            if (lt == 0) atomicExch(errFlag, 3);
+            if (lane == 0) atomicExch(errFlag, 3);
             abortF = 1;
         }
         normIn = warpSumD(normIn);
         if (lane == 0 && measure) atomicAdd(nl.in, normIn);
     } else if (warp < kMmaWarp) {
         // ------------------------------------------------ epilogue
+        // epilogue group eg drains accumulator eg, i.e. tiles tl with tl % EG == eg
         const int et = threadIdx.x - 32 * kEpiWarp0;
-        const int ew = et >> 5;
-        const uint32_t colSw = swzColumn(p, et);
-        const uint32_t sb0 = (4u * et) ^ (uint32_t)(et >> 3), sb1 = sb0 ^ 16u;
-        const float* const ee0 = es + (sb0 ^ 0u);
-        const float* const ee1 = es + (sb0 ^ 1u);
-        const float* const ee2 = es + (sb0 ^ 2u);
-        const float* const ee3 = es + (sb0 ^ 3u);
-        const float* const eo0 = es + (sb1 ^ 0u);
-        const float* const eo1 = es + (sb1 ^ 1u);
-        const float* const eo2 = es + (sb1 ^ 2u);
-        const float* const eo3 = es + (sb1 ^ 3u);
-        const uint32_t laneSel = (uint32_t)(32 * ew) << 16;
+        const int eg = et >> 7;
+        const uint64_t laneA = p.laneOff[lane];
+        const uint32_t colBase = p.colLane[lane];
+        float* const er = es + (size_t)(eg * 4 + rw) * R;
         // the previous pass's drift correction, folded into this pass's G:
         // G' = (1 + sm1) (Gh + Gl), split again into TF32 parts (the sum of
         // the two parts is exact in FP32)
@@ -631,73 +622,70 @@ __global__ void __launch_bounds__((4 * LG + 5) * 32, 1) kApplyTC2(float* __restr
         const float sm1 = driftCorrection(nl);
         recordScale(nl, sm1, blockIdx.x == 0 && et == 0);
         if (ok && sm1 != 0.f) {
-            for (uint32_t i = et; i < kGFloats; i += 128) {
+            for (uint32_t i = et; i < kGFloats; i += 128 * EG) {
                 const float g0 = gh[i] + gl[i];
-                const float g = fmaf(g0, sm1, g0);
-                const uint32_t h = tf32Bits(g);
+                const float g1 = fmaf(g0, sm1, g0);
+                const uint32_t h = tf32Bits(g1);
                 gh[i] = __uint_as_float(h);
-                gl[i] = __uint_as_float(tf32Bits(g - __uint_as_float(h)));
+                gl[i] = __uint_as_float(tf32Bits(g1 - __uint_as_float(h)));
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // visible to the MMAs
         }
         mbarArrive(&gReady);
-        uint32_t tl = 0;
+        uint32_t tl = eg;
         double normOut = 0.0;
-        for (uint64_t tile = blockIdx.x; tile < numTiles && ok; tile += gridDim.x, ++tl) {
-            const uint64_t tb = tileBase(p, tile) + 4u * lane;
+        for (uint64_t tile = blockIdx.x + (uint64_t)eg * gridDim.x; tile < numTiles && ok;
+             tile += (uint64_t)EG * gridDim.x, tl += EG) {
+            const uint64_t tb = tileBase(p, tile) + laneA;
             const int bd = tl & 1;
-            if (et == 0) roleOk[LG] = mbarWaitOrAbort(&dFullB[bd], (tl >> 1) & 1, &abortF);
-            namedBar(kEpiBar, 128);
-            if (!roleOk[LG]) {
+            if (!warpWaitOrAbort(&dFullB[bd], (tl >> 1) & 1, &abortF, lane)) {
                 ok = false;
                 break;
             }
             fenceAfter();
             const uint32_t dA = tmem + laneSel + kDCol0 + bd * N;
             float nrmTile = 0.f;
+            float* const cb = er + colBase;
+            const float* const rb = er + rowBase;
 #pragma unroll
-            for (int pe = 0; pe < EPASS; ++pe) {
-                constexpr int COLS = N / EPASS;
-#pragma unroll
-                for (int c0 = 0; c0 < COLS; c0 += 32) {
-                    uint32_t va[16], vb[16];
-                    tmemLd16(dA + pe * COLS + c0, va);
-                    tmemLd16(dA + pe * COLS + c0 + 16, vb);
-                    tmemWaitLd();
-#pragma unroll
-                    for (int e = 0; e < 32; ++e) {
-                        const int col = pe * COLS + c0 + e;           // output row index r in [0, 2D)
-                        const int plLocal = (EPASS == 2) ? 0 : col / D;
-                        const float y = __uint_as_float(e < 16 ? va[e] : vb[e - 16]);
-                        nrmTile = fmaf(y, y, nrmTile);
-                        (es + plLocal * TILE)[colSw ^ p.sj[col % D]] = y;
-                    }
-                }
-                if (pe == EPASS - 1) {                                // accumulator drained
+            for (int ep = 0; ep < EPARTS; ++ep) {
+                // part ep: plane pl (output rows r = pl * D + j), matrix indices j = h * 32 + jj
+                const int pl = (KQ == 6) ? ep >> 1 : ep;
+                const int h = (KQ == 6) ? ep & 1 : 0;
+                const int c0 = pl * D + h * 32;
+                uint32_t va[16], vb[16];
+                tmemLd16(dA + c0, va);
+                if (JP == 32) tmemLd16(dA + c0 + 16, vb);
+                tmemWaitLd();
+                if (ep == EPARTS - 1) {                              // accumulator drained
                     fenceBefore();
                     mbarArrive(&dEmptyB[bd]);
                 }
-                namedBar(kEpiBar, 128);
 #pragma unroll
-                for (int pl = 0; pl < 2 / EPASS; ++pl) {
-                    float* dstPlane = (((EPASS == 2) ? pe : pl) == 0 ? re : im) + tb;
-#pragma unroll
-                    for (int m = 0; m < V4; ++m) {
-                        const int off = pl * TILE + 512 * m;
-                        float4 w;
-                        w.x = (m & 1 ? eo0 : ee0)[off];
-                        w.y = (m & 1 ? eo1 : ee1)[off];
-                        w.z = (m & 1 ? eo2 : ee2)[off];
-                        w.w = (m & 1 ? eo3 : ee3)[off];
-                        __stcs(reinterpret_cast<float4*>(dstPlane + offTab[ew][m]), w);
-                    }
+                for (int e = 0; e < JP; ++e) {
+                    const float y = __uint_as_float(e < 16 ? va[e] : vb[e - 16]);
+                    nrmTile = fmaf(y, y, nrmTile);
+                    cb[p.colJ[h * 32 + e]] = y;
                 }
-                namedBar(kEpiBar, 128);
+                __syncwarp();
+                float* const dstPlane = (pl == 0 ? re : im) + tb;
+#pragma unroll
+                for (int mm = 0; mm < V4P; ++mm) {
+                    const int off = (int)padIdx(128u * mm);
+                    const int m = (KQ == 6) ? V4P * h + mm : mm;
+                    float4 w;
+                    w.x = rb[off + 0];
+                    w.y = rb[off + 1];
+                    w.z = rb[off + 2];
+                    w.w = rb[off + 3];
+                    __stcs(reinterpret_cast<float4*>(dstPlane + p.warpOff[rw][m]), w);
+                }
+                __syncwarp();
             }
             normOut += (double)nrmTile;
         }
         if (!ok) {
-            if (et == 0) atomicExch(errFlag, 4);
+            if (lane == 0) atomicExch(errFlag, 4);
             abortF = 1;
         }
         normOut = warpSumD(normOut);
@@ -845,19 +833,18 @@ bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* i
 }
 
 
-uint32_t hostSwz(uint32_t q) { return q ^ ((q >> 5) & 31u); }
-
-template <int KQ, int LG>
+template <int KQ, int LG, int EG>
 bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, const NormLinks& nl,
                cudaStream_t st) {
     constexpr int D = 1 << KQ;
     constexpr int K = 2 * D, N = 2 * D;
     constexpr int TILE = 1 << (KQ + kTileBitsC);
-    constexpr int PLS = (KQ == 6) ? 1 : 2;
-    constexpr int EPASS = (KQ == 6) ? 2 : 1;
-    const size_t smem = ((size_t)2 * N * K + 2 * (size_t)TILE * PLS + (size_t)TILE * (2 / EPASS)) * 4 + 128;
+    constexpr int PART = (KQ == 6) ? TILE / 8 : TILE / 4;
+    constexpr int R = (int)((padIdx(PART - 1) + 1 + 3) & ~3u);
+    constexpr int V4 = TILE / 512;
+    const size_t smem = ((size_t)2 * N * K + (size_t)LG * 4 * 2 * R + (size_t)EG * 4 * R) * 4;
     TC2Params<KQ> p{};
-    // I = targets + the 7 lowest other qubits (ascending)
+    // I = targets + the 7 lowest other qubits (ascending); tile position b <-> qubit I[b]
     uint64_t tmask = 0;
     for (int b = 0; b < KQ; ++b) tmask |= 1ull << pass.targets[b];
     uint64_t imask = tmask;
@@ -880,32 +867,68 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
             if (h >> i & 1u) a |= 1ull << I[run + i];
         p.scatterHigh[h] = a;
     }
+    // amplitude offset of a tile position
+    auto addrOf = [&](uint32_t pos) -> uint64_t {
+        return (uint64_t)(pos & ((1u << run) - 1u)) | p.scatterHigh[pos >> run];
+    };
     int posOf[64];
     for (int b = 0; b < ni; ++b) posOf[I[b]] = b;
+    int pcPos[kTileBitsC];
+    for (int b = 0, m = 0; b < ni; ++b)
+        if (!(tmask >> I[b] & 1ull)) pcPos[m++] = b;
+    // warp regions: the positions whose bits pcPos[5], pcPos[6] equal the warp
+    // index.  Region index = the position with those two bits removed, the
+    // others in ascending order, except at k = 6 the top target bit, which goes
+    // to the top (it selects the part)
+    const int P5 = pcPos[5], P6 = pcPos[6];
+    const int J5 = (KQ == 6) ? posOf[pass.targets[5]] : -1;
+    int order[24], no = 0;
+    for (int b = 0; b < ni; ++b)
+        if (b != P5 && b != P6 && b != J5) order[no++] = b;
+    if (KQ == 6) order[no++] = J5;
+    auto compress = [&](uint32_t pos) -> uint32_t {
+        uint32_t q = 0;
+        for (int o = 0; o < no; ++o)
+            if (pos >> order[o] & 1u) q |= 1u << o;
+        return q;
+    };
+    auto deposit = [&](uint32_t q) -> uint32_t {
+        uint32_t pos = 0;
+        for (int o = 0; o < no; ++o)
+            if (q >> o & 1u) pos |= 1u << order[o];
+        return pos;
+    };
+    for (int w = 0; w < 4; ++w)
+        for (int m = 0; m < V4; ++m)
+            p.warpOff[w][m] = addrOf(deposit(128u * m) | ((uint32_t)(w & 1) << P5) | ((uint32_t)(w >> 1) << P6));
+    for (int l = 0; l < 32; ++l) {
+        p.laneOff[l] = addrOf(deposit(4u * l));
+        uint32_t pc = 0;
+        for (int b = 0; b < 5; ++b)
+            if (l >> b & 1) pc |= 1u << pcPos[b];
+        p.colLane[l] = padIdx(compress(pc) % PART);
+    }
     for (int j = 0; j < D; ++j) {
         uint32_t v = 0;
         for (int b = 0; b < KQ; ++b)
             if (j >> b & 1) v |= 1u << posOf[pass.targets[b]];
-        p.sj[j] = hostSwz(v);
+        p.colJ[j] = padIdx(compress(v) % PART);
     }
-    for (int b = 0, m = 0; b < ni; ++b)
-        if (!(tmask >> I[b] & 1ull)) p.pcPos[m++] = b;
     const uint64_t numTiles = 1ull << (n - KQ - kTileBitsC);
-    static bool configured[8][3] = {};
-    if (!configured[KQ][LG]) {
-        if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ, LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+    static bool configured = false;
+    if (!configured) {
+        if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ, LG, EG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "applyPlanF32"))
             return false;
-        configured[KQ][LG] = true;
+        configured = true;
     }
     const uint64_t grid = std::min<uint64_t>(numTiles, (uint64_t)numSMs());
-    kApplyTC2<KQ, LG><<<(unsigned)grid, (4 * LG + 5) * 32, smem, st>>>(re, im, img, numTiles, errFlag, nl, p);
+    kApplyTC2<KQ, LG, EG><<<(unsigned)grid, (4 * (LG + EG) + 1) * 32, smem, st>>>(re, im, img, numTiles, errFlag, nl, p);
     return !launchFailed("applyPlanF32");
 }
 
 bool g_tcEnabled = true;
 int g_tcVersion = 0;      // 0: per pass by target layout; 1, 2, 3: force one kernel
-bool g_tcChecked = false;
 
 }  // namespace
 
@@ -990,19 +1013,22 @@ void tcNoteSimtPass(void* devPlan, size_t index) {
 }
 
 // Which applier runs a pass on registers of n qubits: 0 = the FP32 SIMT
-// applier, 1 = the direct-load tensor-core kernel, 2 / 3 = the pipelined one
-// with two / one loader groups.  Default choice (measured at 30 qubits, ms
-// per pass): passes on 1..3 qubits and 4-qubit passes whose targets are all
-// at or above qubit 5 run on the SIMT applier (3.2 ms against 3.7 ms for the
-// direct-load kernel: every lane's group is part of a coalesced warp line and
-// the multiply is cheap); the other 4-qubit passes (SIMT 9.0 ms) and all 5-
-// and 6-qubit passes run on the pipelined kernel, whose shared-memory staging
-// keeps them coalesced.
+// applier, 1 = the direct-load tensor-core kernel, 2 / 3 / 4 = the pipelined
+// one with 2+1 / 1+1 / 1+2 loader + epilogue warp groups.  Default choice
+// (measured at 30 qubits, ms per pass): passes on 1..3 qubits and 4-qubit
+// passes whose targets are all at or above qubit 5 run on the SIMT applier
+// (3.2 ms: every lane's group is part of a coalesced warp line and the
+// multiply is cheap); the other 4-qubit passes (SIMT 9.0 ms, pipelined 3.1)
+// and the 5-qubit passes run on the pipelined kernel with two loader groups
+// (2.6-3.2 ms; its loaders are the busier role); 6-qubit passes run on the
+// one with two epilogue groups (3.3-3.8 ms against 3.7-4.1; the epilogue's
+// staging is the busier role at 2 x 128 output values per group).
 int tcKernelFor(const FusedPass& pass, int n) {
     const int k = (int)pass.targets.size();
     if (!g_tcEnabled || k < 4 || k > 6 || n < k + 7) return 0;
     if (g_tcVersion != 0) return g_tcVersion;
-    return (k == 4 && pass.targets[0] >= 5) ? 0 : 2;
+    if (k == 4 && pass.targets[0] >= 5) return 0;
+    return k == 6 ? 4 : 2;
 }
 
 // explicit entry used by the FP32 engine with the pass index: 1 = applied on
@@ -1035,16 +1061,18 @@ int applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, 
     }
     bool ok = false;
     if (version >= 2) {
-        const bool two = version == 2;       // 2: two loader groups, 3: one
+        // 2: two loader groups + one epilogue group; 3: one + one; 4: one + two
+#define QG_TC2(KQ)                                                                                     \
+    (version == 2   ? launchTC2<KQ, 2, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)     \
+     : version == 3 ? launchTC2<KQ, 1, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)     \
+                    : launchTC2<KQ, 1, 2>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st))
         switch (k) {
-            case 4: ok = two ? launchTC2<4, 2>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)
-                             : launchTC2<4, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st); break;
-            case 5: ok = two ? launchTC2<5, 2>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)
-                             : launchTC2<5, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st); break;
-            case 6: ok = two ? launchTC2<6, 2>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)
-                             : launchTC2<6, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st); break;
+            case 4: ok = QG_TC2(4); break;
+            case 5: ok = QG_TC2(5); break;
+            case 6: ok = QG_TC2(6); break;
             default: return 0;
         }
+#undef QG_TC2
     } else {
         switch (k) {
             case 4: ok = launchTC<4>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st); break;
@@ -1069,7 +1097,7 @@ int tcErrorFlag(const void* devPlan) {
 }
 
 void setTensorCoresEnabled(bool on) { g_tcEnabled = on; }
-void setTensorCoreKernel(int version) { g_tcVersion = (version >= 1 && version <= 3) ? version : 0; }
+void setTensorCoreKernel(int version) { g_tcVersion = (version >= 1 && version <= 4) ? version : 0; }
 bool tensorCoresEnabled() { return g_tcEnabled; }
 
 }  // namespace qg

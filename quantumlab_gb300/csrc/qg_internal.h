@@ -46,8 +46,25 @@ struct SV {
     double* re;
     double* im;
     int n;                      // qubits in the state vector (2N for a density matrix)
+    void* cap = nullptr;        // capture record: gate launchers queue the gate instead (capture.cpp)
 };
 inline SV svOf(const Qureg& q) { return SV{q.deviceStateVec.real, q.deviceStateVec.imag, q.numQubitsInStateVec}; }
+
+// ---- op-stream capture (capture.cpp) ----------------------------------------
+void* captureHandle(const double* re);            // the register's capture record, or null
+void captureRegister(const double* re, int n);    // at creation: capture on if QUEST_GB300_CAPTURE=fp32
+void captureFlush(double* re, double* im);        // apply the queued gates (FP32 fused engine)
+void captureDiscard(const double* re);            // drop the queued gates (the state is overwritten next)
+void captureDrop(const double* re);               // at destruction
+// launcher hooks: queue the gate and return true, or return false (after a
+// flush) when it touches more than 6 qubits
+bool capturePair(SV s, int target, uint64_t ctrl, uint64_t flip, const double ur[4], const double ui[4]);
+bool captureNot(SV s, uint64_t ctrl, uint64_t targMask);
+bool capturePhase(SV s, uint64_t mask, double tr, double ti);
+bool captureRotateZ(SV s, uint64_t ctrl, uint64_t targ, double angle);
+bool capturePauliRotation(SV s, uint64_t ctrl, uint64_t xmask, uint64_t ymask, uint64_t zmask, double angle, int conj);
+bool captureSwap(SV s, int q1, int q2);
+bool captureMatrixN(SV s, uint64_t ctrl, const int* targs, int k, const double* mr, const double* mi);
 
 struct Mat2 { double r[2][2], i[2][2]; };
 

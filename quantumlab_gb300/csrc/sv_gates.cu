@@ -324,34 +324,55 @@ size_t g_matCap = 0;
 
 // --------------------------------------------------------------- launchers
 void gateMatrix2(SV s, int target, uint64_t ctrl, uint64_t flip, const Mat2& u) {   // QuEST_gpu.cu:966, 1231, 1299
+    if (s.cap) {
+        const double ur[4] = {u.r[0][0], u.r[0][1], u.r[1][0], u.r[1][1]}, ui[4] = {u.i[0][0], u.i[0][1], u.i[1][0], u.i[1][1]};
+        if (capturePair(s, target, ctrl, flip, ur, ui)) return;
+    }
     launchPair(s, ctrl, ctrl & ~flip, 1ull << target, OpMatrix2{u}, "unitary");
 }
 
 void gateCompact(SV s, int target, uint64_t ctrl, double ar, double ai, double br, double bi) {   // QuEST_gpu.cu:838, 905
+    if (s.cap) {
+        const double ur[4] = {ar, -br, br, ar}, ui[4] = {ai, bi, bi, -ai};     // [alpha, -conj(beta); beta, conj(alpha)]
+        if (capturePair(s, target, ctrl, 0, ur, ui)) return;
+    }
     launchPair(s, ctrl, ctrl, 1ull << target, OpCompact{ar, ai, br, bi}, "compactUnitary");
 }
 
 void gateHadamard(SV s, int target) {                                                // QuEST_gpu.cu:1820
+    if (s.cap) {
+        const double f = 0.70710678118654752440;
+        const double ur[4] = {f, f, f, -f}, ui[4] = {0, 0, 0, 0};
+        if (capturePair(s, target, 0, 0, ur, ui)) return;
+    }
     launchPair(s, 0, 0, 1ull << target, OpHadamard{0.70710678118654752440}, "hadamard");
 }
 
 void gateNot(SV s, uint64_t ctrl, uint64_t targMask) {                               // QuEST_gpu.cu:1354, 1867, 1912
+    if (s.cap && captureNot(s, ctrl, targMask)) return;
     launchPair(s, ctrl, ctrl, targMask, OpSwap{}, "controlledNot");
 }
 
 void gatePauliY(SV s, int target, uint64_t ctrl, double conjFac) {                   // QuEST_gpu.cu:1387, 1439
+    if (s.cap) {
+        const double ur[4] = {0, 0, 0, 0}, ui[4] = {0, -conjFac, conjFac, 0};   // [0, -i; i, 0] (conjugated: conjFac = -1)
+        if (capturePair(s, target, ctrl, 0, ur, ui)) return;
+    }
     launchPair(s, ctrl, ctrl, 1ull << target, OpPauliY{conjFac}, "pauliY");
 }
 
 void gatePhase(SV s, uint64_t mask, double tr, double ti) {                          // QuEST_gpu.cu:1485, 1521, 1552, 1702
+    if (s.cap && capturePhase(s, mask, tr, ti)) return;
     launchDiag(s, mask, mask, OpPhase{tr, ti}, "phaseShift");
 }
 
 void gateRotateZ(SV s, uint64_t ctrl, uint64_t targ, double angle) {                 // QuEST_gpu.cu:1582, 1615
+    if (s.cap && captureRotateZ(s, ctrl, targ, angle)) return;
     launchDiag(s, ctrl, ctrl, OpRotZ{targ, cos(angle / 2), sin(angle / 2)}, "multiRotateZ");
 }
 
 void gatePauliRotation(SV s, uint64_t ctrl, uint64_t xmask, uint64_t ymask, uint64_t zmask, double angle, int conj) {
+    if (s.cap && capturePauliRotation(s, ctrl, xmask, ymask, zmask, angle, conj)) return;
     if (xmask == 0) {                                      // diagonal: plain Z-rotation on the Y/Z-free mask
         gateRotateZ(s, ctrl, zmask, conj ? -angle : angle);
         return;
@@ -382,6 +403,7 @@ void gatePauliRotation(SV s, uint64_t ctrl, uint64_t xmask, uint64_t ymask, uint
 }
 
 void gateSwap(SV s, int q1, int q2) {
+    if (s.cap && captureSwap(s, q1, q2)) return;
     const InsSpec ins = makeIns((1ull << q1) | (1ull << q2));
     const uint64_t n = 1ull << (s.n - 2);
     kSwap<<<blocksFor(n), kThreads, 0, stream()>>>(s.re, s.im, ins, 1ull << q1, 1ull << q2, n);
@@ -389,6 +411,7 @@ void gateSwap(SV s, int q1, int q2) {
 }
 
 void gateMatrixN(SV s, uint64_t ctrl, const int* targs, int k, const double* mr, const double* mi) {   // QuEST_gpu.cu:1033, 1166
+    if (s.cap && captureMatrixN(s, ctrl, targs, k, mr, mi)) return;
     const int D = 1 << k;
     const size_t matDoubles = 2 * (size_t)D * D;
     const size_t need = matDoubles * sizeof(double) + 64 * sizeof(int);

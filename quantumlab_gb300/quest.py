@@ -197,6 +197,10 @@ SIGNATURES = {
     "quest_gb300_planPassUsesTensorCores": (_I, [C.c_void_p, _I]),
     "quest_gb300_setTensorCores": (None, [_I]),
     "quest_gb300_setTensorCoreKernel": (None, [_I]),
+    "quest_gb300_setCapture": (_I, [_Q, _I]),
+    "quest_gb300_flushCapture": (None, [_Q]),
+    "quest_gb300_capturedGates": (_I, [_Q]),
+    "quest_gb300_setCaptureFusion": (None, [_I]),
     "quest_gb300_swapTestBatchCreate": (C.c_void_p, [_P(qreal), _P(c_ll), _P(_I), _I, _P(_I), _P(_I), _I]),
     "quest_gb300_swapTestBatchRun": (_I, [C.c_void_p, _P(qreal)]),
     "quest_gb300_swapTestBatchDestroy": (None, [C.c_void_p]),

@@ -1,0 +1,172 @@
+"""Op-stream capture (GPU): gate calls through the QuEST API with capture on
+are queued and applied through the fused FP32 engine at the first
+state-reading call; the result must match the same calls run directly in
+FP64 to the fused engine's bounds (1 - F <= 1e-6, max |d amp| <= 1e-5)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from quantumlab_gb300 import workloads as W
+from quantumlab_gb300.quest import Complex, ComplexMatrix2, ComplexMatrix4, Vector
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def no_library_errors(gpulib):
+    gpulib.capture_errors()
+    gpulib.errors.clear()
+    yield
+    errors = list(gpulib.errors)
+    gpulib.errors.clear()
+    assert not errors, errors
+
+
+def haar(rng, k):
+    z = rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k))
+    return np.linalg.qr(z)[0]
+
+
+def mixed_circuit(L, q, n, seed, reads=None):
+    """Every kind of gate call the capture path handles; `reads` (a list) gets
+    a reduction in the middle, which must flush the queue."""
+    lib = L.lib
+    rng = np.random.default_rng(seed)
+    for layer in range(3):
+        for t in range(n):
+            a, b = rng.normal(size=2) + 1j * rng.normal(size=2)
+            s = np.sqrt(abs(a) ** 2 + abs(b) ** 2)
+            lib.compactUnitary(q, t, Complex(a.real / s, a.imag / s), Complex(b.real / s, b.imag / s))
+        for t in range(0, n - 1, 2):
+            lib.controlledNot(q, t + layer % 2, t + 1 - layer % 2)
+        lib.hadamard(q, 1)
+        lib.pauliY(q, 2)
+        lib.sGate(q, 3)
+        lib.tGate(q, 4)
+        lib.phaseShift(q, 5, 0.3)
+        lib.rotateX(q, 6, 0.7)
+        lib.rotateY(q, 7, -0.4)
+        lib.rotateZ(q, 8, 1.1)
+        lib.rotateAroundAxis(q, 9, 0.5, Vector(1, 2, 3))
+        lib.controlledPhaseShift(q, 0, n - 1, 0.9)
+        lib.controlledPhaseFlip(q, 2, 7)
+        lib.controlledRotateY(q, 3, 11, 0.6)
+        lib.controlledPauliY(q, 12, 1)
+        lib.swapGate(q, 0, n - 2)
+        lib.sqrtSwapGate(q, 4, 10)
+        L.multiControlledPhaseFlip(q, [1, 5, 9])
+        L.multiRotateZ(q, [2, 6, 13], 0.8)
+        L.multiRotatePauli(q, [0, 3, 8], [1, 2, 3], 0.45)
+        L.multiControlledMultiQubitNot(q, [4], [6, 12])
+        u4 = haar(rng, 2)
+        m4 = ComplexMatrix4()
+        for r in range(4):
+            for c in range(4):
+                m4.real[r][c] = u4[r, c].real
+                m4.imag[r][c] = u4[r, c].imag
+        lib.twoQubitUnitary(q, 5, 14, m4)
+        L.multiQubitUnitary(q, [1, 6, 11, 13], haar(rng, 4))
+        u2 = haar(rng, 1)
+        m2 = ComplexMatrix2()
+        for r in range(2):
+            for c in range(2):
+                m2.real[r][c] = u2[r, c].real
+                m2.imag[r][c] = u2[r, c].imag
+        lib.controlledUnitary(q, 9, 3, m2)
+        if reads is not None and layer == 1:
+            reads.append(lib.calcProbOfOutcome(q, 3, 1))
+
+
+@pytest.mark.parametrize("n", [15, 20])
+def test_capture_matches_direct_fp64(gpulib, n):
+    L = gpulib
+    lib = L.lib
+    direct = L.create(n)
+    lib.initZeroState(direct)
+    reads_d = []
+    mixed_circuit(L, direct, n, 7, reads_d)
+    cap = L.create(n)
+    assert lib.quest_gb300_setCapture(cap, 1) == 0
+    lib.initZeroState(cap)
+    reads_c = []
+    mixed_circuit(L, cap, n, 7, reads_c)
+    queued = lib.quest_gb300_capturedGates(cap)
+    assert queued >= n + 20                             # the last layer is still queued
+    a, b = L.amps(direct), L.amps(cap)                  # amps() flushes (copyStateFromGPU)
+    assert lib.quest_gb300_capturedGates(cap) == 0
+    f = abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real)
+    print(f"n={n}: queued {queued}, 1-F={1 - f:.2e}, max|d|={np.max(np.abs(a - b)):.2e}")
+    assert 1 - f <= 1e-6 and np.max(np.abs(a - b)) <= 1e-5
+    assert abs(reads_c[0] - reads_d[0]) < 1e-6         # mid-circuit read saw the flushed state
+    L.destroy(direct)
+    L.destroy(cap)
+
+
+def test_capture_density_matrix_and_channels(gpulib):
+    """Density matrix: gates are doubled (U on t, conj U on t + N) and queued;
+    a channel flushes the queue first."""
+    L = gpulib
+    lib = L.lib
+    n = 7
+    ops = W.c3_circuit(nq=n, layers=2, seed=4)
+    direct = L.create(n, density=True)
+    cap = L.create(n, density=True)
+    lib.quest_gb300_setCapture(cap, 1)
+    for q in (direct, cap):
+        lib.initZeroState(q)
+        W.run_ops(L, q, ops)
+    a, b = L.amps(direct), L.amps(cap)
+    assert np.max(np.abs(a - b)) <= 1e-5
+    assert abs(lib.calcPurity(direct) - lib.calcPurity(cap)) < 1e-5
+    L.destroy(direct)
+    L.destroy(cap)
+
+
+def test_capture_drops_queue_on_overwrite_and_off_flushes(gpulib):
+    L = gpulib
+    lib = L.lib
+    n = 12
+    q = L.create(n)
+    lib.quest_gb300_setCapture(q, 1)
+    lib.initZeroState(q)
+    for t in range(n):
+        lib.hadamard(q, t)
+    assert lib.quest_gb300_capturedGates(q) == n
+    lib.initZeroState(q)                                # overwrite: queue dropped
+    assert lib.quest_gb300_capturedGates(q) == 0
+    assert abs(lib.getRealAmp(q, 0) - 1) < 1e-12
+    lib.pauliX(q, 3)
+    assert lib.quest_gb300_capturedGates(q) == 1
+    lib.quest_gb300_setCapture(q, 0)                    # off: flushes
+    assert lib.quest_gb300_capturedGates(q) == 0
+    assert abs(lib.getRealAmp(q, 1 << 3) - 1) < 1e-6
+    lib.pauliX(q, 3)                                    # runs directly now
+    assert abs(lib.getRealAmp(q, 0) - 1) < 1e-6
+    L.destroy(q)
+
+
+def test_capture_speeds_up_a_26_qubit_circuit(gpulib):
+    """The 26-qubit random circuit through the QuEST API: captured (one fused
+    FP32 flush) against direct FP64 per-gate calls."""
+    L = gpulib
+    lib = L.lib
+    n = 26
+    ops = W.c2_circuit(n=n, layers=10, seed=2)
+    res = {}
+    for mode in (0, 1):
+        q = L.create(n)
+        lib.quest_gb300_setCapture(q, mode)
+        lib.initZeroState(q)
+        W.run_ops(L, q, ops)
+        lib.calcTotalProb(q)                            # warm-up (plan upload, FP32 scratch)
+        lib.initZeroState(q)
+        lib.quest_gb300_eventRecord(20)
+        W.run_ops(L, q, ops)
+        p = lib.calcTotalProb(q)
+        lib.quest_gb300_eventRecord(21)
+        res[mode] = (lib.quest_gb300_eventElapsedMs(20, 21), p)
+        L.destroy(q)
+    print(f"26q 10 layers: direct {res[0][0]:.1f} ms, captured {res[1][0]:.1f} ms")
+    assert abs(res[1][1] - 1) < 1e-5
+    assert res[1][0] < res[0][0] / 3
