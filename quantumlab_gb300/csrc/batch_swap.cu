@@ -16,10 +16,12 @@
 //            half: chi(1, a, b) = phi(1, b, a)) + H(anc) + the probability
 //            P0 = sum_{a,b} |(chi(0,a,b) + chi(1,a,b)) / sqrt2|^2.
 // Small states (2^(2d+1) <= kSmemAmps) live in shared memory; larger ones in
-// a per-CTA slice of a global arena, where pass B reads the swapped half
-// through a shared-memory tile transpose so both reads stay coalesced.
-// Amplitudes are FP32; each thread sums its |omega|^2 terms with FP32 Kahan
-// compensation and the thread / block totals are combined in FP64.
+// a per-CTA slice of a global arena: pass A writes it with 16-byte stores,
+// and in pass B each warp takes 32 x 32 (a, b) tiles, reading the swapped
+// half row by row (coalesced) and transposing it through its own
+// shared-memory tile, so no block-wide barrier is needed inside the pass.
+// Amplitudes are FP32; |omega|^2 terms are summed in FP32 within a thread's
+// share of a tile (at most 32 terms) and in FP64 above that.
 //
 // Scheduling: tests are sorted by size (largest first) and CTAs take the
 // next one from a global ticket (atomicAdd), so uneven sizes balance.
@@ -36,7 +38,10 @@ namespace qg {
 namespace {
 
 constexpr int kSwapThreads = 256;
+constexpr int kSwapCtasPerSM = 4;
+constexpr int kAreaFloats = (kSwapThreads / 32) * 32 * 33;   // 8 transpose tiles (33.8 KB)
 constexpr int kSmemAmps = 8192;          // pass A/B in shared memory up to 2^13 amplitudes (d <= 6)
+static_assert(kSmemAmps <= kAreaFloats, "a small state must fit the tile area");
 constexpr int kMaxD = 10;
 constexpr double kInvSqrt2 = 0.70710678118654752440;
 
@@ -45,13 +50,6 @@ struct SwapJob {
     int d;
     int out;                 // index into the result array
 };
-
-__device__ __forceinline__ void kahanAdd(float& s, float& c, float x) {
-    const float y = x - c;
-    const float t = s + y;
-    c = (t - s) - y;
-    s = t;
-}
 
 __device__ double blockSum(double v, double* red) {
 #pragma unroll
@@ -66,15 +64,18 @@ __device__ double blockSum(double v, double* red) {
     return t;
 }
 
-__global__ void __launch_bounds__(kSwapThreads) kSwapTests(const float* __restrict__ pool, const SwapJob* __restrict__ jobs,
-                                                           int numJobs, unsigned int* __restrict__ ticket,
-                                                           float* __restrict__ arena, size_t arenaPerCta,
-                                                           double* __restrict__ out) {
-    __shared__ float su[1 << kMaxD], sv[1 << kMaxD];
-    __shared__ float sstate[kSmemAmps];
-    __shared__ float tile[32][33];
+__global__ void __launch_bounds__(kSwapThreads, kSwapCtasPerSM) kSwapTests(const float* __restrict__ pool,
+                                                                           const SwapJob* __restrict__ jobs, int numJobs,
+                                                                           unsigned int* __restrict__ ticket,
+                                                                           float* __restrict__ arena, size_t arenaPerCta,
+                                                                           double* __restrict__ out) {
+    __shared__ __align__(16) float su[1 << kMaxD];
+    __shared__ float sv[1 << kMaxD];
+    // the whole state of a small test, or the warps' 32 x 33 transpose tiles
+    __shared__ __align__(16) float area[kAreaFloats];
     __shared__ double red[kSwapThreads / 32];
     __shared__ int sJob;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float* myArena = arena + (size_t)blockIdx.x * arenaPerCta;
     for (;;) {
         if (threadIdx.x == 0) sJob = (int)atomicAdd(ticket, 1u);
@@ -91,43 +92,62 @@ __global__ void __launch_bounds__(kSwapThreads) kSwapTests(const float* __restri
             sv[i] = pool[job.offB + i];
         }
         __syncthreads();
-        const bool inSmem = 2 * half <= (uint64_t)kSmemAmps;
-        float* phi = inSmem ? sstate : myArena;
-        // ---- pass A: |0>|v>|u> then H(anc): both halves = u_a v_b / sqrt2
-        for (uint64_t idx = threadIdx.x; idx < half; idx += kSwapThreads) {
-            const int a = (int)(idx & (D - 1)), b = (int)(idx >> d);
-            const float val = su[a] * sv[b] * (float)kInvSqrt2;
-            phi[idx] = val;
-            phi[half + idx] = val;
-        }
-        __syncthreads();
-        // ---- pass B: CSWAPs (anc=1 half: u <-> v), H(anc), P(anc = 0)
-        float s = 0.f, c = 0.f;
-        if (inSmem || D < 32) {
-            for (uint64_t idx = threadIdx.x; idx < half; idx += kSwapThreads) {
-                const int a = (int)(idx & (D - 1)), b = (int)(idx >> d);
-                const float w = (phi[idx] + phi[half + (uint64_t)b + ((uint64_t)a << d)]) * (float)kInvSqrt2;
-                kahanAdd(s, c, w * w);
+        double total = 0.0;
+        if (2 * half <= (uint64_t)kSmemAmps) {
+            // ---- small state, in shared memory
+            float* phi = area;
+            for (uint32_t idx = threadIdx.x; idx < half; idx += kSwapThreads) {
+                const float val = su[idx & (D - 1)] * sv[idx >> d] * (float)kInvSqrt2;
+                phi[idx] = val;
+                phi[half + idx] = val;
             }
+            __syncthreads();
+            float s = 0.f;
+            for (uint32_t idx = threadIdx.x; idx < half; idx += kSwapThreads) {
+                const uint32_t a = idx & (D - 1), b = idx >> d;
+                const float w = (phi[idx] + phi[half + b + (a << d)]) * (float)kInvSqrt2;
+                s = fmaf(w, w, s);
+            }
+            total = (double)s;
         } else {
-            // 32 x 32 tiles of (a, b); the swapped half is read transposed via smem
-            const int tiles = D / 32;
-            const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;     // 8 rows of 32
-            for (int t = 0; t < tiles * tiles; ++t) {
-                const int a0 = (t % tiles) * 32, b0 = (t / tiles) * 32;
-                // load anc=1 half at (row a0+r, col b0+tx): element phi(1, b, a) for a = a0+r, b = b0+tx
-                for (int r = ty; r < 32; r += kSwapThreads / 32)
-                    tile[r][tx] = phi[half + (uint64_t)(b0 + tx) + ((uint64_t)(a0 + r) << d)];
-                __syncthreads();
-                for (int r = ty; r < 32; r += kSwapThreads / 32) {
-                    const int a = a0 + tx, b = b0 + r;
-                    const float w = (phi[(uint64_t)a + ((uint64_t)b << d)] + tile[tx][r]) * (float)kInvSqrt2;
-                    kahanAdd(s, c, w * w);
+            // ---- pass A: |0>|v>|u> then H(anc): both halves = u_a v_b / sqrt2,
+            // written as 16-byte vectors (4 consecutive a, one b)
+            float4* phi4 = reinterpret_cast<float4*>(myArena);
+            const uint32_t half4 = (uint32_t)(half >> 2);
+            for (uint32_t i4 = threadIdx.x; i4 < half4; i4 += kSwapThreads) {
+                const uint32_t idx = i4 << 2;
+                const float vb = sv[idx >> d] * (float)kInvSqrt2;
+                const float4 u4 = *reinterpret_cast<const float4*>(su + (idx & (D - 1)));
+                const float4 val = make_float4(u4.x * vb, u4.y * vb, u4.z * vb, u4.w * vb);
+                __stcg(phi4 + i4, val);
+                __stcg(phi4 + half4 + i4, val);
+            }
+            __syncthreads();
+            // ---- pass B: CSWAPs (anc=1 half: u <-> v), H(anc), P(anc = 0),
+            // over 32 x 32 (a, b) tiles, one warp per tile: the swapped half
+            // is read row by row (coalesced) and transposed through the
+            // warp's own shared-memory tile
+            const float* phi = myArena;
+            float(*tile)[33] = reinterpret_cast<float(*)[33]>(area + warp * 32 * 33);
+            const int T = D / 32;
+            for (int t = warp; t < T * T; t += kSwapThreads / 32) {
+                const int a0 = (t % T) * 32, b0 = (t / T) * 32;
+                const float* row1 = phi + half + (uint64_t)(b0 + lane) + ((uint64_t)a0 << d);
+#pragma unroll 8
+                for (int r = 0; r < 32; ++r) tile[r][lane] = __ldcg(row1 + ((uint64_t)r << d));   // phi(1, b0+lane, a0+r)
+                __syncwarp();
+                const float* col0 = phi + (uint64_t)(a0 + lane) + ((uint64_t)b0 << d);
+                float s = 0.f;
+#pragma unroll 8
+                for (int r = 0; r < 32; ++r) {
+                    const float w = (__ldcg(col0 + ((uint64_t)r << d)) + tile[lane][r]) * (float)kInvSqrt2;
+                    s = fmaf(w, w, s);
                 }
-                __syncthreads();
+                __syncwarp();
+                total += (double)s;                      // FP32 within a tile (32 terms), FP64 across tiles
             }
         }
-        const double p0 = blockSum((double)s - (double)c, red);
+        const double p0 = blockSum(total, red);
         if (threadIdx.x == 0) out[job.out] = p0;
         __syncthreads();
     }
@@ -199,7 +219,7 @@ void* quest_gb300_swapTestBatchCreate(const double* vectors, const long long* of
     std::stable_sort(jobs.begin(), jobs.end(), [](const SwapJob& x, const SwapJob& y) { return x.d > y.d; });
     SwapBatch* b = new SwapBatch();
     b->numTests = numTests;
-    b->grid = qg::numSMs() * 2;
+    b->grid = qg::numSMs() * qg::kSwapCtasPerSM;
     const size_t arenaNeed = (2ull << (2 * maxD)) > (size_t)qg::kSmemAmps ? (2ull << (2 * maxD)) : 0;
     b->arenaPerCta = arenaNeed;
     std::vector<float> pool32(poolLen);
