@@ -299,19 +299,26 @@ def run_gpu(args, rank, world):
 
 
 # ------------------------------------------------------- batched swap tests
-def run_swaps(args):
+def run_swaps(args, rank=0, world=1):
     """65,536 QKMeans swap tests (4096 vectors x 16 centroids, 9..21 qubits):
     the batched engine (one persistent kernel, CUDA-graph replay) against one
     circuit at a time through the QuEST API (the reference pattern, per-gate
-    FP64 kernels) on a per-size subsample, extrapolated over the size mix."""
+    FP64 kernels) on a per-size subsample, extrapolated over the size mix.
+    With N ranks the tests are dealt by size (no device collective); the
+    batch time is the maximum over ranks and the results are gathered to
+    rank 0.  Returns None on ranks other than 0."""
     import ctypes as C
     import quantumlab_gb300 as qg
+    from quantumlab_gb300 import sharding
     from quantumlab_gb300 import workloads as W
 
     L = qg.load()
     lib = L.lib
     ds, comps, vecs, cents = W.gaussian_mixture_vectors(count=args.swap_vectors, seed=5)
-    pool, offsets, dims, ia, ib = W.swap_test_pool(vecs, cents)
+    pool, offsets, dims, ia_all, ib_all = W.swap_test_pool(vecs, cents)
+    mine = sharding.shard_units(sharding.swap_test_cost(dims[ia_all]), world, rank)
+    ia = np.ascontiguousarray(ia_all[mine])
+    ib = np.ascontiguousarray(ib_all[mine])
     P = lambda a, t: a.ctypes.data_as(C.POINTER(t))
     t0 = time.perf_counter()
     h = lib.quest_gb300_swapTestBatchCreate(P(pool, C.c_double), P(offsets, C.c_longlong), P(dims, C.c_int),
@@ -321,11 +328,16 @@ def run_swaps(args):
     for _ in range(3):
         lib.quest_gb300_swapTestBatchRun(h, P(out, C.c_double))
     reps = 5
+    barrier(world)
     t0 = time.perf_counter()
     for _ in range(reps):
         lib.quest_gb300_swapTestBatchRun(h, P(out, C.c_double))
-    batch_s = (time.perf_counter() - t0) / reps
+    batch_s = sharding.max_over_ranks((time.perf_counter() - t0) / reps, world)
     lib.quest_gb300_swapTestBatchDestroy(h)
+    full = sharding.gather_to_rank0(mine, out, len(ia_all), world)
+    if rank != 0:
+        return None
+    ia, ib, out = ia_all, ib_all, full
     items = list(vecs) + [m for d in range(4, 11) for m in cents[d]]
     want = np.array([(1 + np.dot(items[a], items[b]) ** 2) / 2 for a, b in zip(ia, ib)])
     err = float(np.max(np.abs(out - want)))
@@ -344,6 +356,7 @@ def run_swaps(args):
     plain_total = sum(counts[d] * per_size[d] for d in counts)
     return {
         "tests": int(len(ia)), "qubits": "9..21", "tests_per_s": round(len(ia) / batch_s, 1),
+        "ranks": world, "partitioning": "tests dealt by state size, no device collective" if world > 1 else "1 GPU",
         "batch_ms": round(batch_s * 1e3, 3), "create_s": round(create_s, 3),
         "max_abs_err_vs_fp64_closed_form": err,
         "per_gate_tests_per_s": round(len(ia) / plain_total, 1),
@@ -438,7 +451,9 @@ def main():
         return
     out = run_gpu(args, rank, world)
     if not args.no_swap:
-        out["swap_tests"] = run_swaps(args)
+        sw = run_swaps(args, rank, world)
+        if rank == 0:
+            out["swap_tests"] = sw
     if rank == 0:
         if not args.no_cpu_baseline:
             gbs, secs, kind, nops = cpu_sample(args.qubits, args.layers, args.cpu_sample_ops)
