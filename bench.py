@@ -186,9 +186,10 @@ def run_gpu(args, rank, world):
     groups = {}
     for i in range(npass):
         key = {0: f"kApplySimt<{kk[i]}> (FP32 FFMA)", 1: f"kApplyTC<{kk[i]}> (tcgen05 split-TF32, direct loads)",
-               2: f"kApplyTC2<{kk[i]},2,1> (tcgen05 split-TF32, pipelined)",
-               3: f"kApplyTC2<{kk[i]},1,1> (tcgen05 split-TF32, pipelined)",
-               4: f"kApplyTC2<{kk[i]},1,2> (tcgen05 split-TF32, pipelined)"}[tc[i]]
+               2: f"kApplyTC2<{kk[i]},2,1,1> (tcgen05 split-TF32, pipelined)",
+               3: f"kApplyTC2<{kk[i]},1,1,1> (tcgen05 split-TF32, pipelined)",
+               4: f"kApplyTC2<{kk[i]},1,2,1> (tcgen05 split-TF32, pipelined)",
+               5: f"kApplyTC2<{kk[i]},2,2,2> (tcgen05 split-TF32, pipelined)"}[tc[i]]
         g = groups.setdefault(key, [0, 0.0])
         g[0] += 1
         g[1] += pass_ms[i]
@@ -231,20 +232,30 @@ def run_gpu(args, rank, world):
     src_re[0] = 1.0
     lib.quest_gb300_setCapture(q64, 1)
 
+    split = [0.0, 0.0, 0.0]                            # host -> device, gates + flush, device -> host
+
     def e2e_step():
+        t = time.perf_counter()
         lib.initStateFromAmps(q64, src.stateVec.real, src.stateVec.imag)
+        t1 = time.perf_counter()
         run_plain_step(L, q64, ops)
         p = lib.calcTotalProb(q64)
+        t2 = time.perf_counter()
         lib.copyStateFromGPU(q64)
+        t3 = time.perf_counter()
+        for i, d in enumerate((t1 - t, t2 - t1, t3 - t2)):
+            split[i] += d
         return p
 
     e2e_step()
+    split[:] = [0.0, 0.0, 0.0]
     e2e_steps = max(1, min(args.steps, 2))
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_prob = e2e_step()
     e2e_s = barrier_max((time.perf_counter() - t0) / e2e_steps, world)
+    split = [x / e2e_steps for x in split]
     lib.quest_gb300_setCapture(q64, 0)
     state_bytes = (1 << n) * 16
     L.destroy(src)
@@ -286,7 +297,10 @@ def run_gpu(args, rank, world):
                 "ms_per_step": round(e2e_s * 1e3, 2),
                 "path": "QuEST C ABI: initStateFromAmps (pinned host FP64), one API call per gate with op-stream "
                         "capture on, calcTotalProb, copyStateFromGPU",
-                "total_prob": e2e_prob},
+                "total_prob": e2e_prob,
+                "split_ms": {"h2d_initStateFromAmps": round(split[0] * 1e3, 1),
+                             "gates_and_flush": round(split[1] * 1e3, 1),
+                             "d2h_copyStateFromGPU": round(split[2] * 1e3, 1)}},
         "gpu_launches": int(launches // max(1, args.steps)),
         "gpu_launches_timed_region": int(launches),
         "total_prob_fp32": total32,

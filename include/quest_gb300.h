@@ -72,15 +72,16 @@ void quest_gb300_copyToQureg(void* qureg32, Qureg destination);
 int quest_gb300_applyPlanF32(void* qureg32, void* plan);
 /* apply passes [firstPass, firstPass + numPasses) only (timing, stepping) */
 int quest_gb300_applyPlanF32Range(void* qureg32, void* plan, int firstPass, int numPasses);
-/* applier of pass i: 0 = SIMT, 1 = direct-load tensor-core kernel, 2..4 =
+/* applier of pass i: 0 = SIMT, 1 = direct-load tensor-core kernel, 2..5 =
  * pipelined tensor-core kernel (as setTensorCoreKernel); -1 if invalid */
 int quest_gb300_planPassUsesTensorCores(void* plan, int i);
 /* passes on 4..6 qubits run on the tensor cores (split-TF32) unless disabled
  * here (1 = enabled, the default; 0 = FP32 SIMT applier for k <= 5) */
 void quest_gb300_setTensorCores(int enabled);
 /* tensor-core kernel: 0 = chosen per pass (default), 1 = always the
- * direct-load kernel, 2..4 = always the pipelined kernel with 2 loader + 1
- * epilogue warp groups (2), 1 + 1 (3) or 1 + 2 (4) */
+ * direct-load kernel, 2..5 = always the pipelined kernel with 2 loader + 1
+ * epilogue warp groups (2), 1 + 1 (3), 1 + 2 (4), or 2 + 2 with the loader
+ * groups splitting every chunk (5) */
 void quest_gb300_setTensorCoreKernel(int version);
 double quest_gb300_calcTotalProbF32(void* qureg32);
 double quest_gb300_calcProbOfOutcomeF32(void* qureg32, int measureQubit, int outcome);
@@ -120,6 +121,18 @@ void quest_gb300_flushCapture(Qureg qureg);
 int quest_gb300_capturedGates(Qureg qureg);
 /* widest fused pass of the flushes, 1..6 (default 6) */
 void quest_gb300_setCaptureFusion(int maxFusedQubits);
+
+/* ---- repeated measurement ------------------------------------------------------
+ * No counterpart in the reference; it replaces the lab's shot loop "measure
+ * each listed qubit in order, then copyStateToGPU to restore the state"
+ * (Code/QuantumLab/Simulator/QLSimulatorMeasure.cpp:70-109) by one call.
+ * Writes numShots outcome codes (bit j = outcome of qubits[j]) drawn from the
+ * same global MT19937 stream, with the same rule and the same number of draws
+ * as that loop (QuEST_common.c:165-180), so a seeded run gives the loop's
+ * outcomes.  The register is left unchanged (the loop leaves the last shot's
+ * collapse).  1 <= numQubits <= 24.  Returns 0, or -1 after reporting an
+ * invalid argument through invalidQuESTInputError. */
+int quest_gb300_sampleMeasurements(Qureg qureg, const int* qubits, int numQubits, int numShots, int* outcomes);
 
 /* ---- total probability without allocating ---------------------------------
  * No counterpart in the reference.  For callers that hold their own FP64

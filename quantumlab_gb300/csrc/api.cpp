@@ -1139,6 +1139,60 @@ int measure(Qureg q, int t) {
     return measureWithStats(q, t, &p);
 }
 
+// ---- repeated measurement without a state copy per shot (extension) ----
+// QuantumLab samples a register by repeating, shot after shot, "measure each
+// listed qubit in order" and restoring the pre-measurement state with
+// copyStateToGPU before every shot but the first
+// (Code/QuantumLab/Simulator/QLSimulatorMeasure.cpp:70-109): a full host ->
+// device copy and k reductions per shot.  Measuring qubit j after outcomes
+// o_0..o_{j-1} has P(0) = the conditional probability of 0 given those
+// outcomes, and QuEST's rule (QuEST_common.c:165-180: outcome 1 if P0 <
+// REAL_EPS, 0 if 1 - P0 < REAL_EPS, else genrand_real1() > P0) consumes one
+// draw of the global MT19937 stream only when the outcome is not certain.
+// So one histogram of the 2^k joint outcomes, reduced once on the device, and
+// a tree of its partial sums give every shot's conditional probabilities on
+// the host; with the same draws the outcomes are those of the loop (up to the
+// rounding of P0, which can matter only for a draw within ~1e-15 of it).
+extern "C" int quest_gb300_sampleMeasurements(Qureg q, const int* qubits, int numQubits, int numShots, int* outcomes) {
+    const char* caller = "sampleMeasurements";
+    if (!vMultiTargets(q, qubits, numQubits, caller)) return -1;
+    if (!REQUIRE(numQubits <= 24, "Invalid number of measured qubits. Must be >0 and <=24.")) return -1;
+    if (!REQUIRE(numShots >= 0 && (numShots == 0 || outcomes), "Invalid number of shots. Must be >=0, with an output array.")) return -1;
+    const size_t M = (size_t)1 << numQubits;
+    // tree[j] (offset 2^j - 1): mass of every assignment of the first j listed
+    // qubits (bit i of the index = qubit i's outcome); tree level numQubits
+    // is the histogram itself
+    std::vector<double> tree(2 * M - 1);
+    double* hist = tree.data() + (M - 1);
+    qg::reduceProbAllOutcomes(sv(q), q.isDensityMatrix, q.numQubitsRepresented, qubits, numQubits, hist,
+                              qg::scratchOf(q));
+    for (int j = numQubits - 1; j >= 0; --j) {
+        const size_t n = (size_t)1 << j;
+        double* lvl = tree.data() + (n - 1);
+        const double* up = tree.data() + (2 * n - 1);
+        for (size_t pfx = 0; pfx < n; ++pfx) lvl[pfx] = up[pfx] + up[pfx + n];
+    }
+    for (int shot = 0; shot < numShots; ++shot) {
+        size_t pfx = 0;
+        int code = 0;
+        for (int j = 0; j < numQubits; ++j) {
+            const size_t n = (size_t)1 << j;
+            const double mass = tree[(n - 1) + pfx];
+            const double p0 = mass > 0 ? tree[(2 * n - 1) + pfx] / mass : 0.0;
+            int o;
+            if (p0 < REAL_EPS) o = 1;
+            else if (1 - p0 < REAL_EPS) o = 0;
+            else o = (g_mt.real1() > p0);
+            if (o) {
+                pfx |= n;
+                code |= 1 << j;
+            }
+        }
+        outcomes[shot] = code;
+    }
+    return 0;
+}
+
 // ---- reductions ----
 qreal calcTotalProb(Qureg q) {                                            // QuEST.c:1152
     if (q.isDensityMatrix) return qg::reduceTotalProbDM(sv(q), q.numQubitsRepresented, qg::scratchOf(q));

@@ -455,7 +455,7 @@ __device__ __forceinline__ uint64_t tileBase(const TC2Params<KQ>& p, uint64_t ti
     return tb;
 }
 
-template <int KQ, int LG, int EG>
+template <int KQ, int LG, int EG, int LS>
 __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* __restrict__ re, float* __restrict__ im,
                                                                   const float* __restrict__ gImage, uint64_t numTiles,
                                                                   int* __restrict__ errFlag, const NormLinks nl,
@@ -478,12 +478,16 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
     constexpr uint32_t kLBO = 128, kSBO = (K / 4) * 128;
     constexpr uint32_t idesc = idescTF32(kTile, N);
     constexpr int kEpiWarp0 = 4 * LG, kMmaWarp = 4 * (LG + EG);
+    // LS = 1: loader groups take alternate chunks; LS = 2: the two loader
+    // groups split every chunk, group g taking its part g
+    static_assert(LS == 1 || LG == 2, "part-split loading needs two loader groups");
+    constexpr int PPG = (LS == 2) ? 1 : 2;                // parts per loader group per chunk
 
     extern __shared__ __align__(1024) uint8_t smem[];
     float* gh = reinterpret_cast<float*>(smem);
     float* gl = gh + kGFloats;
     float* xs = gl + kGFloats;                           // [loader group][warp][part][R]
-    float* es = xs + LG * 4 * 2 * R;                     // [epilogue group][warp][R]
+    float* es = xs + LG * 4 * PPG * R;                   // [epilogue group][warp][R]
     __shared__ __align__(8) uint64_t barG, gReady, fullB[2], emptyB[2], dFullB[2], dEmptyB[2];
     __shared__ uint32_t tmemBase;
     __shared__ volatile int abortF;
@@ -495,7 +499,7 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
             mbarInit(&barG, 1);
             mbarInit(&gReady, 128 * EG);
             for (int b = 0; b < 2; ++b) {
-                mbarInit(&fullB[b], 128);
+                mbarInit(&fullB[b], 128 * (LS == 2 ? LG : 1));
                 mbarInit(&emptyB[b], 1);
                 mbarInit(&dFullB[b], 1);
                 mbarInit(&dEmptyB[b], 128);
@@ -518,45 +522,49 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         const uint64_t laneA = p.laneOff[lane];
         const uint32_t colBase = p.colLane[lane];
         // this CTA's chunks, in order: chunk s = (tile blockIdx.x + (s / NCH) * gridDim.x, K stage s % NCH);
-        // group g takes s = g, g + LG, ...
+        // LS = 1: group g takes s = g, g + LG, ...; LS = 2: every s, part g
+        const int p0 = (LS == 2) ? g : 0;
+        const uint32_t s0 = (LS == 2) ? 0u : (uint32_t)g, sStep = (LS == 2) ? 1u : (uint32_t)LG;
         const uint32_t nMy = blockIdx.x < numTiles ? (uint32_t)((numTiles - 1 - blockIdx.x) / gridDim.x + 1) * NCH : 0u;
         double normIn = 0.0;
         const bool measure = nl.in != nullptr;             // input norm wanted (uniform)
         // a chunk's two parts: k <= 5 the real and imaginary planes, k = 6 the
         // two halves (region indices 128 m, m < 8 and m >= 8) of one plane
-        float4 v[2][V4P];
+        float4 v[PPG][V4P];
         auto issue = [&](uint32_t sc) {
             const uint64_t tile = blockIdx.x + (uint64_t)(sc / NCH) * gridDim.x;
             const int ch = sc % NCH;
             const uint64_t tb = tileBase(p, tile) + laneA;
 #pragma unroll
-            for (int pt = 0; pt < 2; ++pt) {
+            for (int pp = 0; pp < PPG; ++pp) {
+                const int pt = p0 + pp;
                 const float* src = (((NCH == 2) ? ch : pt) == 0 ? re : im) + tb;
 #pragma unroll
                 for (int mm = 0; mm < V4P; ++mm) {
                     const int m = (KQ == 6) ? V4P * pt + mm : mm;
-                    v[pt][mm] = __ldcs(reinterpret_cast<const float4*>(src + p.warpOff[rw][m]));
+                    v[pp][mm] = __ldcs(reinterpret_cast<const float4*>(src + p.warpOff[rw][m]));
                 }
             }
         };
-        if (nMy > (uint32_t)g) issue(g);
+        if (nMy > s0) issue(s0);
         bool ok = true;
-        for (uint32_t sq = g; sq < nMy; sq += LG) {
-            const int b = (LG == 2) ? g : (int)(sq & 1);      // the stage (group g owns stage g when LG = 2)
+        for (uint32_t sq = s0; sq < nMy; sq += sStep) {
+            // the TMEM stage (with LS = 1 and LG = 2, group g owns stage g)
+            const int b = (LS == 1 && LG == 2) ? g : (int)(sq & 1);
             const uint32_t u = sq >> 1;
             if (u > 0 && !warpWaitOrAbort(&emptyB[b], (u - 1) & 1, &abortF, lane)) {
                 ok = false;
                 break;
             }
-            float* const xr = xs + (size_t)(g * 4 + rw) * 2 * R;   // the group's warp buffer (one chunk at a time)
+            float* const xr = xs + (size_t)(g * 4 + rw) * PPG * R;   // the group's warp buffer (one chunk at a time)
             {
                 float* const rb = xr + rowBase;
 #pragma unroll
-                for (int pt = 0; pt < 2; ++pt)
+                for (int pp = 0; pp < PPG; ++pp)
 #pragma unroll
                     for (int m = 0; m < V4P; ++m) {
-                        const int off = pt * R + (int)padIdx(128u * m);
-                        const float4 x = v[pt][m];
+                        const int off = pp * R + (int)padIdx(128u * m);
+                        const float4 x = v[pp][m];
                         rb[off + 0] = x.x;
                         rb[off + 1] = x.y;
                         rb[off + 2] = x.z;
@@ -566,26 +574,27 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
             if (measure) {
                 float nrm = 0.f;
 #pragma unroll
-                for (int pt = 0; pt < 2; ++pt)
+                for (int pp = 0; pp < PPG; ++pp)
 #pragma unroll
                     for (int m = 0; m < V4P; ++m) {
-                        const float4 x = v[pt][m];
+                        const float4 x = v[pp][m];
                         nrm = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, nrm))));
                     }
                 normIn += (double)nrm;
             }
             __syncwarp();
-            if (sq + LG < nMy) issue(sq + LG);               // next chunk's loads fly during the split below
-            const uint32_t aH = tmem + laneSel + b * kStageCols;
+            if (sq + sStep < nMy) issue(sq + sStep);         // next chunk's loads fly during the split below
+            // this group's stage columns: [p0 JP, (p0 + PPG) JP)
+            const uint32_t aH = tmem + laneSel + b * kStageCols + p0 * JP;
             const float* const cb = xr + colBase;
 #pragma unroll
-            for (int c0 = 0; c0 < KC; c0 += 8) {
+            for (int c0 = 0; c0 < PPG * JP; c0 += 8) {
                 uint32_t hi[8], lo[8];
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
-                    const int kl = c0 + e;                   // stage column: part kl / JP
-                    const int pl = kl / JP;
-                    const int j = (NCH == 2) ? kl : kl % D;
+                    const int cl = c0 + e;                   // local column: buffer part cl / JP
+                    const int pl = cl / JP;
+                    const int j = (NCH == 2) ? p0 * JP + cl : cl % D;
                     // hi = x rounded to TF32; lo = x - hi (exact), which the
                     // MMA reads as its leading TF32 bits; lo takes both signs,
                     // so that truncation is unbiased
@@ -647,7 +656,8 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
             float nrmTile = 0.f;
             float* const cb = er + colBase;
             const float* const rb = er + rowBase;
-#pragma unroll
+            // (rolled at k = 6, whose four unrolled parts would not fit the registers)
+#pragma unroll(KQ == 6 ? 1 : EPARTS)
             for (int ep = 0; ep < EPARTS; ++ep) {
                 // part ep: plane pl (output rows r = pl * D + j), matrix indices j = h * 32 + jj
                 const int pl = (KQ == 6) ? ep >> 1 : ep;
@@ -716,21 +726,17 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                 }
                 fenceAfter();
                 const uint32_t aH = tmem + b * kStageCols, aL = aH + KC;
+                // K step ks reads the 256 bytes at +256 (ch KC/8 + ks) of Gh / Gl: the
+                // descriptor's start field (address >> 4) advances by 16 per step
+                const uint64_t dH = smemDesc(ghA + 256u * (ch * (KC / 8)), kLBO, kSBO);
+                const uint64_t dL = smemDesc(glA + 256u * (ch * (KC / 8)), kLBO, kSBO);
 #pragma unroll
-                for (int ks = 0; ks < KC / 8; ++ks) {
-                    const uint32_t sg = ch * (KC / 8) + ks;
-                    mmaTF32(dT, aH + 8 * ks, smemDesc(ghA + 256u * sg, kLBO, kSBO), idesc, (ch | ks) != 0);
-                }
+                for (int ks = 0; ks < KC / 8; ++ks)
+                    mmaTF32(dT, aH + 8 * ks, dH + 16u * ks, idesc, (ch | ks) != 0);
 #pragma unroll
-                for (int ks = 0; ks < KC / 8; ++ks) {
-                    const uint32_t sg = ch * (KC / 8) + ks;
-                    mmaTF32(dT, aL + 8 * ks, smemDesc(ghA + 256u * sg, kLBO, kSBO), idesc, 1);
-                }
+                for (int ks = 0; ks < KC / 8; ++ks) mmaTF32(dT, aL + 8 * ks, dH + 16u * ks, idesc, 1);
 #pragma unroll
-                for (int ks = 0; ks < KC / 8; ++ks) {
-                    const uint32_t sg = ch * (KC / 8) + ks;
-                    mmaTF32(dT, aH + 8 * ks, smemDesc(glA + 256u * sg, kLBO, kSBO), idesc, 1);
-                }
+                for (int ks = 0; ks < KC / 8; ++ks) mmaTF32(dT, aH + 8 * ks, dL + 16u * ks, idesc, 1);
                 mmaCommit(&emptyB[b]);
             }
             if (!ok) break;
@@ -833,7 +839,7 @@ bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* i
 }
 
 
-template <int KQ, int LG, int EG>
+template <int KQ, int LG, int EG, int LS>
 bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, const NormLinks& nl,
                cudaStream_t st) {
     constexpr int D = 1 << KQ;
@@ -842,7 +848,7 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
     constexpr int PART = (KQ == 6) ? TILE / 8 : TILE / 4;
     constexpr int R = (int)((padIdx(PART - 1) + 1 + 3) & ~3u);
     constexpr int V4 = TILE / 512;
-    const size_t smem = ((size_t)2 * N * K + (size_t)LG * 4 * 2 * R + (size_t)EG * 4 * R) * 4;
+    const size_t smem = ((size_t)2 * N * K + (size_t)LG * 4 * (LS == 2 ? 1 : 2) * R + (size_t)EG * 4 * R) * 4;
     TC2Params<KQ> p{};
     // I = targets + the 7 lowest other qubits (ascending); tile position b <-> qubit I[b]
     uint64_t tmask = 0;
@@ -917,13 +923,13 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
     const uint64_t numTiles = 1ull << (n - KQ - kTileBitsC);
     static bool configured = false;
     if (!configured) {
-        if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ, LG, EG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+        if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ, LG, EG, LS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "applyPlanF32"))
             return false;
         configured = true;
     }
     const uint64_t grid = std::min<uint64_t>(numTiles, (uint64_t)numSMs());
-    kApplyTC2<KQ, LG, EG><<<(unsigned)grid, (4 * (LG + EG) + 1) * 32, smem, st>>>(re, im, img, numTiles, errFlag, nl, p);
+    kApplyTC2<KQ, LG, EG, LS><<<(unsigned)grid, (4 * (LG + EG) + 1) * 32, smem, st>>>(re, im, img, numTiles, errFlag, nl, p);
     return !launchFailed("applyPlanF32");
 }
 
@@ -1013,22 +1019,23 @@ void tcNoteSimtPass(void* devPlan, size_t index) {
 }
 
 // Which applier runs a pass on registers of n qubits: 0 = the FP32 SIMT
-// applier, 1 = the direct-load tensor-core kernel, 2 / 3 / 4 = the pipelined
-// one with 2+1 / 1+1 / 1+2 loader + epilogue warp groups.  Default choice
-// (measured at 30 qubits, ms per pass): passes on 1..3 qubits and 4-qubit
-// passes whose targets are all at or above qubit 5 run on the SIMT applier
-// (3.2 ms: every lane's group is part of a coalesced warp line and the
-// multiply is cheap); the other 4-qubit passes (SIMT 9.0 ms, pipelined 3.1)
-// and the 5-qubit passes run on the pipelined kernel with two loader groups
-// (2.6-3.2 ms; its loaders are the busier role); 6-qubit passes run on the
-// one with two epilogue groups (3.3-3.8 ms against 3.7-4.1; the epilogue's
-// staging is the busier role at 2 x 128 output values per group).
+// applier, 1 = the direct-load tensor-core kernel, 2..5 = the pipelined one
+// (2: 2 loader groups on alternate chunks + 1 epilogue group; 3: 1 + 1;
+// 4: 1 + 2; 5: 2 loader groups splitting every chunk + 2 epilogue groups).
+// Default choice (measured at 30 qubits, ms per pass): passes on 1..3 qubits
+// and 4-qubit passes whose targets are all at or above qubit 5 run on the SIMT
+// applier (3.2 ms: every lane's group is part of a coalesced warp line and the
+// multiply is cheap); the other 4-qubit passes (SIMT 9.0 ms, kernel 2: 3.1)
+// and the 5-qubit passes run on kernel 2 (2.6-3.2 ms; the loaders are the
+// busier role); 6-qubit passes run on kernel 5 (3.1-3.7 ms against 3.2-3.8 for
+// kernel 4 and 3.4-3.9 for kernel 2: at 2 x 128 values per group both the
+// loaders' and the epilogue's staging are busy, and kernel 5 doubles both).
 int tcKernelFor(const FusedPass& pass, int n) {
     const int k = (int)pass.targets.size();
     if (!g_tcEnabled || k < 4 || k > 6 || n < k + 7) return 0;
     if (g_tcVersion != 0) return g_tcVersion;
     if (k == 4 && pass.targets[0] >= 5) return 0;
-    return k == 6 ? 4 : 2;
+    return k == 6 ? 5 : 2;
 }
 
 // explicit entry used by the FP32 engine with the pass index: 1 = applied on
@@ -1061,11 +1068,14 @@ int applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, 
     }
     bool ok = false;
     if (version >= 2) {
-        // 2: two loader groups + one epilogue group; 3: one + one; 4: one + two
-#define QG_TC2(KQ)                                                                                     \
-    (version == 2   ? launchTC2<KQ, 2, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)     \
-     : version == 3 ? launchTC2<KQ, 1, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)     \
-                    : launchTC2<KQ, 1, 2>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st))
+        // 2: two loader groups (alternate chunks) + one epilogue group; 3: one
+        // + one; 4: one + two; 5: two loader groups (each half of every chunk)
+        // + two epilogue groups
+#define QG_TC2(KQ)                                                                                      \
+    (version == 2   ? launchTC2<KQ, 2, 1, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)    \
+     : version == 3 ? launchTC2<KQ, 1, 1, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)    \
+     : version == 4 ? launchTC2<KQ, 1, 2, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)    \
+                    : launchTC2<KQ, 2, 2, 2>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st))
         switch (k) {
             case 4: ok = QG_TC2(4); break;
             case 5: ok = QG_TC2(5); break;
@@ -1097,7 +1107,7 @@ int tcErrorFlag(const void* devPlan) {
 }
 
 void setTensorCoresEnabled(bool on) { g_tcEnabled = on; }
-void setTensorCoreKernel(int version) { g_tcVersion = (version >= 1 && version <= 4) ? version : 0; }
+void setTensorCoreKernel(int version) { g_tcVersion = (version >= 1 && version <= 5) ? version : 0; }
 bool tensorCoresEnabled() { return g_tcEnabled; }
 
 }  // namespace qg

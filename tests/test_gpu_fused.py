@@ -115,11 +115,12 @@ def _single_gate_plan(L, n, targets, seed):
 
 @pytest.mark.parametrize("targets", [[0, 1, 2, 3], [0, 2, 4, 6, 8], [0, 1, 2, 3, 4, 5], [1, 3, 5, 7, 9, 11],
                                      [2, 9, 10, 14], [4, 5, 6, 7, 15, 16], [12, 13, 14, 15, 16, 17]])
-@pytest.mark.parametrize("version", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("version", [0, 1, 2, 3, 4, 5])
 def test_tensor_core_target_layouts(gpulib, targets, version):
     """One dense gate on low, interleaved and high target sets, every
-    tensor-core kernel (direct-load; pipelined with 2+1, 1+1 and 1+2 loader +
-    epilogue warp groups), against the FP64 engine."""
+    tensor-core kernel (direct-load; pipelined with 2+1, 1+1, 1+2 loader +
+    epilogue warp groups, and 2+2 with the loaders splitting each chunk),
+    against the FP64 engine."""
     L = gpulib
     n = 18
     rng = np.random.default_rng(3)
@@ -143,7 +144,7 @@ def test_tensor_core_target_layouts(gpulib, targets, version):
     L.destroy(q64)
 
 
-@pytest.mark.parametrize("version", [0, 1, 3, 4])
+@pytest.mark.parametrize("version", [0, 1, 3, 4, 5])
 def test_non_unitary_passes_keep_their_norm(gpulib, version):
     """A plan mixing non-unitary and unitary dense gates on the tensor cores:
     the drift correction must not undo a pass that changes the norm on
