@@ -122,6 +122,17 @@ int quest_gb300_capturedGates(Qureg qureg);
 /* widest fused pass of the flushes, 1..6 (default 6) */
 void quest_gb300_setCaptureFusion(int maxFusedQubits);
 
+/* ---- amplitude-encoded product states ------------------------------------------
+ * No counterpart in the reference; it replaces the lab's amplitude-encoding
+ * circuits (Code/QuantumLab/Circuit/Gates/AmplitudeEncodeCuda.cu:691-776) for
+ * state preparation.  Sets a state-vector register to v_{R-1} (x) ... (x) v_0:
+ * register r holds v_r / |v_r| on the next regQubits[r] qubits, starting at
+ * qubit 0; the qubits above are |0>.  re / im hold the R vectors one after
+ * another (lengths 2^regQubits[r]); im may be NULL for real vectors.
+ * 1 <= R <= 16.  Returns 0, or -1 after reporting an invalid argument
+ * through invalidQuESTInputError. */
+int quest_gb300_initProductState(Qureg qureg, int numRegs, const int* regQubits, const double* re, const double* im);
+
 /* ---- repeated measurement ------------------------------------------------------
  * No counterpart in the reference; it replaces the lab's shot loop "measure
  * each listed qubit in order, then copyStateToGPU to restore the state"

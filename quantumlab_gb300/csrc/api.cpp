@@ -709,6 +709,49 @@ void initPureState(Qureg q, Qureg pure) {
     else cloneQureg(q, pure);
 }
 void initDebugState(Qureg q) { qg::stateDebug(svOverwrite(q)); }
+
+// ---- amplitude-encoded product states (extension) ----
+// QuantumLab prepares |0>|v>|u> for its swap tests by amplitude-encoding each
+// vector as a circuit of uniformly controlled rotations (AmplitudeEncodeCuda.cu:
+// 691-776, FRGate.cu:181-466): device allocations and a host round trip per
+// vector, then O(2^d) gates per register.  Applied to |0..0>, that circuit
+// prepares v / |v| on the register's qubits.  This call writes the same
+// product state directly, in one pass: register r holds its vector's
+// normalised amplitudes on qubits [sum of the previous registers' sizes,
+// + regQubits[r]); the qubits above the registers are |0>.  (The circuit may
+// differ from it by a global phase of each register, which no measurement or
+// swap test sees.)
+extern "C" int quest_gb300_initProductState(Qureg q, int numRegs, const int* regQubits, const double* re,
+                                            const double* im) {
+    const char* caller = "initProductState";
+    if (!vStateVec(q, caller)) return -1;
+    if (!REQUIRE(numRegs >= 1 && numRegs <= 16 && regQubits && re, "Invalid registers. Need 1 to 16 registers and their amplitudes.")) return -1;
+    int total = 0;
+    size_t len = 0;
+    for (int r = 0; r < numRegs; ++r) {
+        if (!REQUIRE(regQubits[r] >= 1 && regQubits[r] <= q.numQubitsRepresented, E_INVALID_NUM_TARGETS)) return -1;
+        total += regQubits[r];
+        len += (size_t)1 << regQubits[r];
+    }
+    if (!REQUIRE(total <= q.numQubitsRepresented, "Invalid registers. Their qubits exceed the register's.")) return -1;
+    std::vector<double> vr(re, re + len), vi(len, 0.0);
+    if (im) vi.assign(im, im + len);
+    size_t base = 0;
+    for (int r = 0; r < numRegs; ++r) {
+        const size_t L = (size_t)1 << regQubits[r];
+        double nrm = 0;
+        for (size_t i = base; i < base + L; ++i) nrm += vr[i] * vr[i] + vi[i] * vi[i];
+        if (!REQUIRE(nrm > 0 && std::isfinite(nrm), "Invalid vector. A register's amplitudes must not all be zero.")) return -1;
+        const double f = 1.0 / std::sqrt(nrm);
+        for (size_t i = base; i < base + L; ++i) {
+            vr[i] *= f;
+            vi[i] *= f;
+        }
+        base += L;
+    }
+    qg::stateProduct(svOverwrite(q), numRegs, regQubits, vr.data(), vi.data());
+    return syncStream(caller) ? 0 : -1;
+}
 void setAmps(Qureg q, idx_t start, qreal* re, qreal* im, idx_t n) {
     const char* caller = "setAmps";
     if (!vStateVec(q, caller) || !vNumAmps(q, start, n, caller)) return;

@@ -93,6 +93,8 @@ void gateMatrixN(SV s, uint64_t ctrl, const int* targs, int k, const double* mr,
 void stateFill(SV s, double re, double im);
 void stateSetOne(SV s, idx_t index, double re, double im);   // one element, others untouched
 void stateDebug(SV s);
+// product of unit vectors on consecutive qubit ranges from qubit 0 (<= 16 registers)
+void stateProduct(SV s, int numRegs, const int* regBits, const double* vr, const double* vi);
 void statePlusDM(SV s, int nRep);
 void statePureDM(SV rho, const double* psiRe, const double* psiIm, int nRep);
 void stateWeighted(SV out, double f1r, double f1i, SV a, double f2r, double f2i, SV b, double for_, double foi);

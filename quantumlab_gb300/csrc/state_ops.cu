@@ -31,6 +31,34 @@ __global__ void kFill(double* __restrict__ re, double* __restrict__ im, uint64_t
     st2(im + 2 * t, make_double2(vi, vi));
 }
 
+// Product state of registers on consecutive qubit ranges (register r on
+// qubits [off_r, off_r + bits_r), its vector at base_r in vr/vi); qubits above
+// the registers are |0>.  No counterpart in the reference.
+constexpr int kMaxProductRegs = 16;
+struct ProductSpec {
+    int numRegs;
+    int off[kMaxProductRegs], bits[kMaxProductRegs];
+    uint64_t base[kMaxProductRegs];
+};
+__global__ void kProduct(double* __restrict__ re, double* __restrict__ im, const double* __restrict__ vr,
+                         const double* __restrict__ vi, const ProductSpec ps, uint64_t used, uint64_t n) {
+    const uint64_t t = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (t >= n) return;
+    double ar = 0.0, ai = 0.0;
+    if (t < used) {
+        ar = 1.0;
+        for (int r = 0; r < ps.numRegs; ++r) {
+            const uint64_t f = ps.base[r] + ((t >> ps.off[r]) & ((1ull << ps.bits[r]) - 1ull));
+            const double br = vr[f], bi = vi[f];
+            const double nr = ar * br - ai * bi;
+            ai = ar * bi + ai * br;
+            ar = nr;
+        }
+    }
+    re[t] = ar;
+    im[t] = ai;
+}
+
 // QuEST_gpu.cu:659-684 (initDebugState): amp_k = (2k + i(2k+1)) / 10
 __global__ void kDebug(double* __restrict__ re, double* __restrict__ im, uint64_t n) {
     const uint64_t t = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
@@ -183,6 +211,40 @@ void launchChannel(SV s, int t, int N, const Op& op, const char* caller) {
 }
 
 }  // namespace
+
+// vectors (host, unit norm), regBits per register, concatenated in vr / vi
+void stateProduct(SV s, int numRegs, const int* regBits, const double* vr, const double* vi) {
+    static double* buf = nullptr;          // grow-only device copy of the vectors
+    static size_t cap = 0;
+    ProductSpec ps{};
+    ps.numRegs = numRegs;
+    uint64_t len = 0;
+    int off = 0;
+    for (int r = 0; r < numRegs; ++r) {
+        ps.off[r] = off;
+        ps.bits[r] = regBits[r];
+        ps.base[r] = len;
+        off += regBits[r];
+        len += 1ull << regBits[r];
+    }
+    cudaStream_t st = stream();
+    if (2 * len > cap) {
+        if (buf) {
+            cudaStreamSynchronize(st);
+            cudaFree(buf);
+        }
+        buf = nullptr;
+        cap = 0;
+        if (QG_CUDA(cudaMalloc(&buf, 2 * len * sizeof(double)), "initProductState")) return;
+        cap = 2 * len;
+    }
+    // pageable sources: the copies return once the host data is staged
+    if (QG_CUDA(cudaMemcpyAsync(buf, vr, len * sizeof(double), cudaMemcpyHostToDevice, st), "initProductState")) return;
+    if (QG_CUDA(cudaMemcpyAsync(buf + len, vi, len * sizeof(double), cudaMemcpyHostToDevice, st), "initProductState")) return;
+    const uint64_t n = 1ull << s.n;
+    kProduct<<<blocksFor(n), kThreads, 0, st>>>(s.re, s.im, buf, buf + len, ps, 1ull << off, n);
+    launchFailed("initProductState");
+}
 
 void stateFill(SV s, double vr, double vi) {
     const uint64_t n = 1ull << s.n;

@@ -291,16 +291,18 @@ def swap_test_pool(vecs, centroids, dmin: int = 4, dmax: int = 10):
     return pool, offsets, np.array(dims, dtype=np.int32), np.array(idx_a, dtype=np.int32), np.array(idx_b, dtype=np.int32)
 
 
-def swap_test_plain(L, q, u, v, d: int) -> float:
+def swap_test_plain(L, q, u, v, d: int, prepared: bool = False) -> float:
     """One swap test through the QuEST API, one kernel per gate (the
     reference pattern): initStateFromAmps(|0>|v>|u>) with u on qubits 0..d-1,
     v on d..2d-1, ancilla 2d; H; d controlled swaps as CNOT(v_i -> u_i),
     Toffoli(anc, u_i -> v_i), CNOT(v_i -> u_i); H; P(anc = 0).  `q` is a
-    (2d+1)-qubit register that is reused between calls."""
+    (2d+1)-qubit register that is reused between calls; with prepared=True it
+    already holds |0>|v>|u>."""
     n = 2 * d + 1
-    psi = np.zeros(1 << n, dtype=np.complex128)
-    psi[: 1 << (2 * d)] = np.kron(v, u)
-    L.set_amps(q, psi)
+    if not prepared:
+        psi = np.zeros(1 << n, dtype=np.complex128)
+        psi[: 1 << (2 * d)] = np.kron(v, u)
+        L.set_amps(q, psi)
     anc = 2 * d
     L.lib.hadamard(q, anc)
     for i in range(d):
