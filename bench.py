@@ -379,6 +379,106 @@ def run_swaps(args, rank=0, world=1):
     }
 
 
+# ------------------------------------------------ the other configurations
+def run_configs(args):
+    """Secondary lines for the configurations the headline does not cover
+    (their parity is in tests/): C1 the 20-qubit plain FP64 circuit (GPU
+    per-gate engine against the CPU QuEST path, whole circuit); C3 the noisy
+    14-qubit density matrix (per-gate FP64, and with op-stream capture: gates
+    fused between the channels); C4 Fermi-Hubbard Trotter instances at 24
+    qubits (one multiRotatePauli pass per term, and captured: the Trotter
+    rotations fused), on a sample of instances."""
+    import quantumlab_gb300 as qg
+    from quantumlab_gb300 import workloads as W
+
+    L = qg.load()
+    lib = L.lib
+    out = {}
+
+    def gpu_ms(fn):
+        lib.quest_gb300_eventRecord(30)
+        r = fn()
+        lib.quest_gb300_eventRecord(31)
+        return lib.quest_gb300_eventElapsedMs(30, 31), r
+
+    # ---- C1 ----
+    n1 = 20
+    ops1 = W.c1_circuit(n=n1, layers=40, seed=1)
+    alg1 = W.algorithmic_bytes(ops1, n1)
+
+    def c1(L_, q_):
+        L_.lib.initZeroState(q_)
+        W.run_ops(L_, q_, ops1)
+        return L_.lib.calcTotalProb(q_)
+
+    q = L.create(n1)
+    c1(L, q)
+    ms1 = statistics.median([gpu_ms(lambda: c1(L, q))[0] for _ in range(3)])
+    L.destroy(q)
+    Lc, kind = cpu_library()
+    qc = Lc.create(n1)
+    t0 = time.perf_counter()
+    c1(Lc, qc)
+    cpu1 = (time.perf_counter() - t0) * 1e3
+    Lc.destroy(qc)
+    out["c1_plain_fp64_20q"] = {"gates": len(ops1), "gpu_ms": round(ms1, 2), "gpu_gbs": round(alg1 / ms1 / 1e6, 1),
+                                "cpu_ms": round(cpu1, 1), "cpu_kind": kind, "cpu_cores": os.cpu_count(),
+                                "speedup_gpu_vs_cpu": round(cpu1 / ms1, 1)}
+    # ---- C3 ----
+    n3 = 14
+    ops3 = W.c3_circuit(nq=n3, layers=10, seed=3)
+    res3 = {}
+    for mode in (0, 1):
+        q = L.create(n3, density=True)
+        lib.quest_gb300_setCapture(q, mode)
+        lib.initZeroState(q)
+        W.run_ops(L, q, ops3[:63])                     # warm-up: one layer
+        lib.calcTotalProb(q)
+
+        def c3():
+            lib.initZeroState(q)
+            W.run_ops(L, q, ops3)
+            return lib.calcPurity(q)
+
+        res3[mode] = gpu_ms(c3)
+        L.destroy(q)
+    out["c3_noisy_dm_14q"] = {"ops": len(ops3), "plain_ms": round(res3[0][0], 1), "captured_ms": round(res3[1][0], 1),
+                              "purity_plain": res3[0][1], "purity_captured": res3[1][1],
+                              "speedup_captured": round(res3[0][0] / res3[1][0], 2)}
+    # ---- C4 ----
+    sites, n4, T = 12, 24, 1.0
+    inst = W.hubbard_instances(64)
+    rows = []
+    ws = L.create(n4)
+    for i in (0, 1, 2, 9):
+        U, dt, order = inst[i]
+        codes, coeffs, const = W.hubbard_terms(sites, U)
+        h = L.pauli_hamil(codes, coeffs)
+        steps = int(round(T / dt))
+        r = {}
+        for mode in (0, 1):
+            q = L.create(n4)
+            lib.quest_gb300_setCapture(q, mode)
+
+            def c4():
+                lib.initClassicalState(q, W.neel_index(sites))
+                lib.applyTrotterCircuit(q, h, T, order, steps)
+                return lib.calcExpecPauliHamil(q, h, ws) + const
+
+            c4()                                       # warm-up (plan upload, FP32 scratch)
+            r[mode] = gpu_ms(c4)
+            L.destroy(q)
+        lib.destroyPauliHamil(h)
+        rows.append({"instance": i, "U": U, "dt": dt, "order": order, "steps": steps,
+                     "plain_ms": round(r[0][0], 2), "captured_ms": round(r[1][0], 2),
+                     "energy_plain": r[0][1], "energy_captured": r[1][1]})
+    L.destroy(ws)
+    out["c4_hubbard_24q"] = {"instances_timed": len(rows), "rows": rows,
+                             "max_abs_energy_diff": max(abs(x["energy_plain"] - x["energy_captured"]) for x in rows),
+                             "speedup_captured": round(sum(x["plain_ms"] for x in rows) / sum(x["captured_ms"] for x in rows), 2)}
+    return out
+
+
 # --------------------------------------------------------- CPU (QuEST) side
 def cpu_library():
     """The reference's own QuEST CPU build when it is built for this host,
@@ -455,6 +555,7 @@ def main():
     ap.add_argument("--no-swap", action="store_true")
     ap.add_argument("--swap-vectors", type=int, default=4096)
     ap.add_argument("--swap-sample", type=int, default=6)
+    ap.add_argument("--no-configs", action="store_true", help="skip the configuration 1/3/4 lines")
     args = ap.parse_args()
     rank, world, local = dist_info()
     os.environ.setdefault("QUEST_GB300_DEVICE", str(local))
@@ -468,6 +569,8 @@ def main():
         sw = run_swaps(args, rank, world)
         if rank == 0:
             out["swap_tests"] = sw
+    if not args.no_configs and rank == 0:
+        out["configs"] = run_configs(args)
     if rank == 0:
         if not args.no_cpu_baseline:
             gbs, secs, kind, nops = cpu_sample(args.qubits, args.layers, args.cpu_sample_ops)
