@@ -98,6 +98,11 @@ static void flushRecord(Capture* c, double* re, double* im) {
     plan->maxFused = std::min(g_capMaxFused, c->n);
     plan->gates.swap(c->gates);
     compilePlan(*plan);
+    if (!plan->compiled) {
+        invalidQuESTInputError("The captured gates could not be fused.", "captureFlush");
+        delete plan;
+        return;
+    }
     if (!c->q32) c->q32 = quest_gb300_createQuregF32(c->n);
     if (!c->q32) {
         invalidQuESTInputError("Could not allocate the FP32 register of the captured gates.", "captureFlush");

@@ -325,6 +325,10 @@ int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPas
         return -1;
     }
     if (!p->compiled) qg::compilePlan(*p);
+    if (!p->compiled) {
+        invalidQuESTInputError("The fusion plan could not be compiled.", "applyPlanF32");
+        return -1;
+    }
     if (!p->device) {
         p->device = qg::uploadPlanTC(*p);
         p->deviceFree = qg::freePlanTC;

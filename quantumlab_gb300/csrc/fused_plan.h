@@ -29,6 +29,7 @@ struct FusedPass {
 struct FusedPlan {
     int numQubits = 0;
     int maxFused = 4;
+    int beamWidth = 8;          // sets kept per level of the pass search
     std::vector<FusedGate> gates;
     std::vector<FusedPass> passes;
     bool compiled = false;
@@ -38,7 +39,8 @@ struct FusedPlan {
     void (*deviceFree)(void*) = nullptr;
 };
 
-// Greedy fusion over blocks with disjoint qubit sets (see fused_plan.cpp).
+// Beam search over qubit sets at the circuit front (see fused_plan.cpp).
+// Leaves plan.compiled false if it fails.
 void compilePlan(FusedPlan& plan);
 
 }  // namespace qg

@@ -21,15 +21,25 @@ def lib():
     L.quest_gb300_planAddControlledNot.argtypes = [C.c_void_p, C.c_int, C.c_int]
     L.quest_gb300_planAddControlledPhaseShift.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double]
     L.quest_gb300_planAddHadamard.argtypes = [C.c_void_p, C.c_int]
+    L.quest_gb300_planAddGate.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.quest_gb300_planSetBeamWidth.argtypes = [C.c_void_p, C.c_int]
     L.quest_gb300_planCompile.argtypes = [C.c_void_p]
     L.quest_gb300_planPass.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double)]
     return L
 
 
-def make_plan(L, n, kmax, ops):
+def make_plan(L, n, kmax, ops, beam=None):
     p = L.quest_gb300_planCreate(n, kmax)
+    if beam is not None:
+        assert L.quest_gb300_planSetBeamWidth(p, beam) == 0
     for op in ops:
-        if op[0] == "cu":
+        if op[0] == "m":                          # ("m", qubits, matrix)
+            re = np.ascontiguousarray(op[2].real.ravel())
+            im = np.ascontiguousarray(op[2].imag.ravel())
+            assert L.quest_gb300_planAddGate(p, (C.c_int * len(op[1]))(*op[1]), len(op[1]),
+                                             re.ctypes.data_as(C.POINTER(C.c_double)),
+                                             im.ctypes.data_as(C.POINTER(C.c_double))) == 0
+        elif op[0] == "cu":
             assert L.quest_gb300_planAddCompactUnitary(p, *op[1:]) == 0
         elif op[0] == "cx":
             assert L.quest_gb300_planAddControlledNot(p, op[1], op[2]) == 0
@@ -72,7 +82,50 @@ def reference(n, ops):
             psi = apply_matrix(psi, n, [op[1], op[2]], m)
         elif op[0] == "cp":
             psi = apply_matrix(psi, n, [op[1], op[2]], np.diag([1, 1, 1, np.exp(1j * op[3])]))
+        elif op[0] == "m":
+            psi = apply_matrix(psi, n, list(op[1]), op[2])
     return psi
+
+
+def haar(rng, k):
+    z = rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k))
+    return np.linalg.qr(z)[0]
+
+
+def controlled(u, nc):
+    """controls on matrix bits 0..nc-1, u on the bits above"""
+    D = len(u) << nc
+    m = np.eye(D, dtype=complex)
+    on = (1 << nc) - 1
+    rows = [r for r in range(D) if r & on == on]
+    m[np.ix_(rows, rows)] = u
+    return m
+
+
+def mixed_ops(n, count, seed):
+    """Dense, diagonal and controlled gates on 1-5 qubits: the planner's
+    commutation rule meets every case (diagonal on all, some or none of a
+    gate's qubits)."""
+    rng = np.random.default_rng(seed)
+    ops = []
+    for _ in range(count):
+        kind = rng.integers(5)
+        k = int(rng.integers(1, 6)) if kind < 2 else int(rng.integers(2, 5))
+        qs = [int(x) for x in rng.choice(n, size=k, replace=False)]
+        if kind == 0:
+            m = haar(rng, k)
+        elif kind == 1:
+            m = np.diag(np.exp(1j * rng.uniform(0, 2 * np.pi, size=1 << k)))
+        elif kind == 2:
+            nc = int(rng.integers(1, k))
+            m = controlled(haar(rng, k - nc), nc)
+        elif kind == 3:                            # controlled diagonal on a target: diagonal everywhere
+            m = controlled(np.diag(np.exp(1j * rng.uniform(0, 2 * np.pi, size=1 << (k - 1)))), 1)
+        else:                                      # CNOT-like permutation with one control
+            perm = np.eye(1 << (k - 1))[rng.permutation(1 << (k - 1))]
+            m = controlled(perm.astype(complex), 1)
+        ops.append(("m", qs, m))
+    return ops
 
 
 @pytest.mark.parametrize("kmax", [1, 2, 3, 4, 5, 6])
@@ -94,12 +147,36 @@ def test_plan_reproduces_circuit(lib, kmax):
         assert np.allclose(m @ m.conj().T, np.eye(len(m)), atol=1e-12)
 
 
+@pytest.mark.parametrize("kmax,beam,seed", [(5, 8, 1), (6, 8, 2), (6, 1, 3), (6, 32, 4), (4, 4, 5)])
+def test_plan_reproduces_mixed_circuit(lib, kmax, beam, seed):
+    n = 9
+    ops = mixed_ops(n, 60, seed)
+    ops = [o for o in ops if len(o[1]) <= kmax]
+    passes = make_plan(lib, n, kmax, ops, beam)
+    assert all(len(t) <= kmax and t == sorted(t) for t, _ in passes)
+    rng = np.random.default_rng(seed)
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    want = psi.copy()
+    for op in ops:
+        want = apply_matrix(want, n, list(op[1]), op[2])
+    for t, m in passes:
+        psi = apply_matrix(psi, n, t, m)
+    assert np.max(np.abs(psi - want)) < 1e-12
+
+
 def test_plan_pass_count_30q(lib):
     ops = W.c2_circuit(n=30, layers=20, seed=2)
     counts = {k: len(make_plan(lib, 30, k, ops)) for k in (4, 5, 6)}
-    # plain per-gate execution would need 1190 passes
-    assert counts[4] < 260 and counts[5] < 220 and counts[6] < 180, counts
+    # plain per-gate execution would need 1190 passes; merging gates into
+    # open blocks in program order took 205, 168 and 130
+    assert counts[4] <= 190 and counts[5] <= 140 and counts[6] <= 105, counts
     assert counts[6] <= counts[5] <= counts[4]
+
+
+def test_plan_pass_count_brickwork(lib):
+    ops = W.c1_circuit(n=20, layers=40, seed=1)
+    # 1180 gates; merging in program order took 85 passes
+    assert len(make_plan(lib, 20, 6, ops)) <= 45
 
 
 def test_invalid_gates_rejected(lib):
