@@ -92,6 +92,18 @@ __device__ __forceinline__ void bulkG2S(void* dst, const void* src, uint32_t byt
                  : "memory");
 }
 
+// 4-byte asynchronous copy global -> shared (no register staging); completion
+// is tracked per thread by commit groups
+__device__ __forceinline__ void cpAsync4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smemAddr(dst)), "l"(__cvta_generic_to_global(src))
+                 : "memory");
+}
+__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpAsyncWait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 __device__ __forceinline__ void tmemAlloc(uint32_t* dstSmem, uint32_t ncols) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(dstSmem)), "r"(ncols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -417,6 +429,29 @@ struct TC2Params {
     int runBits;                          // I contains qubits [0, runBits)
 };
 
+// Shared-memory layout of kApplyTC2<KQ, LG, EG, LS>, used by the kernel and
+// its launcher.  G: Gh then Gl.  At k = 6 each is the compact real form
+// [-Im G; Re G; Im G] (192 rows x 64 K): the B operand of the K-chunk of the
+// real parts of X is rows 64..191 ([Re; Im]), that of the imaginary parts rows
+// 0..127 ([-Im; Re]).  Loader row buffers: XST stages per loader warp, two
+// when they fit next to G and the epilogue buffers.
+template <int KQ, int LG, int EG, int LS>
+struct TC2Shape {
+    static constexpr int D = 1 << KQ, K = 2 * D, N = 2 * D;
+    static constexpr int TILE = 1 << (KQ + kTileBitsC);       // amplitudes per plane per tile
+    static constexpr int NCH = (KQ == 6) ? 2 : 1;             // K chunks per tile
+    static constexpr int KC = K / NCH;                        // K columns per chunk (<= 64)
+    static constexpr int PART = (KQ == 6) ? TILE / 8 : TILE / 4;   // positions per warp per part (<= 1024)
+    static constexpr int R = (int)((padIdx(PART - 1) + 1 + 3) & ~3u);   // floats per part buffer
+    static constexpr int PPG = (LS == 2) ? 1 : 2;             // parts per loader group per chunk
+    static constexpr uint32_t GFL = (KQ == 6) ? 3u * D * D : (uint32_t)(N * K);   // floats of Gh (and of Gl)
+    static constexpr uint32_t GSBO = (uint32_t)(((KQ == 6) ? KC : K) / 4) * 128u;  // B descriptor stride
+    static constexpr size_t fixedFloats = 2 * (size_t)GFL + (size_t)EG * 4 * R;
+    static constexpr size_t stageFloats = (size_t)LG * 4 * PPG * R;
+    static constexpr int XST = ((fixedFloats + 2 * stageFloats) * 4 + 2048 <= 227 * 1024) ? 2 : 1;
+    static constexpr size_t smemBytes = (fixedFloats + (size_t)XST * stageFloats) * 4;
+};
+
 __device__ __forceinline__ void mbarArrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smemAddr(bar)) : "memory");
 }
@@ -460,34 +495,29 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                                                                   const float* __restrict__ gImage, uint64_t numTiles,
                                                                   int* __restrict__ errFlag, const NormLinks nl,
                                                                   const __grid_constant__ TC2Params<KQ> p) {
-    constexpr int D = 1 << KQ;
-    constexpr int K = 2 * D, N = 2 * D;
-    constexpr int TILE = 1 << (KQ + kTileBitsC);         // amplitudes per plane per tile
-    constexpr int NCH = (KQ == 6) ? 2 : 1;               // K stages per tile
-    constexpr int KC = K / NCH;                          // K columns per stage (<= 64)
-    constexpr uint32_t kGFloats = (uint32_t)N * K;
-    constexpr int PART = (KQ == 6) ? TILE / 8 : TILE / 4;   // positions per warp per part (<= 1024)
-    constexpr int V4P = PART / 128;                      // 16-byte accesses per lane per part
+    using S = TC2Shape<KQ, LG, EG, LS>;
+    constexpr int D = S::D, N = S::N;
+    constexpr int NCH = S::NCH, KC = S::KC, PART = S::PART, R = S::R, PPG = S::PPG, XST = S::XST;
+    constexpr uint32_t kGFl = S::GFL;
+    constexpr int V4P = PART / 128;                      // 128-position blocks per part
     constexpr int JP = (KQ == 6) ? 32 : D;               // matrix indices per part
     constexpr int EPARTS = (KQ == 6) ? 4 : 2;            // epilogue parts per tile (plane x half)
-    constexpr int R = (int)((padIdx(PART - 1) + 1 + 3) & ~3u);   // floats per part buffer
     constexpr uint32_t kStageCols = 2 * KC;
     constexpr uint32_t kDCol0 = 2 * kStageCols;
     constexpr uint32_t kUsed = kDCol0 + 2 * N;
     constexpr uint32_t kCols = kUsed <= 64 ? 64 : (kUsed <= 128 ? 128 : (kUsed <= 256 ? 256 : 512));
-    constexpr uint32_t kLBO = 128, kSBO = (K / 4) * 128;
+    constexpr uint32_t kLBO = 128;
     constexpr uint32_t idesc = idescTF32(kTile, N);
     constexpr int kEpiWarp0 = 4 * LG, kMmaWarp = 4 * (LG + EG);
     // LS = 1: loader groups take alternate chunks; LS = 2: the two loader
     // groups split every chunk, group g taking its part g
     static_assert(LS == 1 || LG == 2, "part-split loading needs two loader groups");
-    constexpr int PPG = (LS == 2) ? 1 : 2;                // parts per loader group per chunk
 
     extern __shared__ __align__(1024) uint8_t smem[];
     float* gh = reinterpret_cast<float*>(smem);
-    float* gl = gh + kGFloats;
-    float* xs = gl + kGFloats;                           // [loader group][warp][part][R]
-    float* es = xs + LG * 4 * PPG * R;                   // [epilogue group][warp][R]
+    float* gl = gh + kGFl;
+    float* xs = gl + kGFl;                               // [loader group][warp][stage][part][R]
+    float* es = xs + (size_t)XST * LG * 4 * PPG * R;     // [epilogue group][warp][R]
     __shared__ __align__(8) uint64_t barG, gReady, fullB[2], emptyB[2], dFullB[2], dEmptyB[2];
     __shared__ uint32_t tmemBase;
     __shared__ volatile int abortF;
@@ -519,74 +549,61 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
     if (warp < kEpiWarp0) {
         // ------------------------------------------------ loaders
         const int g = warp >> 2;
-        const uint64_t laneA = p.laneOff[lane];
+        // offset of this lane's amplitude in each row of 32 positions of a part:
+        // region index bits 0..4 are qubits 0..4, so a row is 32 consecutive
+        // amplitudes and every copy instruction reads one 128-byte line
+        const uint64_t laneLow = p.laneOff[lane >> 2] + (uint64_t)(lane & 3);
         const uint32_t colBase = p.colLane[lane];
-        // this CTA's chunks, in order: chunk s = (tile blockIdx.x + (s / NCH) * gridDim.x, K stage s % NCH);
+        // this CTA's chunks, in order: chunk s = (tile blockIdx.x + (s / NCH) * gridDim.x, K chunk s % NCH);
         // LS = 1: group g takes s = g, g + LG, ...; LS = 2: every s, part g
         const int p0 = (LS == 2) ? g : 0;
         const uint32_t s0 = (LS == 2) ? 0u : (uint32_t)g, sStep = (LS == 2) ? 1u : (uint32_t)LG;
         const uint32_t nMy = blockIdx.x < numTiles ? (uint32_t)((numTiles - 1 - blockIdx.x) / gridDim.x + 1) * NCH : 0u;
+        const uint32_t nMine = nMy > s0 ? (nMy - s0 + sStep - 1) / sStep : 0u;     // chunks of this group
         double normIn = 0.0;
         const bool measure = nl.in != nullptr;             // input norm wanted (uniform)
-        // a chunk's two parts: k <= 5 the real and imaginary planes, k = 6 the
-        // two halves (region indices 128 m, m < 8 and m >= 8) of one plane
-        float4 v[PPG][V4P];
-        auto issue = [&](uint32_t sc) {
+        float* const wbuf = xs + (size_t)(g * 4 + rw) * XST * PPG * R;             // this warp's stages
+        // Copy chunk sc into a stage.  Its parts: k <= 5 the real and imaginary
+        // planes, k = 6 the two halves (region indices < 1024, >= 1024) of one
+        // plane.  Element q = 32 i + lane of a part lands at pad(q) = 33 i + lane.
+        auto issue = [&](uint32_t sc, float* buf) {
             const uint64_t tile = blockIdx.x + (uint64_t)(sc / NCH) * gridDim.x;
             const int ch = sc % NCH;
-            const uint64_t tb = tileBase(p, tile) + laneA;
+            const uint64_t tb = tileBase(p, tile) + laneLow;
 #pragma unroll
             for (int pp = 0; pp < PPG; ++pp) {
                 const int pt = p0 + pp;
-                const float* src = (((NCH == 2) ? ch : pt) == 0 ? re : im) + tb;
+                const float* const src = (((NCH == 2) ? ch : pt) == 0 ? re : im) + tb;
+                float* const dst = buf + pp * R + lane;
 #pragma unroll
-                for (int mm = 0; mm < V4P; ++mm) {
-                    const int m = (KQ == 6) ? V4P * pt + mm : mm;
-                    v[pp][mm] = __ldcs(reinterpret_cast<const float4*>(src + p.warpOff[rw][m]));
+                for (int i = 0; i < PART / 32; ++i) {
+                    const int m = ((KQ == 6) ? V4P * pt : 0) + (i >> 2);
+                    cpAsync4(dst + 33 * i, src + p.warpOff[rw][m] + p.laneOff[(i & 3) << 3]);
                 }
             }
         };
-        if (nMy > s0) issue(s0);
+        // XST chunks in flight ahead of the split (one commit group each)
+        for (int st = 0; st < XST; ++st) {
+            if ((uint32_t)st < nMine) issue(s0 + st * sStep, wbuf + (size_t)st * PPG * R);
+            cpAsyncCommit();
+        }
         bool ok = true;
-        for (uint32_t sq = s0; sq < nMy; sq += sStep) {
+        for (uint32_t idx = 0; idx < nMine; ++idx) {
+            const uint32_t sq = s0 + idx * sStep;
             // the TMEM stage (with LS = 1 and LG = 2, group g owns stage g)
             const int b = (LS == 1 && LG == 2) ? g : (int)(sq & 1);
             const uint32_t u = sq >> 1;
+            float* const xr = wbuf + (size_t)((XST == 2) ? (idx & 1u) : 0u) * PPG * R;
             if (u > 0 && !warpWaitOrAbort(&emptyB[b], (u - 1) & 1, &abortF, lane)) {
                 ok = false;
                 break;
             }
-            float* const xr = xs + (size_t)(g * 4 + rw) * PPG * R;   // the group's warp buffer (one chunk at a time)
-            {
-                float* const rb = xr + rowBase;
-#pragma unroll
-                for (int pp = 0; pp < PPG; ++pp)
-#pragma unroll
-                    for (int m = 0; m < V4P; ++m) {
-                        const int off = pp * R + (int)padIdx(128u * m);
-                        const float4 x = v[pp][m];
-                        rb[off + 0] = x.x;
-                        rb[off + 1] = x.y;
-                        rb[off + 2] = x.z;
-                        rb[off + 3] = x.w;
-                    }
-            }
-            if (measure) {
-                float nrm = 0.f;
-#pragma unroll
-                for (int pp = 0; pp < PPG; ++pp)
-#pragma unroll
-                    for (int m = 0; m < V4P; ++m) {
-                        const float4 x = v[pp][m];
-                        nrm = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, nrm))));
-                    }
-                normIn += (double)nrm;
-            }
-            __syncwarp();
-            if (sq + sStep < nMy) issue(sq + sStep);         // next chunk's loads fly during the split below
+            cpAsyncWait<XST - 1>();                          // this lane's copies of the chunk landed
+            __syncwarp();                                    // ... and every lane's
             // this group's stage columns: [p0 JP, (p0 + PPG) JP)
             const uint32_t aH = tmem + laneSel + b * kStageCols + p0 * JP;
             const float* const cb = xr + colBase;
+            float nrm = 0.f;
 #pragma unroll
             for (int c0 = 0; c0 < PPG * JP; c0 += 8) {
                 uint32_t hi[8], lo[8];
@@ -599,17 +616,22 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                     // MMA reads as its leading TF32 bits; lo takes both signs,
                     // so that truncation is unbiased
                     const float x = (cb + pl * R)[p.colJ[j]];
+                    nrm = fmaf(x, x, nrm);                   // the warp reads every element once
                     hi[e] = tf32Bits(x);
                     lo[e] = __float_as_uint(x - __uint_as_float(hi[e]));
                 }
                 tmemSt8(aH + c0, hi);
                 tmemSt8(aH + KC + c0, lo);
             }
+            if (measure) normIn += (double)nrm;
             tmemWaitSt();
             fenceBefore();
             mbarArrive(&fullB[b]);
-            __syncwarp();                                    // column reads done before the region is rewritten
+            __syncwarp();                                    // column reads done before the stage is refilled
+            if (idx + XST < nMine) issue(sq + XST * sStep, xr);
+            cpAsyncCommit();
         }
+        cpAsyncWait<0>();                                    // no copy in flight when the warp leaves
         if (!ok) {
             if (lane == 0) atomicExch(errFlag, 3);
             abortF = 1;
@@ -631,7 +653,7 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         const float sm1 = driftCorrection(nl);
         recordScale(nl, sm1, blockIdx.x == 0 && et == 0);
         if (ok && sm1 != 0.f) {
-            for (uint32_t i = et; i < kGFloats; i += 128 * EG) {
+            for (uint32_t i = et; i < kGFl; i += 128 * EG) {
                 const float g0 = gh[i] + gl[i];
                 const float g1 = fmaf(g0, sm1, g0);
                 const uint32_t h = tf32Bits(g1);
@@ -702,9 +724,9 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         if (lane == 0 && nl.out) atomicAdd(nl.out, normOut);
     } else if (lane == 0) {
         // ------------------------------------------------ TMA of G, then MMAs
-        mbarExpectTx(&barG, 2 * kGFloats * 4);
-        bulkG2S(gh, gImage, kGFloats * 4, &barG);
-        bulkG2S(gl, gImage + kGFloats, kGFloats * 4, &barG);
+        mbarExpectTx(&barG, 2 * kGFl * 4);
+        bulkG2S(gh, gImage, kGFl * 4, &barG);
+        bulkG2S(gl, gImage + kGFl, kGFl * 4, &barG);
         bool ok = mbarWaitOrAbort(&barG, 0, &abortF);
         if (!ok) mbarWaitOrAbort(&barG, 0, &abortF);                // once more for the copies in flight
         ok = ok && mbarWaitOrAbort(&gReady, 0, &abortF);            // G rescaled by the epilogue warps
@@ -726,10 +748,13 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                 }
                 fenceAfter();
                 const uint32_t aH = tmem + b * kStageCols, aL = aH + KC;
-                // K step ks reads the 256 bytes at +256 (ch KC/8 + ks) of Gh / Gl: the
+                // chunk ch's B: k <= 5 the whole of Gh / Gl; k = 6 rows 64..191 of the
+                // compact form for the real parts of X (ch 0), rows 0..127 for the
+                // imaginary parts (ch 1).  K step ks reads the next 256 bytes: the
                 // descriptor's start field (address >> 4) advances by 16 per step
-                const uint64_t dH = smemDesc(ghA + 256u * (ch * (KC / 8)), kLBO, kSBO);
-                const uint64_t dL = smemDesc(glA + 256u * (ch * (KC / 8)), kLBO, kSBO);
+                const uint32_t gOff = (KQ == 6 && ch == 0) ? 8u * S::GSBO : 0u;
+                const uint64_t dH = smemDesc(ghA + gOff, kLBO, S::GSBO);
+                const uint64_t dL = smemDesc(glA + gOff, kLBO, S::GSBO);
 #pragma unroll
                 for (int ks = 0; ks < KC / 8; ++ks)
                     mmaTF32(dT, aH + 8 * ks, dH + 16u * ks, idesc, (ch | ks) != 0);
@@ -842,13 +867,11 @@ bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* i
 template <int KQ, int LG, int EG, int LS>
 bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, const NormLinks& nl,
                cudaStream_t st) {
-    constexpr int D = 1 << KQ;
-    constexpr int K = 2 * D, N = 2 * D;
-    constexpr int TILE = 1 << (KQ + kTileBitsC);
-    constexpr int PART = (KQ == 6) ? TILE / 8 : TILE / 4;
-    constexpr int R = (int)((padIdx(PART - 1) + 1 + 3) & ~3u);
-    constexpr int V4 = TILE / 512;
-    const size_t smem = ((size_t)2 * N * K + (size_t)LG * 4 * (LS == 2 ? 1 : 2) * R + (size_t)EG * 4 * R) * 4;
+    using S = TC2Shape<KQ, LG, EG, LS>;
+    constexpr int D = S::D, K = S::K, N = S::N, PART = S::PART;
+    constexpr int V4 = S::TILE / 512;
+    const size_t smem = S::smemBytes;
+    if (KQ == 6) img += (size_t)2 * N * K;           // the compact image follows the full one
     TC2Params<KQ> p{};
     // I = targets + the 7 lowest other qubits (ascending); tile position b <-> qubit I[b]
     uint64_t tmask = 0;
@@ -970,9 +993,25 @@ void* uploadPlanTC(const FusedPlan& plan) {
                 hi[(size_t)r * K + j] = h;
                 lo[(size_t)r * K + j] = hostTf32RN((float)(v - (double)h));
             }
-        std::vector<float> img(2 * (size_t)N * K);
+        // k = 6: the compact form [-Im G; Re G; Im G] (3D rows, D K columns)
+        // of the pipelined kernel follows
+        const size_t full = (size_t)N * K, compact = (k == 6) ? (size_t)3 * D * D : 0;
+        std::vector<float> img(2 * (full + compact));
         packKMajor(hi, N, K, img.data());
-        packKMajor(lo, N, K, img.data() + (size_t)N * K);
+        packKMajor(lo, N, K, img.data() + full);
+        if (k == 6) {
+            std::vector<float> ch(compact), cl(compact);
+            for (int r = 0; r < 3 * D; ++r)
+                for (int j = 0; j < D; ++j) {
+                    // rows 0..D-1 take the (r, D + j) entries of the real form
+                    // (-Im), rows D..3D-1 the (r - D, j) entries (Re, then Im)
+                    const int rr = (r < D) ? r : r - D, jj = (r < D) ? D + j : j;
+                    ch[(size_t)r * D + j] = hi[(size_t)rr * K + jj];
+                    cl[(size_t)r * D + j] = lo[(size_t)rr * K + jj];
+                }
+            packKMajor(ch, 3 * D, D, img.data() + 2 * full);
+            packKMajor(cl, 3 * D, D, img.data() + 2 * full + compact);
+        }
         float* d = nullptr;
         if (cudaMalloc(&d, img.size() * sizeof(float)) != cudaSuccess) {
             cudaGetLastError();
