@@ -73,6 +73,10 @@ void quest_gb300_copyFromQureg(void* qureg32, Qureg source);
 void quest_gb300_copyToQureg(void* qureg32, Qureg destination);
 /* apply every pass of the plan (compiling it first if needed); 0 on success */
 int quest_gb300_applyPlanF32(void* qureg32, void* plan);
+/* Norm record of pass i of the plan's last application, if it ran on the
+ * tensor cores: {sum |x|^2 in, sum |y|^2 out, square of the drift-correction
+ * scale it applied}.  Returns 1, or 0 if there is no record. */
+int quest_gb300_planPassNorms(void* plan, int i, double* inOutScaleSq);
 /* apply passes [firstPass, firstPass + numPasses) only (timing, stepping) */
 int quest_gb300_applyPlanF32Range(void* qureg32, void* plan, int firstPass, int numPasses);
 /* applier of pass i: 0 = SIMT, 1 = direct-load tensor-core kernel, 2..5 =

@@ -116,7 +116,7 @@ static void flushRecord(Capture* c, double* re, double* im) {
     view.deviceStateVec.imag = im;
     quest_gb300_copyFromQureg(c->q32, view);
     quest_gb300_applyPlanF32(c->q32, plan);
-    quest_gb300_copyToQureg(c->q32, view);
+    copyToQuregAfterPlan(c->q32, view, plan);
     c->gatesApplied += (long long)plan->gates.size();
     c->flushes += 1;
     quest_gb300_planDestroy(plan);

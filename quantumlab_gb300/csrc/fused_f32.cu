@@ -42,6 +42,8 @@ int applyPassTCIndexed(QuregF32& q, const FusedPass& p, const void* devPlan, siz
 void* uploadPlanTC(const FusedPlan& plan);
 void freePlanTC(void* d);
 int tcErrorFlag(const void* devPlan);
+int tcPassNorms(const void* devPlan, size_t index, double* out3);
+bool tcFinalNorms(const void* devPlan, const double** target, const double** out);
 void tcBeginPlan(void* devPlan, size_t numPasses);
 void tcBeginRange(void* devPlan);
 void tcNoteSimtPass(void* devPlan, size_t index);
@@ -153,6 +155,18 @@ __global__ void kF32toF64(const float* __restrict__ sr, const float* __restrict_
     if (t >= n) return;
     dr[t] = (double)sr[t];
     di[t] = (double)si[t];
+}
+// the same, times sqrt(*target / *out) (the last norm correction of a plan;
+// both are FP64 sums written by the tensor-core passes)
+__global__ void kF32toF64Scaled(const float* __restrict__ sr, const float* __restrict__ si, double* __restrict__ dr,
+                                double* __restrict__ di, uint64_t n, const double* __restrict__ target,
+                                const double* __restrict__ out) {
+    const uint64_t t = (uint64_t)blockIdx.x * 256 + threadIdx.x;
+    if (t >= n) return;
+    const double o = *out;
+    const double s = (o > 0.0) ? sqrt(*target / o) : 1.0;
+    dr[t] = (double)sr[t] * s;
+    di[t] = (double)si[t] * s;
 }
 
 // ------------------------------------------------------------ reductions
@@ -283,6 +297,7 @@ void quest_gb300_copyToQureg(void* h, Qureg dst) {
     qg::launchFailed("copyToQureg");
 }
 
+
 // host FP64 amplitudes -> FP32 register, through a bounded FP64 staging
 // buffer on the device (chunks of at most 2^26 amplitudes)
 void quest_gb300_initStateFromAmpsF32(void* h, const double* re, const double* im) {
@@ -377,6 +392,15 @@ int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPas
 
 int quest_gb300_applyPlanF32(void* h, void* plan) { return quest_gb300_applyPlanF32Range(h, plan, 0, 1 << 30); }
 
+/* norm record of pass i of the plan's last application on the tensor cores:
+   in, out (FP64 sums of |amp|^2) and the square of the scale it applied;
+   returns 1, or 0 if pass i has no record */
+int quest_gb300_planPassNorms(void* plan, int i, double* inOutScaleSq) {
+    qg::FusedPlan* p = reinterpret_cast<qg::FusedPlan*>(plan);
+    if (!p || !p->device || i < 0 || !inOutScaleSq) return 0;
+    return qg::tcPassNorms(p->device, (size_t)i, inOutScaleSq);
+}
+
 /* applier of pass i of the plan for registers of its size (tcKernelFor) */
 int quest_gb300_planPassUsesTensorCores(void* plan, int i) {
     qg::FusedPlan* p = reinterpret_cast<qg::FusedPlan*>(plan);
@@ -433,3 +457,28 @@ double quest_gb300_compareF32(void* h, Qureg ref, double* maxAmpErr) {
 }
 
 }  // extern "C"
+
+namespace qg {
+// FP32 register -> FP64 Qureg after a plan: when the plan ended in a chain of
+// unitary passes, the conversion also removes the norm residue of its last
+// tensor-core pass (scaled back to the norm the chain started from), which no
+// later pass is left to correct
+void copyToQuregAfterPlan(void* h, Qureg& dst, void* plan) {
+    QuregF32* q = Q(h);
+    FusedPlan* p = reinterpret_cast<FusedPlan*>(plan);
+    const double *target = nullptr, *out = nullptr;
+    if (!q || !p || !p->device || !tcFinalNorms(p->device, &target, &out)) {
+        quest_gb300_copyToQureg(h, dst);
+        return;
+    }
+    const uint64_t n = 1ull << q->n;
+    if (dst.numAmpsTotal != (long long)n) {
+        invalidQuESTInputError("Dimensions of the qubit registers don't match.", "copyToQureg");
+        return;
+    }
+    kF32toF64Scaled<<<(unsigned)((n + 255) / 256), 256, 0, stream()>>>(q->re, q->im, dst.deviceStateVec.real,
+                                                                       dst.deviceStateVec.imag, n, target, out);
+    launchFailed("copyToQureg");
+}
+}  // namespace qg
+

@@ -36,6 +36,8 @@
 #include "fused_plan.h"
 #include "qg_internal.h"
 
+#include <cuda_bf16.h>
+
 #include <cstdint>
 #include <algorithm>
 #include <cstring>
@@ -92,10 +94,10 @@ __device__ __forceinline__ void bulkG2S(void* dst, const void* src, uint32_t byt
                  : "memory");
 }
 
-// 4-byte asynchronous copy global -> shared (no register staging); completion
-// is tracked per thread by commit groups
-__device__ __forceinline__ void cpAsync4(float* dst, const float* src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smemAddr(dst)), "l"(__cvta_generic_to_global(src))
+// 16-byte asynchronous copy global -> shared (no register staging, L1
+// bypassed); completion is tracked per thread by commit groups
+__device__ __forceinline__ void cpAsync16(float* dst, const float* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smemAddr(dst)), "l"(__cvta_generic_to_global(src))
                  : "memory");
 }
 __device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
@@ -147,6 +149,15 @@ __device__ __forceinline__ void mmaTF32(uint32_t dT, uint32_t aT, uint64_t bDesc
         "r"(aT), "l"(bDesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
+// D[tmem] (+)= A[tmem] * B[smem desc], A and B bf16 (two per 32-bit TMEM
+// column, the lower K index in the low half), D f32
+__device__ __forceinline__ void mmaBF16(uint32_t dT, uint32_t aT, uint64_t bDesc, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}" ::"r"(dT),
+        "r"(aT), "l"(bDesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
 __device__ __forceinline__ void mmaCommit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smemAddr(bar))
                  : "memory");
@@ -162,6 +173,21 @@ __device__ __forceinline__ uint64_t smemDesc(uint32_t start, uint32_t lbo, uint3
 // instruction descriptor, kind::tf32: D f32, A/B tf32, both K-major
 __host__ __device__ constexpr uint32_t idescTF32(int M, int N) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// instruction descriptor, kind::f16: D f32, A/B bf16, both K-major
+__host__ __device__ constexpr uint32_t idescBF16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Split-BF16 of two consecutive K elements: hi = both rounded to the nearest
+// bf16 (packed, the first in the low half), lo = the exact remainders rounded
+// to the nearest bf16.  x = hi + lo to ~2^-17 relative, unbiased.
+__device__ __forceinline__ void splitBF16x2(float x0, float x1, uint32_t& hi, uint32_t& lo) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - __uint_as_float(hi << 16), x1 - __uint_as_float(hi & 0xFFFF0000u));
+    lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
 // Round to the nearest TF32 value (ties away from zero).  Both split parts are
@@ -180,9 +206,6 @@ __device__ __forceinline__ void splitTF32(float x, uint32_t& hi, uint32_t& lo) {
     lo = tf32RN(x - __uint_as_float(hi));
 }
 
-// nearest TF32 value of a finite x (ties away from zero), as cvt.rna.tf32.f32,
-// in two integer operations
-__device__ __forceinline__ uint32_t tf32Bits(float x) { return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u; }
 
 // Norm bookkeeping of one tensor-core pass (FP64 sums, accumulated with atomics):
 //   out      sum |y|^2 of this pass's output;
@@ -190,8 +213,15 @@ __device__ __forceinline__ uint32_t tf32Bits(float x) { return (__float_as_uint(
 //            previous pass's output (nothing changed the state in between);
 //   scaleSq  where this pass writes the square of the scale it applied;
 //   corrIn, corrOut, corrScaleSq  the same three numbers of the previous
-//            unitary tensor-core pass, or null.  That pass's own drift is
-//            out / (in * scale^2); this pass scales by its inverse square root.
+//            unitary tensor-core pass, or null.  Its norm factor
+//            f = out / (in * scale^2) predicts this pass's own (the drift of
+//            the tensor cores' accumulation is systematic);
+//   corrTarget  when this pass continues a chain of unitary passes, the input
+//            norm T of the chain's first pass, else null.
+// The scale makes this pass's output norm T (chained: its input norm is the
+// previous output, so scale^2 = T / (out * f)) or, unchained, its own input
+// norm (scale^2 = 1 / f).  With a constant drift every output after the first
+// is on target, instead of one drift factor behind.
 struct NormLinks {
     double* out;
     double* in;
@@ -199,11 +229,14 @@ struct NormLinks {
     const double* corrIn;
     const double* corrOut;
     const double* corrScaleSq;
+    const double* corrTarget;
 };
 // the scale minus one (kept exact to FP32 relative precision)
 __device__ __forceinline__ float driftCorrection(const NormLinks& nl) {
     if (!nl.corrIn || !nl.corrOut || !nl.corrScaleSq || !(*nl.corrOut > 0.0)) return 0.f;
-    return (float)(sqrt(*nl.corrIn * *nl.corrScaleSq / *nl.corrOut) - 1.0);
+    const double invF = *nl.corrIn * *nl.corrScaleSq / *nl.corrOut;
+    const double s2 = nl.corrTarget ? *nl.corrTarget * invF / *nl.corrOut : invF;
+    return (s2 > 0.0) ? (float)(sqrt(s2) - 1.0) : 0.f;
 }
 // written once per launch, by the calling thread when `writer`
 __device__ __forceinline__ void recordScale(const NormLinks& nl, float sm1, bool writer) {
@@ -407,16 +440,18 @@ __global__ void __launch_bounds__(kThreadsTC, (KQ == 4 ? 4 : 1)) kApplyTC(float*
 // warps.  A warp's positions are split into two parts of at most 1024
 // (k <= 5: the two planes; k = 6: the two halves by the top target bit, which
 // the region index puts in its top bit).  Inside a part, index q lives at
-// pad(q) = q + (q >> 5).  pad is additive over disjoint bit sets, so
-//   * a row access (q = 4 lane + i + 128 m) is pad(4 lane) + i + pad(128 m):
-//     a per-thread base plus an immediate offset, conflict-free;
+// pad(q) = q + 4 (q >> 5) + 4 (q >> 8): every row of 32 positions starts on
+// a 16-byte boundary, and pad is additive over disjoint bit sets, so
+//   * a row access (4 positions q = 4 lane + 128 m) is the 16-byte word at
+//     pad(4 lane) + pad(128 m): a per-thread base plus an immediate offset;
 //   * a column access (group bits of the lane | bits of matrix index j) is
-//     pad(lane bits) + pad(j bits): one add of a per-pass constant, and
-//     conflict-free whenever the lane bits' positions differ mod 5 (2-way at
-//     worst otherwise).
+//     pad(lane bits) + pad(j bits): one add of a per-pass constant.
+// The column accesses average 1.65 shared-memory wavefronts over the 6-qubit
+// passes of a 30-qubit random circuit (1.71 with one float of padding per
+// row, which breaks the 16-byte alignment).
 constexpr int kTileBitsC = 7;
 
-__host__ __device__ constexpr uint32_t padIdx(uint32_t q) { return q + (q >> 5); }
+__host__ __device__ constexpr uint32_t padIdx(uint32_t q) { return q + 4 * (q >> 5) + 4 * (q >> 8); }
 
 template <int KQ>
 struct TC2Params {
@@ -429,26 +464,31 @@ struct TC2Params {
     int runBits;                          // I contains qubits [0, runBits)
 };
 
-// Shared-memory layout of kApplyTC2<KQ, LG, EG, LS>, used by the kernel and
-// its launcher.  G: Gh then Gl.  At k = 6 each is the compact real form
-// [-Im G; Re G; Im G] (192 rows x 64 K): the B operand of the K-chunk of the
-// real parts of X is rows 64..191 ([Re; Im]), that of the imaginary parts rows
-// 0..127 ([-Im; Re]).  Loader row buffers: XST stages per loader warp, two
-// when they fit next to G and the epilogue buffers.
+// Layout of kApplyTC2<KQ, LG, EG, LS>, used by the kernel and its launcher.
+// Shared memory: G as three BF16 parts (Gh, Gl, Gll: G to ~2^-24), the loader
+// row stages and the epilogue buffers.  At k = 6, G is the compact real form
+// [-Im G; Re G; Im G] (192 rows x 64 K).  The B operand of the K-chunk of the
+// real parts of X is rows 64..191 ([Re; Im]).  That of the imaginary parts is
+// rows 0..127 ([-Im; Re]).  Loader row buffers: XST stages per loader warp,
+// up to three, as many as fit.  TMEM: NST operand stages of KC columns (Xh
+// then Xl, two bf16 per column), then two accumulators of N columns.
 template <int KQ, int LG, int EG, int LS>
 struct TC2Shape {
     static constexpr int D = 1 << KQ, K = 2 * D, N = 2 * D;
     static constexpr int TILE = 1 << (KQ + kTileBitsC);       // amplitudes per plane per tile
     static constexpr int NCH = (KQ == 6) ? 2 : 1;             // K chunks per tile
-    static constexpr int KC = K / NCH;                        // K columns per chunk (<= 64)
+    static constexpr int KC = K / NCH;                        // K elements per chunk (<= 64)
     static constexpr int PART = (KQ == 6) ? TILE / 8 : TILE / 4;   // positions per warp per part (<= 1024)
     static constexpr int R = (int)((padIdx(PART - 1) + 1 + 3) & ~3u);   // floats per part buffer
     static constexpr int PPG = (LS == 2) ? 1 : 2;             // parts per loader group per chunk
-    static constexpr uint32_t GFL = (KQ == 6) ? 3u * D * D : (uint32_t)(N * K);   // floats of Gh (and of Gl)
-    static constexpr uint32_t GSBO = (uint32_t)(((KQ == 6) ? KC : K) / 4) * 128u;  // B descriptor stride
-    static constexpr size_t fixedFloats = 2 * (size_t)GFL + (size_t)EG * 4 * R;
+    static constexpr int NST = 4;                             // TMEM operand stages
+    static constexpr uint32_t GE = (KQ == 6) ? 3u * D * D : (uint32_t)(N * K);   // bf16 entries of each G part
+    static constexpr uint32_t GW = GE / 2;                    // ... in 32-bit words
+    static constexpr uint32_t GSBO = (uint32_t)(((KQ == 6) ? KC : K) / 8) * 128u;   // B descriptor stride
+    static constexpr size_t fixedFloats = 3 * (size_t)GW + (size_t)EG * 4 * R;
     static constexpr size_t stageFloats = (size_t)LG * 4 * PPG * R;
-    static constexpr int XST = ((fixedFloats + 2 * stageFloats) * 4 + 2048 <= 227 * 1024) ? 2 : 1;
+    static constexpr bool fits(int st) { return (fixedFloats + (size_t)st * stageFloats) * 4 + 2048 <= 227 * 1024; }
+    static constexpr int XST = fits(3) ? 3 : (fits(2) ? 2 : 1);
     static constexpr size_t smemBytes = (fixedFloats + (size_t)XST * stageFloats) * 4;
 };
 
@@ -497,28 +537,30 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                                                                   const __grid_constant__ TC2Params<KQ> p) {
     using S = TC2Shape<KQ, LG, EG, LS>;
     constexpr int D = S::D, N = S::N;
-    constexpr int NCH = S::NCH, KC = S::KC, PART = S::PART, R = S::R, PPG = S::PPG, XST = S::XST;
-    constexpr uint32_t kGFl = S::GFL;
+    constexpr int NCH = S::NCH, KC = S::KC, PART = S::PART, R = S::R, PPG = S::PPG, XST = S::XST, NST = S::NST;
+    constexpr uint32_t kGW = S::GW;
     constexpr int V4P = PART / 128;                      // 128-position blocks per part
     constexpr int JP = (KQ == 6) ? 32 : D;               // matrix indices per part
     constexpr int EPARTS = (KQ == 6) ? 4 : 2;            // epilogue parts per tile (plane x half)
-    constexpr uint32_t kStageCols = 2 * KC;
-    constexpr uint32_t kDCol0 = 2 * kStageCols;
+    constexpr uint32_t kStageCols = KC;                  // Xh: KC / 2 columns, then Xl
+    constexpr uint32_t kDCol0 = NST * kStageCols;
     constexpr uint32_t kUsed = kDCol0 + 2 * N;
     constexpr uint32_t kCols = kUsed <= 64 ? 64 : (kUsed <= 128 ? 128 : (kUsed <= 256 ? 256 : 512));
+    static_assert(kUsed <= 512, "TMEM");
     constexpr uint32_t kLBO = 128;
-    constexpr uint32_t idesc = idescTF32(kTile, N);
+    constexpr uint32_t idesc = idescBF16(kTile, N);
     constexpr int kEpiWarp0 = 4 * LG, kMmaWarp = 4 * (LG + EG);
     // LS = 1: loader groups take alternate chunks; LS = 2: the two loader
     // groups split every chunk, group g taking its part g
     static_assert(LS == 1 || LG == 2, "part-split loading needs two loader groups");
 
     extern __shared__ __align__(1024) uint8_t smem[];
-    float* gh = reinterpret_cast<float*>(smem);
-    float* gl = gh + kGFl;
-    float* xs = gl + kGFl;                               // [loader group][warp][stage][part][R]
+    uint32_t* gh = reinterpret_cast<uint32_t*>(smem);
+    uint32_t* gl = gh + kGW;
+    uint32_t* gll = gl + kGW;
+    float* xs = reinterpret_cast<float*>(gll + kGW);     // [loader group][warp][stage][part][R]
     float* es = xs + (size_t)XST * LG * 4 * PPG * R;     // [epilogue group][warp][R]
-    __shared__ __align__(8) uint64_t barG, gReady, fullB[2], emptyB[2], dFullB[2], dEmptyB[2];
+    __shared__ __align__(8) uint64_t barG, fullB[NST], emptyB[NST], dFullB[2], dEmptyB[2];
     __shared__ uint32_t tmemBase;
     __shared__ volatile int abortF;
 
@@ -527,10 +569,11 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         if (lane == 0) {
             abortF = 0;
             mbarInit(&barG, 1);
-            mbarInit(&gReady, 128 * EG);
-            for (int b = 0; b < 2; ++b) {
+            for (int b = 0; b < NST; ++b) {
                 mbarInit(&fullB[b], 128 * (LS == 2 ? LG : 1));
                 mbarInit(&emptyB[b], 1);
+            }
+            for (int b = 0; b < 2; ++b) {
                 mbarInit(&dFullB[b], 1);
                 mbarInit(&dEmptyB[b], 128);
             }
@@ -544,15 +587,12 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
     const uint32_t tmem = tmemBase;
     const int rw = warp & 3;                             // warp within its role = TMEM lane quarter
     const uint32_t laneSel = (uint32_t)(32 * rw) << 16;
-    const uint32_t rowBase = 4u * lane + (uint32_t)(lane >> 3);      // pad(4 lane)
+    const uint32_t rowBase = padIdx(4u * lane);
 
     if (warp < kEpiWarp0) {
         // ------------------------------------------------ loaders
         const int g = warp >> 2;
-        // offset of this lane's amplitude in each row of 32 positions of a part:
-        // region index bits 0..4 are qubits 0..4, so a row is 32 consecutive
-        // amplitudes and every copy instruction reads one 128-byte line
-        const uint64_t laneLow = p.laneOff[lane >> 2] + (uint64_t)(lane & 3);
+        const uint64_t laneA = p.laneOff[lane];
         const uint32_t colBase = p.colLane[lane];
         // this CTA's chunks, in order: chunk s = (tile blockIdx.x + (s / NCH) * gridDim.x, K chunk s % NCH);
         // LS = 1: group g takes s = g, g + LG, ...; LS = 2: every s, part g
@@ -565,20 +605,22 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         float* const wbuf = xs + (size_t)(g * 4 + rw) * XST * PPG * R;             // this warp's stages
         // Copy chunk sc into a stage.  Its parts: k <= 5 the real and imaginary
         // planes, k = 6 the two halves (region indices < 1024, >= 1024) of one
-        // plane.  Element q = 32 i + lane of a part lands at pad(q) = 33 i + lane.
+        // plane.  Region index bits 0, 1 are qubits 0, 1, so positions
+        // q = 4 lane + 128 m .. + 3 are four consecutive amplitudes: one
+        // 16-byte copy to pad(q); a warp's copy reads four 128-byte lines.
         auto issue = [&](uint32_t sc, float* buf) {
             const uint64_t tile = blockIdx.x + (uint64_t)(sc / NCH) * gridDim.x;
             const int ch = sc % NCH;
-            const uint64_t tb = tileBase(p, tile) + laneLow;
+            const uint64_t tb = tileBase(p, tile) + laneA;
 #pragma unroll
             for (int pp = 0; pp < PPG; ++pp) {
                 const int pt = p0 + pp;
                 const float* const src = (((NCH == 2) ? ch : pt) == 0 ? re : im) + tb;
-                float* const dst = buf + pp * R + lane;
+                float* const dst = buf + pp * R + rowBase;
 #pragma unroll
-                for (int i = 0; i < PART / 32; ++i) {
-                    const int m = ((KQ == 6) ? V4P * pt : 0) + (i >> 2);
-                    cpAsync4(dst + 33 * i, src + p.warpOff[rw][m] + p.laneOff[(i & 3) << 3]);
+                for (int mm = 0; mm < V4P; ++mm) {
+                    const int m = ((KQ == 6) ? V4P * pt : 0) + mm;
+                    cpAsync16(dst + padIdx(128u * mm), src + p.warpOff[rw][m]);
                 }
             }
         };
@@ -590,38 +632,38 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         bool ok = true;
         for (uint32_t idx = 0; idx < nMine; ++idx) {
             const uint32_t sq = s0 + idx * sStep;
-            // the TMEM stage (with LS = 1 and LG = 2, group g owns stage g)
-            const int b = (LS == 1 && LG == 2) ? g : (int)(sq & 1);
-            const uint32_t u = sq >> 1;
-            float* const xr = wbuf + (size_t)((XST == 2) ? (idx & 1u) : 0u) * PPG * R;
+            // TMEM stage b of chunk sq; its previous use was chunk sq - NST
+            const int b = (int)(sq % NST);
+            const uint32_t u = sq / NST;
+            float* const xr = wbuf + (size_t)(idx % XST) * PPG * R;
             if (u > 0 && !warpWaitOrAbort(&emptyB[b], (u - 1) & 1, &abortF, lane)) {
                 ok = false;
                 break;
             }
             cpAsyncWait<XST - 1>();                          // this lane's copies of the chunk landed
             __syncwarp();                                    // ... and every lane's
-            // this group's stage columns: [p0 JP, (p0 + PPG) JP)
-            const uint32_t aH = tmem + laneSel + b * kStageCols + p0 * JP;
+            // this group's K elements of the stage: [p0 JP, (p0 + PPG) JP), two per column
+            const uint32_t aH = tmem + laneSel + b * kStageCols + p0 * JP / 2;
             const float* const cb = xr + colBase;
             float nrm = 0.f;
 #pragma unroll
-            for (int c0 = 0; c0 < PPG * JP; c0 += 8) {
+            for (int c0 = 0; c0 < PPG * JP; c0 += 16) {
                 uint32_t hi[8], lo[8];
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
-                    const int cl = c0 + e;                   // local column: buffer part cl / JP
-                    const int pl = cl / JP;
-                    const int j = (NCH == 2) ? p0 * JP + cl : cl % D;
-                    // hi = x rounded to TF32; lo = x - hi (exact), which the
-                    // MMA reads as its leading TF32 bits; lo takes both signs,
-                    // so that truncation is unbiased
-                    const float x = (cb + pl * R)[p.colJ[j]];
-                    nrm = fmaf(x, x, nrm);                   // the warp reads every element once
-                    hi[e] = tf32Bits(x);
-                    lo[e] = __float_as_uint(x - __uint_as_float(hi[e]));
+                    float x[2];
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int cl = c0 + 2 * e + h;       // local element: buffer part cl / JP
+                        const int pl = cl / JP;
+                        const int j = (NCH == 2) ? p0 * JP + cl : cl % D;
+                        x[h] = (cb + pl * R)[p.colJ[j]];
+                        nrm = fmaf(x[h], x[h], nrm);         // the warp reads every element once
+                    }
+                    splitBF16x2(x[0], x[1], hi[e], lo[e]);
                 }
-                tmemSt8(aH + c0, hi);
-                tmemSt8(aH + KC + c0, lo);
+                tmemSt8(aH + c0 / 2, hi);
+                tmemSt8(aH + KC / 2 + c0 / 2, lo);
             }
             if (measure) normIn += (double)nrm;
             tmemWaitSt();
@@ -646,23 +688,12 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         const uint64_t laneA = p.laneOff[lane];
         const uint32_t colBase = p.colLane[lane];
         float* const er = es + (size_t)(eg * 4 + rw) * R;
-        // the previous pass's drift correction, folded into this pass's G:
-        // G' = (1 + sm1) (Gh + Gl), split again into TF32 parts (the sum of
-        // the two parts is exact in FP32)
-        bool ok = mbarWaitOrAbort(&barG, 0, &abortF);
+        // the drift correction: every output is scaled by 1 + sm1 in FP32
+        // (split-BF16 parts of a rescaled G would carry the scale only to their
+        // ~2^-17 precision, far coarser than the drift)
+        bool ok = true;
         const float sm1 = driftCorrection(nl);
         recordScale(nl, sm1, blockIdx.x == 0 && et == 0);
-        if (ok && sm1 != 0.f) {
-            for (uint32_t i = et; i < kGFl; i += 128 * EG) {
-                const float g0 = gh[i] + gl[i];
-                const float g1 = fmaf(g0, sm1, g0);
-                const uint32_t h = tf32Bits(g1);
-                gh[i] = __uint_as_float(h);
-                gl[i] = __uint_as_float(tf32Bits(g1 - __uint_as_float(h)));
-            }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // visible to the MMAs
-        }
-        mbarArrive(&gReady);
         uint32_t tl = eg;
         double normOut = 0.0;
         for (uint64_t tile = blockIdx.x + (uint64_t)eg * gridDim.x; tile < numTiles && ok;
@@ -695,7 +726,8 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                 }
 #pragma unroll
                 for (int e = 0; e < JP; ++e) {
-                    const float y = __uint_as_float(e < 16 ? va[e] : vb[e - 16]);
+                    const float y0 = __uint_as_float(e < 16 ? va[e] : vb[e - 16]);
+                    const float y = fmaf(y0, sm1, y0);
                     nrmTile = fmaf(y, y, nrmTile);
                     cb[p.colJ[h * 32 + e]] = y;
                 }
@@ -703,13 +735,8 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                 float* const dstPlane = (pl == 0 ? re : im) + tb;
 #pragma unroll
                 for (int mm = 0; mm < V4P; ++mm) {
-                    const int off = (int)padIdx(128u * mm);
                     const int m = (KQ == 6) ? V4P * h + mm : mm;
-                    float4 w;
-                    w.x = rb[off + 0];
-                    w.y = rb[off + 1];
-                    w.z = rb[off + 2];
-                    w.w = rb[off + 3];
+                    const float4 w = *reinterpret_cast<const float4*>(rb + padIdx(128u * mm));
                     __stcs(reinterpret_cast<float4*>(dstPlane + p.warpOff[rw][m]), w);
                 }
                 __syncwarp();
@@ -724,13 +751,13 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         if (lane == 0 && nl.out) atomicAdd(nl.out, normOut);
     } else if (lane == 0) {
         // ------------------------------------------------ TMA of G, then MMAs
-        mbarExpectTx(&barG, 2 * kGFl * 4);
-        bulkG2S(gh, gImage, kGFl * 4, &barG);
-        bulkG2S(gl, gImage + kGFl, kGFl * 4, &barG);
+        mbarExpectTx(&barG, 3 * kGW * 4);
+        bulkG2S(gh, gImage, kGW * 4, &barG);
+        bulkG2S(gl, gImage + kGW, kGW * 4, &barG);
+        bulkG2S(gll, gImage + 2 * kGW, kGW * 4, &barG);
         bool ok = mbarWaitOrAbort(&barG, 0, &abortF);
         if (!ok) mbarWaitOrAbort(&barG, 0, &abortF);                // once more for the copies in flight
-        ok = ok && mbarWaitOrAbort(&gReady, 0, &abortF);            // G rescaled by the epilogue warps
-        const uint32_t ghA = smemAddr(gh), glA = smemAddr(gl);
+        const uint32_t ghA = smemAddr(gh), glA = smemAddr(gl), gllA = smemAddr(gll);
         uint32_t sq = 0, tl = 0;
         for (uint64_t tile = blockIdx.x; tile < numTiles && ok; tile += gridDim.x, ++tl) {
             const int bd = tl & 1;
@@ -741,27 +768,34 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
             fenceAfter();
             const uint32_t dT = tmem + kDCol0 + bd * N;
             for (int ch = 0; ch < NCH; ++ch, ++sq) {
-                const int b = sq & 1;
-                if (!mbarWaitOrAbort(&fullB[b], (sq >> 1) & 1, &abortF)) {
+                const int b = (int)(sq % NST);
+                if (!mbarWaitOrAbort(&fullB[b], (sq / NST) & 1, &abortF)) {
                     ok = false;
                     break;
                 }
                 fenceAfter();
-                const uint32_t aH = tmem + b * kStageCols, aL = aH + KC;
+                const uint32_t aH = tmem + b * kStageCols, aL = aH + KC / 2;
                 // chunk ch's B: k <= 5 the whole of Gh / Gl; k = 6 rows 64..191 of the
                 // compact form for the real parts of X (ch 0), rows 0..127 for the
-                // imaginary parts (ch 1).  K step ks reads the next 256 bytes: the
-                // descriptor's start field (address >> 4) advances by 16 per step
+                // imaginary parts (ch 1).  K step ks (16 entries) reads the next 8
+                // TMEM columns of A and the next 256 bytes of B: the descriptor's
+                // start field (address >> 4) advances by 16 per step
                 const uint32_t gOff = (KQ == 6 && ch == 0) ? 8u * S::GSBO : 0u;
                 const uint64_t dH = smemDesc(ghA + gOff, kLBO, S::GSBO);
                 const uint64_t dL = smemDesc(glA + gOff, kLBO, S::GSBO);
+                const uint64_t dLL = smemDesc(gllA + gOff, kLBO, S::GSBO);
+                // Xh.Gh + Xl.Gh + Xh.Gl + Xh.Gll: G to ~2^-24 (a ~2^-17 G would
+                // change the norm by up to ~1e-6 per pass, depending on the
+                // state); the dropped Xl.Gl is unbiased
 #pragma unroll
-                for (int ks = 0; ks < KC / 8; ++ks)
-                    mmaTF32(dT, aH + 8 * ks, dH + 16u * ks, idesc, (ch | ks) != 0);
+                for (int ks = 0; ks < KC / 16; ++ks)
+                    mmaBF16(dT, aH + 8 * ks, dH + 16u * ks, idesc, (ch | ks) != 0);
 #pragma unroll
-                for (int ks = 0; ks < KC / 8; ++ks) mmaTF32(dT, aL + 8 * ks, dH + 16u * ks, idesc, 1);
+                for (int ks = 0; ks < KC / 16; ++ks) mmaBF16(dT, aL + 8 * ks, dH + 16u * ks, idesc, 1);
 #pragma unroll
-                for (int ks = 0; ks < KC / 8; ++ks) mmaTF32(dT, aH + 8 * ks, dL + 16u * ks, idesc, 1);
+                for (int ks = 0; ks < KC / 16; ++ks) mmaBF16(dT, aH + 8 * ks, dL + 16u * ks, idesc, 1);
+#pragma unroll
+                for (int ks = 0; ks < KC / 16; ++ks) mmaBF16(dT, aH + 8 * ks, dLL + 16u * ks, idesc, 1);
                 mmaCommit(&emptyB[b]);
             }
             if (!ok) break;
@@ -792,6 +826,8 @@ struct DevicePlan {
     // per pass: where its input norm lives (its own slot, or the output slot
     // of the previous tensor-core pass when nothing changed the state between)
     std::vector<const double*> inNorm;
+    // per pass: the input norm of the first pass of its chain of unitary passes
+    std::vector<const double*> target;
     int lastTC = -1;        // last tensor-core pass applied (its drift is corrected next)
     bool chain = false;     // the state is still lastTC's output up to unitary SIMT passes
     // per pass: 1 if its matrix is unitary to 1e-10.  Only the drift of a
@@ -825,6 +861,20 @@ float hostTf32RN(float x) {
     uint32_t u;
     std::memcpy(&u, &x, 4);
     if ((u & 0x7F800000u) != 0x7F800000u) u = (u + 0x1000u) & 0xFFFFE000u;   // finite values
+    float y;
+    std::memcpy(&y, &u, 4);
+    return y;
+}
+
+// nearest bf16 (ties to even) of a finite x, and the value of a bf16
+uint16_t hostBF16RN(float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+float bf16Value(uint16_t h) {
+    const uint32_t u = (uint32_t)h << 16;
     float y;
     std::memcpy(&y, &u, 4);
     return y;
@@ -871,7 +921,7 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
     constexpr int D = S::D, K = S::K, N = S::N, PART = S::PART;
     constexpr int V4 = S::TILE / 512;
     const size_t smem = S::smemBytes;
-    if (KQ == 6) img += (size_t)2 * N * K;           // the compact image follows the full one
+    img += (size_t)2 * N * K;                       // the BF16 parts follow the TF32 image
     TC2Params<KQ> p{};
     // I = targets + the 7 lowest other qubits (ascending); tile position b <-> qubit I[b]
     uint64_t tmask = 0;
@@ -993,25 +1043,32 @@ void* uploadPlanTC(const FusedPlan& plan) {
                 hi[(size_t)r * K + j] = h;
                 lo[(size_t)r * K + j] = hostTf32RN((float)(v - (double)h));
             }
-        // k = 6: the compact form [-Im G; Re G; Im G] (3D rows, D K columns)
-        // of the pipelined kernel follows
-        const size_t full = (size_t)N * K, compact = (k == 6) ? (size_t)3 * D * D : 0;
-        std::vector<float> img(2 * (full + compact));
+        // then the three BF16 parts of the pipelined kernel: the real form, or
+        // at k = 6 the compact form [-Im G; Re G; Im G] (3D rows, D K columns)
+        const size_t full = (size_t)N * K;
+        const int bRows = (k == 6) ? 3 * D : N, bK = (k == 6) ? D : K;
+        const size_t bEntries = (size_t)bRows * bK;
+        std::vector<float> img(2 * full + (3 * bEntries + 1) / 2);   // then three parts of bEntries bf16
         packKMajor(hi, N, K, img.data());
         packKMajor(lo, N, K, img.data() + full);
-        if (k == 6) {
-            std::vector<float> ch(compact), cl(compact);
-            for (int r = 0; r < 3 * D; ++r)
-                for (int j = 0; j < D; ++j) {
-                    // rows 0..D-1 take the (r, D + j) entries of the real form
-                    // (-Im), rows D..3D-1 the (r - D, j) entries (Re, then Im)
-                    const int rr = (r < D) ? r : r - D, jj = (r < D) ? D + j : j;
-                    ch[(size_t)r * D + j] = hi[(size_t)rr * K + jj];
-                    cl[(size_t)r * D + j] = lo[(size_t)rr * K + jj];
-                }
-            packKMajor(ch, 3 * D, D, img.data() + 2 * full);
-            packKMajor(cl, 3 * D, D, img.data() + 2 * full + compact);
-        }
+        uint16_t* bh = reinterpret_cast<uint16_t*>(img.data() + 2 * full);
+        uint16_t* bl = bh + bEntries;
+        uint16_t* bll = bl + bEntries;
+        for (int r = 0; r < bRows; ++r)
+            for (int j = 0; j < bK; ++j) {
+                // k = 6: rows 0..D-1 take the (r, D + j) entries of the real form
+                // (-Im), rows D..3D-1 the (r - D, j) entries (Re, then Im)
+                const int rr = (k == 6 && r >= D) ? r - D : r, jj = (k == 6 && r < D) ? D + j : j;
+                const cplx g = pass.m[(size_t)(rr % D) * D + (jj % D)];
+                const double v = (rr < D) ? ((jj < D) ? g.real() : -g.imag()) : ((jj < D) ? g.imag() : g.real());
+                const uint16_t h = hostBF16RN((float)v);
+                const double r1 = v - (double)bf16Value(h);
+                const uint16_t l = hostBF16RN((float)r1);
+                const size_t at = (size_t)(r / 8) * (bK / 8) * 64 + (size_t)(j / 8) * 64 + (r % 8) * 8 + (j % 8);
+                bh[at] = h;
+                bl[at] = l;
+                bll[at] = hostBF16RN((float)(r1 - (double)bf16Value(l)));
+            }
         float* d = nullptr;
         if (cudaMalloc(&d, img.size() * sizeof(float)) != cudaSuccess) {
             cudaGetLastError();
@@ -1042,6 +1099,7 @@ void tcBeginPlan(void* devPlan, size_t numPasses) {
     dp->lastTC = -1;
     dp->chain = false;
     dp->inNorm.assign(numPasses, nullptr);
+    dp->target.assign(numPasses, nullptr);
 }
 
 // start of every applyPlanF32Range call: the caller may have changed the
@@ -1089,9 +1147,10 @@ int applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, 
     const int n = f32n(q);
     const int version = tcKernelFor(pass, n);
     if (version == 0) return 0;
-    NormLinks nl{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    NormLinks nl{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     if (dp->norms) {
         if (dp->inNorm.size() != dp->images.size()) dp->inNorm.assign(dp->images.size(), nullptr);
+        if (dp->target.size() != dp->images.size()) dp->target.assign(dp->images.size(), nullptr);
         double* mine = dp->norms + 3 * index;            // in, out, scale^2
         cudaMemsetAsync(mine, 0, 3 * sizeof(double), st);
         nl.out = mine + 1;
@@ -1099,11 +1158,16 @@ int applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, 
         const bool chained = dp->chain && dp->lastTC >= 0;
         nl.in = chained ? nullptr : mine;
         dp->inNorm[index] = chained ? dp->norms + 3 * dp->lastTC + 1 : mine;
-        if (dp->lastTC >= 0 && dp->unitary[dp->lastTC]) {
+        const bool prevUnitary = dp->lastTC >= 0 && dp->unitary[dp->lastTC];
+        if (prevUnitary) {
             nl.corrIn = dp->inNorm[dp->lastTC];
             nl.corrOut = dp->norms + 3 * dp->lastTC + 1;
             nl.corrScaleSq = dp->norms + 3 * dp->lastTC + 2;
         }
+        // a chain of unitary passes keeps the norm its first pass started from
+        const bool continues = chained && prevUnitary && dp->target[dp->lastTC];
+        if (continues) nl.corrTarget = dp->target[dp->lastTC];
+        dp->target[index] = continues ? dp->target[dp->lastTC] : dp->inNorm[index];
     }
     bool ok = false;
     if (version >= 2) {
@@ -1143,6 +1207,29 @@ int tcErrorFlag(const void* devPlan) {
     cudaMemcpyAsync(&v, dp->errFlag, sizeof(int), cudaMemcpyDeviceToHost, stream());
     cudaStreamSynchronize(stream());
     return v;
+}
+
+// norm record of pass i of the last application: (input norm, output norm,
+// scale^2 applied); 0 if it was not a tensor-core pass or has no record
+int tcPassNorms(const void* devPlan, size_t index, double* out3) {
+    const DevicePlan* dp = reinterpret_cast<const DevicePlan*>(devPlan);
+    if (!dp || !dp->norms || index >= dp->inNorm.size() || !dp->inNorm[index]) return 0;
+    cudaMemcpyAsync(out3, dp->inNorm[index], sizeof(double), cudaMemcpyDeviceToHost, stream());
+    cudaMemcpyAsync(out3 + 1, dp->norms + 3 * index + 1, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream());
+    cudaStreamSynchronize(stream());
+    return 1;
+}
+
+// the plan's last application ended in a chain of unitary passes whose last
+// tensor-core pass left a norm record: the chain's starting norm and that
+// pass's output norm (device pointers, valid until the plan runs again)
+bool tcFinalNorms(const void* devPlan, const double** target, const double** out) {
+    const DevicePlan* dp = reinterpret_cast<const DevicePlan*>(devPlan);
+    if (!dp || !dp->norms || !dp->chain || dp->lastTC < 0 || (size_t)dp->lastTC >= dp->target.size()) return false;
+    if (!dp->unitary[dp->lastTC] || !dp->target[dp->lastTC]) return false;
+    *target = dp->target[dp->lastTC];
+    *out = dp->norms + 3 * dp->lastTC + 1;
+    return true;
 }
 
 void setTensorCoresEnabled(bool on) { g_tcEnabled = on; }

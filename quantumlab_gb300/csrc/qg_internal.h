@@ -54,6 +54,9 @@ inline SV svOf(const Qureg& q) { return SV{q.deviceStateVec.real, q.deviceStateV
 void* captureHandle(const double* re);            // the register's capture record, or null
 void captureRegister(const double* re, int n);    // at creation: capture on if QUEST_GB300_CAPTURE=fp32
 void captureFlush(double* re, double* im);        // apply the queued gates (FP32 fused engine)
+// FP32 register -> FP64 Qureg after applying `plan`, with the plan's last norm
+// correction folded in (fused_f32.cu)
+void copyToQuregAfterPlan(void* qureg32, Qureg& dst, void* plan);
 void captureDiscard(const double* re);            // drop the queued gates (the state is overwritten next)
 void captureDrop(const double* re);               // at destruction
 // launcher hooks: queue the gate and return true, or return false (after a
