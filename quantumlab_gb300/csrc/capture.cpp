@@ -93,6 +93,19 @@ void captureRegister(const double* re, int n) {
 // apply and clear the queue of a capture record (caller holds no lock)
 static void flushRecord(Capture* c, double* re, double* im) {
     if (!c || c->gates.empty()) return;
+    if (!c->q32) c->q32 = quest_gb300_createQuregF32(c->n);
+    if (!c->q32) {
+        invalidQuESTInputError("Could not allocate the FP32 register of the captured gates.", "captureFlush");
+        c->gates.clear();
+        return;
+    }
+    Qureg view;
+    memset(&view, 0, sizeof view);
+    view.numAmpsTotal = 1LL << c->n;
+    view.deviceStateVec.real = re;
+    view.deviceStateVec.imag = im;
+    // the FP64 -> FP32 conversion runs on the device while the host plans
+    quest_gb300_copyFromQureg(c->q32, view);
     FusedPlan* plan = new FusedPlan();
     plan->numQubits = c->n;
     plan->maxFused = std::min(g_capMaxFused, c->n);
@@ -103,18 +116,6 @@ static void flushRecord(Capture* c, double* re, double* im) {
         delete plan;
         return;
     }
-    if (!c->q32) c->q32 = quest_gb300_createQuregF32(c->n);
-    if (!c->q32) {
-        invalidQuESTInputError("Could not allocate the FP32 register of the captured gates.", "captureFlush");
-        delete plan;
-        return;
-    }
-    Qureg view;
-    memset(&view, 0, sizeof view);
-    view.numAmpsTotal = 1LL << c->n;
-    view.deviceStateVec.real = re;
-    view.deviceStateVec.imag = im;
-    quest_gb300_copyFromQureg(c->q32, view);
     quest_gb300_applyPlanF32(c->q32, plan);
     copyToQuregAfterPlan(c->q32, view, plan);
     c->gatesApplied += (long long)plan->gates.size();
@@ -175,6 +176,7 @@ static bool captureGate(SV s, uint64_t mask, const std::function<void(std::vecto
         apply(v, l);
         for (int r = 0; r < D; ++r) g.m[(size_t)r * D + col] = v[r];
     }
+    g.unitary = matrixIsUnitary(g.m, D);
     c->gates.push_back(std::move(g));
     return true;
 }

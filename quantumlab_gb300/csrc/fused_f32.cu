@@ -142,31 +142,51 @@ __global__ void kZeroF32(float* __restrict__ re, float* __restrict__ im) {
     re[0] = 1.f;
     (void)im;
 }
+// FP64 <-> FP32 conversions: four amplitudes per thread with 16-byte accesses
+// (the arrays start on 32-byte boundaries); the tail of n % 4 amplitudes is
+// converted one by one
+constexpr unsigned kConvThreads = 256;
+inline unsigned convBlocks(uint64_t n) { return (unsigned)(((n + 3) / 4 + kConvThreads - 1) / kConvThreads); }
+
 __global__ void kF64toF32(const double* __restrict__ sr, const double* __restrict__ si, float* __restrict__ dr,
                           float* __restrict__ di, uint64_t n) {
-    const uint64_t t = (uint64_t)blockIdx.x * 256 + threadIdx.x;
-    if (t >= n) return;
-    dr[t] = (float)sr[t];
-    di[t] = (float)si[t];
+    const uint64_t i = 4 * ((uint64_t)blockIdx.x * kConvThreads + threadIdx.x);
+    if (i + 3 < n) {
+        const double2 r0 = *reinterpret_cast<const double2*>(sr + i), r1 = *reinterpret_cast<const double2*>(sr + i + 2);
+        const double2 m0 = *reinterpret_cast<const double2*>(si + i), m1 = *reinterpret_cast<const double2*>(si + i + 2);
+        *reinterpret_cast<float4*>(dr + i) = make_float4((float)r0.x, (float)r0.y, (float)r1.x, (float)r1.y);
+        *reinterpret_cast<float4*>(di + i) = make_float4((float)m0.x, (float)m0.y, (float)m1.x, (float)m1.y);
+    } else {
+        for (uint64_t j = i; j < n; ++j) {
+            dr[j] = (float)sr[j];
+            di[j] = (float)si[j];
+        }
+    }
 }
+// FP32 -> FP64, each amplitude times *scale when scale is given
 __global__ void kF32toF64(const float* __restrict__ sr, const float* __restrict__ si, double* __restrict__ dr,
-                          double* __restrict__ di, uint64_t n) {
-    const uint64_t t = (uint64_t)blockIdx.x * 256 + threadIdx.x;
-    if (t >= n) return;
-    dr[t] = (double)sr[t];
-    di[t] = (double)si[t];
+                          double* __restrict__ di, uint64_t n, const double* __restrict__ scale) {
+    const uint64_t i = 4 * ((uint64_t)blockIdx.x * kConvThreads + threadIdx.x);
+    const double s = scale ? *scale : 1.0;
+    if (i + 3 < n) {
+        const float4 r = *reinterpret_cast<const float4*>(sr + i), m = *reinterpret_cast<const float4*>(si + i);
+        *reinterpret_cast<double2*>(dr + i) = make_double2(r.x * s, r.y * s);
+        *reinterpret_cast<double2*>(dr + i + 2) = make_double2(r.z * s, r.w * s);
+        *reinterpret_cast<double2*>(di + i) = make_double2(m.x * s, m.y * s);
+        *reinterpret_cast<double2*>(di + i + 2) = make_double2(m.z * s, m.w * s);
+    } else {
+        for (uint64_t j = i; j < n; ++j) {
+            dr[j] = (double)sr[j] * s;
+            di[j] = (double)si[j] * s;
+        }
+    }
 }
-// the same, times sqrt(*target / *out) (the last norm correction of a plan;
-// both are FP64 sums written by the tensor-core passes)
-__global__ void kF32toF64Scaled(const float* __restrict__ sr, const float* __restrict__ si, double* __restrict__ dr,
-                                double* __restrict__ di, uint64_t n, const double* __restrict__ target,
-                                const double* __restrict__ out) {
-    const uint64_t t = (uint64_t)blockIdx.x * 256 + threadIdx.x;
-    if (t >= n) return;
+// sqrt(*target / *out) into g_planScale (the last norm correction of a plan);
+// launched on the library stream right before the conversion that reads it
+__device__ double g_planScale;
+__global__ void kFinalScale(const double* __restrict__ target, const double* __restrict__ out) {
     const double o = *out;
-    const double s = (o > 0.0) ? sqrt(*target / o) : 1.0;
-    dr[t] = (double)sr[t] * s;
-    di[t] = (double)si[t] * s;
+    g_planScale = (o > 0.0) ? sqrt(*target / o) : 1.0;
 }
 
 // ------------------------------------------------------------ reductions
@@ -280,7 +300,7 @@ void quest_gb300_copyFromQureg(void* h, Qureg src) {
         invalidQuESTInputError("Dimensions of the qubit registers don't match.", "copyFromQureg");
         return;
     }
-    qg::kF64toF32<<<(unsigned)((n + 255) / 256), 256, 0, qg::stream()>>>(src.deviceStateVec.real, src.deviceStateVec.imag,
+    qg::kF64toF32<<<qg::convBlocks(n), qg::kConvThreads, 0, qg::stream()>>>(src.deviceStateVec.real, src.deviceStateVec.imag,
                                                                         q->re, q->im, n);
     qg::launchFailed("copyFromQureg");
 }
@@ -292,8 +312,8 @@ void quest_gb300_copyToQureg(void* h, Qureg dst) {
         invalidQuESTInputError("Dimensions of the qubit registers don't match.", "copyToQureg");
         return;
     }
-    qg::kF32toF64<<<(unsigned)((n + 255) / 256), 256, 0, qg::stream()>>>(q->re, q->im, dst.deviceStateVec.real,
-                                                                        dst.deviceStateVec.imag, n);
+    qg::kF32toF64<<<qg::convBlocks(n), qg::kConvThreads, 0, qg::stream()>>>(q->re, q->im, dst.deviceStateVec.real,
+                                                                           dst.deviceStateVec.imag, n, nullptr);
     qg::launchFailed("copyToQureg");
 }
 
@@ -310,7 +330,7 @@ void quest_gb300_initStateFromAmpsF32(void* h, const double* re, const double* i
         const uint64_t c = std::min(chunk, n - s);
         if (QG_CUDA(cudaMemcpyAsync(q->staging, re + s, c * sizeof(double), cudaMemcpyHostToDevice, st), "initStateFromAmpsF32")) return;
         if (QG_CUDA(cudaMemcpyAsync(q->staging + chunk, im + s, c * sizeof(double), cudaMemcpyHostToDevice, st), "initStateFromAmpsF32")) return;
-        qg::kF64toF32<<<(unsigned)((c + 255) / 256), 256, 0, st>>>(q->staging, q->staging + chunk, q->re + s, q->im + s, c);
+        qg::kF64toF32<<<qg::convBlocks(c), qg::kConvThreads, 0, st>>>(q->staging, q->staging + chunk, q->re + s, q->im + s, c);
         if (qg::launchFailed("initStateFromAmpsF32")) return;
     }
     QG_CUDA(cudaStreamSynchronize(st), "initStateFromAmpsF32");
@@ -324,7 +344,8 @@ void quest_gb300_copyStateToHostF32(void* h, double* re, double* im) {
     cudaStream_t st = qg::stream();
     for (uint64_t s = 0; s < n; s += chunk) {
         const uint64_t c = std::min(chunk, n - s);
-        qg::kF32toF64<<<(unsigned)((c + 255) / 256), 256, 0, st>>>(q->re + s, q->im + s, q->staging, q->staging + chunk, c);
+        qg::kF32toF64<<<qg::convBlocks(c), qg::kConvThreads, 0, st>>>(q->re + s, q->im + s, q->staging, q->staging + chunk, c,
+                                                                       nullptr);
         if (qg::launchFailed("copyStateToHostF32")) return;
         if (QG_CUDA(cudaMemcpyAsync(re + s, q->staging, c * sizeof(double), cudaMemcpyDeviceToHost, st), "copyStateToHostF32")) return;
         if (QG_CUDA(cudaMemcpyAsync(im + s, q->staging + chunk, c * sizeof(double), cudaMemcpyDeviceToHost, st), "copyStateToHostF32")) return;
@@ -476,8 +497,11 @@ void copyToQuregAfterPlan(void* h, Qureg& dst, void* plan) {
         invalidQuESTInputError("Dimensions of the qubit registers don't match.", "copyToQureg");
         return;
     }
-    kF32toF64Scaled<<<(unsigned)((n + 255) / 256), 256, 0, stream()>>>(q->re, q->im, dst.deviceStateVec.real,
-                                                                       dst.deviceStateVec.imag, n, target, out);
+    double* scale = nullptr;
+    if (QG_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&scale), g_planScale), "copyToQureg")) return;
+    kFinalScale<<<1, 1, 0, stream()>>>(target, out);
+    kF32toF64<<<convBlocks(n), kConvThreads, 0, stream()>>>(q->re, q->im, dst.deviceStateVec.real,
+                                                           dst.deviceStateVec.imag, n, scale);
     launchFailed("copyToQureg");
 }
 }  // namespace qg

@@ -317,6 +317,20 @@ void mulGate(double* __restrict Mr, double* __restrict Mi, int D, const FusedGat
 
 }  // namespace
 
+bool matrixIsUnitary(const std::vector<cplx>& m, int D) {
+    for (int r = 0; r < D; ++r)
+        for (int c = r; c < D; ++c) {
+            double ar = 0, ai = 0;
+            for (int j = 0; j < D; ++j) {
+                const cplx a = m[(size_t)r * D + j], b = m[(size_t)c * D + j];
+                ar += a.real() * b.real() + a.imag() * b.imag();     // a conj(b)
+                ai += a.imag() * b.real() - a.real() * b.imag();
+            }
+            if (std::fabs(ar - (r == c ? 1.0 : 0.0)) > 1e-12 || std::fabs(ai) > 1e-12) return false;
+        }
+    return true;
+}
+
 // product of the absorbed gates of one pass on its qubit set S
 void buildPass(const FusedPlan& plan, uint64_t S, const std::vector<int>& absorbed, FusedPass& p) {
     p.targets.clear();
@@ -336,6 +350,8 @@ void buildPass(const FusedPlan& plan, uint64_t S, const std::vector<int>& absorb
     p.m.resize((size_t)D * D);
     for (size_t e = 0; e < p.m.size(); ++e) p.m[e] = cplx(Mr[e], Mi[e]);
     p.numGates = (int)absorbed.size();
+    p.unitary = true;
+    for (int i : absorbed) p.unitary = p.unitary && plan.gates[i].unitary;
 }
 
 void compilePlan(FusedPlan& plan) {
@@ -387,7 +403,8 @@ int addGate(void* plan, std::vector<int> qs, std::vector<cplx> m) {
     for (size_t i = 0; i < qs.size(); ++i)
         for (size_t j = i + 1; j < qs.size(); ++j)
             if (qs[i] == qs[j]) return -1;
-    p->gates.push_back(FusedGate{std::move(qs), std::move(m)});
+    const bool u = qg::matrixIsUnitary(m, 1 << (int)qs.size());
+    p->gates.push_back(FusedGate{std::move(qs), std::move(m), u});
     p->compiled = false;
     return 0;
 }

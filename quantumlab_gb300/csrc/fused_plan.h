@@ -18,12 +18,14 @@ using cplx = std::complex<double>;
 struct FusedGate {
     std::vector<int> qubits;   // matrix bit b <-> qubits[b]
     std::vector<cplx> m;       // row-major 2^q x 2^q
+    bool unitary = false;      // m m^+ = I to 1e-12 (matrixIsUnitary)
 };
 
 struct FusedPass {
     std::vector<int> targets;  // ascending; matrix bit b <-> targets[b]
     std::vector<cplx> m;       // row-major D x D, D = 2^targets.size()
     int numGates = 0;
+    bool unitary = false;      // every absorbed gate is unitary
 };
 
 struct FusedPlan {
@@ -38,6 +40,9 @@ struct FusedPlan {
     void* device = nullptr;
     void (*deviceFree)(void*) = nullptr;
 };
+
+// |m m^+ - I| <= 1e-12 entrywise for a row-major D x D matrix.
+bool matrixIsUnitary(const std::vector<cplx>& m, int D);
 
 // Beam search over qubit sets at the circuit front (see fused_plan.cpp).
 // Leaves plan.compiled false if it fails.

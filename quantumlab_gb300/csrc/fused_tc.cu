@@ -38,9 +38,11 @@
 
 #include <cuda_bf16.h>
 
-#include <cstdint>
 #include <algorithm>
+#include <atomic>
+#include <cstdint>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 namespace qg {
@@ -816,7 +818,8 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
 
 // ------------------------------------------------------------ host side
 struct DevicePlan {
-    std::vector<float*> images;      // per pass: Gh image then Gl image (or nullptr)
+    std::vector<float*> images;      // per pass: its operand images (or nullptr), inside imageBuf
+    float* imageBuf = nullptr;
     int* errFlag = nullptr;
     // per pass: (sum |x|^2 of its input, sum |y|^2 of its output, square of
     // the scale it applied) in FP64, written by the tensor-core kernels.  The
@@ -834,17 +837,6 @@ struct DevicePlan {
     // unitary pass is corrected; a non-unitary pass changes the norm on purpose.
     std::vector<char> unitary;
 };
-
-bool isUnitary(const FusedPass& pass) {
-    const int D = 1 << (int)pass.targets.size();
-    for (int r = 0; r < D; ++r)
-        for (int c = 0; c < D; ++c) {
-            cplx acc = 0;
-            for (int j = 0; j < D; ++j) acc += pass.m[(size_t)r * D + j] * std::conj(pass.m[(size_t)c * D + j]);
-            if (std::abs(acc - cplx(r == c ? 1.0 : 0.0, 0.0)) > 1e-10) return false;
-        }
-    return true;
-}
 
 // Canonical no-swizzle K-major image of an N x K operand (rows r, K index j):
 // byte (r/8)*SBO + (j/4)*128 + (r%8)*16 + (j%4)*4 with SBO = (K/4)*128.
@@ -1011,6 +1003,57 @@ int g_tcVersion = 0;      // 0: per pass by target layout; 1, 2, 3: force one ke
 
 }  // namespace
 
+// the images of one pass (layouts above); buildImage writes imageFloats(k) floats
+static size_t imageFloats(int k) {
+    if (k < 4 || k > 6) return 0;
+    const size_t D = (size_t)1 << k, full = 4 * D * D;
+    const size_t bEntries = (k == 6) ? 3 * D * D : full;
+    return (2 * full + (3 * bEntries + 1) / 2 + 3) & ~(size_t)3;     // 16-byte multiple
+}
+static void buildImage(const FusedPass& pass, float* img) {
+    const int k = (int)pass.targets.size();
+    const int D = 1 << k, K = 2 * D, N = 2 * D;
+    // real form [[Re, -Im], [Im, Re]] as B = Gr (rows r = output index, K index j)
+    std::vector<float> hi((size_t)N * K), lo((size_t)N * K);
+    for (int r = 0; r < N; ++r)
+        for (int j = 0; j < K; ++j) {
+            const cplx g = pass.m[(size_t)(r % D) * D + (j % D)];
+            double v;
+            if (r < D) v = (j < D) ? g.real() : -g.imag();
+            else v = (j < D) ? g.imag() : g.real();
+            const float h = hostTf32RN((float)v);
+            hi[(size_t)r * K + j] = h;
+            lo[(size_t)r * K + j] = hostTf32RN((float)(v - (double)h));
+        }
+    // then the three BF16 parts of the pipelined kernel: the real form, or
+    // at k = 6 the compact form [-Im G; Re G; Im G] (3D rows, D K columns)
+    const size_t full = (size_t)N * K;
+    const int bRows = (k == 6) ? 3 * D : N, bK = (k == 6) ? D : K;
+    const size_t bEntries = (size_t)bRows * bK;
+    packKMajor(hi, N, K, img);
+    packKMajor(lo, N, K, img + full);
+    uint16_t* bh = reinterpret_cast<uint16_t*>(img + 2 * full);
+    uint16_t* bl = bh + bEntries;
+    uint16_t* bll = bl + bEntries;
+    for (int r = 0; r < bRows; ++r)
+        for (int j = 0; j < bK; ++j) {
+            // k = 6: rows 0..D-1 take the (r, D + j) entries of the real form
+            // (-Im), rows D..3D-1 the (r - D, j) entries (Re, then Im)
+            const int rr = (k == 6 && r >= D) ? r - D : r, jj = (k == 6 && r < D) ? D + j : j;
+            const cplx g = pass.m[(size_t)(rr % D) * D + (jj % D)];
+            const double v = (rr < D) ? ((jj < D) ? g.real() : -g.imag()) : ((jj < D) ? g.imag() : g.real());
+            const uint16_t h = hostBF16RN((float)v);
+            const double r1 = v - (double)bf16Value(h);
+            const uint16_t l = hostBF16RN((float)r1);
+            const size_t at = (size_t)(r / 8) * (bK / 8) * 64 + (size_t)(j / 8) * 64 + (r % 8) * 8 + (j % 8);
+            bh[at] = h;
+            bl[at] = l;
+            bll[at] = hostBF16RN((float)(r1 - (double)bf16Value(l)));
+        }
+}
+
+// Operand images of every tensor-core pass, built on up to 8 host threads
+// and uploaded in one allocation and one copy.
 void* uploadPlanTC(const FusedPlan& plan) {
     DevicePlan* dp = new DevicePlan();
     if (cudaMalloc(&dp->errFlag, sizeof(int)) != cudaSuccess) {
@@ -1023,61 +1066,36 @@ void* uploadPlanTC(const FusedPlan& plan) {
         cudaGetLastError();
         dp->norms = nullptr;
     }
-    for (const FusedPass& pass : plan.passes) {
+    const size_t np = plan.passes.size();
+    std::vector<size_t> offset(np + 1, 0);
+    for (size_t i = 0; i < np; ++i) {
+        const FusedPass& pass = plan.passes[i];
         const int k = (int)pass.targets.size();
-        dp->unitary.push_back(isUnitary(pass) ? 1 : 0);
-        if (k < 4 || k > 6 || plan.numQubits < k + 7) {
-            dp->images.push_back(nullptr);
-            continue;
-        }
-        const int D = 1 << k, K = 2 * D, N = 2 * D;
-        // real form [[Re, -Im], [Im, Re]] as B = Gr (rows r = output index, K index j)
-        std::vector<float> hi((size_t)N * K), lo((size_t)N * K);
-        for (int r = 0; r < N; ++r)
-            for (int j = 0; j < K; ++j) {
-                const cplx g = pass.m[(size_t)(r % D) * D + (j % D)];
-                double v;
-                if (r < D) v = (j < D) ? g.real() : -g.imag();
-                else v = (j < D) ? g.imag() : g.real();
-                const float h = hostTf32RN((float)v);
-                hi[(size_t)r * K + j] = h;
-                lo[(size_t)r * K + j] = hostTf32RN((float)(v - (double)h));
-            }
-        // then the three BF16 parts of the pipelined kernel: the real form, or
-        // at k = 6 the compact form [-Im G; Re G; Im G] (3D rows, D K columns)
-        const size_t full = (size_t)N * K;
-        const int bRows = (k == 6) ? 3 * D : N, bK = (k == 6) ? D : K;
-        const size_t bEntries = (size_t)bRows * bK;
-        std::vector<float> img(2 * full + (3 * bEntries + 1) / 2);   // then three parts of bEntries bf16
-        packKMajor(hi, N, K, img.data());
-        packKMajor(lo, N, K, img.data() + full);
-        uint16_t* bh = reinterpret_cast<uint16_t*>(img.data() + 2 * full);
-        uint16_t* bl = bh + bEntries;
-        uint16_t* bll = bl + bEntries;
-        for (int r = 0; r < bRows; ++r)
-            for (int j = 0; j < bK; ++j) {
-                // k = 6: rows 0..D-1 take the (r, D + j) entries of the real form
-                // (-Im), rows D..3D-1 the (r - D, j) entries (Re, then Im)
-                const int rr = (k == 6 && r >= D) ? r - D : r, jj = (k == 6 && r < D) ? D + j : j;
-                const cplx g = pass.m[(size_t)(rr % D) * D + (jj % D)];
-                const double v = (rr < D) ? ((jj < D) ? g.real() : -g.imag()) : ((jj < D) ? g.imag() : g.real());
-                const uint16_t h = hostBF16RN((float)v);
-                const double r1 = v - (double)bf16Value(h);
-                const uint16_t l = hostBF16RN((float)r1);
-                const size_t at = (size_t)(r / 8) * (bK / 8) * 64 + (size_t)(j / 8) * 64 + (r % 8) * 8 + (j % 8);
-                bh[at] = h;
-                bl[at] = l;
-                bll[at] = hostBF16RN((float)(r1 - (double)bf16Value(l)));
-            }
-        float* d = nullptr;
-        if (cudaMalloc(&d, img.size() * sizeof(float)) != cudaSuccess) {
-            cudaGetLastError();
-            dp->images.push_back(nullptr);
-            continue;
-        }
-        cudaMemcpy(d, img.data(), img.size() * sizeof(float), cudaMemcpyHostToDevice);
-        dp->images.push_back(d);
+        dp->unitary.push_back(pass.unitary ? 1 : 0);
+        const bool tc = k >= 4 && k <= 6 && plan.numQubits >= k + 7;
+        offset[i + 1] = offset[i] + (tc ? imageFloats(k) : 0);
     }
+    dp->images.assign(np, nullptr);
+    if (offset[np] == 0) return dp;
+    std::vector<float> host(offset[np]);
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+        for (size_t i; (i = next.fetch_add(1)) < np;)
+            if (offset[i + 1] > offset[i]) buildImage(plan.passes[i], host.data() + offset[i]);
+    };
+    const unsigned nt = (unsigned)std::min<size_t>({(size_t)8, (size_t)std::max(1u, std::thread::hardware_concurrency()), np});
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+    if (cudaMalloc(&dp->imageBuf, offset[np] * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        dp->imageBuf = nullptr;
+        return dp;                                   // every pass then runs on the SIMT applier
+    }
+    cudaMemcpy(dp->imageBuf, host.data(), offset[np] * sizeof(float), cudaMemcpyHostToDevice);
+    for (size_t i = 0; i < np; ++i)
+        if (offset[i + 1] > offset[i]) dp->images[i] = dp->imageBuf + offset[i];
     return dp;
 }
 
@@ -1085,8 +1103,7 @@ void freePlanTC(void* h) {
     DevicePlan* dp = reinterpret_cast<DevicePlan*>(h);
     if (!dp) return;
     cudaStreamSynchronize(stream());
-    for (float* f : dp->images)
-        if (f) cudaFree(f);
+    if (dp->imageBuf) cudaFree(dp->imageBuf);
     if (dp->errFlag) cudaFree(dp->errFlag);
     if (dp->norms) cudaFree(dp->norms);
     delete dp;
