@@ -186,10 +186,10 @@ def run_gpu(args, rank, world):
     groups = {}
     for i in range(npass):
         key = {0: f"kApplySimt<{kk[i]}> (FP32 FFMA)", 1: f"kApplyTC<{kk[i]}> (tcgen05 split-TF32, direct loads)",
-               2: f"kApplyTC2<{kk[i]},2,1,1> (tcgen05 split-TF32, pipelined)",
-               3: f"kApplyTC2<{kk[i]},1,1,1> (tcgen05 split-TF32, pipelined)",
-               4: f"kApplyTC2<{kk[i]},1,2,1> (tcgen05 split-TF32, pipelined)",
-               5: f"kApplyTC2<{kk[i]},2,2,2> (tcgen05 split-TF32, pipelined)"}[tc[i]]
+               2: f"kApplyTC2<{kk[i]},2,1,1> (tcgen05 split-BF16, pipelined)",
+               3: f"kApplyTC2<{kk[i]},1,1,1> (tcgen05 split-BF16, pipelined)",
+               4: f"kApplyTC2<{kk[i]},1,2,1> (tcgen05 split-BF16, pipelined)",
+               5: f"kApplyTC2<{kk[i]},2,2,2> (tcgen05 split-BF16, pipelined)"}[tc[i]]
         g = groups.setdefault(key, [0, 0.0])
         g[0] += 1
         g[1] += pass_ms[i]
@@ -273,7 +273,7 @@ def run_gpu(args, rank, world):
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s (per-gate FP64 algorithmic bytes)",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (split-TF32 tensor cores; FP64 fusion products and reductions)",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 state (split-BF16 tensor-core products, FP32 accumulation; FP64 fusion products and reductions)",
         "data": "synthetic (seeded Haar/CPhase-matching/CNOT-brickwork circuit)",
         "config": {"workload": f"{n}-qubit random circuit, {args.layers} layers: fused FP32 engine (k<={k}) vs plain FP64 per-gate engine",
                    "qubits": n, "layers": args.layers, "gates_per_circuit": len(ops), "fusion_max_qubits": k,

@@ -1,34 +1,26 @@
-// fused_tc.cu -- tensor-core applier of the FP32 fused engine (sm_103a,
-// tcgen05 + TMEM, 3-term split-TF32).  No counterpart in the reference.
+// fused_tc.cu -- tensor-core appliers of the FP32 fused engine (sm_103a,
+// tcgen05 + TMEM).  No counterpart in the reference.
 //
 // A pass multiplies the FP32 state by a dense 2^k x 2^k complex matrix G on
-// qubits T (k = 4..6).  With D = 2^k, a tile of 128 consecutive "groups"
-// (the non-target bits, inserted around T) is the GEMM
+// qubits T (k = 4..6).  With D = 2^k, a tile of 128 "groups" (the non-target
+// bits, inserted around T) is the GEMM
 //
 //     Out[c][r] = sum_j X[c][j] * Gr[r][j]          c < 128, r, j < 2D
 //
 // where X[c] = (re of the group's D amplitudes, then im) and Gr is the real
 // form [[Re G, -Im G], [Im G, Re G]].  On tcgen05: A = X (M = 128, K = 2D,
 // kept in TMEM), B = Gr (N = 2D, K-major in shared memory), D = Out in TMEM.
-// Split-TF32: X = Xh + Xl and Gr = Gh + Gl with Xh, Gh exact TF32 values and
-// the MMA truncating Xl, Gl to TF32; Out = Xh.Gh + Xl.Gh + Xh.Gl accumulated
-// in FP32 (relative error ~2^-21 per product instead of 2^-11).
 //
-// Data path (per CTA, persistent over tiles):
-//   * Gh/Gl: prepared on the host in the canonical no-swizzle K-major UMMA
-//     layout and staged once per CTA by a TMA bulk copy (cp.async.bulk) into
-//     shared memory;
-//   * X: each thread owns one tile column (TMEM lane) and loads its 2D values
-//     straight from global memory -- the 32 lanes of a warp read 32
-//     consecutive amplitudes, so every load is a coalesced 128-byte line --
-//     splits them in registers and writes Xh, Xl to TMEM with tcgen05.st.
-//     Staging X through shared memory would add two shared-memory passes over
-//     the data for no gain: the split needs it in registers anyway;
-//   * one thread issues the 3 x (2D/8) MMAs (K = 8 each) and commits them to
-//     an mbarrier; all threads wait on it (bounded spin), read Out with
-//     tcgen05.ld and store it with coalesced 128-byte warp stores.
-// Several CTAs share an SM where TMEM allows, so one CTA's loads overlap
-// another's MMAs and stores.
+// Two kernels:
+//   * kApplyTC2 (the default; "pipelined kernel" below): warp-specialised and
+//     persistent, split-BF16 operands.  X = Xh + Xl (two BF16 parts, ~2^-17)
+//     and Gr = Gh + Gl + Gll (three BF16 parts, ~2^-24); Out = Xh.Gh + Xl.Gh
+//     + Xh.Gl + Xh.Gll accumulated in FP32 by kind::f16 MMAs, which run at
+//     twice the TF32 rate;
+//   * kApplyTC (setTensorCoreKernel(1)): the direct-load kernel, split-TF32.
+//     Each thread owns one tile column and loads its 2D values straight from
+//     global memory (the 32 lanes of a warp read 32 consecutive amplitudes),
+//     X = Xh + Xl and Gr = Gh + Gl in TF32 parts, Out = Xh.Gh + Xl.Gh + Xh.Gl.
 //
 // Every wait is bounded: on timeout the CTA records an error code in a
 // device flag, skips the rest of its tiles, frees its TMEM and returns; the
@@ -414,26 +406,27 @@ __global__ void __launch_bounds__(kThreadsTC, (KQ == 4 ? 4 : 1)) kApplyTC(float*
 }
 
 // ------------------------------------------------------------ pipelined kernel
-// Warp-specialised kernel used for every tensor-core pass by default:
-//   LG loader groups of 4 warps: global -> registers (coalesced 16-byte
-//              loads of a whole chunk, issued one chunk ahead), registers ->
-//              shared memory in row order, then each thread reads its tile
-//              column back, splits it and writes Xh/Xl to the group's TMEM
-//              stage with tcgen05.st.  With LG = 2 the groups take alternate
-//              chunks, so two chunks of loads are in flight per SM;
-//   4 epilogue warps: tcgen05.ld of a finished accumulator, column-order
-//              stores to shared memory, row-order reads, coalesced 16-byte
-//              stores;
-//   1 warp:    TMEM allocation, the one-time TMA bulk copy of Gh/Gl, and the
-//              MMA issue loop (one thread).
-// TMEM holds two operand stages and two accumulators, so loading tile t+1,
-// multiplying tile t and storing tile t-1 overlap.  A tile is 128 groups
-// (TMEM lanes) over the qubit set I = targets + the 7 lowest other qubits; I
-// always contains qubits [0, r) with r >= 7, so the tile is made of
-// contiguous runs of >= 128 amplitudes and every global access is coalesced
-// whatever the targets are.  For k = 6 a tile's K = 128 is split into two
-// stages (real rows, imaginary rows) so the operand stages and both
-// accumulators fit the 512 TMEM columns.
+// Warp-specialised kernel used for every tensor-core pass by default (one
+// persistent CTA per SM):
+//   LG loader groups of 4 warps: 16-byte cp.async copies of their part of a
+//              chunk into one of XST shared-memory row stages (up to three
+//              chunks in flight per warp, no register staging); then each
+//              thread reads its tile column back, splits it into BF16 parts
+//              (two K entries per 32-bit word) and writes Xh/Xl to the TMEM
+//              operand stage of the chunk with tcgen05.st;
+//   EG epilogue groups of 4 warps: tcgen05.ld of a finished accumulator, the
+//              drift-correction scale in FP32, column-order stores to shared
+//              memory, 16-byte row-order reads, coalesced 16-byte stores;
+//   1 warp:    TMEM allocation, the one-time TMA bulk copy of the three G
+//              parts, and the MMA issue loop (one thread).
+// TMEM holds four operand stages (64 columns each at k = 6) and two
+// accumulators, so the loaders can run three chunks ahead of the MMAs while
+// the epilogue drains the previous tile.  A tile is 128 groups (TMEM lanes)
+// over the qubit set I = targets + the 7 lowest other qubits; I always
+// contains qubits [0, r) with r >= 7, so the tile is made of contiguous runs
+// of >= 128 amplitudes and every global access is coalesced whatever the
+// targets are.  For k = 6 a tile's K = 128 is split into two chunks (real
+// parts, imaginary parts of X).
 //
 // Warp-local staging.  Warp w of a role owns TMEM lanes (groups) 32w..32w+31,
 // whose tile positions have the 6th and 7th column bits equal to w.  Each
@@ -1136,20 +1129,23 @@ void tcNoteSimtPass(void* devPlan, size_t index) {
 // applier, 1 = the direct-load tensor-core kernel, 2..5 = the pipelined one
 // (2: 2 loader groups on alternate chunks + 1 epilogue group; 3: 1 + 1;
 // 4: 1 + 2; 5: 2 loader groups splitting every chunk + 2 epilogue groups).
-// Default choice (measured at 30 qubits, ms per pass): passes on 1..3 qubits
-// and 4-qubit passes whose targets are all at or above qubit 5 run on the SIMT
-// applier (3.2 ms: every lane's group is part of a coalesced warp line and the
-// multiply is cheap); the other 4-qubit passes (SIMT 9.0 ms, kernel 2: 3.1)
-// and the 5-qubit passes run on kernel 2 (2.6-3.2 ms; the loaders are the
-// busier role); 6-qubit passes run on kernel 5 (3.1-3.7 ms against 3.2-3.8 for
-// kernel 4 and 3.4-3.9 for kernel 2: at 2 x 128 values per group both the
-// loaders' and the epilogue's staging are busy, and kernel 5 doubles both).
+// Default choice, measured at 30 qubits in ms per pass; "high" means every
+// target is at or above qubit 5.
+//   * 1..3 qubits: the SIMT applier.
+//   * 4 qubits, high targets: kernel 2 (2.6-2.8, against SIMT 3.1-3.2).
+//   * 4 qubits, other targets: kernel 5 (2.7-3.0).
+//   * 5 qubits: kernel 5 (2.7-3.0, against 2.9-3.1 for kernel 2).
+//   * 6 qubits: kernel 5 (2.7-3.0).  Kernels 2 and 4 are each a few percent
+//     faster on some target sets.  Choosing by target set came to the same
+//     total over the 30-qubit circuit (297.4 against 296.3 ms).
 int tcKernelFor(const FusedPass& pass, int n) {
     const int k = (int)pass.targets.size();
     if (!g_tcEnabled || k < 4 || k > 6 || n < k + 7) return 0;
     if (g_tcVersion != 0) return g_tcVersion;
-    if (k == 4 && pass.targets[0] >= 5) return 0;
-    return k == 6 ? 5 : 2;
+    const bool high = pass.targets[0] >= 5;
+    if (k == 5) return 5;
+    if (k == 4) return high ? 2 : 5;
+    return 5;
 }
 
 // explicit entry used by the FP32 engine with the pass index: 1 = applied on
