@@ -28,9 +28,12 @@ double quest_gb300_eventElapsedMs(int slotA, int slotB);
 /* ---- gate-fusion plans ---------------------------------------------------
  * A plan records a gate stream on numQubits qubits and compiles it into
  * passes: dense 2^k x 2^k complex matrices on k <= maxFusedQubits (<= 6)
- * qubits, formed as FP64 products of the absorbed gates.  Matrices are
- * row-major with matrix bit b on targets[b]; compactUnitary and friends keep
- * the QuEST conventions.  Add functions return 0, or -1 on invalid input.   */
+ * qubits, formed as FP64 products of the absorbed gates.  maxFusedQubits is
+ * capped at the widest pass the FP32 appliers take on numQubits qubits: 6
+ * from 13 qubits up, else 5 (or numQubits).  Matrices are row-major with
+ * matrix bit b on targets[b]; compactUnitary and friends keep the QuEST
+ * conventions.  Add functions return 0, or -1 on invalid input (a gate wider
+ * than the capped width included).                                          */
 void* quest_gb300_planCreate(int numQubits, int maxFusedQubits);
 void quest_gb300_planDestroy(void* plan);
 int quest_gb300_planAddGate(void* plan, const int* targets, int numTargets, const double* re, const double* im);

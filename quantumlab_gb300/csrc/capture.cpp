@@ -108,7 +108,7 @@ static void flushRecord(Capture* c, double* re, double* im) {
     quest_gb300_copyFromQureg(c->q32, view);
     FusedPlan* plan = new FusedPlan();
     plan->numQubits = c->n;
-    plan->maxFused = std::min(g_capMaxFused, c->n);
+    plan->maxFused = std::min(g_capMaxFused, widestPass(c->n));
     plan->gates.swap(c->gates);
     compilePlan(*plan);
     if (!plan->compiled) {
@@ -155,13 +155,14 @@ void captureDrop(const double* re) {
 
 // Queue the gate acting on the qubits of `mask` whose effect on a basis state
 // is given by `apply` (it maps a 2^k state over the local qubits in place).
-// Returns false (after flushing the queue) when the gate touches more than 6
-// qubits: the caller then runs it directly.
+// Returns false (after flushing the queue) when the gate is wider than the
+// widest pass the fused engine takes on this register: the caller then runs
+// it directly.
 static bool captureGate(SV s, uint64_t mask, const std::function<void(std::vector<cplx>&, const Local&)>& apply) {
     Capture* c = reinterpret_cast<Capture*>(s.cap);
     const Local l = localOf(mask);
     const int k = (int)l.qubits.size();
-    if (k < 1 || k > 6) {
+    if (k < 1 || k > std::min(g_capMaxFused, widestPass(c->n))) {
         flushRecord(c, s.re, s.im);
         return false;
     }

@@ -416,7 +416,7 @@ void* quest_gb300_planCreate(int numQubits, int maxFusedQubits) {
     if (numQubits < 1 || numQubits > 40 || maxFusedQubits < 1 || maxFusedQubits > 6) return nullptr;
     FusedPlan* p = new FusedPlan();
     p->numQubits = numQubits;
-    p->maxFused = std::min(maxFusedQubits, numQubits);
+    p->maxFused = std::min(maxFusedQubits, qg::widestPass(numQubits));
     return p;
 }
 

@@ -41,6 +41,11 @@ struct FusedPlan {
     void (*deviceFree)(void*) = nullptr;
 };
 
+// Widest pass the FP32 appliers take on registers of n qubits: six qubits
+// need the tensor-core applier (n >= 13: a tile is 2^(6+7) amplitudes), the
+// SIMT applier takes up to five.
+inline int widestPass(int n) { return n >= 13 ? 6 : (n < 5 ? n : 5); }
+
 // |m m^+ - I| <= 1e-12 entrywise for a row-major D x D matrix.
 bool matrixIsUnitary(const std::vector<cplx>& m, int D);
 

@@ -172,6 +172,10 @@ def run_ops(L, q, ops: Sequence[tuple], density_doubling: bool = True):
             lib.controlledPhaseShift(q, op[1], op[2], op[3])
         elif k == "h":
             lib.hadamard(q, op[1])
+        elif k == "ps":
+            lib.phaseShift(q, op[1], op[2])
+        elif k == "rz":
+            lib.rotateZ(q, op[1], op[2])
         elif k == "deph":
             lib.mixDephasing(q, op[1], op[2])
         elif k == "depol":
@@ -227,6 +231,35 @@ def neel_index(sites: int) -> int:
         q = 2 * i + (i % 2)
         idx |= 1 << q
     return idx
+
+
+def lab_trotter_ops(codes, coeffs, dt: float, steps: int, ancilla: int):
+    """The gate sequence QuantumLab's Pauli-Trotter builder emits for a
+    first-order Trotter circuit (PauliProduct::OneStepGate,
+    Circuit/Gates/PauliSimulate.cpp:30-80): per term, a basis change and a CNOT
+    ladder that computes the parity of the term's qubits into an ancilla
+    (X: H, CX; Y: P(-pi/2), H, CX; Z: CX), Rz(-2 dt c) on the ancilla, then the
+    same gates inverted in reverse order.  With the ancilla in |0> this is
+    exp(-i phi/2 P) on the system with phi = -2 dt c, i.e. multiRotatePauli(P,
+    phi).  Ops: ("h", q), ("ps", q, theta), ("cx", c, t), ("rz", q, theta)."""
+    ops = []
+    for _ in range(steps):
+        for code, c in zip(codes, coeffs):
+            prep = []
+            for i, pa in enumerate(code):
+                if pa == 1:
+                    prep += [("h", i), ("cx", i, ancilla)]
+                elif pa == 2:
+                    prep += [("ps", i, -math.pi / 2), ("h", i), ("cx", i, ancilla)]
+                elif pa == 3:
+                    prep += [("cx", i, ancilla)]
+            if not prep:
+                continue
+            ops += prep
+            ops.append(("rz", ancilla, -2.0 * dt * c))
+            for op in reversed(prep):                   # the dagger: inverse gates, reversed
+                ops.append(("ps", op[1], -op[2]) if op[0] == "ps" else op)
+    return ops
 
 
 def hubbard_instances(count: int = 64):
