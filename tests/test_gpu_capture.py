@@ -170,3 +170,51 @@ def test_capture_speeds_up_a_26_qubit_circuit(gpulib):
     print(f"26q 10 layers: direct {res[0][0]:.1f} ms, captured {res[1][0]:.1f} ms")
     assert abs(res[1][1] - 1) < 1e-5
     assert res[1][0] < res[0][0] / 3
+
+
+@pytest.mark.parametrize("n", [3, 5, 8, 11, 12, 13])
+def test_capture_small_registers(gpulib, n):
+    """Registers below and at the 13-qubit size from which 6-qubit passes are
+    possible: random 1-, 2- and multi-qubit gates (some as wide as the
+    register or six qubits) queued and fused must match direct FP64 calls."""
+    L = gpulib
+    lib = L.lib
+
+    def circuit(q):
+        r = np.random.default_rng(7 * n)
+        for _ in range(12 * n):
+            kind = r.integers(5)
+            if kind == 0:
+                t = int(r.integers(n))
+                a, b = r.normal(size=2) + 1j * r.normal(size=2)
+                s = np.sqrt(abs(a) ** 2 + abs(b) ** 2)
+                lib.compactUnitary(q, t, Complex(a.real / s, a.imag / s), Complex(b.real / s, b.imag / s))
+            elif kind == 1 and n > 1:
+                c, t = (int(x) for x in r.choice(n, size=2, replace=False))
+                lib.controlledNot(q, c, t)
+            elif kind == 2 and n > 1:
+                a, b = (int(x) for x in r.choice(n, size=2, replace=False))
+                lib.controlledPhaseShift(q, a, b, float(r.uniform(0, 2 * np.pi)))
+            elif kind == 3:
+                k = int(r.integers(1, min(n, 6) + 1))
+                ts = [int(x) for x in r.choice(n, size=k, replace=False)]
+                L.multiQubitUnitary(q, ts, haar(r, k))
+            else:
+                k = int(r.integers(1, min(n, 4) + 1))
+                ts = [int(x) for x in r.choice(n, size=k, replace=False)]
+                L.multiRotateZ(q, ts, float(r.uniform(0, 2 * np.pi)))
+
+    direct = L.create(n)
+    lib.initZeroState(direct)
+    circuit(direct)
+    cap = L.create(n)
+    lib.quest_gb300_setCapture(cap, 1)
+    lib.initZeroState(cap)
+    circuit(cap)
+    a, b = L.amps(direct), L.amps(cap)
+    f = abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real)
+    print(f"n={n}: 1-F={1 - f:.2e}, max|d|={np.max(np.abs(a - b)):.2e}")
+    assert 1 - f <= 1e-6 and np.max(np.abs(a - b)) <= 1e-5
+    assert abs(lib.calcTotalProb(cap) - 1) < 1e-6
+    L.destroy(direct)
+    L.destroy(cap)
