@@ -49,6 +49,8 @@ void tcBeginRange(void* devPlan);
 void tcNoteSimtPass(void* devPlan, size_t index);
 void setTensorCoresEnabled(bool on);
 void setTensorCoreKernel(int version);
+bool setTensorCorePrecision(int mode);
+int tensorCorePrecision();
 bool tensorCoresEnabled();
 int tcKernelFor(const FusedPass& pass, int n);
 float* f32re(QuregF32& q) { return q.re; }
@@ -431,6 +433,8 @@ int quest_gb300_planPassUsesTensorCores(void* plan, int i) {
 
 void quest_gb300_setTensorCores(int enabled) { qg::setTensorCoresEnabled(enabled != 0); }
 void quest_gb300_setTensorCoreKernel(int version) { qg::setTensorCoreKernel(version); }
+int quest_gb300_setTensorCorePrecision(int mode) { return qg::setTensorCorePrecision(mode) ? 0 : -1; }
+int quest_gb300_getTensorCorePrecision(void) { return qg::tensorCorePrecision(); }
 
 double quest_gb300_calcTotalProbF32(void* h) {
     QuregF32* q = qg::Q(h);

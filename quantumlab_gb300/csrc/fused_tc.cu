@@ -184,6 +184,10 @@ __device__ __forceinline__ void splitBF16x2(float x0, float x1, uint32_t& hi, ui
     lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
+// nearest TF32 value of a finite x (ties away from zero), as cvt.rna.tf32.f32,
+// in two integer operations
+__device__ __forceinline__ uint32_t tf32Bits(float x) { return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u; }
+
 // Round to the nearest TF32 value (ties away from zero).  Both split parts are
 // rounded to nearest: the MMA reads operands by dropping their low 13 bits,
 // and a truncated split (hi = x with the low bits cleared) leaves lo with the
@@ -459,28 +463,35 @@ struct TC2Params {
     int runBits;                          // I contains qubits [0, runBits)
 };
 
-// Layout of kApplyTC2<KQ, LG, EG, LS>, used by the kernel and its launcher.
-// Shared memory: G as three BF16 parts (Gh, Gl, Gll: G to ~2^-24), the loader
-// row stages and the epilogue buffers.  At k = 6, G is the compact real form
+// Operand precision of kApplyTC2: 3-term split-TF32 or 4-term split-BF16.
+constexpr int kPrecTF32 = 0, kPrecBF16 = 1;
+
+// Layout of kApplyTC2<KQ, LG, EG, LS, PR>, used by the kernel and its
+// launcher.  Shared memory: the parts of G (split-TF32: Gh, Gl in FP32 words,
+// G to ~2^-22; split-BF16: Gh, Gl, Gll in BF16, G to ~2^-24), the loader row
+// stages and the epilogue buffers.  At k = 6, G is the compact real form
 // [-Im G; Re G; Im G] (192 rows x 64 K).  The B operand of the K-chunk of the
 // real parts of X is rows 64..191 ([Re; Im]).  That of the imaginary parts is
 // rows 0..127 ([-Im; Re]).  Loader row buffers: XST stages per loader warp,
-// up to three, as many as fit.  TMEM: NST operand stages of KC columns (Xh
-// then Xl, two bf16 per column), then two accumulators of N columns.
-template <int KQ, int LG, int EG, int LS>
+// up to three, as many as fit.  TMEM: NST operand stages (Xh then Xl; one
+// TF32 or two BF16 per column), then two accumulators of N columns.
+template <int KQ, int LG, int EG, int LS, int PR>
 struct TC2Shape {
     static constexpr int D = 1 << KQ, K = 2 * D, N = 2 * D;
     static constexpr int TILE = 1 << (KQ + kTileBitsC);       // amplitudes per plane per tile
     static constexpr int NCH = (KQ == 6) ? 2 : 1;             // K chunks per tile
-    static constexpr int KC = K / NCH;                        // K elements per chunk (<= 64)
+    static constexpr int KC = K / NCH;                        // K entries per chunk (<= 64)
     static constexpr int PART = (KQ == 6) ? TILE / 8 : TILE / 4;   // positions per warp per part (<= 1024)
     static constexpr int R = (int)((padIdx(PART - 1) + 1 + 3) & ~3u);   // floats per part buffer
     static constexpr int PPG = (LS == 2) ? 1 : 2;             // parts per loader group per chunk
-    static constexpr int NST = 4;                             // TMEM operand stages
-    static constexpr uint32_t GE = (KQ == 6) ? 3u * D * D : (uint32_t)(N * K);   // bf16 entries of each G part
-    static constexpr uint32_t GW = GE / 2;                    // ... in 32-bit words
-    static constexpr uint32_t GSBO = (uint32_t)(((KQ == 6) ? KC : K) / 8) * 128u;   // B descriptor stride
-    static constexpr size_t fixedFloats = 3 * (size_t)GW + (size_t)EG * 4 * R;
+    static constexpr int ESZ = (PR == kPrecBF16) ? 2 : 4;     // bytes per operand entry
+    static constexpr int NST = (PR == kPrecBF16) ? 4 : 2;     // TMEM operand stages
+    static constexpr uint32_t STAGE_COLS = (uint32_t)(2 * KC * ESZ / 4);   // Xh then Xl
+    static constexpr int NGP = (PR == kPrecBF16) ? 3 : 2;     // parts of G
+    static constexpr uint32_t GE = (KQ == 6) ? 3u * D * D : (uint32_t)(N * K);   // entries of each G part
+    static constexpr uint32_t GW = GE * ESZ / 4;              // ... in 32-bit words
+    static constexpr uint32_t GSBO = (uint32_t)(((KQ == 6) ? KC : K) * ESZ / 16) * 128u;   // B descriptor stride
+    static constexpr size_t fixedFloats = (size_t)NGP * GW + (size_t)EG * 4 * R;
     static constexpr size_t stageFloats = (size_t)LG * 4 * PPG * R;
     static constexpr bool fits(int st) { return (fixedFloats + (size_t)st * stageFloats) * 4 + 2048 <= 227 * 1024; }
     static constexpr int XST = fits(3) ? 3 : (fits(2) ? 2 : 1);
@@ -525,25 +536,26 @@ __device__ __forceinline__ uint64_t tileBase(const TC2Params<KQ>& p, uint64_t ti
     return tb;
 }
 
-template <int KQ, int LG, int EG, int LS>
+template <int KQ, int LG, int EG, int LS, int PR>
 __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* __restrict__ re, float* __restrict__ im,
                                                                   const float* __restrict__ gImage, uint64_t numTiles,
                                                                   int* __restrict__ errFlag, const NormLinks nl,
                                                                   const __grid_constant__ TC2Params<KQ> p) {
-    using S = TC2Shape<KQ, LG, EG, LS>;
+    using S = TC2Shape<KQ, LG, EG, LS, PR>;
+    constexpr bool BF = (PR == kPrecBF16);
     constexpr int D = S::D, N = S::N;
     constexpr int NCH = S::NCH, KC = S::KC, PART = S::PART, R = S::R, PPG = S::PPG, XST = S::XST, NST = S::NST;
     constexpr uint32_t kGW = S::GW;
     constexpr int V4P = PART / 128;                      // 128-position blocks per part
     constexpr int JP = (KQ == 6) ? 32 : D;               // matrix indices per part
     constexpr int EPARTS = (KQ == 6) ? 4 : 2;            // epilogue parts per tile (plane x half)
-    constexpr uint32_t kStageCols = KC;                  // Xh: KC / 2 columns, then Xl
+    constexpr uint32_t kStageCols = S::STAGE_COLS;       // Xh, then Xl at + kStageCols / 2
     constexpr uint32_t kDCol0 = NST * kStageCols;
     constexpr uint32_t kUsed = kDCol0 + 2 * N;
     constexpr uint32_t kCols = kUsed <= 64 ? 64 : (kUsed <= 128 ? 128 : (kUsed <= 256 ? 256 : 512));
     static_assert(kUsed <= 512, "TMEM");
     constexpr uint32_t kLBO = 128;
-    constexpr uint32_t idesc = idescBF16(kTile, N);
+    constexpr uint32_t idesc = BF ? idescBF16(kTile, N) : idescTF32(kTile, N);
     constexpr int kEpiWarp0 = 4 * LG, kMmaWarp = 4 * (LG + EG);
     // LS = 1: loader groups take alternate chunks; LS = 2: the two loader
     // groups split every chunk, group g taking its part g
@@ -552,8 +564,8 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
     extern __shared__ __align__(1024) uint8_t smem[];
     uint32_t* gh = reinterpret_cast<uint32_t*>(smem);
     uint32_t* gl = gh + kGW;
-    uint32_t* gll = gl + kGW;
-    float* xs = reinterpret_cast<float*>(gll + kGW);     // [loader group][warp][stage][part][R]
+    uint32_t* gll = gl + kGW;                            // (split-BF16 only)
+    float* xs = reinterpret_cast<float*>(gh + S::NGP * kGW);   // [loader group][warp][stage][part][R]
     float* es = xs + (size_t)XST * LG * 4 * PPG * R;     // [epilogue group][warp][R]
     __shared__ __align__(8) uint64_t barG, fullB[NST], emptyB[NST], dFullB[2], dEmptyB[2];
     __shared__ uint32_t tmemBase;
@@ -637,28 +649,37 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
             }
             cpAsyncWait<XST - 1>();                          // this lane's copies of the chunk landed
             __syncwarp();                                    // ... and every lane's
-            // this group's K elements of the stage: [p0 JP, (p0 + PPG) JP), two per column
-            const uint32_t aH = tmem + laneSel + b * kStageCols + p0 * JP / 2;
+            // this group's K entries of the stage: [p0 JP, (p0 + PPG) JP); EPW per column
+            constexpr int EPW = BF ? 2 : 1;
+            const uint32_t aH = tmem + laneSel + b * kStageCols + p0 * JP / EPW;
             const float* const cb = xr + colBase;
             float nrm = 0.f;
 #pragma unroll
-            for (int c0 = 0; c0 < PPG * JP; c0 += 16) {
+            for (int c0 = 0; c0 < PPG * JP; c0 += 8 * EPW) {
                 uint32_t hi[8], lo[8];
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
-                    float x[2];
+                    float x[EPW];
 #pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const int cl = c0 + 2 * e + h;       // local element: buffer part cl / JP
+                    for (int h = 0; h < EPW; ++h) {
+                        const int cl = c0 + EPW * e + h;     // local entry: buffer part cl / JP
                         const int pl = cl / JP;
                         const int j = (NCH == 2) ? p0 * JP + cl : cl % D;
                         x[h] = (cb + pl * R)[p.colJ[j]];
                         nrm = fmaf(x[h], x[h], nrm);         // the warp reads every element once
                     }
-                    splitBF16x2(x[0], x[1], hi[e], lo[e]);
+                    if constexpr (BF) {
+                        splitBF16x2(x[0], x[EPW - 1], hi[e], lo[e]);
+                    } else {
+                        // hi = x rounded to TF32; lo = x - hi (exact), which the MMA
+                        // reads as its leading TF32 bits; lo takes both signs, so
+                        // that truncation is unbiased
+                        hi[e] = tf32Bits(x[0]);
+                        lo[e] = __float_as_uint(x[0] - __uint_as_float(hi[e]));
+                    }
                 }
-                tmemSt8(aH + c0 / 2, hi);
-                tmemSt8(aH + KC / 2 + c0 / 2, lo);
+                tmemSt8(aH + c0 / EPW, hi);
+                tmemSt8(aH + kStageCols / 2 + c0 / EPW, lo);
             }
             if (measure) normIn += (double)nrm;
             tmemWaitSt();
@@ -746,10 +767,10 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         if (lane == 0 && nl.out) atomicAdd(nl.out, normOut);
     } else if (lane == 0) {
         // ------------------------------------------------ TMA of G, then MMAs
-        mbarExpectTx(&barG, 3 * kGW * 4);
+        mbarExpectTx(&barG, S::NGP * kGW * 4);
         bulkG2S(gh, gImage, kGW * 4, &barG);
         bulkG2S(gl, gImage + kGW, kGW * 4, &barG);
-        bulkG2S(gll, gImage + 2 * kGW, kGW * 4, &barG);
+        if (BF) bulkG2S(gll, gImage + 2 * kGW, kGW * 4, &barG);
         bool ok = mbarWaitOrAbort(&barG, 0, &abortF);
         if (!ok) mbarWaitOrAbort(&barG, 0, &abortF);                // once more for the copies in flight
         const uint32_t ghA = smemAddr(gh), glA = smemAddr(gl), gllA = smemAddr(gll);
@@ -769,7 +790,7 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                     break;
                 }
                 fenceAfter();
-                const uint32_t aH = tmem + b * kStageCols, aL = aH + KC / 2;
+                const uint32_t aH = tmem + b * kStageCols, aL = aH + kStageCols / 2;
                 // chunk ch's B: k <= 5 the whole of Gh / Gl; k = 6 rows 64..191 of the
                 // compact form for the real parts of X (ch 0), rows 0..127 for the
                 // imaginary parts (ch 1).  K step ks (16 entries) reads the next 8
@@ -779,18 +800,29 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                 const uint64_t dH = smemDesc(ghA + gOff, kLBO, S::GSBO);
                 const uint64_t dL = smemDesc(glA + gOff, kLBO, S::GSBO);
                 const uint64_t dLL = smemDesc(gllA + gOff, kLBO, S::GSBO);
-                // Xh.Gh + Xl.Gh + Xh.Gl + Xh.Gll: G to ~2^-24 (a ~2^-17 G would
-                // change the norm by up to ~1e-6 per pass, depending on the
-                // state); the dropped Xl.Gl is unbiased
+                if constexpr (BF) {
+                    // Xh.Gh + Xl.Gh + Xh.Gl + Xh.Gll: G to ~2^-24 (a ~2^-17 G
+                    // would change the norm by up to ~1e-6 per pass, depending
+                    // on the state); the dropped Xl.Gl is unbiased
 #pragma unroll
-                for (int ks = 0; ks < KC / 16; ++ks)
-                    mmaBF16(dT, aH + 8 * ks, dH + 16u * ks, idesc, (ch | ks) != 0);
+                    for (int ks = 0; ks < KC / 16; ++ks)
+                        mmaBF16(dT, aH + 8 * ks, dH + 16u * ks, idesc, (ch | ks) != 0);
 #pragma unroll
-                for (int ks = 0; ks < KC / 16; ++ks) mmaBF16(dT, aL + 8 * ks, dH + 16u * ks, idesc, 1);
+                    for (int ks = 0; ks < KC / 16; ++ks) mmaBF16(dT, aL + 8 * ks, dH + 16u * ks, idesc, 1);
 #pragma unroll
-                for (int ks = 0; ks < KC / 16; ++ks) mmaBF16(dT, aH + 8 * ks, dL + 16u * ks, idesc, 1);
+                    for (int ks = 0; ks < KC / 16; ++ks) mmaBF16(dT, aH + 8 * ks, dL + 16u * ks, idesc, 1);
 #pragma unroll
-                for (int ks = 0; ks < KC / 16; ++ks) mmaBF16(dT, aH + 8 * ks, dLL + 16u * ks, idesc, 1);
+                    for (int ks = 0; ks < KC / 16; ++ks) mmaBF16(dT, aH + 8 * ks, dLL + 16u * ks, idesc, 1);
+                } else {
+                    // Xh.Gh + Xl.Gh + Xh.Gl (K = 8 per MMA)
+#pragma unroll
+                    for (int ks = 0; ks < KC / 8; ++ks)
+                        mmaTF32(dT, aH + 8 * ks, dH + 16u * ks, idesc, (ch | ks) != 0);
+#pragma unroll
+                    for (int ks = 0; ks < KC / 8; ++ks) mmaTF32(dT, aL + 8 * ks, dH + 16u * ks, idesc, 1);
+#pragma unroll
+                    for (int ks = 0; ks < KC / 8; ++ks) mmaTF32(dT, aH + 8 * ks, dL + 16u * ks, idesc, 1);
+                }
                 mmaCommit(&emptyB[b]);
             }
             if (!ok) break;
@@ -899,14 +931,17 @@ bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* i
 }
 
 
-template <int KQ, int LG, int EG, int LS>
+template <int KQ, int LG, int EG, int LS, int PR>
 bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, const NormLinks& nl,
                cudaStream_t st) {
-    using S = TC2Shape<KQ, LG, EG, LS>;
+    using S = TC2Shape<KQ, LG, EG, LS, PR>;
     constexpr int D = S::D, K = S::K, N = S::N, PART = S::PART;
     constexpr int V4 = S::TILE / 512;
     const size_t smem = S::smemBytes;
-    img += (size_t)2 * N * K;                       // the BF16 parts follow the TF32 image
+    // the pass image: full TF32 hi, lo (k <= 5: the split-TF32 operands), the
+    // three BF16 parts, then at k = 6 the compact TF32 hi, lo
+    if (PR == kPrecBF16) img += (size_t)2 * N * K;
+    else if (KQ == 6) img += (size_t)2 * N * K + (size_t)3 * S::GE / 2;
     TC2Params<KQ> p{};
     // I = targets + the 7 lowest other qubits (ascending); tile position b <-> qubit I[b]
     uint64_t tmask = 0;
@@ -981,17 +1016,18 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
     const uint64_t numTiles = 1ull << (n - KQ - kTileBitsC);
     static bool configured = false;
     if (!configured) {
-        if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ, LG, EG, LS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+        if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ, LG, EG, LS, PR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "applyPlanF32"))
             return false;
         configured = true;
     }
     const uint64_t grid = std::min<uint64_t>(numTiles, (uint64_t)numSMs());
-    kApplyTC2<KQ, LG, EG, LS><<<(unsigned)grid, (4 * (LG + EG) + 1) * 32, smem, st>>>(re, im, img, numTiles, errFlag, nl, p);
+    kApplyTC2<KQ, LG, EG, LS, PR><<<(unsigned)grid, (4 * (LG + EG) + 1) * 32, smem, st>>>(re, im, img, numTiles, errFlag, nl, p);
     return !launchFailed("applyPlanF32");
 }
 
 bool g_tcEnabled = true;
+int g_tcPrecision = kPrecBF16;   // operands of the pipelined kernel
 int g_tcVersion = 0;      // 0: per pass by target layout; 1, 2, 3: force one kernel
 
 }  // namespace
@@ -1001,7 +1037,8 @@ static size_t imageFloats(int k) {
     if (k < 4 || k > 6) return 0;
     const size_t D = (size_t)1 << k, full = 4 * D * D;
     const size_t bEntries = (k == 6) ? 3 * D * D : full;
-    return (2 * full + (3 * bEntries + 1) / 2 + 3) & ~(size_t)3;     // 16-byte multiple
+    const size_t tf32Compact = (k == 6) ? 2 * 3 * D * D : 0;
+    return (2 * full + (3 * bEntries + 1) / 2 + tf32Compact + 3) & ~(size_t)3;     // 16-byte multiple
 }
 static void buildImage(const FusedPass& pass, float* img) {
     const int k = (int)pass.targets.size();
@@ -1043,6 +1080,19 @@ static void buildImage(const FusedPass& pass, float* img) {
             bl[at] = l;
             bll[at] = hostBF16RN((float)(r1 - (double)bf16Value(l)));
         }
+    if (k == 6) {
+        // the compact TF32 form for the split-TF32 pipelined kernel
+        std::vector<float> ch((size_t)3 * D * D), cl((size_t)3 * D * D);
+        for (int r = 0; r < 3 * D; ++r)
+            for (int j = 0; j < D; ++j) {
+                const int rr = (r < D) ? r : r - D, jj = (r < D) ? D + j : j;
+                ch[(size_t)r * D + j] = hi[(size_t)rr * K + jj];
+                cl[(size_t)r * D + j] = lo[(size_t)rr * K + jj];
+            }
+        float* const tc = img + 2 * full + (3 * bEntries + 1) / 2;
+        packKMajor(ch, 3 * D, D, tc);
+        packKMajor(cl, 3 * D, D, tc + (size_t)3 * D * D);
+    }
 }
 
 // Operand images of every tensor-core pass, built on up to 8 host threads
@@ -1187,11 +1237,12 @@ int applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, 
         // 2: two loader groups (alternate chunks) + one epilogue group; 3: one
         // + one; 4: one + two; 5: two loader groups (each half of every chunk)
         // + two epilogue groups
-#define QG_TC2(KQ)                                                                                      \
-    (version == 2   ? launchTC2<KQ, 2, 1, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)    \
-     : version == 3 ? launchTC2<KQ, 1, 1, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)    \
-     : version == 4 ? launchTC2<KQ, 1, 2, 1>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)    \
-                    : launchTC2<KQ, 2, 2, 2>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st))
+#define QG_TC2P(KQ, PR)                                                                                     \
+    (version == 2   ? launchTC2<KQ, 2, 1, 1, PR>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)    \
+     : version == 3 ? launchTC2<KQ, 1, 1, 1, PR>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)    \
+     : version == 4 ? launchTC2<KQ, 1, 2, 1, PR>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)    \
+                    : launchTC2<KQ, 2, 2, 2, PR>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st))
+#define QG_TC2(KQ) (g_tcPrecision == kPrecTF32 ? QG_TC2P(KQ, kPrecTF32) : QG_TC2P(KQ, kPrecBF16))
         switch (k) {
             case 4: ok = QG_TC2(4); break;
             case 5: ok = QG_TC2(5); break;
@@ -1199,6 +1250,7 @@ int applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, 
             default: return 0;
         }
 #undef QG_TC2
+#undef QG_TC2P
     } else {
         switch (k) {
             case 4: ok = launchTC<4>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st); break;
@@ -1246,6 +1298,12 @@ bool tcFinalNorms(const void* devPlan, const double** target, const double** out
 }
 
 void setTensorCoresEnabled(bool on) { g_tcEnabled = on; }
+bool setTensorCorePrecision(int mode) {
+    if (mode != kPrecTF32 && mode != kPrecBF16) return false;
+    g_tcPrecision = mode;
+    return true;
+}
+int tensorCorePrecision() { return g_tcPrecision; }
 void setTensorCoreKernel(int version) { g_tcVersion = (version >= 1 && version <= 5) ? version : 0; }
 bool tensorCoresEnabled() { return g_tcEnabled; }
 

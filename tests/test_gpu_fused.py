@@ -113,10 +113,19 @@ def _single_gate_plan(L, n, targets, seed):
     return p, u
 
 
+@pytest.fixture(params=[1, 0], ids=["bf16", "tf32"])
+def precision(request, gpulib):
+    """Operands of the pipelined kernel: 1 = 4-term split-BF16 (default),
+    0 = 3-term split-TF32."""
+    assert gpulib.lib.quest_gb300_setTensorCorePrecision(request.param) == 0
+    yield request.param
+    gpulib.lib.quest_gb300_setTensorCorePrecision(1)
+
+
 @pytest.mark.parametrize("targets", [[0, 1, 2, 3], [0, 2, 4, 6, 8], [0, 1, 2, 3, 4, 5], [1, 3, 5, 7, 9, 11],
                                      [2, 9, 10, 14], [4, 5, 6, 7, 15, 16], [12, 13, 14, 15, 16, 17]])
 @pytest.mark.parametrize("version", [0, 1, 2, 3, 4, 5])
-def test_tensor_core_target_layouts(gpulib, targets, version):
+def test_tensor_core_target_layouts(gpulib, targets, version, precision):
     """One dense gate on low, interleaved and high target sets, every
     tensor-core kernel (direct-load; pipelined with 2+1, 1+1, 1+2 loader +
     epilogue warp groups, and 2+2 with the loaders splitting each chunk),
@@ -137,7 +146,7 @@ def test_tensor_core_target_layouts(gpulib, targets, version):
     L.multiQubitUnitary(q64, targets, u)
     err = C.c_double(0)
     omf = L.lib.quest_gb300_compareF32(q32, q64, C.byref(err))
-    print(f"TC v{version} targets={targets}: 1-F={omf:.2e} max|d amp|={err.value:.2e}")
+    print(f"TC v{version} prec={precision} targets={targets}: 1-F={omf:.2e} max|d amp|={err.value:.2e}")
     assert omf < 1e-9 and err.value < 1e-5
     L.lib.quest_gb300_planDestroy(plan)
     L.lib.quest_gb300_destroyQuregF32(q32)
@@ -145,7 +154,7 @@ def test_tensor_core_target_layouts(gpulib, targets, version):
 
 
 @pytest.mark.parametrize("version", [0, 1, 3, 4, 5])
-def test_non_unitary_passes_keep_their_norm(gpulib, version):
+def test_non_unitary_passes_keep_their_norm(gpulib, version, precision):
     """A plan mixing non-unitary and unitary dense gates on the tensor cores:
     the drift correction must not undo a pass that changes the norm on
     purpose (only unitary passes are corrected)."""
@@ -188,13 +197,13 @@ def test_non_unitary_passes_keep_their_norm(gpulib, version):
 
 
 @pytest.mark.parametrize("kmax", [4, 6])
-def test_fused_30q_headline_accuracy(gpulib, kmax):
+def test_fused_30q_headline_accuracy(gpulib, kmax, precision):
     """The 30-qubit, 20-layer circuit: fused FP32 vs plain FP64."""
     L = gpulib
     ops = W.c2_circuit(n=30, layers=20, seed=2)
     q64, q32, plan, omf, err = run_both(L, 30, kmax, ops)
     norm = L.lib.quest_gb300_calcTotalProbF32(q32)
-    print(f"30q k={kmax}: 1-F={omf:.3e} max|d amp|={err:.3e} norm-1={norm - 1:.2e}")
+    print(f"30q k={kmax} prec={precision}: 1-F={omf:.3e} max|d amp|={err:.3e} norm-1={norm - 1:.2e}")
     assert omf <= 1e-6 and abs(norm - 1) < 1e-5
     L.lib.quest_gb300_planDestroy(plan)
     L.lib.quest_gb300_destroyQuregF32(q32)
