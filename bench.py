@@ -143,6 +143,9 @@ def run_gpu(args, rank, world):
     pass_bytes = 2 * (1 << n) * 8                   # one fused pass: read + write the FP32 state
 
     # ---- fused FP32 engine (the headline) --------------------------------
+    prec = 0 if args.precision == "tf32" else 1
+    pname = "split-TF32" if prec == 0 else "split-BF16"
+    lib.quest_gb300_setTensorCorePrecision(prec)
     t0 = time.perf_counter()
     plan = L.plan(n, k, ops)
     plan_s = time.perf_counter() - t0
@@ -187,10 +190,10 @@ def run_gpu(args, rank, world):
     keys = []
     for i in range(npass):
         key = {0: f"kApplySimt<{kk[i]}> (FP32 FFMA)", 1: f"kApplyTC<{kk[i]}> (tcgen05 split-TF32, direct loads)",
-               2: f"kApplyTC2<{kk[i]},2,1,1> (tcgen05 split-BF16, pipelined)",
-               3: f"kApplyTC2<{kk[i]},1,1,1> (tcgen05 split-BF16, pipelined)",
-               4: f"kApplyTC2<{kk[i]},1,2,1> (tcgen05 split-BF16, pipelined)",
-               5: f"kApplyTC2<{kk[i]},2,2,2> (tcgen05 split-BF16, pipelined)"}[tc[i]]
+               2: f"kApplyTC2<{kk[i]},2,1,1> (tcgen05 {pname}, pipelined)",
+               3: f"kApplyTC2<{kk[i]},1,1,1> (tcgen05 {pname}, pipelined)",
+               4: f"kApplyTC2<{kk[i]},1,2,1> (tcgen05 {pname}, pipelined)",
+               5: f"kApplyTC2<{kk[i]},2,2,2> (tcgen05 {pname}, pipelined)"}[tc[i]]
         keys.append(key)
         g = groups.setdefault(key, [0, 0.0])
         g[0] += 1
@@ -222,7 +225,7 @@ def run_gpu(args, rank, world):
     # 4-term split-BF16)
     tf32 = None
     dom_idx = [i for i in range(npass) if keys[i] == dom_name]
-    if lib.quest_gb300_setTensorCorePrecision(0) == 0:
+    if prec == 1 and lib.quest_gb300_setTensorCorePrecision(0) == 0:
         fused_step()                                   # warm-up
         tf_pass = [0.0] * npass
         lib.quest_gb300_eventRecord(4)
@@ -292,16 +295,19 @@ def run_gpu(args, rank, world):
     achieved = pass_bytes / (dom_avg / 1e3) / 1e9
     if tf32:
         tf32["dominant_kernel_frac"] = round(pass_bytes / (tf32["dominant_kernel_avg_ms"] / 1e3) / 1e9 / peak, 4)
-    traffic = None
+    traffic = tensor_pct = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
-        t = json.load(open(tp)).get(dom_name.split(" ")[0])
+        prof = json.load(open(tp))
+        kname = dom_name.split(" ")[0] + (" tf32" if prec == 0 and "kApplyTC2" in dom_name else "")
+        t = prof.get(kname)
         if t:
             traffic = t * (1 << n)
+        tensor_pct = prof.get("_tensor_pipe_pct", {}).get(kname)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s (per-gate FP64 algorithmic bytes)",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 state (4-term split-BF16 tensor-core products, FP32 accumulation; 3-term split-TF32 arm in fused_fp32_split_tf32; FP64 fusion products and reductions)",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": ("f32 state (4-term split-BF16 tensor-core products, FP32 accumulation; 3-term split-TF32 arm in fused_fp32_split_tf32; FP64 fusion products and reductions)" if prec == 1 else "f32 state (3-term split-TF32 tensor-core products, FP32 accumulation; FP64 fusion products and reductions)"),
         "data": "synthetic (seeded Haar/CPhase-matching/CNOT-brickwork circuit)",
         "config": {"workload": f"{n}-qubit random circuit, {args.layers} layers: fused FP32 engine (k<={k}) vs plain FP64 per-gate engine",
                    "qubits": n, "layers": args.layers, "gates_per_circuit": len(ops), "fusion_max_qubits": k,
@@ -320,7 +326,8 @@ def run_gpu(args, rank, world):
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                      "avg_launch_ms": round(dom_avg, 4), "launches_per_circuit": dom_count,
-                     "bytes_per_launch": pass_bytes},
+                     "bytes_per_launch": pass_bytes,
+                     "tensor_pipe_active_pct_ncu": tensor_pct},
         "e2e": {"value": round(world * alg_bytes / e2e_s / 1e9, 2), "unit": "GB/s (per-gate FP64 algorithmic bytes)",
                 "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes + 8,
                 "ms_per_step": round(e2e_s * 1e3, 2),
@@ -607,6 +614,8 @@ def main():
     ap.add_argument("--cpu-sample-ops", type=int, default=60)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fusion", type=int, default=6, help="max qubits per fused pass (1..6)")
+    ap.add_argument("--precision", default="bf16", choices=["bf16", "tf32"],
+                    help="operands of the pipelined tensor-core kernel for the headline arm")
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--no-swap", action="store_true")
     ap.add_argument("--swap-vectors", type=int, default=4096)
