@@ -461,6 +461,8 @@ struct TC2Params {
     uint32_t colJ[1 << KQ];               // pad(in-part index of the position bits of matrix index j)
     int insI[KQ + kTileBitsC];            // ascending qubits of I
     int runBits;                          // I contains qubits [0, runBits)
+    uint64_t outMask;                     // the qubits outside I (where tile index bits go)
+    uint64_t gridStep;                    // the tile base offset of gridDim.x tiles
 };
 
 // Operand precision of kApplyTC2: 3-term split-TF32 or 4-term split-BF16.
@@ -535,6 +537,25 @@ __device__ __forceinline__ uint64_t tileBase(const TC2Params<KQ>& p, uint64_t ti
     }
     return tb;
 }
+// Tile bases of one role's increasing tile sequence (tiles differ by
+// multiples of gridDim.x).  The base is the tile index deposited into
+// outMask, and deposits add by masked addition:
+// base(t + gridDim.x) = ((base(t) | ~outMask) + gridStep) & outMask.
+template <int KQ>
+struct TileWalker {
+    uint64_t tile = ~0ull, base = 0;
+    __device__ __forceinline__ uint64_t at(const TC2Params<KQ>& p, uint64_t t) {
+        if (tile == ~0ull || t < tile) {
+            base = tileBase(p, t);
+            tile = t;
+        }
+        while (tile < t) {
+            base = ((base | ~p.outMask) + p.gridStep) & p.outMask;
+            tile += gridDim.x;
+        }
+        return base;
+    }
+};
 
 template <int KQ, int LG, int EG, int LS, int PR>
 __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* __restrict__ re, float* __restrict__ im,
@@ -615,10 +636,11 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         // plane.  Region index bits 0, 1 are qubits 0, 1, so positions
         // q = 4 lane + 128 m .. + 3 are four consecutive amplitudes: one
         // 16-byte copy to pad(q); a warp's copy reads four 128-byte lines.
+        TileWalker<KQ> walk;
         auto issue = [&](uint32_t sc, float* buf) {
             const uint64_t tile = blockIdx.x + (uint64_t)(sc / NCH) * gridDim.x;
             const int ch = sc % NCH;
-            const uint64_t tb = tileBase(p, tile) + laneA;
+            const uint64_t tb = walk.at(p, tile) + laneA;
 #pragma unroll
             for (int pp = 0; pp < PPG; ++pp) {
                 const int pt = p0 + pp;
@@ -712,9 +734,10 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         recordScale(nl, sm1, blockIdx.x == 0 && et == 0);
         uint32_t tl = eg;
         double normOut = 0.0;
+        TileWalker<KQ> walk;
         for (uint64_t tile = blockIdx.x + (uint64_t)eg * gridDim.x; tile < numTiles && ok;
              tile += (uint64_t)EG * gridDim.x, tl += EG) {
-            const uint64_t tb = tileBase(p, tile) + laneA;
+            const uint64_t tb = walk.at(p, tile) + laneA;
             const int bd = tl & 1;
             if (!warpWaitOrAbort(&dFullB[bd], (tl >> 1) & 1, &abortF, lane)) {
                 ok = false;
@@ -1014,6 +1037,18 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
         p.colJ[j] = padIdx(compress(v) % PART);
     }
     const uint64_t numTiles = 1ull << (n - KQ - kTileBitsC);
+    const uint64_t grid = std::min<uint64_t>(numTiles, (uint64_t)numSMs());
+    p.outMask = ~imask;
+    {
+        // gridStep = grid deposited into the qubits outside I
+        uint64_t dep = 0, src = grid;
+        for (int q = 0; q < 64 && src; ++q)
+            if (p.outMask >> q & 1ull) {
+                if (src & 1ull) dep |= 1ull << q;
+                src >>= 1;
+            }
+        p.gridStep = dep;
+    }
     static bool configured = false;
     if (!configured) {
         if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ, LG, EG, LS, PR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -1021,7 +1056,6 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
             return false;
         configured = true;
     }
-    const uint64_t grid = std::min<uint64_t>(numTiles, (uint64_t)numSMs());
     kApplyTC2<KQ, LG, EG, LS, PR><<<(unsigned)grid, (4 * (LG + EG) + 1) * 32, smem, st>>>(re, im, img, numTiles, errFlag, nl, p);
     return !launchFailed("applyPlanF32");
 }
