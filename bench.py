@@ -220,12 +220,11 @@ def run_gpu(args, rank, world):
     else:
         one_minus_f = max_amp_err = None
 
-    # ---- the same plan with 3-term split-TF32 operands --------------------
-    # (the pipelined kernel's other precision; the headline uses the default,
-    # 4-term split-BF16)
-    tf32 = None
+    # ---- the same plan with the pipelined kernel's other operands ---------
+    # (3-term split-TF32 is the default; 4-term split-BF16 is the other)
+    other = None
     dom_idx = [i for i in range(npass) if keys[i] == dom_name]
-    if prec == 1 and lib.quest_gb300_setTensorCorePrecision(0) == 0:
+    if lib.quest_gb300_setTensorCorePrecision(1 - prec) == 0:
         fused_step()                                   # warm-up
         tf_pass = [0.0] * npass
         lib.quest_gb300_eventRecord(4)
@@ -235,14 +234,15 @@ def run_gpu(args, rank, world):
         lib.quest_gb300_eventRecord(5)
         tf_ms = lib.quest_gb300_eventElapsedMs(4, 5) / args.steps
         tf_dom = sum(tf_pass[i] for i in dom_idx) / args.steps / max(1, len(dom_idx))
-        tf32 = {"ms_per_circuit": round(tf_ms, 2), "gbs": round(alg_bytes / (tf_ms / 1e3) / 1e9, 1),
-                "dominant_kernel_avg_ms": round(tf_dom, 4)}
+        other = {"ms_per_circuit": round(tf_ms, 2), "gbs": round(alg_bytes / (tf_ms / 1e3) / 1e9, 1),
+                 "dominant_kernel_avg_ms": round(tf_dom, 4),
+                 "note": "same plan; the applier choice of this precision may differ per pass"}
         if plain_ms:
             err = C.c_double(0)
-            tf32["one_minus_fidelity"] = lib.quest_gb300_compareF32(q32, q64, C.byref(err))
-            tf32["max_amp_err"] = err.value
-            tf32["speedup_vs_plain"] = round(plain_ms / tf_ms, 2)
-        lib.quest_gb300_setTensorCorePrecision(1)
+            other["one_minus_fidelity"] = lib.quest_gb300_compareF32(q32, q64, C.byref(err))
+            other["max_amp_err"] = err.value
+            other["speedup_vs_plain"] = round(plain_ms / tf_ms, 2)
+        lib.quest_gb300_setTensorCorePrecision(prec)
 
     # ---- end to end through the QuEST C ABI with host buffers ------------
     # The lab's call pattern, unchanged: initStateFromAmps from pinned host
@@ -293,13 +293,13 @@ def run_gpu(args, rank, world):
 
     peak, peak_kind = peaks()
     achieved = pass_bytes / (dom_avg / 1e3) / 1e9
-    if tf32:
-        tf32["dominant_kernel_frac"] = round(pass_bytes / (tf32["dominant_kernel_avg_ms"] / 1e3) / 1e9 / peak, 4)
+    if other:
+        other["dominant_kernel_frac"] = round(pass_bytes / (other["dominant_kernel_avg_ms"] / 1e3) / 1e9 / peak, 4)
     traffic = tensor_pct = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         prof = json.load(open(tp))
-        kname = dom_name.split(" ")[0] + (" tf32" if prec == 0 and "kApplyTC2" in dom_name else "")
+        kname = dom_name.split(" ")[0] + ((" tf32" if prec == 0 else " bf16") if "kApplyTC2" in dom_name else "")
         t = prof.get(kname)
         if t:
             traffic = t * (1 << n)
@@ -307,7 +307,7 @@ def run_gpu(args, rank, world):
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s (per-gate FP64 algorithmic bytes)",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": ("f32 state (4-term split-BF16 tensor-core products, FP32 accumulation; 3-term split-TF32 arm in fused_fp32_split_tf32; FP64 fusion products and reductions)" if prec == 1 else "f32 state (3-term split-TF32 tensor-core products, FP32 accumulation; FP64 fusion products and reductions)"),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": ("f32 state (3-term split-TF32 tensor-core products, FP32 accumulation; 4-term split-BF16 arm in fused_fp32_split_bf16; FP64 fusion products and reductions)" if prec == 0 else "f32 state (4-term split-BF16 tensor-core products, FP32 accumulation; 3-term split-TF32 arm in fused_fp32_split_tf32; FP64 fusion products and reductions)"),
         "data": "synthetic (seeded Haar/CPhase-matching/CNOT-brickwork circuit)",
         "config": {"workload": f"{n}-qubit random circuit, {args.layers} layers: fused FP32 engine (k<={k}) vs plain FP64 per-gate engine",
                    "qubits": n, "layers": args.layers, "gates_per_circuit": len(ops), "fusion_max_qubits": k,
@@ -319,7 +319,7 @@ def run_gpu(args, rank, world):
                        "plan_compile_s": round(plan_s, 3), "one_minus_fidelity": one_minus_f,
                        "max_amp_err": max_amp_err,
                        "kernels": {name: {"passes": c, "ms_per_circuit": round(t, 2)} for name, (c, t) in groups.items()}},
-        "fused_fp32_split_tf32": tf32,
+        ("fused_fp32_split_bf16" if prec == 0 else "fused_fp32_split_tf32"): other,
         "plain_fp64": ({"ms_per_circuit": round(plain_ms, 1), "gbs": round(alg_bytes / (plain_ms / 1e3) / 1e9, 1),
                         "launches": len(ops)} if plain_ms else None),
         "speedup_fused_vs_plain": round(plain_ms / ms_step, 2) if plain_ms else None,
@@ -614,7 +614,7 @@ def main():
     ap.add_argument("--cpu-sample-ops", type=int, default=60)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fusion", type=int, default=6, help="max qubits per fused pass (1..6)")
-    ap.add_argument("--precision", default="bf16", choices=["bf16", "tf32"],
+    ap.add_argument("--precision", default="tf32", choices=["tf32", "bf16"],
                     help="operands of the pipelined tensor-core kernel for the headline arm")
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--no-swap", action="store_true")

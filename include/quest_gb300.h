@@ -94,9 +94,9 @@ void quest_gb300_setTensorCores(int enabled);
  * groups splitting every chunk (5) */
 void quest_gb300_setTensorCoreKernel(int version);
 /* Operands of the pipelined tensor-core kernel: 0 = 3-term split-TF32
- * (X, G in two TF32 parts; Xh.Gh + Xl.Gh + Xh.Gl), 1 = 4-term split-BF16 (X in
- * two BF16 parts, G in three; Xh.Gh + Xl.Gh + Xh.Gl + Xh.Gll), the default.
- * Both accumulate in FP32.  Returns 0, or -1 for another mode. */
+ * (X, G in two TF32 parts; Xh.Gh + Xl.Gh + Xh.Gl), the default; 1 = 4-term
+ * split-BF16 (X in two BF16 parts, G in three; Xh.Gh + Xl.Gh + Xh.Gl +
+ * Xh.Gll).  Both accumulate in FP32.  Returns 0, or -1 for another mode. */
 int quest_gb300_setTensorCorePrecision(int mode);
 int quest_gb300_getTensorCorePrecision(void);
 double quest_gb300_calcTotalProbF32(void* qureg32);

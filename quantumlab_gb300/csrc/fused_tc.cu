@@ -481,23 +481,40 @@ template <int KQ, int LG, int EG, int LS, int PR>
 struct TC2Shape {
     static constexpr int D = 1 << KQ, K = 2 * D, N = 2 * D;
     static constexpr int TILE = 1 << (KQ + kTileBitsC);       // amplitudes per plane per tile
-    static constexpr int NCH = (KQ == 6) ? 2 : 1;             // K chunks per tile
-    static constexpr int KC = K / NCH;                        // K entries per chunk (<= 64)
-    static constexpr int PART = (KQ == 6) ? TILE / 8 : TILE / 4;   // positions per warp per part (<= 1024)
-    static constexpr int R = (int)((padIdx(PART - 1) + 1 + 3) & ~3u);   // floats per part buffer
-    static constexpr int PPG = (LS == 2) ? 1 : 2;             // parts per loader group per chunk
     static constexpr int ESZ = (PR == kPrecBF16) ? 2 : 4;     // bytes per operand entry
-    static constexpr int NST = (PR == kPrecBF16) ? 4 : 2;     // TMEM operand stages
+    // K chunks per tile: chunks of <= 64 (BF16) or <= 32 (TF32) K entries,
+    // so that four operand stages fit beside the two accumulators
+    static constexpr int NCH = (PR == kPrecBF16) ? ((KQ == 6) ? 2 : 1) : ((KQ == 6) ? 4 : (KQ == 5) ? 2 : 1);
+    static constexpr int KC = K / NCH;                        // K entries per chunk
+    // Parts: the positions a warp stages at once (<= 1024).  k <= 5: the two
+    // planes; k = 6: the halves of a plane by the top target bit.  A chunk is
+    // one part (a plane at k = 5 in TF32; a plane half at k = 6 in TF32) or
+    // two (both planes at k <= 5; both halves of a plane at k = 6 in BF16).
+    static constexpr int PART = (KQ == 6) ? TILE / 8 : TILE / 4;   // positions per warp per part (<= 1024)
+    static constexpr int PPC = ((KQ == 6) ? (NCH == 2) : (NCH == 1)) ? 2 : 1;   // parts per chunk
+    static constexpr int JPP = KC / PPC;                      // K entries (matrix indices) per part
+    // SPLIT: the loader groups split every chunk, group g taking part g;
+    // otherwise each group takes whole chunks, the groups alternating
+    static constexpr bool SPLIT = (LS == 2 && PPC == 2);
+    static constexpr int PPG = SPLIT ? 1 : PPC;               // parts per loader group per chunk
+    static constexpr int R = (int)((padIdx(PART - 1) + 1 + 3) & ~3u);   // floats per part buffer
+    static constexpr int NST = 4;                             // TMEM operand stages
     static constexpr uint32_t STAGE_COLS = (uint32_t)(2 * KC * ESZ / 4);   // Xh then Xl
     static constexpr int NGP = (PR == kPrecBF16) ? 3 : 2;     // parts of G
     static constexpr uint32_t GE = (KQ == 6) ? 3u * D * D : (uint32_t)(N * K);   // entries of each G part
     static constexpr uint32_t GW = GE * ESZ / 4;              // ... in 32-bit words
-    static constexpr uint32_t GSBO = (uint32_t)(((KQ == 6) ? KC : K) * ESZ / 16) * 128u;   // B descriptor stride
+    static constexpr uint32_t GSBO = (uint32_t)(((KQ == 6) ? D : K) * ESZ / 16) * 128u;    // B descriptor stride
     static constexpr size_t fixedFloats = (size_t)NGP * GW + (size_t)EG * 4 * R;
     static constexpr size_t stageFloats = (size_t)LG * 4 * PPG * R;
     static constexpr bool fits(int st) { return (fixedFloats + (size_t)st * stageFloats) * 4 + 2048 <= 227 * 1024; }
     static constexpr int XST = fits(3) ? 3 : (fits(2) ? 2 : 1);
     static constexpr size_t smemBytes = (fixedFloats + (size_t)XST * stageFloats) * 4;
+    static_assert(NST * STAGE_COLS + 2 * N <= 512, "TMEM");
+    // plane, plane half (k = 6) and first matrix index of part pt of chunk ch
+    __host__ __device__ static constexpr int plane(int ch, int pt) {
+        return (KQ == 6) ? ((NCH == 2) ? ch : ch >> 1) : ((NCH == 1) ? pt : ch);
+    }
+    __host__ __device__ static constexpr int half(int ch, int pt) { return (NCH == 4) ? (ch & 1) : pt; }
 };
 
 __device__ __forceinline__ void mbarArrive(uint64_t* bar) {
@@ -568,7 +585,7 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
     constexpr int NCH = S::NCH, KC = S::KC, PART = S::PART, R = S::R, PPG = S::PPG, XST = S::XST, NST = S::NST;
     constexpr uint32_t kGW = S::GW;
     constexpr int V4P = PART / 128;                      // 128-position blocks per part
-    constexpr int JP = (KQ == 6) ? 32 : D;               // matrix indices per part
+    constexpr int JP = S::JPP;                           // matrix indices per part
     constexpr int EPARTS = (KQ == 6) ? 4 : 2;            // epilogue parts per tile (plane x half)
     constexpr uint32_t kStageCols = S::STAGE_COLS;       // Xh, then Xl at + kStageCols / 2
     constexpr uint32_t kDCol0 = NST * kStageCols;
@@ -578,8 +595,7 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
     constexpr uint32_t kLBO = 128;
     constexpr uint32_t idesc = BF ? idescBF16(kTile, N) : idescTF32(kTile, N);
     constexpr int kEpiWarp0 = 4 * LG, kMmaWarp = 4 * (LG + EG);
-    // LS = 1: loader groups take alternate chunks; LS = 2: the two loader
-    // groups split every chunk, group g taking its part g
+    // loader groups split every chunk (S::SPLIT) or take alternate chunks
     static_assert(LS == 1 || LG == 2, "part-split loading needs two loader groups");
 
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -598,7 +614,7 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
             abortF = 0;
             mbarInit(&barG, 1);
             for (int b = 0; b < NST; ++b) {
-                mbarInit(&fullB[b], 128 * (LS == 2 ? LG : 1));
+                mbarInit(&fullB[b], 128 * (S::SPLIT ? LG : 1));
                 mbarInit(&emptyB[b], 1);
             }
             for (int b = 0; b < 2; ++b) {
@@ -623,19 +639,19 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         const uint64_t laneA = p.laneOff[lane];
         const uint32_t colBase = p.colLane[lane];
         // this CTA's chunks, in order: chunk s = (tile blockIdx.x + (s / NCH) * gridDim.x, K chunk s % NCH);
-        // LS = 1: group g takes s = g, g + LG, ...; LS = 2: every s, part g
-        const int p0 = (LS == 2) ? g : 0;
-        const uint32_t s0 = (LS == 2) ? 0u : (uint32_t)g, sStep = (LS == 2) ? 1u : (uint32_t)LG;
+        // split: every s, part g; otherwise group g takes s = g, g + LG, ...
+        const int p0 = S::SPLIT ? g : 0;
+        const uint32_t s0 = S::SPLIT ? 0u : (uint32_t)g, sStep = S::SPLIT ? 1u : (uint32_t)LG;
         const uint32_t nMy = blockIdx.x < numTiles ? (uint32_t)((numTiles - 1 - blockIdx.x) / gridDim.x + 1) * NCH : 0u;
         const uint32_t nMine = nMy > s0 ? (nMy - s0 + sStep - 1) / sStep : 0u;     // chunks of this group
         double normIn = 0.0;
         const bool measure = nl.in != nullptr;             // input norm wanted (uniform)
         float* const wbuf = xs + (size_t)(g * 4 + rw) * XST * PPG * R;             // this warp's stages
-        // Copy chunk sc into a stage.  Its parts: k <= 5 the real and imaginary
-        // planes, k = 6 the two halves (region indices < 1024, >= 1024) of one
-        // plane.  Region index bits 0, 1 are qubits 0, 1, so positions
-        // q = 4 lane + 128 m .. + 3 are four consecutive amplitudes: one
-        // 16-byte copy to pad(q); a warp's copy reads four 128-byte lines.
+        // Copy this group's parts of chunk sc into a stage (a k = 6 part is a
+        // plane half: region indices < 1024 or >= 1024).  Region index bits
+        // 0, 1 are qubits 0, 1, so positions q = 4 lane + 128 m .. + 3 are four
+        // consecutive amplitudes: one 16-byte copy to pad(q); a warp's copy
+        // reads four 128-byte lines.
         TileWalker<KQ> walk;
         auto issue = [&](uint32_t sc, float* buf) {
             const uint64_t tile = blockIdx.x + (uint64_t)(sc / NCH) * gridDim.x;
@@ -644,11 +660,11 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
 #pragma unroll
             for (int pp = 0; pp < PPG; ++pp) {
                 const int pt = p0 + pp;
-                const float* const src = (((NCH == 2) ? ch : pt) == 0 ? re : im) + tb;
+                const float* const src = (S::plane(ch, pt) == 0 ? re : im) + tb;
                 float* const dst = buf + pp * R + rowBase;
 #pragma unroll
                 for (int mm = 0; mm < V4P; ++mm) {
-                    const int m = ((KQ == 6) ? V4P * pt : 0) + mm;
+                    const int m = ((KQ == 6) ? V4P * S::half(ch, pt) : 0) + mm;
                     cpAsync16(dst + padIdx(128u * mm), src + p.warpOff[rw][m]);
                 }
             }
@@ -674,6 +690,7 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
             // this group's K entries of the stage: [p0 JP, (p0 + PPG) JP); EPW per column
             constexpr int EPW = BF ? 2 : 1;
             const uint32_t aH = tmem + laneSel + b * kStageCols + p0 * JP / EPW;
+            const int chq = (int)(sq % NCH);
             const float* const cb = xr + colBase;
             float nrm = 0.f;
 #pragma unroll
@@ -686,7 +703,7 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                     for (int h = 0; h < EPW; ++h) {
                         const int cl = c0 + EPW * e + h;     // local entry: buffer part cl / JP
                         const int pl = cl / JP;
-                        const int j = (NCH == 2) ? p0 * JP + cl : cl % D;
+                        const int j = (KQ == 6) ? 32 * S::half(chq, p0 + pl) + cl % JP : cl % JP;
                         x[h] = (cb + pl * R)[p.colJ[j]];
                         nrm = fmaf(x[h], x[h], nrm);         // the warp reads every element once
                     }
@@ -814,12 +831,15 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                 }
                 fenceAfter();
                 const uint32_t aH = tmem + b * kStageCols, aL = aH + kStageCols / 2;
-                // chunk ch's B: k <= 5 the whole of Gh / Gl; k = 6 rows 64..191 of the
-                // compact form for the real parts of X (ch 0), rows 0..127 for the
-                // imaginary parts (ch 1).  K step ks (16 entries) reads the next 8
-                // TMEM columns of A and the next 256 bytes of B: the descriptor's
-                // start field (address >> 4) advances by 16 per step
-                const uint32_t gOff = (KQ == 6 && ch == 0) ? 8u * S::GSBO : 0u;
+                // chunk ch's B: k <= 5 the rows of G's real form and K entries
+                // [ch KC, (ch + 1) KC); k = 6 rows 64..191 of the compact form for
+                // the real parts of X, rows 0..127 for the imaginary parts, and
+                // the chunk's plane half of the 64 K entries.  Each K step (8 TF32
+                // or 16 BF16 entries) reads the next 8 TMEM columns of A and the
+                // next 256 bytes of B: the descriptor's start field (address >> 4)
+                // advances by 16 per step
+                const uint32_t kEnt = (KQ == 6) ? 32u * (uint32_t)S::half(ch, 0) * (NCH == 4) : (uint32_t)(ch * KC);
+                const uint32_t gOff = ((KQ == 6 && S::plane(ch, 0) == 0) ? 8u * S::GSBO : 0u) + kEnt * S::ESZ / 16u * 128u;
                 const uint64_t dH = smemDesc(ghA + gOff, kLBO, S::GSBO);
                 const uint64_t dL = smemDesc(glA + gOff, kLBO, S::GSBO);
                 const uint64_t dLL = smemDesc(gllA + gOff, kLBO, S::GSBO);
@@ -1061,7 +1081,7 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
 }
 
 bool g_tcEnabled = true;
-int g_tcPrecision = kPrecBF16;   // operands of the pipelined kernel
+int g_tcPrecision = kPrecTF32;   // operands of the pipelined kernel
 int g_tcVersion = 0;      // 0: per pass by target layout; 1, 2, 3: force one kernel
 
 }  // namespace
@@ -1214,11 +1234,15 @@ void tcNoteSimtPass(void* devPlan, size_t index) {
 // (2: 2 loader groups on alternate chunks + 1 epilogue group; 3: 1 + 1;
 // 4: 1 + 2; 5: 2 loader groups splitting every chunk + 2 epilogue groups).
 // Default choice, measured at 30 qubits in ms per pass; "high" means every
-// target is at or above qubit 5.
-//   * 1..3 qubits: the SIMT applier.
-//   * 4 qubits, high targets: kernel 2 (2.6-2.8, against SIMT 3.1-3.2).
-//   * 4 qubits, other targets: kernel 5 (2.7-3.0).
-//   * 5 qubits: kernel 5 (2.7-3.0, against 2.9-3.1 for kernel 2).
+// target is at or above qubit 5.  1..3 qubits: the SIMT applier.
+// Split-TF32 operands (the default):
+//   * 4 qubits: kernel 3 (2.8-3.0, against 2.8-3.1 for kernel 2, 3.1-3.2 SIMT);
+//   * 5 qubits: kernel 2 (2.5-2.9, against 2.8-3.0 for kernel 5);
+//   * 6 qubits: kernel 5 (2.6-3.0, against 2.8-3.1 for kernel 2).
+// Split-BF16 operands:
+//   * 4 qubits, high targets: kernel 2 (2.6-2.8, against SIMT 3.1-3.2);
+//   * 4 qubits, other targets: kernel 5 (2.7-3.0);
+//   * 5 qubits: kernel 5 (2.7-3.0, against 2.9-3.1 for kernel 2);
 //   * 6 qubits: kernel 5 (2.7-3.0).  Kernels 2 and 4 are each a few percent
 //     faster on some target sets.  Choosing by target set came to the same
 //     total over the 30-qubit circuit (297.4 against 296.3 ms).
@@ -1226,6 +1250,7 @@ int tcKernelFor(const FusedPass& pass, int n) {
     const int k = (int)pass.targets.size();
     if (!g_tcEnabled || k < 4 || k > 6 || n < k + 7) return 0;
     if (g_tcVersion != 0) return g_tcVersion;
+    if (g_tcPrecision == kPrecTF32) return k == 4 ? 3 : k == 5 ? 2 : 5;
     const bool high = pass.targets[0] >= 5;
     if (k == 5) return 5;
     if (k == 4) return high ? 2 : 5;
