@@ -436,7 +436,7 @@ Qureg allocQureg(int nsv, int isDM, int nrep, const char* caller) {
     cudaMemsetAsync(scratch, 0, qg::kScratchDoubles * sizeof(double), qg::stream());
     q.deviceStateVec.real = dev;
     q.deviceStateVec.imag = dev + n;
-    qg::captureRegister(dev, nsv);
+    qg::captureRegister(dev, nsv, isDM ? nrep : 0);
     q.stateVec.real = host;
     q.stateVec.imag = host + n;
     q.pairStateVec.real = nullptr;
@@ -1337,7 +1337,7 @@ void mixDephasing(Qureg q, int t, qreal p) {
     if (!vDensity(q, caller) || !vTarget(q, t, caller) || !vProb(p, caller) ||
         !REQUIRE(p <= 1 / 2.0, E_INVALID_ONE_QUBIT_DEPHASE_PROB))
         return;
-    qg::dmDephase(sv(q), t, q.numQubitsRepresented, 1 - 2 * p);
+    qg::dmDephase(svg(q), t, q.numQubitsRepresented, 1 - 2 * p);
 }
 void mixDepolarising(Qureg q, int t, qreal p) {
     const char* caller = "mixDepolarising";
@@ -1346,7 +1346,7 @@ void mixDepolarising(Qureg q, int t, qreal p) {
         return;
     const double level = (4 * p) / 3.0;
     if (level == 0) return;                                   // QuEST_gpu.cu:3029-3030
-    qg::dmDepolarise(sv(q), t, q.numQubitsRepresented, level);
+    qg::dmDepolarise(svg(q), t, q.numQubitsRepresented, level);
 }
 void mixDamping(Qureg q, int t, qreal p) {
     const char* caller = "mixDamping";
@@ -1354,7 +1354,7 @@ void mixDamping(Qureg q, int t, qreal p) {
         !REQUIRE(p <= 1.0, E_INVALID_ONE_QUBIT_DEPOL_PROB))
         return;
     if (p == 0) return;                                       // QuEST_gpu.cu:3055-3056
-    qg::dmDamp(sv(q), t, q.numQubitsRepresented, p);
+    qg::dmDamp(svg(q), t, q.numQubitsRepresented, p);
 }
 void mixDensityMatrix(Qureg a, qreal p, Qureg b) {                        // QuEST.c:1018
     const char* caller = "mixDensityMatrix";

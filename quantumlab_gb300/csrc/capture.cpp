@@ -31,6 +31,8 @@ namespace qg {
 
 struct Capture {
     int n = 0;
+    int dmQubits = 0;             // N of a density matrix, 0 for a state vector
+    bool tracePreserving = true;  // every queued op is a unitary gate or a channel
     std::vector<FusedGate> gates;
     void* q32 = nullptr;          // FP32 scratch register of the flushes (kept between flushes)
     long long flushes = 0, gatesApplied = 0;
@@ -81,11 +83,12 @@ void* captureHandle(const double* re) {
     return find(re);
 }
 
-void captureRegister(const double* re, int n) {
+void captureRegister(const double* re, int n, int dmQubits) {
     std::lock_guard<std::mutex> lk(g_capMutex);
     if (defaultMode() == 1 && !find(re)) {
         Capture* c = new Capture();
         c->n = n;
+        c->dmQubits = dmQubits;
         g_caps[re] = c;
     }
 }
@@ -104,6 +107,11 @@ static void flushRecord(Capture* c, double* re, double* im) {
     view.numAmpsTotal = 1LL << c->n;
     view.deviceStateVec.real = re;
     view.deviceStateVec.imag = im;
+    // density matrix under trace-preserving ops only: the trace is restored
+    // after the plan
+    const bool keepTrace = c->dmQubits > 0 && c->tracePreserving;
+    c->tracePreserving = true;
+    if (keepTrace) traceBeforePlan(re, c->dmQubits);
     // the FP64 -> FP32 conversion runs on the device while the host plans
     quest_gb300_copyFromQureg(c->q32, view);
     FusedPlan* plan = new FusedPlan();
@@ -117,7 +125,8 @@ static void flushRecord(Capture* c, double* re, double* im) {
         return;
     }
     quest_gb300_applyPlanF32(c->q32, plan);
-    copyToQuregAfterPlan(c->q32, view, plan);
+    if (keepTrace) copyToQuregTraceKept(c->q32, view, c->dmQubits);
+    else copyToQuregAfterPlan(c->q32, view, plan);
     c->gatesApplied += (long long)plan->gates.size();
     c->flushes += 1;
     quest_gb300_planDestroy(plan);
@@ -134,7 +143,10 @@ void captureFlush(double* re, double* im) {
 
 void captureDiscard(const double* re) {
     std::lock_guard<std::mutex> lk(g_capMutex);
-    if (Capture* c = find(re)) c->gates.clear();
+    if (Capture* c = find(re)) {
+        c->gates.clear();
+        c->tracePreserving = true;
+    }
 }
 
 void captureDrop(const double* re) {
@@ -158,7 +170,8 @@ void captureDrop(const double* re) {
 // Returns false (after flushing the queue) when the gate is wider than the
 // widest pass the fused engine takes on this register: the caller then runs
 // it directly.
-static bool captureGate(SV s, uint64_t mask, const std::function<void(std::vector<cplx>&, const Local&)>& apply) {
+static bool captureGate(SV s, uint64_t mask, const std::function<void(std::vector<cplx>&, const Local&)>& apply,
+                        bool channel = false) {
     Capture* c = reinterpret_cast<Capture*>(s.cap);
     const Local l = localOf(mask);
     const int k = (int)l.qubits.size();
@@ -178,6 +191,7 @@ static bool captureGate(SV s, uint64_t mask, const std::function<void(std::vecto
         for (int r = 0; r < D; ++r) g.m[(size_t)r * D + col] = v[r];
     }
     g.unitary = matrixIsUnitary(g.m, D);
+    if (!g.unitary && !channel) c->tracePreserving = false;
     c->gates.push_back(std::move(g));
     return true;
 }
@@ -259,6 +273,18 @@ bool captureSwap(SV s, int q1, int q2) {
     });
 }
 
+bool captureChannel(SV s, int t, int N, const double S[16]) {
+    return captureGate(s, (1ull << t) | (1ull << (t + N)), [&](std::vector<cplx>& v, const Local&) {
+        // the two qubits are t < t + N: local bit 0 is the row qubit
+        cplx out[4];
+        for (int r = 0; r < 4; ++r) {
+            out[r] = 0;
+            for (int c = 0; c < 4; ++c) out[r] += S[4 * r + c] * v[c];
+        }
+        for (int r = 0; r < 4; ++r) v[r] = out[r];
+    }, true);
+}
+
 bool captureMatrixN(SV s, uint64_t ctrl, const int* targs, int k, const double* mr, const double* mi) {
     uint64_t tmask = 0;
     for (int i = 0; i < k; ++i) tmask |= 1ull << targs[i];
@@ -308,6 +334,7 @@ int quest_gb300_setCapture(Qureg q, int mode) {
     if (!qg::find(q.deviceStateVec.real)) {
         qg::Capture* c = new qg::Capture();
         c->n = q.numQubitsInStateVec;
+        c->dmQubits = q.isDensityMatrix ? q.numQubitsRepresented : 0;
         qg::g_caps[q.deviceStateVec.real] = c;
     }
     return 0;

@@ -191,6 +191,34 @@ __global__ void kFinalScale(const double* __restrict__ target, const double* __r
     g_planScale = (o > 0.0) ? sqrt(*target / o) : 1.0;
 }
 
+// Trace of a density matrix of N qubits held as a 2N-qubit vector: the sum of
+// the real parts at i (2^N + 1), one block, FP64 accumulation.  Into
+// g_trace[slot].
+__device__ double g_trace[2];
+constexpr int kTraceThreads = 1024;
+template <class T>
+__global__ void __launch_bounds__(kTraceThreads) kTraceDM(const T* __restrict__ re, int N, int slot) {
+    __shared__ double part[kTraceThreads / 32];
+    const uint64_t dim = 1ull << N;
+    double acc = 0.0;
+    for (uint64_t i = threadIdx.x; i < dim; i += kTraceThreads) acc += (double)re[i * (dim + 1)];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        acc = part[threadIdx.x];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (threadIdx.x == 0) g_trace[slot] = acc;
+    }
+}
+// g_planScale = trace in / trace out (the correction of a trace-preserving plan)
+__global__ void kTraceScale() {
+    const double o = g_trace[1];
+    g_planScale = (o != 0.0) ? g_trace[0] / o : 1.0;
+}
+
 // ------------------------------------------------------------ reductions
 struct NormF32 {
     const float *re, *im;
@@ -484,6 +512,33 @@ double quest_gb300_compareF32(void* h, Qureg ref, double* maxAmpErr) {
 }  // extern "C"
 
 namespace qg {
+// Trace of the FP64 density matrix (N qubits) about to be converted to FP32,
+// recorded on the device for copyToQuregTraceKept
+void traceBeforePlan(const double* re, int N) {
+    kTraceDM<double><<<1, kTraceThreads, 0, stream()>>>(re, N, 0);
+    launchFailed("captureFlush");
+}
+
+// FP32 register -> FP64 Qureg after a trace-preserving plan on a density
+// matrix of N qubits: the conversion also scales by the trace before the plan
+// over the trace after it, which removes the FP32 accumulation's bias (a
+// near-uniform shrink of all entries) from trace and purity alike
+void copyToQuregTraceKept(void* h, Qureg& dst, int N) {
+    QuregF32* q = Q(h);
+    const uint64_t n = 1ull << q->n;
+    if (dst.numAmpsTotal != (long long)n) {
+        invalidQuESTInputError("Dimensions of the qubit registers don't match.", "copyToQureg");
+        return;
+    }
+    double* scale = nullptr;
+    if (QG_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&scale), g_planScale), "copyToQureg")) return;
+    kTraceDM<float><<<1, kTraceThreads, 0, stream()>>>(q->re, N, 1);
+    kTraceScale<<<1, 1, 0, stream()>>>();
+    kF32toF64<<<convBlocks(n), kConvThreads, 0, stream()>>>(q->re, q->im, dst.deviceStateVec.real,
+                                                           dst.deviceStateVec.imag, n, scale);
+    launchFailed("copyToQureg");
+}
+
 // FP32 register -> FP64 Qureg after a plan: when the plan ended in a chain of
 // unitary passes, the conversion also removes the norm residue of its last
 // tensor-core pass (scaled back to the norm the chain started from), which no

@@ -52,11 +52,17 @@ inline SV svOf(const Qureg& q) { return SV{q.deviceStateVec.real, q.deviceStateV
 
 // ---- op-stream capture (capture.cpp) ----------------------------------------
 void* captureHandle(const double* re);            // the register's capture record, or null
-void captureRegister(const double* re, int n);    // at creation: capture on if QUEST_GB300_CAPTURE=fp32
+// at creation: capture on if QUEST_GB300_CAPTURE=fp32; dmQubits = N for a
+// density matrix of N qubits (a 2N-qubit vector), 0 for a state vector
+void captureRegister(const double* re, int n, int dmQubits);
 void captureFlush(double* re, double* im);        // apply the queued gates (FP32 fused engine)
 // FP32 register -> FP64 Qureg after applying `plan`, with the plan's last norm
 // correction folded in (fused_f32.cu)
 void copyToQuregAfterPlan(void* qureg32, Qureg& dst, void* plan);
+// the same for a trace-preserving plan on a density matrix of N qubits: the
+// trace recorded by traceBeforePlan is restored (fused_f32.cu)
+void traceBeforePlan(const double* re, int N);
+void copyToQuregTraceKept(void* qureg32, Qureg& dst, int N);
 void captureDiscard(const double* re);            // drop the queued gates (the state is overwritten next)
 void captureDrop(const double* re);               // at destruction
 // launcher hooks: queue the gate and return true, or return false (after a
@@ -68,6 +74,10 @@ bool captureRotateZ(SV s, uint64_t ctrl, uint64_t targ, double angle);
 bool capturePauliRotation(SV s, uint64_t ctrl, uint64_t xmask, uint64_t ymask, uint64_t zmask, double angle, int conj);
 bool captureSwap(SV s, int q1, int q2);
 bool captureMatrixN(SV s, uint64_t ctrl, const int* targs, int k, const double* mr, const double* mi);
+// a one-qubit decoherence channel on a density matrix of N qubits, as the
+// real 4 x 4 superoperator S on (row qubit t, column qubit t + N): local index
+// = row bit + 2 column bit, out = S in
+bool captureChannel(SV s, int t, int N, const double S[16]);
 
 struct Mat2 { double r[2][2], i[2][2]; };
 

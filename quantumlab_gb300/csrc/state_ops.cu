@@ -312,8 +312,24 @@ void collapseDM(SV s, int target, int nRep, int outcome, double renorm) {
     launchFailed("collapseToOutcome");
 }
 
-void dmDephase(SV s, int t, int N, double retain) { launchChannel(s, t, N, Dephase{retain}, "mixDephasing"); }
-void dmDepolarise(SV s, int t, int N, double level) { launchChannel(s, t, N, Depolarise{level}, "mixDepolarising"); }
-void dmDamp(SV s, int t, int N, double p) { launchChannel(s, t, N, Damp{p, sqrt(1 - p)}, "mixDamping"); }
+// With capture on, each channel is queued as its superoperator on
+// (t, t + N), local index = row bit + 2 column bit (the functors above)
+void dmDephase(SV s, int t, int N, double retain) {
+    const double S[16] = {1, 0, 0, 0, 0, retain, 0, 0, 0, 0, retain, 0, 0, 0, 0, 1};
+    if (s.cap && captureChannel(s, t, N, S)) return;
+    launchChannel(s, t, N, Dephase{retain}, "mixDephasing");
+}
+void dmDepolarise(SV s, int t, int N, double level) {
+    const double d = 1 - level / 2, x = level / 2, o = 1 - level;
+    const double S[16] = {d, 0, 0, x, 0, o, 0, 0, 0, 0, o, 0, x, 0, 0, d};
+    if (s.cap && captureChannel(s, t, N, S)) return;
+    launchChannel(s, t, N, Depolarise{level}, "mixDepolarising");
+}
+void dmDamp(SV s, int t, int N, double p) {
+    const double o = sqrt(1 - p);
+    const double S[16] = {1, 0, 0, p, 0, o, 0, 0, 0, 0, o, 0, 0, 0, 0, 1 - p};
+    if (s.cap && captureChannel(s, t, N, S)) return;
+    launchChannel(s, t, N, Damp{p, o}, "mixDamping");
+}
 
 }  // namespace qg
