@@ -42,7 +42,7 @@ int quest_gb300_planAddUnitary(void* plan, int target, const double* re4, const 
 int quest_gb300_planAddHadamard(void* plan, int target);
 int quest_gb300_planAddControlledNot(void* plan, int control, int target);
 int quest_gb300_planAddControlledPhaseShift(void* plan, int qubit1, int qubit2, double angle);
-/* Sets kept per level of the pass search (1..256, default 8); wider finds
+/* Sets kept per level of the pass search (1..256, default 16); wider finds
  * fewer passes on some circuits at more host time.  Returns 0 or -1. */
 int quest_gb300_planSetBeamWidth(void* plan, int width);
 /* Compile; returns the number of passes, or -1. */

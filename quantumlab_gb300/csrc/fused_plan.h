@@ -31,7 +31,7 @@ struct FusedPass {
 struct FusedPlan {
     int numQubits = 0;
     int maxFused = 4;
-    int beamWidth = 8;          // sets kept per level of the pass search
+    int beamWidth = 16;         // sets kept per level of the pass search
     std::vector<FusedGate> gates;
     std::vector<FusedPass> passes;
     bool compiled = false;
