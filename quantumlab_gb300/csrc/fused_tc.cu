@@ -574,7 +574,9 @@ struct TileWalker {
     }
 };
 
-template <int KQ, int LG, int EG, int LS, int PR>
+// CV = 4: the targets include qubits 0 and 1, and columns are read and
+// written as 16-byte words (see colWords4)
+template <int KQ, int LG, int EG, int LS, int PR, int CV>
 __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* __restrict__ re, float* __restrict__ im,
                                                                   const float* __restrict__ gImage, uint64_t numTiles,
                                                                   int* __restrict__ errFlag, const NormLinks nl,
@@ -696,25 +698,54 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
 #pragma unroll
             for (int c0 = 0; c0 < PPG * JP; c0 += 8 * EPW) {
                 uint32_t hi[8], lo[8];
+                if constexpr (CV == 4) {
+                    // targets on qubits 0, 1: a column's entries j .. j + 3 are one
+                    // 16-byte word (scalar reads would be a 4-way bank conflict);
+                    // four consecutive local entries stay in one part
+                    float xv[8 * EPW];
 #pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    float x[EPW];
-#pragma unroll
-                    for (int h = 0; h < EPW; ++h) {
-                        const int cl = c0 + EPW * e + h;     // local entry: buffer part cl / JP
+                    for (int v = 0; v < 2 * EPW; ++v) {
+                        const int cl = c0 + 4 * v;
                         const int pl = cl / JP;
                         const int j = (KQ == 6) ? 32 * S::half(chq, p0 + pl) + cl % JP : cl % JP;
-                        x[h] = (cb + pl * R)[p.colJ[j]];
-                        nrm = fmaf(x[h], x[h], nrm);         // the warp reads every element once
+                        const float4 f = *reinterpret_cast<const float4*>(cb + pl * R + p.colJ[j]);
+                        xv[4 * v] = f.x;
+                        xv[4 * v + 1] = f.y;
+                        xv[4 * v + 2] = f.z;
+                        xv[4 * v + 3] = f.w;
                     }
-                    if constexpr (BF) {
-                        splitBF16x2(x[0], x[EPW - 1], hi[e], lo[e]);
-                    } else {
-                        // hi = x rounded to TF32; lo = x - hi (exact), which the MMA
-                        // reads as its leading TF32 bits; lo takes both signs, so
-                        // that truncation is unbiased
-                        hi[e] = tf32Bits(x[0]);
-                        lo[e] = __float_as_uint(x[0] - __uint_as_float(hi[e]));
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+#pragma unroll
+                        for (int h = 0; h < EPW; ++h) nrm = fmaf(xv[EPW * e + h], xv[EPW * e + h], nrm);
+                        if constexpr (BF) {
+                            splitBF16x2(xv[2 * e], xv[2 * e + 1], hi[e], lo[e]);
+                        } else {
+                            hi[e] = tf32Bits(xv[e]);
+                            lo[e] = __float_as_uint(xv[e] - __uint_as_float(hi[e]));
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        float x[EPW];
+#pragma unroll
+                        for (int h = 0; h < EPW; ++h) {
+                            const int cl = c0 + EPW * e + h;     // local entry: buffer part cl / JP
+                            const int pl = cl / JP;
+                            const int j = (KQ == 6) ? 32 * S::half(chq, p0 + pl) + cl % JP : cl % JP;
+                            x[h] = (cb + pl * R)[p.colJ[j]];
+                            nrm = fmaf(x[h], x[h], nrm);         // the warp reads every element once
+                        }
+                        if constexpr (BF) {
+                            splitBF16x2(x[0], x[EPW - 1], hi[e], lo[e]);
+                        } else {
+                            // hi = x rounded to TF32; lo = x - hi (exact), which the MMA
+                            // reads as its leading TF32 bits; lo takes both signs, so
+                            // that truncation is unbiased
+                            hi[e] = tf32Bits(x[0]);
+                            lo[e] = __float_as_uint(x[0] - __uint_as_float(hi[e]));
+                        }
                     }
                 }
                 tmemSt8(aH + c0 / EPW, hi);
@@ -780,12 +811,28 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                     fenceBefore();
                     mbarArrive(&dEmptyB[bd]);
                 }
+                if constexpr (CV == 4) {
+                    // targets on qubits 0, 1: 16-byte column words
 #pragma unroll
-                for (int e = 0; e < JP; ++e) {
-                    const float y0 = __uint_as_float(e < 16 ? va[e] : vb[e - 16]);
-                    const float y = fmaf(y0, sm1, y0);
-                    nrmTile = fmaf(y, y, nrmTile);
-                    cb[p.colJ[h * 32 + e]] = y;
+                    for (int e = 0; e < JP; ++e) {
+                        uint32_t& w = e < 16 ? va[e] : vb[e - 16];
+                        const float y0 = __uint_as_float(w);
+                        const float y = fmaf(y0, sm1, y0);
+                        nrmTile = fmaf(y, y, nrmTile);
+                        w = __float_as_uint(y);
+                    }
+                    auto yAt = [&](int e) { return __uint_as_float(e < 16 ? va[e] : vb[e - 16]); };
+#pragma unroll
+                    for (int e = 0; e < JP; e += 4)
+                        *reinterpret_cast<float4*>(cb + p.colJ[h * 32 + e]) = make_float4(yAt(e), yAt(e + 1), yAt(e + 2), yAt(e + 3));
+                } else {
+#pragma unroll
+                    for (int e = 0; e < JP; ++e) {
+                        const float y0 = __uint_as_float(e < 16 ? va[e] : vb[e - 16]);
+                        const float y = fmaf(y0, sm1, y0);
+                        nrmTile = fmaf(y, y, nrmTile);
+                        cb[p.colJ[h * 32 + e]] = y;
+                    }
                 }
                 __syncwarp();
                 float* const dstPlane = (pl == 0 ? re : im) + tb;
@@ -974,7 +1021,20 @@ bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* i
 }
 
 
-template <int KQ, int LG, int EG, int LS, int PR>
+// Whether a column's entries j .. j + 3 (j % 4 = 0) are one 16-byte word
+// for every lane: true when targets[0..1] are qubits 0, 1, which are bits 0, 1
+// of every in-part index, while the lanes' group bits sit above them.
+template <int KQ>
+bool colWords4(const TC2Params<KQ>& p) {
+    for (int l = 0; l < 32; ++l)
+        if (p.colLane[l] % 4) return false;
+    for (int j = 0; j < (1 << KQ); j += 4)
+        for (uint32_t c = 0; c < 4; ++c)
+            if (p.colJ[j] % 4 || p.colJ[j + c] != p.colJ[j] + c) return false;
+    return true;
+}
+
+template <int KQ, int LG, int EG, int LS, int PR, int CV = 1>
 bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, const NormLinks& nl,
                cudaStream_t st) {
     using S = TC2Shape<KQ, LG, EG, LS, PR>;
@@ -1056,6 +1116,9 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
             if (j >> b & 1) v |= 1u << posOf[pass.targets[b]];
         p.colJ[j] = padIdx(compress(v) % PART);
     }
+    if constexpr (CV == 4) {
+        if (!colWords4(p)) return launchTC2<KQ, LG, EG, LS, PR, 1>(re, im, n, pass, img, errFlag, nl, st);
+    }
     const uint64_t numTiles = 1ull << (n - KQ - kTileBitsC);
     const uint64_t grid = std::min<uint64_t>(numTiles, (uint64_t)numSMs());
     p.outMask = ~imask;
@@ -1071,12 +1134,12 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
     }
     static bool configured = false;
     if (!configured) {
-        if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ, LG, EG, LS, PR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+        if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ, LG, EG, LS, PR, CV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "applyPlanF32"))
             return false;
         configured = true;
     }
-    kApplyTC2<KQ, LG, EG, LS, PR><<<(unsigned)grid, (4 * (LG + EG) + 1) * 32, smem, st>>>(re, im, img, numTiles, errFlag, nl, p);
+    kApplyTC2<KQ, LG, EG, LS, PR, CV><<<(unsigned)grid, (4 * (LG + EG) + 1) * 32, smem, st>>>(re, im, img, numTiles, errFlag, nl, p);
     return !launchFailed("applyPlanF32");
 }
 
@@ -1292,7 +1355,24 @@ int applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, 
         dp->target[index] = continues ? dp->target[dp->lastTC] : dp->inNorm[index];
     }
     bool ok = false;
-    if (version >= 2) {
+    // the default kernels, when the targets include qubits 0 and 1: the
+    // variant with 16-byte column words
+    bool done = false;
+    if (g_tcVersion == 0 && pass.targets[0] == 0 && pass.targets[1] == 1) {
+#define QG_TC2W(KQ, LG, EG, LS, PR) \
+    (done = true, launchTC2<KQ, LG, EG, LS, PR, 4>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st))
+        const bool tf = g_tcPrecision == kPrecTF32;
+        if (tf && k == 4 && version == 3) ok = QG_TC2W(4, 1, 1, 1, kPrecTF32);
+        else if (tf && k == 5 && version == 2) ok = QG_TC2W(5, 2, 1, 1, kPrecTF32);
+        else if (tf && k == 6 && version == 5) ok = QG_TC2W(6, 2, 2, 2, kPrecTF32);
+        else if (!tf && k == 4 && version == 5) ok = QG_TC2W(4, 2, 2, 2, kPrecBF16);
+        else if (!tf && k == 5 && version == 5) ok = QG_TC2W(5, 2, 2, 2, kPrecBF16);
+        else if (!tf && k == 6 && version == 5) ok = QG_TC2W(6, 2, 2, 2, kPrecBF16);
+#undef QG_TC2W
+    }
+    if (done) {
+        // launched above
+    } else if (version >= 2) {
         // 2: two loader groups (alternate chunks) + one epilogue group; 3: one
         // + one; 4: one + two; 5: two loader groups (each half of every chunk)
         // + two epilogue groups

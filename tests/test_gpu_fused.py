@@ -123,11 +123,14 @@ def precision(request, gpulib):
 
 
 @pytest.mark.parametrize("targets", [[0, 1, 2, 3], [0, 2, 4, 6, 8], [0, 1, 2, 3, 4, 5], [1, 3, 5, 7, 9, 11],
-                                     [2, 9, 10, 14], [4, 5, 6, 7, 15, 16], [12, 13, 14, 15, 16, 17]])
+                                     [2, 9, 10, 14], [4, 5, 6, 7, 15, 16], [12, 13, 14, 15, 16, 17],
+                                     [0, 1, 9, 17], [0, 1, 7, 12, 13], [0, 1, 5, 9, 13, 17],
+                                     [0, 5, 9, 12], [0, 3, 8, 9, 15, 17]])
 @pytest.mark.parametrize("version", [0, 1, 2, 3, 4, 5])
 def test_tensor_core_target_layouts(gpulib, targets, version, precision):
-    """One dense gate on low, interleaved and high target sets, every
-    tensor-core kernel (direct-load; pipelined with 2+1, 1+1, 1+2 loader +
+    """One dense gate on low, interleaved and high target sets (with qubit 0,
+    or qubits 0 and 1, among the targets, the pipelined kernel reads and
+    writes columns as 8- or 16-byte words), every tensor-core kernel (direct-load; pipelined with 2+1, 1+1, 1+2 loader +
     epilogue warp groups, and 2+2 with the loaders splitting each chunk),
     against the FP64 engine."""
     L = gpulib
