@@ -445,6 +445,10 @@ __global__ void __launch_bounds__(kThreadsTC, (KQ == 4 ? 4 : 1)) kApplyTC(float*
 //     pad(4 lane) + pad(128 m): a per-thread base plus an immediate offset;
 //   * a column access (group bits of the lane | bits of matrix index j) is
 //     pad(lane bits) + pad(j bits): one add of a per-pass constant.
+// When qubits 0 and 1 are both targets, the lanes' group bits all sit above
+// bit 1 of the in-part index, and a scalar column access would be a 4-way bank
+// conflict; the CV = 4 variant reads and writes entries j .. j + 3 of a column
+// as one 16-byte word instead.
 // The column accesses average 1.65 shared-memory wavefronts over the 6-qubit
 // passes of a 30-qubit random circuit (1.71 with one float of padding per
 // row, which breaks the 16-byte alignment).
