@@ -130,6 +130,29 @@ def run_plain_step(L, q, ops):
             lib.controlledPhaseShift(q, op[1], op[2], op[3])
 
 
+def link_probe(nbytes: int = 1 << 30):
+    """Best of three plain copies of nbytes each way between page-locked host
+    memory and the device, in GB/s: the host link as this process sees it."""
+    try:
+        import torch
+        h = torch.empty(nbytes // 4, dtype=torch.float32, pin_memory=True)
+        d = torch.empty(nbytes // 4, dtype=torch.float32, device="cuda")
+        out = {}
+        for name, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+            best = float("inf")
+            for _ in range(3):
+                torch.cuda.synchronize()
+                t = time.perf_counter()
+                dst.copy_(src, non_blocking=True)
+                torch.cuda.synchronize()
+                best = min(best, time.perf_counter() - t)
+            out[name] = round(nbytes / best / 1e9, 1)
+        del h, d
+        return out
+    except Exception as e:   # diagnostics only
+        return {"error": str(e)[:120]}
+
+
 def run_gpu(args, rank, world):
     import ctypes as C
     import quantumlab_gb300 as qg
@@ -262,6 +285,7 @@ def run_gpu(args, rank, world):
     lib.quest_gb300_setCapture(q64, 1)
 
     split = [0.0, 0.0, 0.0]                            # host -> device, gates + flush, device -> host
+    d2h_each = []
 
     def e2e_step():
         t = time.perf_counter()
@@ -274,10 +298,12 @@ def run_gpu(args, rank, world):
         t3 = time.perf_counter()
         for i, d in enumerate((t1 - t, t2 - t1, t3 - t2)):
             split[i] += d
+        d2h_each.append(round((t3 - t2) * 1e3, 1))
         return p
 
     e2e_step()
     split[:] = [0.0, 0.0, 0.0]
+    d2h_each.clear()
     e2e_steps = max(1, min(args.steps, 2))
     barrier(world)
     t0 = time.perf_counter()
@@ -286,6 +312,10 @@ def run_gpu(args, rank, world):
     e2e_s = barrier_max((time.perf_counter() - t0) / e2e_steps, world)
     split = [x / e2e_steps for x in split]
     lib.quest_gb300_setCapture(q64, 0)
+    # what the host link gave this process: whether both host mirrors are
+    # page-locked, and plain 1 GiB copies between pinned and device memory
+    mirrors_pinned = [lib.quest_gb300_hostMirrorPinned(src) == 1, lib.quest_gb300_hostMirrorPinned(q64) == 1]
+    link = link_probe()
     state_bytes = (1 << n) * 16
     L.destroy(src)
     L.destroy(q64)
@@ -336,7 +366,8 @@ def run_gpu(args, rank, world):
                 "total_prob": e2e_prob,
                 "split_ms": {"h2d_initStateFromAmps": round(split[0] * 1e3, 1),
                              "gates_and_flush": round(split[1] * 1e3, 1),
-                             "d2h_copyStateFromGPU": round(split[2] * 1e3, 1)}},
+                             "d2h_copyStateFromGPU": round(split[2] * 1e3, 1)},
+                "d2h_ms_each_step": d2h_each, "host_mirrors_pinned": mirrors_pinned, "link_probe_1GiB": link},
         "gpu_launches": int(launches // max(1, args.steps)),
         "gpu_launches_timed_region": int(launches),
         "total_prob_fp32": total32,

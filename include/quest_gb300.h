@@ -24,6 +24,10 @@ long long quest_gb300_launchCount(void);
 int quest_gb300_eventRecord(int slot);
 /* Milliseconds between two recorded events (waits for `slotB`); -1 on error. */
 double quest_gb300_eventElapsedMs(int slotA, int slotB);
+/* 1 when the register's host mirror is page-locked (cudaMallocHost), 0 when
+ * that failed and it fell back to pageable memory, -1 for an unknown register.
+ * Host <-> device copies of a pageable mirror run several times slower. */
+int quest_gb300_hostMirrorPinned(Qureg qureg);
 
 /* ---- gate-fusion plans ---------------------------------------------------
  * A plan records a gate stream on numQubits qubits and compiles it into

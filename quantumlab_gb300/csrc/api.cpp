@@ -1362,6 +1362,12 @@ void mixDensityMatrix(Qureg a, qreal p, Qureg b) {                        // QuE
     qg::stateMixDM(sv(a), p, sv(b));
 }
 
+int quest_gb300_hostMirrorPinned(Qureg q) {
+    std::lock_guard<std::mutex> lk(g_regMutex);
+    auto it = g_pinnedMirror.find(q.deviceStateVec.real);
+    return it == g_pinnedMirror.end() ? -1 : (it->second ? 1 : 0);
+}
+
 // ---- QASM: recording is not supported; calls are accepted and ignored ----
 void startRecordingQASM(Qureg q) { (void)q; }
 void stopRecordingQASM(Qureg q) { (void)q; }

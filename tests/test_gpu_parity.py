@@ -104,3 +104,14 @@ def test_validation_messages_match_reference(gpulib):
                     "Invalid measurement outcome -- must be either 0 or 1."]
     assert np.array_equal(L.amps(q), before)
     L.destroy(q)
+
+
+def test_host_mirror_is_page_locked(gpulib):
+    """createQureg page-locks its host mirror (cudaMallocHost), so that
+    copyStateToGPU / copyStateFromGPU run at the host link's speed; the query
+    answers -1 for a register it does not know."""
+    L = gpulib
+    q = L.create(10)
+    assert L.lib.quest_gb300_hostMirrorPinned(q) == 1
+    L.destroy(q)
+    assert L.lib.quest_gb300_hostMirrorPinned(q) == -1
