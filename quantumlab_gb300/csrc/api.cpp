@@ -1301,9 +1301,10 @@ static double expecTerms(const Qureg& q, const enum pauliOpType* codes, const qr
     }
     double total = 0;
     if (identity != 0) total += identity * calcTotalProb(q);
-    for (auto& g : groups)
-        total += qg::reduceExpecPauliGroup(sv(q), q.isDensityMatrix, q.numQubitsRepresented, g.first, g.second.data(),
-                                           (int)g.second.size(), qg::scratchOf(q));
+    std::vector<qg::PauliTermGroup> list;
+    list.reserve(groups.size());
+    for (auto& g : groups) list.push_back(qg::PauliTermGroup{g.first, std::move(g.second)});
+    total += qg::reduceExpecPauliGroups(sv(q), q.isDensityMatrix, q.numQubitsRepresented, list, qg::scratchOf(q));
     return total;
 }
 qreal calcExpecPauliProd(Qureg q, int* ts, enum pauliOpType* ps, int n, Qureg ws) {   // QuEST.c:1208

@@ -6,6 +6,7 @@
 #include <stdint.h>
 #include <atomic>
 #include <stddef.h>
+#include <vector>
 
 #include "QuEST.h"
 
@@ -130,10 +131,12 @@ double reduceDotReal(SV a, SV b, const Scratch& w);          // sum re*re' + im*
 double reduceNormSq(SV s, const Scratch& w);                 // sum |amp|^2 (no Kahan split)
 double reduceDistSq(SV a, SV b, const Scratch& w);
 double reduceFidelityDM(SV rho, SV psi, int nRep, const Scratch& w);
-// Expectation sum_t coeff_t <psi|P_t|psi> of Pauli strings that share one
-// X/Y mask (SV), or Tr(P_t rho) (DM).  yz/nY per term.
+// Expectation sum_t coeff_t <psi|P_t|psi> (SV) or Tr(P_t rho) (DM) of Pauli
+// strings grouped by their X/Y mask (one read of the state per group); yz/nY
+// per term.  Every group's reduction is queued before one synchronisation.
 struct PauliTerm { uint64_t yz; int nY; double coeff; };
-double reduceExpecPauliGroup(SV s, int isDM, int nRep, uint64_t xmask, const PauliTerm* terms, int numTerms, const Scratch& w);
+struct PauliTermGroup { uint64_t xmask; std::vector<PauliTerm> terms; };
+double reduceExpecPauliGroups(SV s, int isDM, int nRep, const std::vector<PauliTermGroup>& groups, const Scratch& w);
 void reduceProbAllOutcomes(SV s, int isDM, int nRep, const int* qubits, int numQubits, double* hostOut, const Scratch& w);
 
 }  // namespace qg

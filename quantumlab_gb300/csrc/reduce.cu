@@ -96,69 +96,111 @@ struct FidelityDM {
     }
 };
 
+// ---- Pauli-string expectation values -----------------------------------
+// GB300 runs FP64 at a small fraction of its FP32 rate, and a Pauli sum
+// (C4's 80-term Fermi-Hubbard energy) has many terms per X/Y group, so the
+// FP64 work per amplitude, not the read of the state, set the time of these
+// reductions.  The per-term algebra is therefore done on the host:
+//   * pairs (j, k = j ^ x): with w = conj(psi_j) psi_k and s_q(j) =
+//     (-1)^popc(j & yz_q), term q adds c_q s_q(j) [Re((-i)^ph w) +
+//     tau_q Re((-i)^ph conj w)], tau_q = (-1)^popc(x & yz_q); that is
+//     2 c_q s_q(j) (+-Re w or +-Im w) when tau_q fits the phase, else 0.  An
+//     item costs wr A(j) + wi B(j) with A, B = sums of +-c over the terms;
+//   * DM, Tr(P rho) = sum_r s(r) Re((-i)^ph rho[r ^ x, r]) = er A(r) + ei B(r);
+//   * a diagonal group (x = 0, SV): an item is 8 consecutive amplitudes.  A
+//     Walsh-Hadamard transform of their |psi|^2 over the 3 low bits gives
+//     Q[m] = sum_l p_l (-1)^popc(l & m); each term then adds
+//     c (-1)^popc(base & z_high) Q[z & 7].  Terms are bucketed by z & 7 on the
+//     host, so an amplitude costs ~6 FP64 operations plus terms / 8.
+// Reference semantics: QuEST_common.c:506-533 (calcExpecPauliSum: clone,
+// apply the Pauli string, inner product, per term).
 constexpr int kMaxGroupTerms = 32;
-struct PauliGroup {
+struct PauliPairGroup {          // SV pairs (xmask != 0) or DM entries (any xmask)
     uint64_t xmask;
-    int low;                     // lowest bit of xmask
-    int numTerms;
-    uint64_t yz[kMaxGroupTerms];
-    int phase[kMaxGroupTerms];   // nY mod 4
-    double coeff[kMaxGroupTerms];
+    int low;                     // lowest bit of xmask (SV)
+    int nA, nB;                  // terms on Re w (er), on Im w (ei)
+    uint64_t mA[kMaxGroupTerms], mB[kMaxGroupTerms];
+    double cA[kMaxGroupTerms], cB[kMaxGroupTerms];
 };
-
-// Re[(-i)^m w]
-__device__ __forceinline__ double rePhase(int m, double wr, double wi) {
-    switch (m & 3) {
-        case 0: return wr;
-        case 1: return wi;
-        case 2: return -wr;
-        default: return -wi;
-    }
+// sum_q c_q (-1)^popc(j & m_q) for n >= 1 terms (n - 1 FP64 additions)
+__device__ __forceinline__ double signedSum(uint64_t j, const uint64_t* m, const double* c, int n) {
+    double a = (__popcll(j & m[0]) & 1) ? -c[0] : c[0];
+    for (int q = 1; q < n; ++q) a += (__popcll(j & m[q]) & 1) ? -c[q] : c[q];
+    return a;
 }
 
-// SV, xmask != 0: pairs (j, k=j^x); contributes Re(conj(psi_j)(P psi)_j) +
-// Re(conj(psi_k)(P psi)_k) for every term of the group
+// x A(j) + y B(j) for a group with at least one term, skipping an empty list
+// (the counts are uniform across the launch)
+__device__ __forceinline__ double pairValue(uint64_t j, double x, double y, const PauliPairGroup& g) {
+    if (g.nB == 0) return x * signedSum(j, g.mA, g.cA, g.nA);
+    if (g.nA == 0) return y * signedSum(j, g.mB, g.cB, g.nB);
+    return fma(x, signedSum(j, g.mA, g.cA, g.nA), y * signedSum(j, g.mB, g.cB, g.nB));
+}
 struct ExpecPairs {
     const double *re, *im;
-    PauliGroup g;
+    PauliPairGroup g;
     __device__ __forceinline__ double2 operator()(uint64_t t) const {
         const uint64_t j = ins0(t, g.low), k = j ^ g.xmask;
         const double jr = re[j], ji = im[j], kr = re[k], ki = im[k];
-        const double wr = jr * kr + ji * ki, wi = jr * ki - ji * kr;       // conj(psi_j) psi_k
-        double acc = 0.0;
-        for (int q = 0; q < g.numTerms; ++q) {
-            const double sj = (__popcll(j & g.yz[q]) & 1) ? -1.0 : 1.0;
-            const double sk = (__popcll(k & g.yz[q]) & 1) ? -1.0 : 1.0;
-            acc += g.coeff[q] * (sj * rePhase(g.phase[q], wr, wi) + sk * rePhase(g.phase[q], wr, -wi));
-        }
-        return make_double2(acc, 0.0);
+        // conj(psi_j) psi_k, only the parts the group's terms use
+        const double wr = g.nA ? fma(jr, kr, ji * ki) : 0.0;
+        const double wi = g.nB ? fma(jr, ki, -(ji * kr)) : 0.0;
+        return make_double2(pairValue(j, wr, wi, g), 0.0);
     }
 };
-// SV, diagonal group: |psi_j|^2 sum_t c_t (-1)^popc(j & z_t)
-struct ExpecDiag {
-    const double *re, *im;
-    PauliGroup g;
-    __device__ __forceinline__ double2 operator()(uint64_t j) const {
-        const double p = re[j] * re[j] + im[j] * im[j];
-        double acc = 0.0;
-        for (int q = 0; q < g.numTerms; ++q) acc += (__popcll(j & g.yz[q]) & 1) ? -g.coeff[q] : g.coeff[q];
-        return make_double2(p * acc, 0.0);
-    }
-};
-// DM: Tr(P rho) = sum_r (-i)^nY (-1)^popc(r & yz) rho[(r^x) + r D]  (real part)
 struct ExpecDM {
     const double *re, *im;
-    PauliGroup g;
+    PauliPairGroup g;
     int N;
     __device__ __forceinline__ double2 operator()(uint64_t r) const {
         const uint64_t idx = (r ^ g.xmask) + (r << N);
-        const double er = re[idx], ei = im[idx];
+        return make_double2(pairValue(r, re[idx], im[idx], g), 0.0);
+    }
+};
+constexpr int kDiagLow = 3;                      // low bits transformed per item
+constexpr int kDiagItem = 1 << kDiagLow;
+constexpr int kMaxDiagTerms = 64;
+struct PauliDiagGroup {
+    int off[kDiagItem + 1];                      // terms of bucket m (z & 7 = m): [off[m], off[m + 1])
+    uint64_t zh[kMaxDiagTerms];                  // z with the low bits cleared
+    double c[kMaxDiagTerms];
+};
+struct ExpecDiag {                               // SV, x = 0: 8 amplitudes per item (n >= 3)
+    const double *re, *im;
+    PauliDiagGroup g;
+    __device__ __forceinline__ double2 operator()(uint64_t i) const {
+        const uint64_t base = i << kDiagLow;
+        double p[kDiagItem];
+#pragma unroll
+        for (int h = 0; h < kDiagItem / 2; ++h) {
+            const double2 r = ld2(re + base + 2 * h), m = ld2(im + base + 2 * h);
+            p[2 * h] = r.x * r.x + m.x * m.x;
+            p[2 * h + 1] = r.y * r.y + m.y * m.y;
+        }
+#pragma unroll
+        for (int sb = 1; sb < kDiagItem; sb <<= 1)
+#pragma unroll
+            for (int l = 0; l < kDiagItem; ++l)
+                if (!(l & sb)) {
+                    const double a = p[l], b = p[l | sb];
+                    p[l] = a + b;
+                    p[l | sb] = a - b;
+                }
         double acc = 0.0;
-        for (int q = 0; q < g.numTerms; ++q) {
-            const double s = (__popcll(r & g.yz[q]) & 1) ? -1.0 : 1.0;
-            acc += g.coeff[q] * s * rePhase(g.phase[q], er, ei);
+#pragma unroll
+        for (int m = 0; m < kDiagItem; ++m) {
+            double gm = 0.0;
+            for (int t = g.off[m]; t < g.off[m + 1]; ++t) gm += (__popcll(base & g.zh[t]) & 1) ? -g.c[t] : g.c[t];
+            acc = fma(gm, p[m], acc);
         }
         return make_double2(acc, 0.0);
+    }
+};
+struct ExpecDiag1 {                              // SV, x = 0, one amplitude per item (n < 3)
+    const double *re, *im;
+    PauliPairGroup g;
+    __device__ __forceinline__ double2 operator()(uint64_t j) const {
+        return make_double2(pairValue(j, re[j] * re[j] + im[j] * im[j], 0.0, g), 0.0);
     }
 };
 
@@ -246,24 +288,90 @@ double reduceFidelityDM(SV rho, SV psi, int N, const Scratch& w) { // replaces Q
     return v;
 }
 
-double reduceExpecPauliGroup(SV s, int isDM, int N, uint64_t xmask, const PauliTerm* terms, int numTerms, const Scratch& w) {
-    double total = 0;
-    for (int base = 0; base < numTerms; base += kMaxGroupTerms) {
-        PauliGroup g{};
-        g.xmask = xmask;
-        g.low = xmask ? __builtin_ctzll(xmask) : 0;
-        g.numTerms = std::min(kMaxGroupTerms, numTerms - base);
-        for (int q = 0; q < g.numTerms; ++q) {
-            g.yz[q] = terms[base + q].yz;
-            g.phase[q] = terms[base + q].nY & 3;
-            g.coeff[q] = terms[base + q].coeff;
+double reduceExpecPauliGroups(SV s, int isDM, int N, const std::vector<PauliTermGroup>& groups, const Scratch& w) {
+    // Every group (or chunk of a large group) reduces into its own result
+    // slot; the slots are read back once per 32 launches, and summed on the
+    // host in group order.
+    constexpr int kSlots = 32;                   // the scratch holds 64 result doubles
+    const char* caller = "calcExpecPauliSum";
+    cudaStream_t st = stream();
+    double total = 0.0;
+    int used = 0;
+    auto drain = [&]() -> bool {
+        if (!used) return true;
+        if (QG_CUDA(cudaMemcpyAsync(w.host, w.result, 2 * used * sizeof(double), cudaMemcpyDeviceToHost, st), caller) ||
+            QG_CUDA(cudaStreamSynchronize(st), caller))
+            return false;
+        for (int k = 0; k < used; ++k) total += w.host[2 * k];
+        used = 0;
+        return true;
+    };
+    auto queue = [&](auto f, uint64_t nItems) -> bool {
+        if (used == kSlots && !drain()) return false;
+        const int grid = reduceGrid(nItems);
+        kReduce<<<grid, red::kThreads, 0, st>>>(f, nItems, w.partials, w.counter, w.result + 2 * used);
+        if (launchFailed(caller)) return false;
+        ++used;
+        return true;
+    };
+    for (const PauliTermGroup& grp : groups) {
+        const uint64_t x = grp.xmask;
+        const int nt = (int)grp.terms.size();
+        if (!isDM && x == 0 && s.n >= kDiagLow) {
+            // diagonal group: terms bucketed by their low bits
+            for (int b0 = 0; b0 < nt; b0 += kMaxDiagTerms) {
+                const int cnt = std::min(kMaxDiagTerms, nt - b0);
+                PauliDiagGroup g{};
+                int k = 0;
+                for (int m = 0; m < kDiagItem; ++m) {
+                    g.off[m] = k;
+                    for (int t = b0; t < b0 + cnt; ++t)
+                        if ((int)(grp.terms[t].yz & (kDiagItem - 1)) == m) {
+                            g.zh[k] = grp.terms[t].yz & ~(uint64_t)(kDiagItem - 1);
+                            g.c[k++] = grp.terms[t].coeff;    // x = 0: no Y, phase 0
+                        }
+                }
+                g.off[kDiagItem] = k;
+                if (!queue(ExpecDiag{s.re, s.im, g}, 1ull << (s.n - kDiagLow))) return total;
+            }
+            continue;
         }
-        double v = 0;
-        if (isDM) runReduce(ExpecDM{s.re, s.im, g, N}, 1ull << N, w, &v, nullptr, "calcExpecPauliSum");
-        else if (xmask) runReduce(ExpecPairs{s.re, s.im, g}, 1ull << (s.n - 1), w, &v, nullptr, "calcExpecPauliSum");
-        else runReduce(ExpecDiag{s.re, s.im, g}, 1ull << s.n, w, &v, nullptr, "calcExpecPauliSum");
-        total += v;
+        // pairs / DM entries: each term goes to the Re (A) or Im (B) list
+        std::vector<std::pair<uint64_t, double>> A, B;
+        for (const PauliTerm& t : grp.terms) {
+            const int ph = t.nY & 3;
+            if (isDM) {
+                (ph % 2 == 0 ? A : B).push_back({t.yz, ph < 2 ? t.coeff : -t.coeff});
+                continue;
+            }
+            const bool tauPlus = (__builtin_popcountll(x & t.yz) & 1) == 0;
+            if (x == 0) {                        // n < 3 diagonal group: |psi_j|^2 terms
+                A.push_back({t.yz, t.coeff});
+                continue;
+            }
+            if (ph % 2 == 0 && tauPlus) A.push_back({t.yz, ph == 0 ? 2 * t.coeff : -2 * t.coeff});
+            if (ph % 2 == 1 && !tauPlus) B.push_back({t.yz, ph == 1 ? 2 * t.coeff : -2 * t.coeff});
+        }
+        for (size_t a0 = 0, b0 = 0; a0 < A.size() || b0 < B.size();) {
+            PauliPairGroup g{};
+            g.xmask = x;
+            g.low = x ? __builtin_ctzll(x) : 0;
+            for (; a0 < A.size() && g.nA < kMaxGroupTerms; ++a0, ++g.nA) {
+                g.mA[g.nA] = A[a0].first;
+                g.cA[g.nA] = A[a0].second;
+            }
+            for (; b0 < B.size() && g.nB < kMaxGroupTerms; ++b0, ++g.nB) {
+                g.mB[g.nB] = B[b0].first;
+                g.cB[g.nB] = B[b0].second;
+            }
+            bool ok;
+            if (isDM) ok = queue(ExpecDM{s.re, s.im, g, N}, 1ull << N);
+            else if (x) ok = queue(ExpecPairs{s.re, s.im, g}, 1ull << (s.n - 1));
+            else ok = queue(ExpecDiag1{s.re, s.im, g}, 1ull << s.n);
+            if (!ok) return total;
+        }
     }
+    drain();
     return total;
 }
 

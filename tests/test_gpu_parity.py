@@ -115,3 +115,43 @@ def test_host_mirror_is_page_locked(gpulib):
     assert L.lib.quest_gb300_hostMirrorPinned(q) == 1
     L.destroy(q)
     assert L.lib.quest_gb300_hostMirrorPinned(q) == -1
+
+
+def _many_term_sum(n, rng):
+    """181 Pauli strings: 100 diagonal (two diagonal-group chunks), 40 on one
+    shared X/Y support (two pair-group chunks), 40 random (more groups than
+    one batch of result slots) and the identity."""
+    codes = [[3 * int(rng.integers(2)) for _ in range(n)] for _ in range(100)]
+    support = [1, n // 2, n - 1]
+    for _ in range(40):
+        c = [3 * int(rng.integers(2)) for _ in range(n)]
+        for t in support:
+            c[t] = int(rng.integers(1, 3))
+        codes.append(c)
+    codes += [[int(rng.integers(4)) for _ in range(n)] for _ in range(40)]
+    codes.append([0] * n)
+    return np.array(codes, dtype=np.int32), rng.normal(size=len(codes))
+
+
+@pytest.mark.parametrize("density", [False, True])
+def test_many_term_pauli_sum_vs_oracle(gpulib, oracle, density):
+    """calcExpecPauliSum with many terms per X/Y group and many groups, on a
+    state vector (12 qubits) and a density matrix (6 qubits), against the
+    oracle to 1e-10 of the sum of |coefficients|."""
+    n = 6 if density else 12
+    rng = np.random.default_rng(17)
+    codes, coeffs = _many_term_sum(n, rng)
+    vals = []
+    for L in (gpulib, oracle):
+        q = L.create(n, density=density)
+        ws = L.create(n, density=density)
+        L.lib.initPlusState(q)
+        W.run_ops(L, q, W.c1_circuit(n=n, layers=3, seed=5))
+        if density:
+            for t in range(0, n, 2):
+                L.lib.mixDepolarising(q, t, 0.05)
+                L.lib.mixDamping(q, (t + 1) % n, 0.1)
+        vals.append(L.calcExpecPauliSum(q, codes, coeffs, ws))
+        L.destroy(ws)
+        L.destroy(q)
+    assert abs(vals[0] - vals[1]) < 1e-10 * np.sum(np.abs(coeffs)), vals
