@@ -139,6 +139,11 @@ int quest_gb300_setCapture(Qureg qureg, int mode);
 void quest_gb300_flushCapture(Qureg qureg);
 /* gates queued and not yet applied */
 int quest_gb300_capturedGates(Qureg qureg);
+/* Totals of the register's flushes since capture was turned on: flushes,
+ * gates applied, fused passes applied and host milliseconds spent planning
+ * them (any pointer may be null).  Returns 0, or -1 when capture is off. */
+int quest_gb300_captureStats(Qureg qureg, long long* flushes, long long* gatesApplied, long long* passesApplied,
+                             double* compileMs);
 /* widest fused pass of the flushes, 1..6 (default 6) */
 void quest_gb300_setCaptureFusion(int maxFusedQubits);
 

@@ -20,6 +20,7 @@
 #include "quest_gb300.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -35,7 +36,8 @@ struct Capture {
     bool tracePreserving = true;  // every queued op is a unitary gate or a channel
     std::vector<FusedGate> gates;
     void* q32 = nullptr;          // FP32 scratch register of the flushes (kept between flushes)
-    long long flushes = 0, gatesApplied = 0;
+    long long flushes = 0, gatesApplied = 0, passesApplied = 0;
+    double compileMs = 0.0;       // host time spent planning the flushes
 };
 
 namespace {
@@ -118,7 +120,9 @@ static void flushRecord(Capture* c, double* re, double* im) {
     plan->numQubits = c->n;
     plan->maxFused = std::min(g_capMaxFused, widestPass(c->n));
     plan->gates.swap(c->gates);
+    const auto t0 = std::chrono::steady_clock::now();
     compilePlan(*plan);
+    c->compileMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (!plan->compiled) {
         invalidQuESTInputError("The captured gates could not be fused.", "captureFlush");
         delete plan;
@@ -128,6 +132,7 @@ static void flushRecord(Capture* c, double* re, double* im) {
     if (keepTrace) copyToQuregTraceKept(c->q32, view, c->dmQubits);
     else copyToQuregAfterPlan(c->q32, view, plan);
     c->gatesApplied += (long long)plan->gates.size();
+    c->passesApplied += (long long)plan->passes.size();
     c->flushes += 1;
     quest_gb300_planDestroy(plan);
 }
@@ -350,6 +355,19 @@ int quest_gb300_capturedGates(Qureg q) {
     std::lock_guard<std::mutex> lk(qg::g_capMutex);
     qg::Capture* c = qg::find(q.deviceStateVec.real);
     return c ? (int)c->gates.size() : 0;
+}
+
+/* Totals of the register's flushes since capture was turned on. */
+int quest_gb300_captureStats(Qureg q, long long* flushes, long long* gatesApplied, long long* passesApplied,
+                             double* compileMs) {
+    std::lock_guard<std::mutex> lk(qg::g_capMutex);
+    qg::Capture* c = qg::find(q.deviceStateVec.real);
+    if (!c) return -1;
+    if (flushes) *flushes = c->flushes;
+    if (gatesApplied) *gatesApplied = c->gatesApplied;
+    if (passesApplied) *passesApplied = c->passesApplied;
+    if (compileMs) *compileMs = c->compileMs;
+    return 0;
 }
 
 /* Largest fused pass width used by flushes (1..6, default 6). */

@@ -203,6 +203,7 @@ SIGNATURES = {
     "quest_gb300_setTensorCoreKernel": (None, [_I]),
     "quest_gb300_setCapture": (_I, [_Q, _I]),
     "quest_gb300_hostMirrorPinned": (_I, [_Q]),
+    "quest_gb300_captureStats": (_I, [_Q, _P(C.c_longlong), _P(C.c_longlong), _P(C.c_longlong), _P(C.c_double)]),
     "quest_gb300_sampleMeasurements": (_I, [_Q, _P(_I), _I, _I, _P(_I)]),
     "quest_gb300_initProductState": (_I, [_Q, _I, _P(_I), _P(_D), _P(_D)]),
     "quest_gb300_flushCapture": (None, [_Q]),
