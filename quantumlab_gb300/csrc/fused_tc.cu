@@ -478,8 +478,8 @@ constexpr int kPrecTF32 = 0, kPrecBF16 = 1;
 // stages and the epilogue buffers.  At k = 6, G is the compact real form
 // [-Im G; Re G; Im G] (192 rows x 64 K).  The B operand of the K-chunk of the
 // real parts of X is rows 64..191 ([Re; Im]).  That of the imaginary parts is
-// rows 0..127 ([-Im; Re]).  Loader row buffers: XST stages per loader warp,
-// up to three, as many as fit.  TMEM: NST operand stages (Xh then Xl; one
+// rows 0..127 ([-Im; Re]).  Loader row buffers: XST stages per loader warp
+// (three at k = 4, two at k >= 5).  TMEM: NST operand stages (Xh then Xl; one
 // TF32 or two BF16 per column), then two accumulators of N columns.
 template <int KQ, int LG, int EG, int LS, int PR>
 struct TC2Shape {
@@ -511,7 +511,12 @@ struct TC2Shape {
     static constexpr size_t fixedFloats = (size_t)NGP * GW + (size_t)EG * 4 * R;
     static constexpr size_t stageFloats = (size_t)LG * 4 * PPG * R;
     static constexpr bool fits(int st) { return (fixedFloats + (size_t)st * stageFloats) * 4 + 2048 <= 227 * 1024; }
-    static constexpr int XST = fits(3) ? 3 : (fits(2) ? 2 : 1);
+    // loader row stages: three where they fit at k = 4, two at k >= 5.  Measured
+    // on the 30-qubit circuit: at k = 6 (split-BF16) three stages took 282 ms
+    // against 267 with two; at k = 5, 360 / 364 ms against 358 / 364; at
+    // k = 4 two stages took 578 / 514 ms against 509 / 500 with three; one
+    // stage is 15-20 % slower everywhere.
+    static constexpr int XST = (KQ <= 4 && fits(3)) ? 3 : (fits(2) ? 2 : 1);
     static constexpr size_t smemBytes = (fixedFloats + (size_t)XST * stageFloats) * 4;
     static_assert(NST * STAGE_COLS + 2 * N <= 512, "TMEM");
     // plane, plane half (k = 6) and first matrix index of part pt of chunk ch

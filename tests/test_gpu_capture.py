@@ -226,3 +226,28 @@ def test_capture_small_registers(gpulib, n):
     assert abs(lib.calcTotalProb(cap) - 1) < 1e-6
     L.destroy(direct)
     L.destroy(cap)
+
+
+def test_capture_stats_count_the_flushes(gpulib):
+    """quest_gb300_captureStats: -1 with capture off; after two flushes of a
+    queued circuit, the flush and gate totals, at least one fused pass per
+    flush and a non-negative planning time."""
+    L = gpulib
+    lib = L.lib
+    n = 14
+    q = L.create(n)
+    f, g, p, ms = C.c_longlong(), C.c_longlong(), C.c_longlong(), C.c_double()
+    assert lib.quest_gb300_captureStats(q, C.byref(f), C.byref(g), C.byref(p), C.byref(ms)) == -1
+    assert lib.quest_gb300_setCapture(q, 1) == 0
+    ops = W.c2_circuit(n=n, layers=2, seed=4)
+    queued = 0
+    for _ in range(2):
+        lib.initZeroState(q)
+        W.run_ops(L, q, ops)
+        queued += lib.quest_gb300_capturedGates(q)
+        lib.calcTotalProb(q)
+    assert lib.quest_gb300_captureStats(q, C.byref(f), C.byref(g), C.byref(p), C.byref(ms)) == 0
+    assert f.value == 2 and g.value == queued == 2 * len(ops)
+    assert 2 <= p.value <= g.value and ms.value >= 0.0
+    lib.quest_gb300_setCapture(q, 0)
+    L.destroy(q)
