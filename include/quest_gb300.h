@@ -170,6 +170,28 @@ int quest_gb300_initProductState(Qureg qureg, int numRegs, const int* regQubits,
  * invalid argument through invalidQuESTInputError. */
 int quest_gb300_sampleMeasurements(Qureg qureg, const int* qubits, int numQubits, int numShots, int* outcomes);
 
+/* ---- batched Trotter instances ----------------------------------------------
+ * B Hamiltonian instances on n = 11..34 qubits that share Pauli strings,
+ * Trotter order and repetitions (coefficients, time and the classical start
+ * state may differ) evolve together: one fusion plan (searched on instance 0,
+ * reused with each instance's FP64 products), one tensor-core launch per
+ * fused pass over all B FP32 states, and a CUDA graph replayed after the
+ * first run.  The gates are QuEST's applyTrotterCircuit(hamil, time, order,
+ * reps) from initClassicalState(init).  Energies are <H> / <psi|psi> of each
+ * final FP32 state (FP32 products, FP64 sums).  Errors go through
+ * invalidQuESTInputError; functions return 0 or -1.                          */
+void* quest_gb300_trotterBatchCreate(int numQubits, int numInstances);
+int quest_gb300_trotterBatchSetInstance(void* batch, int instance, PauliHamil hamil, double time, int order, int reps,
+                                        long long initClassicalState);
+/* Evolve every instance; energies (may be null): B doubles. */
+int quest_gb300_trotterBatchRun(void* batch, double* energies);
+/* Copy instance `instance`'s final state into an FP64 register of n qubits,
+ * scaled to norm 1 (the start state's) by the norm the last run measured. */
+int quest_gb300_trotterBatchCopyState(void* batch, int instance, Qureg dst);
+/* Fused passes per run (after the first run), else -1. */
+int quest_gb300_trotterBatchNumPasses(void* batch);
+void quest_gb300_trotterBatchDestroy(void* batch);
+
 /* ---- total probability without allocating ---------------------------------
  * No counterpart in the reference.  For callers that hold their own FP64
  * state arrays and must not allocate while they run (a host callback or

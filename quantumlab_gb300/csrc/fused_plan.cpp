@@ -385,6 +385,8 @@ void compilePlan(FusedPlan& plan) {
             members.push_back(absorbed);
         }
     }
+    plan.passSets = sets;
+    plan.passMembers = members;
     // the pass products are independent: a few host threads share them
     const size_t np = sets.size();
     plan.passes.resize(np);
@@ -399,6 +401,64 @@ void compilePlan(FusedPlan& plan) {
     work();
     for (auto& t : pool) t.join();
     plan.compiled = true;
+}
+
+bool compilePlanLike(FusedPlan& plan, const FusedPlan& structure) {
+    plan.compiled = false;
+    plan.passes.clear();
+    if (!structure.compiled || plan.gates.size() != structure.gates.size() || plan.numQubits != structure.numQubits)
+        return false;
+    for (size_t i = 0; i < plan.gates.size(); ++i) {
+        const FusedGate &a = plan.gates[i], &b = structure.gates[i];
+        if (a.qubits != b.qubits) return false;
+        const uint64_t da = diagonalQubits(a), db = diagonalQubits(b);
+        if ((db & ~da) != 0) return false;
+    }
+    plan.passSets = structure.passSets;
+    plan.passMembers = structure.passMembers;
+    const size_t np = plan.passSets.size();
+    plan.passes.resize(np);
+    std::atomic<size_t> nextPass{0};
+    auto work = [&]() {
+        for (size_t i; (i = nextPass.fetch_add(1)) < np;)
+            buildPass(plan, plan.passSets[i], plan.passMembers[i], plan.passes[i]);
+    };
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned nt = (unsigned)std::min<size_t>({(size_t)std::min(hw, 8u), np, 1 + plan.gates.size() / 64});
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+    plan.compiled = true;
+    return true;
+}
+
+FusedGate pauliRotationGate(uint64_t x, uint64_t y, uint64_t z, double angle) {
+    FusedGate g;
+    const uint64_t mask = x | z;
+    for (uint64_t m = mask; m; m &= m - 1) g.qubits.push_back(__builtin_ctzll(m));
+    const int k = (int)g.qubits.size();
+    const uint64_t D = 1ull << k;
+    // the masks on the gate's local qubits (bit b <-> qubits[b])
+    auto local = [&](uint64_t v) {
+        uint64_t r = 0;
+        for (int b = 0; b < k; ++b)
+            if (v >> g.qubits[b] & 1ull) r |= 1ull << b;
+        return r;
+    };
+    const uint64_t xm = local(x), ym = local(y), zm = local(z);
+    static const cplx ipow[4] = {cplx(1, 0), cplx(0, 1), cplx(-1, 0), cplx(0, -1)};
+    const cplx iy = ipow[__builtin_popcountll(ym) & 3];
+    const double c = std::cos(angle / 2), sn = std::sin(angle / 2);
+    g.m.assign(D * D, cplx(0, 0));
+    for (uint64_t i = 0; i < D; ++i) {
+        // P|i> = i^nY (-1)^popcount(i & (Y|Z)) |i ^ X>
+        const cplx ph = iy * ((__builtin_popcountll(i & (ym | zm)) & 1) ? -1.0 : 1.0);
+        g.m[i * D + i] += c;
+        g.m[(i ^ xm) * D + i] += cplx(0, -sn) * ph;
+    }
+    g.unitary = matrixIsUnitary(g.m, (int)D);
+    return g;
 }
 
 }  // namespace qg

@@ -34,6 +34,10 @@ struct FusedPlan {
     int beamWidth = 16;         // sets kept per level of the pass search
     std::vector<FusedGate> gates;
     std::vector<FusedPass> passes;
+    // the search's result: per pass its qubit set and the indices of the
+    // gates it absorbs, in an allowed order (compilePlanLike reuses them)
+    std::vector<uint64_t> passSets;
+    std::vector<std::vector<int>> passMembers;
     bool compiled = false;
     // device copy of the per-pass FP32 (and split-TF32) operands, built on
     // first use by the FP32 engine; owned by the engine
@@ -52,5 +56,17 @@ bool matrixIsUnitary(const std::vector<cplx>& m, int D);
 // Beam search over qubit sets at the circuit front (see fused_plan.cpp).
 // Leaves plan.compiled false if it fails.
 void compilePlan(FusedPlan& plan);
+
+// Compile `plan` with the passes `structure` found, without a search: the
+// gate lists must match gate by gate in qubits, and every gate of `plan` must
+// be diagonal on at least the qubits where `structure`'s gate is (so that the
+// structure's reordering stays valid).  Gates of the same circuit with other
+// angles qualify.  Returns false (plan not compiled) otherwise.
+bool compilePlanLike(FusedPlan& plan, const FusedPlan& structure);
+
+// exp(-i angle/2 P) as a dense gate on the qubits of the Pauli string with
+// X/Y/Z masks x, y, z (Y bits also in x); the operator QuEST's
+// multiRotatePauli applies (QuEST_common.c:411-448).
+FusedGate pauliRotationGate(uint64_t x, uint64_t y, uint64_t z, double angle);
 
 }  // namespace qg

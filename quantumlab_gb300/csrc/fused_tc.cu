@@ -466,7 +466,15 @@ struct TC2Params {
     int insI[KQ + kTileBitsC];            // ascending qubits of I
     int runBits;                          // I contains qubits [0, runBits)
     uint64_t outMask;                     // the qubits outside I (where tile index bits go)
-    uint64_t gridStep;                    // the tile base offset of gridDim.x tiles
+    uint64_t gridStep;                    // the tile base offset of ctasPerInst tiles
+    // Batches of states (one launch for the same pass on several registers):
+    // CTA b runs tiles b % ctasPerInst, + ctasPerInst, ... of state
+    // b / ctasPerInst, which starts instStride floats after the previous one
+    // and has its own operand image, imageStride floats after the previous
+    // one.  A single register: ctasPerInst = gridDim.x, the strides 0.
+    uint32_t ctasPerInst;
+    uint64_t instStride;
+    uint64_t imageStride;
 };
 
 // Operand precision of kApplyTC2: 3-term split-TF32 or 4-term split-BF16.
@@ -564,9 +572,9 @@ __device__ __forceinline__ uint64_t tileBase(const TC2Params<KQ>& p, uint64_t ti
     return tb;
 }
 // Tile bases of one role's increasing tile sequence (tiles differ by
-// multiples of gridDim.x).  The base is the tile index deposited into
+// multiples of ctasPerInst).  The base is the tile index deposited into
 // outMask, and deposits add by masked addition:
-// base(t + gridDim.x) = ((base(t) | ~outMask) + gridStep) & outMask.
+// base(t + ctasPerInst) = ((base(t) | ~outMask) + gridStep) & outMask.
 template <int KQ>
 struct TileWalker {
     uint64_t tile = ~0ull, base = 0;
@@ -577,7 +585,7 @@ struct TileWalker {
         }
         while (tile < t) {
             base = ((base | ~p.outMask) + p.gridStep) & p.outMask;
-            tile += gridDim.x;
+            tile += p.ctasPerInst;
         }
         return base;
     }
@@ -592,6 +600,14 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                                                                   const __grid_constant__ TC2Params<KQ> p) {
     using S = TC2Shape<KQ, LG, EG, LS, PR>;
     constexpr bool BF = (PR == kPrecBF16);
+    // this CTA's register of a batch, and its place among that register's CTAs
+    const uint32_t cta = blockIdx.x % p.ctasPerInst, ncta = p.ctasPerInst;
+    {
+        const uint64_t inst = blockIdx.x / p.ctasPerInst;
+        re += inst * p.instStride;
+        im += inst * p.instStride;
+        gImage += inst * p.imageStride;
+    }
     constexpr int D = S::D, N = S::N;
     constexpr int NCH = S::NCH, KC = S::KC, PART = S::PART, R = S::R, PPG = S::PPG, XST = S::XST, NST = S::NST;
     constexpr uint32_t kGW = S::GW;
@@ -649,11 +665,11 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         const int g = warp >> 2;
         const uint64_t laneA = p.laneOff[lane];
         const uint32_t colBase = p.colLane[lane];
-        // this CTA's chunks, in order: chunk s = (tile blockIdx.x + (s / NCH) * gridDim.x, K chunk s % NCH);
+        // this CTA's chunks, in order: chunk s = (tile cta + (s / NCH) * ncta, K chunk s % NCH);
         // split: every s, part g; otherwise group g takes s = g, g + LG, ...
         const int p0 = S::SPLIT ? g : 0;
         const uint32_t s0 = S::SPLIT ? 0u : (uint32_t)g, sStep = S::SPLIT ? 1u : (uint32_t)LG;
-        const uint32_t nMy = blockIdx.x < numTiles ? (uint32_t)((numTiles - 1 - blockIdx.x) / gridDim.x + 1) * NCH : 0u;
+        const uint32_t nMy = cta < numTiles ? (uint32_t)((numTiles - 1 - cta) / ncta + 1) * NCH : 0u;
         const uint32_t nMine = nMy > s0 ? (nMy - s0 + sStep - 1) / sStep : 0u;     // chunks of this group
         double normIn = 0.0;
         const bool measure = nl.in != nullptr;             // input norm wanted (uniform)
@@ -665,7 +681,7 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         // reads four 128-byte lines.
         TileWalker<KQ> walk;
         auto issue = [&](uint32_t sc, float* buf) {
-            const uint64_t tile = blockIdx.x + (uint64_t)(sc / NCH) * gridDim.x;
+            const uint64_t tile = cta + (uint64_t)(sc / NCH) * ncta;
             const int ch = sc % NCH;
             const uint64_t tb = walk.at(p, tile) + laneA;
 #pragma unroll
@@ -792,8 +808,8 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         uint32_t tl = eg;
         double normOut = 0.0;
         TileWalker<KQ> walk;
-        for (uint64_t tile = blockIdx.x + (uint64_t)eg * gridDim.x; tile < numTiles && ok;
-             tile += (uint64_t)EG * gridDim.x, tl += EG) {
+        for (uint64_t tile = cta + (uint64_t)eg * ncta; tile < numTiles && ok;
+             tile += (uint64_t)EG * ncta, tl += EG) {
             const uint64_t tb = walk.at(p, tile) + laneA;
             const int bd = tl & 1;
             if (!warpWaitOrAbort(&dFullB[bd], (tl >> 1) & 1, &abortF, lane)) {
@@ -871,7 +887,7 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         if (!ok) mbarWaitOrAbort(&barG, 0, &abortF);                // once more for the copies in flight
         const uint32_t ghA = smemAddr(gh), glA = smemAddr(gl), gllA = smemAddr(gll);
         uint32_t sq = 0, tl = 0;
-        for (uint64_t tile = blockIdx.x; tile < numTiles && ok; tile += gridDim.x, ++tl) {
+        for (uint64_t tile = cta; tile < numTiles && ok; tile += ncta, ++tl) {
             const int bd = tl & 1;
             if (tl >= 2 && !mbarWaitOrAbort(&dEmptyB[bd], ((tl >> 1) - 1) & 1, &abortF)) {
                 ok = false;
@@ -1043,9 +1059,11 @@ bool colWords4(const TC2Params<KQ>& p) {
     return true;
 }
 
+// batch > 1: the same pass on `batch` registers of n qubits, instStride floats
+// apart, each with its own image, imageStride floats apart
 template <int KQ, int LG, int EG, int LS, int PR, int CV = 1>
 bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, const NormLinks& nl,
-               cudaStream_t st) {
+               cudaStream_t st, int batch = 1, uint64_t instStride = 0, uint64_t imageStride = 0) {
     using S = TC2Shape<KQ, LG, EG, LS, PR>;
     constexpr int D = S::D, K = S::K, N = S::N, PART = S::PART;
     constexpr int V4 = S::TILE / 512;
@@ -1126,14 +1144,20 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
         p.colJ[j] = padIdx(compress(v) % PART);
     }
     if constexpr (CV == 4) {
-        if (!colWords4(p)) return launchTC2<KQ, LG, EG, LS, PR, 1>(re, im, n, pass, img, errFlag, nl, st);
+        if (!colWords4(p))
+            return launchTC2<KQ, LG, EG, LS, PR, 1>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride);
     }
     const uint64_t numTiles = 1ull << (n - KQ - kTileBitsC);
-    const uint64_t grid = std::min<uint64_t>(numTiles, (uint64_t)numSMs());
+    // one CTA per SM: a batch shares the SMs among its registers
+    const uint64_t ctas = std::min<uint64_t>(numTiles, std::max<uint64_t>(1, (uint64_t)numSMs() / (uint64_t)std::max(1, batch)));
+    const uint64_t grid = ctas * (uint64_t)std::max(1, batch);
     p.outMask = ~imask;
+    p.ctasPerInst = (uint32_t)ctas;
+    p.instStride = instStride;
+    p.imageStride = imageStride;
     {
-        // gridStep = grid deposited into the qubits outside I
-        uint64_t dep = 0, src = grid;
+        // gridStep = ctas deposited into the qubits outside I
+        uint64_t dep = 0, src = ctas;
         for (int q = 0; q < 64 && src; ++q)
             if (p.outMask >> q & 1ull) {
                 if (src & 1ull) dep |= 1ull << q;
@@ -1268,6 +1292,11 @@ void* uploadPlanTC(const FusedPlan& plan) {
     return dp;
 }
 
+// The tensor-core operands of one pass, as uploadPlanTC lays them out: the
+// number of floats, and the image itself.
+size_t tcImageFloats(int k) { return imageFloats(k); }
+void tcBuildImage(const FusedPass& pass, float* img) { buildImage(pass, img); }
+
 void freePlanTC(void* h) {
     DevicePlan* dp = reinterpret_cast<DevicePlan*>(h);
     if (!dp) return;
@@ -1329,6 +1358,58 @@ int tcKernelFor(const FusedPass& pass, int n) {
     return 5;
 }
 
+// Launch tensor-core kernel `version` (tcKernelFor) for a pass of k = 4..6
+// qubits on one register (batch = 1) or on a batch of registers; false if the
+// launch failed.  The direct-load kernel (version 1) takes single registers.
+static bool launchPassTC(int version, const FusedPass& pass, float* re, float* im, int n, const float* img, int* errFlag,
+                         const NormLinks& nl, cudaStream_t st, int batch, uint64_t instStride, uint64_t imageStride) {
+    const int k = (int)pass.targets.size();
+    bool ok = false;
+    // the default kernels, when the targets include qubits 0 and 1: the
+    // variant with 16-byte column words
+    bool done = false;
+    if (g_tcVersion == 0 && pass.targets[0] == 0 && pass.targets[1] == 1) {
+#define QG_TC2W(KQ, LG, EG, LS, PR) \
+    (done = true, launchTC2<KQ, LG, EG, LS, PR, 4>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride))
+        const bool tf = g_tcPrecision == kPrecTF32;
+        if (tf && k == 4 && version == 3) ok = QG_TC2W(4, 1, 1, 1, kPrecTF32);
+        else if (tf && k == 5 && version == 2) ok = QG_TC2W(5, 2, 1, 1, kPrecTF32);
+        else if (tf && k == 6 && version == 5) ok = QG_TC2W(6, 2, 2, 2, kPrecTF32);
+        else if (!tf && k == 4 && version == 5) ok = QG_TC2W(4, 2, 2, 2, kPrecBF16);
+        else if (!tf && k == 5 && version == 5) ok = QG_TC2W(5, 2, 2, 2, kPrecBF16);
+        else if (!tf && k == 6 && version == 5) ok = QG_TC2W(6, 2, 2, 2, kPrecBF16);
+#undef QG_TC2W
+    }
+    if (done) return ok;
+    if (version >= 2) {
+        // 2: two loader groups (alternate chunks) + one epilogue group; 3: one
+        // + one; 4: one + two; 5: two loader groups (each half of every chunk)
+        // + two epilogue groups
+#define QG_TC2P(KQ, PR)                                                                                                   \
+    (version == 2   ? launchTC2<KQ, 2, 1, 1, PR>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride)  \
+     : version == 3 ? launchTC2<KQ, 1, 1, 1, PR>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride)  \
+     : version == 4 ? launchTC2<KQ, 1, 2, 1, PR>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride)  \
+                    : launchTC2<KQ, 2, 2, 2, PR>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride))
+#define QG_TC2(KQ) (g_tcPrecision == kPrecTF32 ? QG_TC2P(KQ, kPrecTF32) : QG_TC2P(KQ, kPrecBF16))
+        switch (k) {
+            case 4: ok = QG_TC2(4); break;
+            case 5: ok = QG_TC2(5); break;
+            case 6: ok = QG_TC2(6); break;
+            default: return false;
+        }
+#undef QG_TC2
+#undef QG_TC2P
+        return ok;
+    }
+    if (batch != 1) return false;
+    switch (k) {
+        case 4: return launchTC<4>(re, im, n, pass, img, errFlag, nl, st);
+        case 5: return launchTC<5>(re, im, n, pass, img, errFlag, nl, st);
+        case 6: return launchTC<6>(re, im, n, pass, img, errFlag, nl, st);
+        default: return false;
+    }
+}
+
 // explicit entry used by the FP32 engine with the pass index: 1 = applied on
 // the tensor cores, 0 = not a tensor-core pass (the caller runs it on SIMT),
 // -1 = the launch failed (already reported)
@@ -1363,50 +1444,7 @@ int applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, 
         if (continues) nl.corrTarget = dp->target[dp->lastTC];
         dp->target[index] = continues ? dp->target[dp->lastTC] : dp->inNorm[index];
     }
-    bool ok = false;
-    // the default kernels, when the targets include qubits 0 and 1: the
-    // variant with 16-byte column words
-    bool done = false;
-    if (g_tcVersion == 0 && pass.targets[0] == 0 && pass.targets[1] == 1) {
-#define QG_TC2W(KQ, LG, EG, LS, PR) \
-    (done = true, launchTC2<KQ, LG, EG, LS, PR, 4>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st))
-        const bool tf = g_tcPrecision == kPrecTF32;
-        if (tf && k == 4 && version == 3) ok = QG_TC2W(4, 1, 1, 1, kPrecTF32);
-        else if (tf && k == 5 && version == 2) ok = QG_TC2W(5, 2, 1, 1, kPrecTF32);
-        else if (tf && k == 6 && version == 5) ok = QG_TC2W(6, 2, 2, 2, kPrecTF32);
-        else if (!tf && k == 4 && version == 5) ok = QG_TC2W(4, 2, 2, 2, kPrecBF16);
-        else if (!tf && k == 5 && version == 5) ok = QG_TC2W(5, 2, 2, 2, kPrecBF16);
-        else if (!tf && k == 6 && version == 5) ok = QG_TC2W(6, 2, 2, 2, kPrecBF16);
-#undef QG_TC2W
-    }
-    if (done) {
-        // launched above
-    } else if (version >= 2) {
-        // 2: two loader groups (alternate chunks) + one epilogue group; 3: one
-        // + one; 4: one + two; 5: two loader groups (each half of every chunk)
-        // + two epilogue groups
-#define QG_TC2P(KQ, PR)                                                                                     \
-    (version == 2   ? launchTC2<KQ, 2, 1, 1, PR>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)    \
-     : version == 3 ? launchTC2<KQ, 1, 1, 1, PR>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)    \
-     : version == 4 ? launchTC2<KQ, 1, 2, 1, PR>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st)    \
-                    : launchTC2<KQ, 2, 2, 2, PR>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st))
-#define QG_TC2(KQ) (g_tcPrecision == kPrecTF32 ? QG_TC2P(KQ, kPrecTF32) : QG_TC2P(KQ, kPrecBF16))
-        switch (k) {
-            case 4: ok = QG_TC2(4); break;
-            case 5: ok = QG_TC2(5); break;
-            case 6: ok = QG_TC2(6); break;
-            default: return 0;
-        }
-#undef QG_TC2
-#undef QG_TC2P
-    } else {
-        switch (k) {
-            case 4: ok = launchTC<4>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st); break;
-            case 5: ok = launchTC<5>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st); break;
-            case 6: ok = launchTC<6>(re, im, n, pass, dp->images[index], dp->errFlag, nl, st); break;
-            default: return 0;
-        }
-    }
+    const bool ok = launchPassTC(version, pass, re, im, n, dp->images[index], dp->errFlag, nl, st, 1, 0, 0);
     if (!ok) return -1;
     dp->lastTC = (int)index;
     dp->chain = true;
@@ -1454,5 +1492,18 @@ bool setTensorCorePrecision(int mode) {
 int tensorCorePrecision() { return g_tcPrecision; }
 void setTensorCoreKernel(int version) { g_tcVersion = (version >= 1 && version <= 5) ? version : 0; }
 bool tensorCoresEnabled() { return g_tcEnabled; }
+
+// One pass on `batch` registers of n qubits: register b's planes start
+// b * 2^n floats into re and im, and its operand image imageStride floats
+// after register b - 1's.  One launch; the registers share the SMs.  No norm
+// drift correction (the callers normalise per register).  Returns false for a
+// pass the tensor cores do not take or a failed launch.
+bool applyPassTCBatch(float* re, float* im, int n, const FusedPass& pass, const float* images, size_t imageStride,
+                      int batch, int* errFlag, cudaStream_t st) {
+    const int version = tcKernelFor(pass, n);
+    if (version < 2 || !images) return false;
+    const NormLinks nl{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    return launchPassTC(version, pass, re, im, n, images, errFlag, nl, st, batch, 1ull << n, (uint64_t)imageStride);
+}
 
 }  // namespace qg

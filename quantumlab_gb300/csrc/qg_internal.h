@@ -137,6 +137,11 @@ double reduceFidelityDM(SV rho, SV psi, int nRep, const Scratch& w);
 struct PauliTerm { uint64_t yz; int nY; double coeff; };
 struct PauliTermGroup { uint64_t xmask; std::vector<PauliTerm> terms; };
 double reduceExpecPauliGroups(SV s, int isDM, int nRep, const std::vector<PauliTermGroup>& groups, const Scratch& w);
+// State vector, X/Y mask x != 0: each pair (j, j ^ x) adds Re(conj(psi_j)
+// psi_k) A(j) + Im(conj(psi_j) psi_k) B(j), A and B sums of +-c over these
+// lists of (yz mask, c): the terms whose pair contributions do not cancel.
+void pauliPairTerms(uint64_t x, const std::vector<PauliTerm>& terms, std::vector<std::pair<uint64_t, double>>& A,
+                    std::vector<std::pair<uint64_t, double>>& B);
 void reduceProbAllOutcomes(SV s, int isDM, int nRep, const int* qubits, int numQubits, double* hostOut, const Scratch& w);
 
 }  // namespace qg

@@ -18,7 +18,6 @@ namespace qg {
 namespace {
 
 using namespace red;
-constexpr int kThreads = red::kThreads;
 
 // ------------------------------------------------------------------ functors
 struct NormSq2 {          // two consecutive amplitudes per item
@@ -288,6 +287,16 @@ double reduceFidelityDM(SV rho, SV psi, int N, const Scratch& w) { // replaces Q
     return v;
 }
 
+void pauliPairTerms(uint64_t x, const std::vector<PauliTerm>& terms, std::vector<std::pair<uint64_t, double>>& A,
+                    std::vector<std::pair<uint64_t, double>>& B) {
+    for (const PauliTerm& t : terms) {
+        const int ph = t.nY & 3;
+        const bool tauPlus = (__builtin_popcountll(x & t.yz) & 1) == 0;
+        if (ph % 2 == 0 && tauPlus) A.push_back({t.yz, ph == 0 ? 2 * t.coeff : -2 * t.coeff});
+        if (ph % 2 == 1 && !tauPlus) B.push_back({t.yz, ph == 1 ? 2 * t.coeff : -2 * t.coeff});
+    }
+}
+
 double reduceExpecPauliGroups(SV s, int isDM, int N, const std::vector<PauliTermGroup>& groups, const Scratch& w) {
     // Every group (or chunk of a large group) reduces into its own result
     // slot; the slots are read back once per 32 launches, and summed on the
@@ -338,19 +347,15 @@ double reduceExpecPauliGroups(SV s, int isDM, int N, const std::vector<PauliTerm
         }
         // pairs / DM entries: each term goes to the Re (A) or Im (B) list
         std::vector<std::pair<uint64_t, double>> A, B;
-        for (const PauliTerm& t : grp.terms) {
-            const int ph = t.nY & 3;
-            if (isDM) {
+        if (isDM) {
+            for (const PauliTerm& t : grp.terms) {
+                const int ph = t.nY & 3;
                 (ph % 2 == 0 ? A : B).push_back({t.yz, ph < 2 ? t.coeff : -t.coeff});
-                continue;
             }
-            const bool tauPlus = (__builtin_popcountll(x & t.yz) & 1) == 0;
-            if (x == 0) {                        // n < 3 diagonal group: |psi_j|^2 terms
-                A.push_back({t.yz, t.coeff});
-                continue;
-            }
-            if (ph % 2 == 0 && tauPlus) A.push_back({t.yz, ph == 0 ? 2 * t.coeff : -2 * t.coeff});
-            if (ph % 2 == 1 && !tauPlus) B.push_back({t.yz, ph == 1 ? 2 * t.coeff : -2 * t.coeff});
+        } else if (x == 0) {                     // n < 3 diagonal group: |psi_j|^2 terms
+            for (const PauliTerm& t : grp.terms) A.push_back({t.yz, t.coeff});
+        } else {
+            pauliPairTerms(x, grp.terms, A, B);
         }
         for (size_t a0 = 0, b0 = 0; a0 < A.size() || b0 < B.size();) {
             PauliPairGroup g{};

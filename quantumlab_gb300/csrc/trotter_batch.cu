@@ -1,0 +1,628 @@
+// trotter_batch.cu -- batched Trotter evolution of many Hamiltonian instances
+// (sm_103a).
+//
+// QuantumLab's Fermi-Hubbard studies run one Trotter circuit per Hamiltonian
+// instance (QuEST.c:1079 applyTrotterCircuit -> QuEST_common.c:762-844 per
+// instance, then calcExpecPauliSum, QuEST_common.c:506-533).  Instances that
+// share the Pauli strings, order and repetitions but differ in coefficients
+// and time give circuits of the same shape with other angles.  A batch holds
+// B such instances as FP32 states of n qubits, side by side in one
+// allocation, and runs them together:
+//   * the fusion planner compiles instance 0's gate stream; every other
+//     instance takes the same passes with its own FP64 products
+//     (compilePlanLike), so the planner runs once;
+//   * each pass is one launch of the tensor-core applier over all B states
+//     (the CTAs are shared out among the states, each state's CTAs load that
+//     state's operands); passes narrower than 4 qubits are widened with
+//     identity factors so that every pass runs on the tensor cores;
+//   * the energies <H_b> are reduced from the FP32 states (FP32 products per
+//     amplitude pair, FP64 sums), divided by each state's norm, which also
+//     removes the norm drift of the FP32 passes to first order;
+//   * after the first run the whole sequence (initial states, passes,
+//     reductions, the copy of the results to pinned host memory) is a CUDA
+//     graph that later runs replay.
+#include "fused_plan.h"
+#include "qg_internal.h"
+#include "quest_gb300.h"
+#include "reduce_kernel.cuh"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <thread>
+#include <vector>
+
+namespace qg {
+
+size_t tcImageFloats(int k);
+void tcBuildImage(const FusedPass& pass, float* img);
+bool applyPassTCBatch(float* re, float* im, int n, const FusedPass& pass, const float* images, size_t imageStride,
+                      int batch, int* errFlag, cudaStream_t st);
+
+namespace {
+
+using red::ins0;
+using red::kReduce;
+using red::reduceGrid;
+
+constexpr int kMaxTerms = 32;
+struct PairGroupF {                  // X/Y mask x != 0: pairs (j, j ^ x)
+    uint64_t xmask;
+    int low, nA, nB;
+    uint64_t mA[kMaxTerms], mB[kMaxTerms];
+    float cA[kMaxTerms], cB[kMaxTerms];
+};
+__device__ __forceinline__ float signedSumF(uint64_t j, const uint64_t* m, const float* c, int n) {
+    float a = 0.f;
+    for (int q = 0; q < n; ++q) a += (__popcll(j & m[q]) & 1) ? -c[q] : c[q];
+    return a;
+}
+// Re(conj(psi_j) psi_k) A(j) + Im(conj(psi_j) psi_k) B(j), in FP32
+struct PairsF32 {
+    const float *re, *im;
+    PairGroupF g;
+    __device__ __forceinline__ double2 operator()(uint64_t t) const {
+        const uint64_t j = ins0(t, g.low), k = j ^ g.xmask;
+        const float jr = re[j], ji = im[j], kr = re[k], ki = im[k];
+        const float wr = fmaf(jr, kr, ji * ki), wi = fmaf(jr, ki, -(ji * kr));
+        return make_double2((double)(wr * signedSumF(j, g.mA, g.cA, g.nA) + wi * signedSumF(j, g.mB, g.cB, g.nB)), 0.0);
+    }
+};
+constexpr int kDiagItem = 8;
+constexpr int kMaxDiag = 64;
+struct DiagGroupF {                  // x = 0: terms bucketed by their 3 low mask bits
+    int off[kDiagItem + 1];
+    uint64_t zh[kMaxDiag];
+    float c[kMaxDiag];
+};
+// sum over 8 amplitudes of |psi|^2 sum_t c_t (-1)^popc(j & z_t), through the
+// Walsh-Hadamard transform of the 8 probabilities (as in reduce.cu), in FP32
+struct DiagF32 {
+    const float *re, *im;
+    DiagGroupF g;
+    __device__ __forceinline__ double2 operator()(uint64_t i) const {
+        const uint64_t base = i * kDiagItem;
+        const float4 r0 = *reinterpret_cast<const float4*>(re + base), r1 = *reinterpret_cast<const float4*>(re + base + 4);
+        const float4 m0 = *reinterpret_cast<const float4*>(im + base), m1 = *reinterpret_cast<const float4*>(im + base + 4);
+        float p[kDiagItem] = {fmaf(r0.x, r0.x, m0.x * m0.x), fmaf(r0.y, r0.y, m0.y * m0.y), fmaf(r0.z, r0.z, m0.z * m0.z),
+                              fmaf(r0.w, r0.w, m0.w * m0.w), fmaf(r1.x, r1.x, m1.x * m1.x), fmaf(r1.y, r1.y, m1.y * m1.y),
+                              fmaf(r1.z, r1.z, m1.z * m1.z), fmaf(r1.w, r1.w, m1.w * m1.w)};
+#pragma unroll
+        for (int sb = 1; sb < kDiagItem; sb <<= 1)
+#pragma unroll
+            for (int l = 0; l < kDiagItem; ++l)
+                if (!(l & sb)) {
+                    const float a = p[l], b = p[l | sb];
+                    p[l] = a + b;
+                    p[l | sb] = a - b;
+                }
+        float acc = 0.f;
+#pragma unroll
+        for (int m = 0; m < kDiagItem; ++m) {
+            float gm = 0.f;
+            for (int t = g.off[m]; t < g.off[m + 1]; ++t) gm += (__popcll(base & g.zh[t]) & 1) ? -g.c[t] : g.c[t];
+            acc = fmaf(gm, p[m], acc);
+        }
+        return make_double2((double)acc, 0.0);
+    }
+};
+struct NormBatchF32 {                // 8 amplitudes per item
+    const float *re, *im;
+    __device__ __forceinline__ double2 operator()(uint64_t i) const {
+        const float4* r4 = reinterpret_cast<const float4*>(re + 8 * i);
+        const float4* m4 = reinterpret_cast<const float4*>(im + 8 * i);
+        const float4 a = r4[0], b = r4[1], c = m4[0], d = m4[1];
+        float s = a.x * a.x;
+        s = fmaf(a.y, a.y, s); s = fmaf(a.z, a.z, s); s = fmaf(a.w, a.w, s);
+        s = fmaf(b.x, b.x, s); s = fmaf(b.y, b.y, s); s = fmaf(b.z, b.z, s); s = fmaf(b.w, b.w, s);
+        s = fmaf(c.x, c.x, s); s = fmaf(c.y, c.y, s); s = fmaf(c.z, c.z, s); s = fmaf(c.w, c.w, s);
+        s = fmaf(d.x, d.x, s); s = fmaf(d.y, d.y, s); s = fmaf(d.z, d.z, s); s = fmaf(d.w, d.w, s);
+        return make_double2((double)s, 0.0);
+    }
+};
+
+__global__ void kBatchClassical(float* re, uint64_t stride, const long long* idx, int B) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < B) re[(uint64_t)b * stride + (uint64_t)idx[b]] = 1.f;
+}
+__global__ void kBatchToF64(const float* __restrict__ sr, const float* __restrict__ si, double* __restrict__ dr,
+                            double* __restrict__ di, uint64_t n, double scale) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        dr[i] = (double)sr[i] * scale;
+        di[i] = (double)si[i] * scale;
+    }
+}
+
+struct Instance {
+    std::vector<int> codes;          // numTerms x n, QuEST pauliOpType values
+    std::vector<double> coeffs;
+    double time = 0.0;
+    int order = 1, reps = 1;
+    long long init = 0;
+    bool set = false;
+};
+
+// The gates QuEST's applyTrotterCircuit applies (QuEST_common.c:762-844):
+// per repetition the symmetrised product of order `order`, each term as
+// exp(-i fac c P) = multiRotatePauli(angle 2 fac c); identity terms apply
+// nothing.
+void trotterTerms(const Instance& in, int n, double time, int order, std::vector<FusedGate>& out) {
+    if (order == 1 || order == 2) {
+        const int T = (int)in.coeffs.size();
+        const double fac = order == 1 ? time : time / 2;
+        for (int pass = 0; pass < order; ++pass)
+            for (int i = 0; i < T; ++i) {
+                const int t = pass == 0 ? i : T - 1 - i;
+                uint64_t x = 0, y = 0, z = 0;
+                for (int q = 0; q < n; ++q) {
+                    const int c = in.codes[(size_t)t * n + q];
+                    if (c == PAULI_X) x |= 1ull << q;
+                    if (c == PAULI_Y) { x |= 1ull << q; y |= 1ull << q; }
+                    if (c == PAULI_Z) z |= 1ull << q;
+                }
+                if ((x | z) == 0) continue;
+                out.push_back(pauliRotationGate(x, y, z, 2 * fac * in.coeffs[t]));
+            }
+        return;
+    }
+    const double p = 1. / (4 - std::pow(4, 1. / (order - 1)));
+    const int lo = order - 2;
+    trotterTerms(in, n, p * time, lo, out);
+    trotterTerms(in, n, p * time, lo, out);
+    trotterTerms(in, n, (1 - 4 * p) * time, lo, out);
+    trotterTerms(in, n, p * time, lo, out);
+    trotterTerms(in, n, p * time, lo, out);
+}
+
+// Widen a pass of k < 4 qubits to 4 with identity factors on the lowest
+// other qubits (the tensor-core applier takes 4..6).
+FusedPass widenTo4(const FusedPass& p, int n) {
+    const int k = (int)p.targets.size();
+    if (k >= 4) return p;
+    std::vector<int> t = p.targets;
+    for (int q = 0; q < n && (int)t.size() < 4; ++q)
+        if (std::find(t.begin(), t.end(), q) == t.end()) t.push_back(q);
+    std::sort(t.begin(), t.end());
+    std::vector<int> pos(k);                       // new matrix bit of old bit b
+    for (int b = 0; b < k; ++b) pos[b] = (int)(std::find(t.begin(), t.end(), p.targets[b]) - t.begin());
+    const int D = 1 << k, W = 16;
+    FusedPass w;
+    w.targets = t;
+    w.numGates = p.numGates;
+    w.unitary = p.unitary;
+    w.m.assign((size_t)W * W, cplx(0, 0));
+    uint64_t oldMask = 0;
+    for (int b = 0; b < k; ++b) oldMask |= 1ull << pos[b];
+    auto gather = [&](int i) {                     // old index of the new index's target bits
+        int r = 0;
+        for (int b = 0; b < k; ++b)
+            if (i >> pos[b] & 1) r |= 1 << b;
+        return r;
+    };
+    for (int r = 0; r < W; ++r)
+        for (int c = 0; c < W; ++c)
+            if ((r & ~oldMask) == (c & ~oldMask)) w.m[(size_t)r * W + c] = p.m[(size_t)gather(r) * D + gather(c)];
+    return w;
+}
+
+}  // namespace
+
+struct TrotterBatch {
+    int n = 0, B = 0;
+    float *re = nullptr, *im = nullptr;
+    std::vector<Instance> inst;
+    bool compiled = false;
+    std::vector<FusedPass> shape;                  // per pass: the targets (instance 0's pass)
+    std::vector<size_t> imgOffset, imgStride;      // per pass, in floats
+    float* images = nullptr;
+    long long* dInit = nullptr;
+    int* errFlag = nullptr;
+    double* partials = nullptr;                    // reduction scratch: partials, then the ticket
+    unsigned int* counter = nullptr;
+    double* dResults = nullptr;
+    double* hResults = nullptr;                    // pinned
+    int numSlots = 0;
+    // energy of instance b = sum of its group slots / its norm slot + identity
+    std::vector<std::vector<int>> groupSlots;
+    std::vector<int> normSlot;
+    std::vector<double> identity;
+    struct Red {
+        int kind;                                  // 0 pairs, 1 diagonal, 2 norm
+        int b;
+        PairGroupF pg;
+        DiagGroupF dg;
+    };
+    std::vector<Red> reds;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long runs = 0;
+};
+
+namespace {
+
+void freeDevice(TrotterBatch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    if (b->images) cudaFree(b->images);
+    if (b->dInit) cudaFree(b->dInit);
+    if (b->dResults) cudaFree(b->dResults);
+    if (b->hResults) cudaFreeHost(b->hResults);
+    b->images = nullptr;
+    b->dInit = nullptr;
+    b->dResults = nullptr;
+    b->hResults = nullptr;
+    b->compiled = false;
+}
+
+const char* kFn = "quest_gb300_trotterBatchRun";
+
+bool compileBatch(TrotterBatch* b) {
+    const int n = b->n, B = b->B;
+    const Instance& i0 = b->inst[0];
+    for (int k = 0; k < B; ++k) {
+        const Instance& in = b->inst[k];
+        if (!in.set) {
+            invalidQuESTInputError("Every instance of the Trotter batch must be set before it runs.", kFn);
+            return false;
+        }
+        if (in.codes != i0.codes || in.order != i0.order || in.reps != i0.reps) {
+            invalidQuESTInputError("The instances of a Trotter batch must share Pauli strings, order and repetitions.", kFn);
+            return false;
+        }
+    }
+    // gate streams and plans: instance 0 searched, the others reuse its passes
+    std::vector<FusedPlan> plans(B);
+    for (int k = 0; k < B; ++k) {
+        FusedPlan& p = plans[k];
+        p.numQubits = n;
+        p.maxFused = widestPass(n);
+        for (int r = 0; r < b->inst[k].reps; ++r)
+            trotterTerms(b->inst[k], n, b->inst[k].time / b->inst[k].reps, b->inst[k].order, p.gates);
+    }
+    compilePlan(plans[0]);
+    bool ok = plans[0].compiled;
+    {
+        std::atomic<int> next{1};
+        std::atomic<bool> good{true};
+        auto work = [&]() {
+            for (int k; (k = next.fetch_add(1)) < B;)
+                if (!compilePlanLike(plans[k], plans[0])) good = false;
+        };
+        const unsigned nt = (unsigned)std::min<int>(8, std::max(1, B - 1));
+        std::vector<std::thread> pool;
+        for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
+        if (ok) work();
+        for (auto& t : pool) t.join();
+        ok = ok && good;
+    }
+    if (!ok) {
+        invalidQuESTInputError("The Trotter circuits of the batch could not be fused with one pass structure.", kFn);
+        return false;
+    }
+    const size_t np = plans[0].passes.size();
+    b->shape.clear();
+    b->imgOffset.assign(np, 0);
+    b->imgStride.assign(np, 0);
+    size_t total = 0;
+    for (size_t p = 0; p < np; ++p) {
+        b->shape.push_back(widenTo4(plans[0].passes[p], n));
+        b->imgStride[p] = tcImageFloats((int)b->shape[p].targets.size());
+        b->imgOffset[p] = total;
+        total += b->imgStride[p] * (size_t)B;
+    }
+    std::vector<float> host(std::max<size_t>(total, 4));
+    {
+        std::atomic<size_t> next{0};
+        const size_t jobs = np * (size_t)B;
+        auto work = [&]() {
+            for (size_t j; (j = next.fetch_add(1)) < jobs;) {
+                const size_t p = j / B, k = j % B;
+                tcBuildImage(widenTo4(plans[k].passes[p], n), host.data() + b->imgOffset[p] + k * b->imgStride[p]);
+            }
+        };
+        const unsigned nt = (unsigned)std::min<size_t>({(size_t)8, (size_t)std::max(1u, std::thread::hardware_concurrency()), jobs});
+        std::vector<std::thread> pool;
+        for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
+        work();
+        for (auto& t : pool) t.join();
+    }
+    // the energy reductions: Pauli strings grouped by X/Y mask (one read of
+    // the state per group), plus the norm
+    std::map<uint64_t, std::vector<int>> groups;   // x -> term indices
+    std::vector<uint64_t> yzOf(i0.coeffs.size());
+    std::vector<int> nYOf(i0.coeffs.size());
+    std::vector<int> identityTerms;
+    for (size_t t = 0; t < i0.coeffs.size(); ++t) {
+        uint64_t x = 0, y = 0, z = 0;
+        for (int q = 0; q < n; ++q) {
+            const int c = i0.codes[t * n + q];
+            if (c == PAULI_X) x |= 1ull << q;
+            if (c == PAULI_Y) { x |= 1ull << q; y |= 1ull << q; }
+            if (c == PAULI_Z) z |= 1ull << q;
+        }
+        yzOf[t] = y | z;
+        nYOf[t] = __builtin_popcountll(y);
+        if ((x | z) == 0) identityTerms.push_back((int)t);
+        else groups[x].push_back((int)t);
+    }
+    b->reds.clear();
+    b->groupSlots.assign(B, {});
+    b->normSlot.assign(B, 0);
+    b->identity.assign(B, 0.0);
+    for (int k = 0; k < B; ++k) {
+        const Instance& in = b->inst[k];
+        for (int t : identityTerms) b->identity[k] += in.coeffs[t];
+        for (auto& g : groups) {
+            const uint64_t x = g.first;
+            if (x == 0) {
+                // diagonal terms, bucketed by their low 3 mask bits
+                for (size_t c0 = 0; c0 < g.second.size(); c0 += kMaxDiag) {
+                    TrotterBatch::Red r{};
+                    r.kind = 1;
+                    r.b = k;
+                    int m = 0;
+                    const size_t c1 = std::min(g.second.size(), c0 + kMaxDiag);
+                    for (int bk = 0; bk < kDiagItem; ++bk) {
+                        r.dg.off[bk] = m;
+                        for (size_t u = c0; u < c1; ++u) {
+                            const int t = g.second[u];
+                            if ((int)(yzOf[t] & (kDiagItem - 1)) == bk) {
+                                r.dg.zh[m] = yzOf[t] & ~(uint64_t)(kDiagItem - 1);
+                                r.dg.c[m++] = (float)in.coeffs[t];
+                            }
+                        }
+                    }
+                    r.dg.off[kDiagItem] = m;
+                    b->groupSlots[k].push_back((int)b->reds.size());
+                    b->reds.push_back(r);
+                }
+                continue;
+            }
+            std::vector<PauliTerm> terms;
+            for (int t : g.second) terms.push_back(PauliTerm{yzOf[t], nYOf[t], in.coeffs[t]});
+            std::vector<std::pair<uint64_t, double>> A, Bl;
+            pauliPairTerms(x, terms, A, Bl);
+            for (size_t a0 = 0, b0 = 0; a0 < A.size() || b0 < Bl.size();) {
+                TrotterBatch::Red r{};
+                r.kind = 0;
+                r.b = k;
+                r.pg.xmask = x;
+                r.pg.low = __builtin_ctzll(x);
+                for (; a0 < A.size() && r.pg.nA < kMaxTerms; ++a0, ++r.pg.nA) {
+                    r.pg.mA[r.pg.nA] = A[a0].first;
+                    r.pg.cA[r.pg.nA] = (float)A[a0].second;
+                }
+                for (; b0 < Bl.size() && r.pg.nB < kMaxTerms; ++b0, ++r.pg.nB) {
+                    r.pg.mB[r.pg.nB] = Bl[b0].first;
+                    r.pg.cB[r.pg.nB] = (float)Bl[b0].second;
+                }
+                b->groupSlots[k].push_back((int)b->reds.size());
+                b->reds.push_back(r);
+            }
+        }
+        TrotterBatch::Red r{};
+        r.kind = 2;
+        r.b = k;
+        b->normSlot[k] = (int)b->reds.size();
+        b->reds.push_back(r);
+    }
+    b->numSlots = (int)b->reds.size();
+    // device side
+    cudaStream_t st = stream();
+    std::vector<long long> init(B);
+    for (int k = 0; k < B; ++k) init[k] = b->inst[k].init;
+    if (QG_CUDA(cudaMalloc(&b->images, host.size() * sizeof(float)), kFn) ||
+        QG_CUDA(cudaMalloc(&b->dInit, B * sizeof(long long)), kFn) ||
+        QG_CUDA(cudaMalloc(&b->dResults, 2 * (size_t)b->numSlots * sizeof(double)), kFn) ||
+        QG_CUDA(cudaMallocHost(&b->hResults, 2 * (size_t)b->numSlots * sizeof(double)), kFn))
+        return false;
+    if (QG_CUDA(cudaMemcpyAsync(b->images, host.data(), host.size() * sizeof(float), cudaMemcpyHostToDevice, st), kFn) ||
+        QG_CUDA(cudaMemcpyAsync(b->dInit, init.data(), B * sizeof(long long), cudaMemcpyHostToDevice, st), kFn) ||
+        QG_CUDA(cudaStreamSynchronize(st), kFn))
+        return false;
+    b->compiled = true;
+    return true;
+}
+
+// the run's work, queued on `st` (the library stream, or a capture stream)
+bool queueRun(TrotterBatch* b, cudaStream_t st) {
+    const uint64_t dim = 1ull << b->n, all = dim * (uint64_t)b->B;
+    if (QG_CUDA(cudaMemsetAsync(b->errFlag, 0, sizeof(int), st), kFn) ||
+        QG_CUDA(cudaMemsetAsync(b->re, 0, all * sizeof(float), st), kFn) ||
+        QG_CUDA(cudaMemsetAsync(b->im, 0, all * sizeof(float), st), kFn))
+        return false;
+    kBatchClassical<<<(b->B + 127) / 128, 128, 0, st>>>(b->re, dim, b->dInit, b->B);
+    if (launchFailed(kFn)) return false;
+    for (size_t p = 0; p < b->shape.size(); ++p)
+        if (!applyPassTCBatch(b->re, b->im, b->n, b->shape[p], b->images + b->imgOffset[p], b->imgStride[p], b->B,
+                              b->errFlag, st)) {
+            invalidQuESTInputError("A pass of the Trotter batch could not be launched on the tensor cores.", kFn);
+            return false;
+        }
+    for (int s = 0; s < b->numSlots; ++s) {
+        const TrotterBatch::Red& r = b->reds[s];
+        const float* re = b->re + (uint64_t)r.b * dim;
+        const float* im = b->im + (uint64_t)r.b * dim;
+        double* out = b->dResults + 2 * s;
+        if (r.kind == 0) {
+            const uint64_t items = dim / 2;
+            kReduce<<<reduceGrid(items), red::kThreads, 0, st>>>(PairsF32{re, im, r.pg}, items, b->partials, b->counter, out);
+        } else {
+            const uint64_t items = dim / kDiagItem;
+            if (r.kind == 1)
+                kReduce<<<reduceGrid(items), red::kThreads, 0, st>>>(DiagF32{re, im, r.dg}, items, b->partials, b->counter, out);
+            else
+                kReduce<<<reduceGrid(items), red::kThreads, 0, st>>>(NormBatchF32{re, im}, items, b->partials, b->counter, out);
+        }
+        if (launchFailed(kFn)) return false;
+    }
+    return !QG_CUDA(cudaMemcpyAsync(b->hResults, b->dResults, 2 * (size_t)b->numSlots * sizeof(double),
+                                    cudaMemcpyDeviceToHost, st), kFn);
+}
+
+}  // namespace
+}  // namespace qg
+
+// ============================================================ C ABI
+using qg::TrotterBatch;
+
+extern "C" {
+
+void* quest_gb300_trotterBatchCreate(int numQubits, int numInstances) {
+    const char* fn = "quest_gb300_trotterBatchCreate";
+    if (numQubits < 11 || numQubits > 34 || numInstances < 1 || numInstances > 4096) {
+        invalidQuESTInputError("A Trotter batch takes 11 to 34 qubits and 1 to 4096 instances.", fn);
+        return nullptr;
+    }
+    TrotterBatch* b = new TrotterBatch();
+    b->n = numQubits;
+    b->B = numInstances;
+    b->inst.resize(numInstances);
+    const size_t all = ((size_t)1 << numQubits) * (size_t)numInstances;
+    if (QG_CUDA(cudaMalloc(&b->re, all * sizeof(float)), fn) || QG_CUDA(cudaMalloc(&b->im, all * sizeof(float)), fn) ||
+        QG_CUDA(cudaMalloc(&b->errFlag, sizeof(int)), fn) ||
+        QG_CUDA(cudaMalloc(&b->partials, (2 * qg::kMaxReduceBlocks + 8) * sizeof(double)), fn)) {
+        if (b->re) cudaFree(b->re);
+        if (b->im) cudaFree(b->im);
+        if (b->errFlag) cudaFree(b->errFlag);
+        if (b->partials) cudaFree(b->partials);
+        delete b;
+        return nullptr;
+    }
+    b->counter = reinterpret_cast<unsigned int*>(b->partials + 2 * qg::kMaxReduceBlocks);
+    cudaMemsetAsync(b->counter, 0, sizeof(unsigned int), qg::stream());
+    return b;
+}
+
+int quest_gb300_trotterBatchSetInstance(void* batch, int instance, PauliHamil hamil, double time, int order, int reps,
+                                        long long initClassicalState) {
+    const char* fn = "quest_gb300_trotterBatchSetInstance";
+    TrotterBatch* b = reinterpret_cast<TrotterBatch*>(batch);
+    if (!b || instance < 0 || instance >= b->B) {
+        invalidQuESTInputError("Invalid Trotter batch or instance index.", fn);
+        return -1;
+    }
+    if (hamil.numQubits != b->n || hamil.numSumTerms < 1 || !hamil.pauliCodes || !hamil.termCoeffs ||
+        !(order == 1 || (order >= 2 && order % 2 == 0)) || reps < 1 || initClassicalState < 0 ||
+        initClassicalState >= (1ll << b->n)) {
+        invalidQuESTInputError("Invalid Hamiltonian, order, repetitions or initial state for the Trotter batch.", fn);
+        return -1;
+    }
+    qg::Instance& in = b->inst[instance];
+    in.codes.resize((size_t)hamil.numSumTerms * b->n);
+    for (size_t i = 0; i < in.codes.size(); ++i) {
+        const int c = (int)hamil.pauliCodes[i];
+        if (c < 0 || c > 3) {
+            invalidQuESTInputError("Invalid Pauli code in the Trotter batch's Hamiltonian.", fn);
+            return -1;
+        }
+        in.codes[i] = c;
+    }
+    in.coeffs.assign(hamil.termCoeffs, hamil.termCoeffs + hamil.numSumTerms);
+    in.time = time;
+    in.order = order;
+    in.reps = reps;
+    in.init = initClassicalState;
+    in.set = true;
+    qg::freeDevice(b);                               // recompiled at the next run
+    return 0;
+}
+
+int quest_gb300_trotterBatchRun(void* batch, double* energies) {
+    const char* fn = "quest_gb300_trotterBatchRun";
+    TrotterBatch* b = reinterpret_cast<TrotterBatch*>(batch);
+    if (!b) return -1;
+    if (!b->compiled && !qg::compileBatch(b)) {
+        qg::freeDevice(b);
+        return -1;
+    }
+    cudaStream_t st = qg::stream();
+    if (b->exec) {
+        if (QG_CUDA(cudaGraphLaunch(b->exec, st), fn)) return -1;
+        qg::g_launches.fetch_add(1);
+    } else {
+        if (!qg::queueRun(b, st)) return -1;
+    }
+    if (QG_CUDA(cudaStreamSynchronize(st), fn)) return -1;
+    int err = 0;
+    if (QG_CUDA(cudaMemcpy(&err, b->errFlag, sizeof(int), cudaMemcpyDeviceToHost), fn)) return -1;
+    if (err) {
+        invalidQuESTInputError("A tensor-core pass of the Trotter batch timed out waiting on its pipeline.", fn);
+        return -1;
+    }
+    if (energies)
+        for (int k = 0; k < b->B; ++k) {
+            double e = 0.0;
+            for (int s : b->groupSlots[k]) e += b->hResults[2 * s];
+            const double norm = b->hResults[2 * b->normSlot[k]];
+            energies[k] = (norm > 0 ? e / norm : 0.0) + b->identity[k];
+        }
+    if (!b->exec) {
+        // later runs replay the same work as one graph
+        cudaStream_t cap = nullptr;
+        if (!QG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), fn)) {
+            bool ok = !QG_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), fn);
+            if (ok) {
+                const bool queued = qg::queueRun(b, cap);
+                ok = !QG_CUDA(cudaStreamEndCapture(cap, &b->graph), fn) && queued;
+            }
+            if (ok) ok = !QG_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0), fn);
+            if (!ok) {
+                if (b->graph) cudaGraphDestroy(b->graph);
+                b->graph = nullptr;
+                b->exec = nullptr;
+            }
+            cudaStreamDestroy(cap);
+        }
+    }
+    ++b->runs;
+    return 0;
+}
+
+int quest_gb300_trotterBatchCopyState(void* batch, int instance, Qureg dst) {
+    const char* fn = "quest_gb300_trotterBatchCopyState";
+    TrotterBatch* b = reinterpret_cast<TrotterBatch*>(batch);
+    if (!b || instance < 0 || instance >= b->B || dst.isDensityMatrix || dst.numQubitsRepresented != b->n ||
+        !dst.deviceStateVec.real) {
+        invalidQuESTInputError("Invalid Trotter batch instance or destination register.", fn);
+        return -1;
+    }
+    qg::captureDiscard(dst.deviceStateVec.real);
+    const uint64_t dim = 1ull << b->n;
+    cudaStream_t st = qg::stream();
+    // the FP32 passes drift the norm by ~1e-7 each (no correction inside a
+    // batch): the copy restores the start state's norm, 1, from the norm the
+    // last run measured
+    double scale = 1.0;
+    if (b->runs > 0 && b->hResults) {
+        const double norm = b->hResults[2 * b->normSlot[instance]];
+        if (norm > 0) scale = 1.0 / std::sqrt(norm);
+    }
+    qg::kBatchToF64<<<4 * qg::numSMs(), 256, 0, st>>>(b->re + instance * dim, b->im + instance * dim,
+                                                      dst.deviceStateVec.real, dst.deviceStateVec.imag, dim, scale);
+    if (qg::launchFailed(fn)) return -1;
+    return QG_CUDA(cudaStreamSynchronize(st), fn) ? -1 : 0;
+}
+
+int quest_gb300_trotterBatchNumPasses(void* batch) {
+    TrotterBatch* b = reinterpret_cast<TrotterBatch*>(batch);
+    return b && b->compiled ? (int)b->shape.size() : -1;
+}
+
+void quest_gb300_trotterBatchDestroy(void* batch) {
+    TrotterBatch* b = reinterpret_cast<TrotterBatch*>(batch);
+    if (!b) return;
+    cudaStreamSynchronize(qg::stream());
+    qg::freeDevice(b);
+    if (b->re) cudaFree(b->re);
+    if (b->im) cudaFree(b->im);
+    if (b->errFlag) cudaFree(b->errFlag);
+    if (b->partials) cudaFree(b->partials);
+    delete b;
+}
+
+}  // extern "C"

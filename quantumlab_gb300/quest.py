@@ -203,6 +203,12 @@ SIGNATURES = {
     "quest_gb300_setTensorCoreKernel": (None, [_I]),
     "quest_gb300_setCapture": (_I, [_Q, _I]),
     "quest_gb300_hostMirrorPinned": (_I, [_Q]),
+    "quest_gb300_trotterBatchCreate": (C.c_void_p, [_I, _I]),
+    "quest_gb300_trotterBatchSetInstance": (_I, [C.c_void_p, _I, PauliHamil, C.c_double, _I, _I, C.c_longlong]),
+    "quest_gb300_trotterBatchRun": (_I, [C.c_void_p, _P(C.c_double)]),
+    "quest_gb300_trotterBatchCopyState": (_I, [C.c_void_p, _I, _Q]),
+    "quest_gb300_trotterBatchNumPasses": (_I, [C.c_void_p]),
+    "quest_gb300_trotterBatchDestroy": (None, [C.c_void_p]),
     "quest_gb300_captureStats": (_I, [_Q, _P(C.c_longlong), _P(C.c_longlong), _P(C.c_longlong), _P(C.c_double)]),
     "quest_gb300_sampleMeasurements": (_I, [_Q, _P(_I), _I, _I, _P(_I)]),
     "quest_gb300_initProductState": (_I, [_Q, _I, _P(_I), _P(_D), _P(_D)]),

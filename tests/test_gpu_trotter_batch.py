@@ -1,0 +1,100 @@
+"""Batched Trotter instances (GPU): several Fermi-Hubbard instances with
+different U evolve together (one fusion plan, one tensor-core launch per pass
+over all states, graph replay after the first run).  Each instance must match
+QuEST's applyTrotterCircuit run alone in FP64 on the plain path: 1 - F <=
+1e-6, max |d amp| <= 1e-5, and its energy to 1e-5 of the coefficients' total
+magnitude (the fused FP32 engine's bounds)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from quantumlab_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def library_errors(gpulib):
+    gpulib.capture_errors()
+    gpulib.errors.clear()
+    yield gpulib.errors
+    gpulib.errors.clear()
+
+
+def plain_run(L, sites, U, time, order, reps):
+    codes, coeffs, _ = W.hubbard_terms(sites, U)
+    n = 2 * sites
+    h = L.pauli_hamil(codes, coeffs)
+    q, ws = L.create(n), L.create(n)
+    L.lib.initClassicalState(q, W.neel_index(sites))
+    L.lib.applyTrotterCircuit(q, h, time, order, reps)
+    amps = L.amps(q).copy()
+    energy = L.lib.calcExpecPauliHamil(q, h, ws)
+    L.destroy(ws)
+    L.destroy(q)
+    L.lib.destroyPauliHamil(h)
+    return amps, energy, float(np.sum(np.abs(coeffs)))
+
+
+@pytest.mark.parametrize("sites,order,reps", [(6, 1, 10), (6, 2, 5), (7, 1, 4)])
+def test_batch_matches_each_instance_alone(gpulib, library_errors, sites, order, reps):
+    L = gpulib
+    lib = L.lib
+    n, time = 2 * sites, 1.0
+    Us = [2.0, 4.0, 8.0]
+    b = lib.quest_gb300_trotterBatchCreate(n, len(Us))
+    assert b
+    hams = []
+    for i, U in enumerate(Us):
+        codes, coeffs, _ = W.hubbard_terms(sites, U)
+        hams.append(L.pauli_hamil(codes, coeffs))
+        assert lib.quest_gb300_trotterBatchSetInstance(b, i, hams[-1], time, order, reps, W.neel_index(sites)) == 0
+    e1 = (C.c_double * len(Us))()
+    assert lib.quest_gb300_trotterBatchRun(b, e1) == 0, list(library_errors)
+    passes = lib.quest_gb300_trotterBatchNumPasses(b)
+    e2 = (C.c_double * len(Us))()
+    assert lib.quest_gb300_trotterBatchRun(b, e2) == 0          # graph replay
+    assert list(e1) == list(e2)
+    q = L.create(n)
+    for i, U in enumerate(Us):
+        want, e_want, scale = plain_run(L, sites, U, time, order, reps)
+        assert lib.quest_gb300_trotterBatchCopyState(b, i, q) == 0
+        got = L.amps(q)
+        f = abs(np.vdot(want, got)) ** 2 / (np.vdot(got, got).real * np.vdot(want, want).real)
+        err = np.max(np.abs(got - want))
+        print(f"sites={sites} order={order} U={U}: {passes} passes, 1-F={1 - f:.2e}, max|d amp|={err:.2e}, "
+              f"dE={e1[i] - e_want:.2e}")
+        assert 1 - f <= 1e-6 and err <= 1e-5
+        assert abs(e1[i] - e_want) <= 1e-5 * scale
+    L.destroy(q)
+    lib.quest_gb300_trotterBatchDestroy(b)
+    for h in hams:
+        lib.destroyPauliHamil(h)
+    assert not library_errors
+
+
+def test_batch_rejects_instances_of_other_shapes(gpulib, library_errors):
+    """Instances must share Pauli strings, order and repetitions."""
+    L = gpulib
+    lib = L.lib
+    sites = 6
+    n = 2 * sites
+    b = lib.quest_gb300_trotterBatchCreate(n, 2)
+    c0, k0, _ = W.hubbard_terms(sites, 2.0)
+    c1, k1, _ = W.hubbard_terms(sites - 1, 2.0)
+    c1 = np.concatenate([c1, np.zeros((len(c1), 2), dtype=c1.dtype)], axis=1)   # other strings, same width
+    h0, h1 = L.pauli_hamil(c0, k0), L.pauli_hamil(c1, k1)
+    assert lib.quest_gb300_trotterBatchSetInstance(b, 0, h0, 1.0, 1, 2, 0) == 0
+    assert lib.quest_gb300_trotterBatchSetInstance(b, 1, h1, 1.0, 1, 2, 0) == 0
+    assert lib.quest_gb300_trotterBatchRun(b, None) == -1
+    assert any("share Pauli strings" in m for _, m in library_errors), list(library_errors)
+    library_errors.clear()
+    assert lib.quest_gb300_trotterBatchSetInstance(b, 1, h0, 1.0, 2, 2, 0) == 0             # other order
+    assert lib.quest_gb300_trotterBatchRun(b, None) == -1
+    library_errors.clear()
+    assert lib.quest_gb300_trotterBatchSetInstance(b, 1, h0, 0.5, 1, 2, 3) == 0             # same shape
+    assert lib.quest_gb300_trotterBatchRun(b, None) == 0
+    lib.quest_gb300_trotterBatchDestroy(b)
+    lib.destroyPauliHamil(h0)
+    lib.destroyPauliHamil(h1)
