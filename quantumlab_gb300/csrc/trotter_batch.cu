@@ -44,48 +44,57 @@ bool applyPassTCBatch(float* re, float* im, int n, const FusedPass& pass, const 
 namespace {
 
 using red::ins0;
-using red::kReduce;
-using red::reduceGrid;
 
 constexpr int kMaxTerms = 32;
-struct PairGroupF {                  // X/Y mask x != 0: pairs (j, j ^ x)
+constexpr int kCoefs = 64;           // coefficients per instance per reduction
+// The reductions of a batch share their Pauli masks; only the coefficients
+// differ per instance (coef[b * kCoefs ...], in device memory).
+struct PairShape {                   // X/Y mask x != 0: pairs (j, j ^ x)
     uint64_t xmask;
     int low, nA, nB;
     uint64_t mA[kMaxTerms], mB[kMaxTerms];
-    float cA[kMaxTerms], cB[kMaxTerms];
 };
 __device__ __forceinline__ float signedSumF(uint64_t j, const uint64_t* m, const float* c, int n) {
     float a = 0.f;
     for (int q = 0; q < n; ++q) a += (__popcll(j & m[q]) & 1) ? -c[q] : c[q];
     return a;
 }
-// Re(conj(psi_j) psi_k) A(j) + Im(conj(psi_j) psi_k) B(j), in FP32
+// Re(conj(psi_j) psi_k) A(j) + Im(conj(psi_j) psi_k) B(j), in FP32, for
+// instance b (A's coefficients at coef[b * kCoefs], B's kMaxTerms later)
 struct PairsF32 {
     const float *re, *im;
-    PairGroupF g;
-    __device__ __forceinline__ double2 operator()(uint64_t t) const {
+    uint64_t dim;
+    PairShape g;
+    const float* coef;
+    __device__ __forceinline__ double operator()(int b, uint64_t t) const {
+        const float* r = re + (uint64_t)b * dim;
+        const float* m = im + (uint64_t)b * dim;
+        const float* cA = coef + b * kCoefs;
         const uint64_t j = ins0(t, g.low), k = j ^ g.xmask;
-        const float jr = re[j], ji = im[j], kr = re[k], ki = im[k];
+        const float jr = r[j], ji = m[j], kr = r[k], ki = m[k];
         const float wr = fmaf(jr, kr, ji * ki), wi = fmaf(jr, ki, -(ji * kr));
-        return make_double2((double)(wr * signedSumF(j, g.mA, g.cA, g.nA) + wi * signedSumF(j, g.mB, g.cB, g.nB)), 0.0);
+        return (double)(wr * signedSumF(j, g.mA, cA, g.nA) + wi * signedSumF(j, g.mB, cA + kMaxTerms, g.nB));
     }
 };
 constexpr int kDiagItem = 8;
-constexpr int kMaxDiag = 64;
-struct DiagGroupF {                  // x = 0: terms bucketed by their 3 low mask bits
+struct DiagShape {                   // x = 0: terms bucketed by their 3 low mask bits
     int off[kDiagItem + 1];
-    uint64_t zh[kMaxDiag];
-    float c[kMaxDiag];
+    uint64_t zh[kCoefs];
 };
 // sum over 8 amplitudes of |psi|^2 sum_t c_t (-1)^popc(j & z_t), through the
 // Walsh-Hadamard transform of the 8 probabilities (as in reduce.cu), in FP32
 struct DiagF32 {
     const float *re, *im;
-    DiagGroupF g;
-    __device__ __forceinline__ double2 operator()(uint64_t i) const {
+    uint64_t dim;
+    DiagShape g;
+    const float* coef;
+    __device__ __forceinline__ double operator()(int b, uint64_t i) const {
         const uint64_t base = i * kDiagItem;
-        const float4 r0 = *reinterpret_cast<const float4*>(re + base), r1 = *reinterpret_cast<const float4*>(re + base + 4);
-        const float4 m0 = *reinterpret_cast<const float4*>(im + base), m1 = *reinterpret_cast<const float4*>(im + base + 4);
+        const float* r = re + (uint64_t)b * dim + base;
+        const float* m = im + (uint64_t)b * dim + base;
+        const float* c = coef + b * kCoefs;
+        const float4 r0 = *reinterpret_cast<const float4*>(r), r1 = *reinterpret_cast<const float4*>(r + 4);
+        const float4 m0 = *reinterpret_cast<const float4*>(m), m1 = *reinterpret_cast<const float4*>(m + 4);
         float p[kDiagItem] = {fmaf(r0.x, r0.x, m0.x * m0.x), fmaf(r0.y, r0.y, m0.y * m0.y), fmaf(r0.z, r0.z, m0.z * m0.z),
                               fmaf(r0.w, r0.w, m0.w * m0.w), fmaf(r1.x, r1.x, m1.x * m1.x), fmaf(r1.y, r1.y, m1.y * m1.y),
                               fmaf(r1.z, r1.z, m1.z * m1.z), fmaf(r1.w, r1.w, m1.w * m1.w)};
@@ -94,34 +103,83 @@ struct DiagF32 {
 #pragma unroll
             for (int l = 0; l < kDiagItem; ++l)
                 if (!(l & sb)) {
-                    const float a = p[l], b = p[l | sb];
-                    p[l] = a + b;
-                    p[l | sb] = a - b;
+                    const float a = p[l], bb = p[l | sb];
+                    p[l] = a + bb;
+                    p[l | sb] = a - bb;
                 }
         float acc = 0.f;
 #pragma unroll
-        for (int m = 0; m < kDiagItem; ++m) {
+        for (int mm = 0; mm < kDiagItem; ++mm) {
             float gm = 0.f;
-            for (int t = g.off[m]; t < g.off[m + 1]; ++t) gm += (__popcll(base & g.zh[t]) & 1) ? -g.c[t] : g.c[t];
-            acc = fmaf(gm, p[m], acc);
+            for (int t = g.off[mm]; t < g.off[mm + 1]; ++t) gm += (__popcll(base & g.zh[t]) & 1) ? -c[t] : c[t];
+            acc = fmaf(gm, p[mm], acc);
         }
-        return make_double2((double)acc, 0.0);
+        return (double)acc;
     }
 };
-struct NormBatchF32 {                // 8 amplitudes per item
+struct NormF32b {                    // 8 amplitudes per item
     const float *re, *im;
-    __device__ __forceinline__ double2 operator()(uint64_t i) const {
-        const float4* r4 = reinterpret_cast<const float4*>(re + 8 * i);
-        const float4* m4 = reinterpret_cast<const float4*>(im + 8 * i);
-        const float4 a = r4[0], b = r4[1], c = m4[0], d = m4[1];
+    uint64_t dim;
+    __device__ __forceinline__ double operator()(int b, uint64_t i) const {
+        const float4* r4 = reinterpret_cast<const float4*>(re + (uint64_t)b * dim + 8 * i);
+        const float4* m4 = reinterpret_cast<const float4*>(im + (uint64_t)b * dim + 8 * i);
+        const float4 a = r4[0], bb = r4[1], c = m4[0], d = m4[1];
         float s = a.x * a.x;
         s = fmaf(a.y, a.y, s); s = fmaf(a.z, a.z, s); s = fmaf(a.w, a.w, s);
-        s = fmaf(b.x, b.x, s); s = fmaf(b.y, b.y, s); s = fmaf(b.z, b.z, s); s = fmaf(b.w, b.w, s);
+        s = fmaf(bb.x, bb.x, s); s = fmaf(bb.y, bb.y, s); s = fmaf(bb.z, bb.z, s); s = fmaf(bb.w, bb.w, s);
         s = fmaf(c.x, c.x, s); s = fmaf(c.y, c.y, s); s = fmaf(c.z, c.z, s); s = fmaf(c.w, c.w, s);
         s = fmaf(d.x, d.x, s); s = fmaf(d.y, d.y, s); s = fmaf(d.z, d.z, s); s = fmaf(d.w, d.w, s);
-        return make_double2((double)s, 0.0);
+        return (double)s;
     }
 };
+
+// One reduction for every instance of the batch: block (x, b) sums items of
+// instance b; the last block of instance b (its ticket in counters[b]) adds
+// the instance's block partials in a fixed order into results[2 b].
+constexpr int kMaxBlocksPerInst = 2048;
+template <class F>
+__global__ void __launch_bounds__(red::kThreads) kReduceBatch(F f, uint64_t nItems, double* __restrict__ partials,
+                                                              unsigned int* __restrict__ counters,
+                                                              double* __restrict__ results) {
+    __shared__ double sx[red::kWarps];
+    __shared__ bool amLast;
+    const int b = blockIdx.y;
+    const uint64_t stride = (uint64_t)gridDim.x * red::kThreads;
+    uint64_t i = (uint64_t)blockIdx.x * red::kThreads + threadIdx.x;
+    double a0 = 0.0, a1 = 0.0;
+    for (; i + stride < nItems; i += 2 * stride) {
+        a0 += f(b, i);
+        a1 += f(b, i + stride);
+    }
+    for (; i < nItems; i += stride) a0 += f(b, i);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double x = red::warpSum(a0 + a1);
+    if (lane == 0) sx[w] = x;
+    __syncthreads();
+    double* part = partials + (size_t)b * kMaxBlocksPerInst;
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < red::kWarps; ++k) t += sx[k];
+        part[blockIdx.x] = t;
+        __threadfence();
+        amLast = atomicAdd(counters + b, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!amLast) return;
+    __threadfence();
+    double v = 0.0;
+    for (unsigned k = threadIdx.x; k < gridDim.x; k += red::kThreads) v += __ldcg(part + k);
+    v = red::warpSum(v);
+    if (lane == 0) sx[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < red::kWarps; ++k) t += sx[k];
+        results[2 * b] = t;
+        results[2 * b + 1] = 0.0;
+        counters[b] = 0u;
+    }
+}
 
 __global__ void kBatchClassical(float* re, uint64_t stride, const long long* idx, int B) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -219,10 +277,11 @@ struct TrotterBatch {
     float* images = nullptr;
     long long* dInit = nullptr;
     int* errFlag = nullptr;
-    double* partials = nullptr;                    // reduction scratch: partials, then the ticket
-    unsigned int* counter = nullptr;
-    double* dResults = nullptr;
+    double* partials = nullptr;                    // per instance kMaxBlocksPerInst block partials
+    unsigned int* counters = nullptr;              // per instance last-block tickets
+    double* dResults = nullptr;                    // slot l * B + b: reduction l of instance b
     double* hResults = nullptr;                    // pinned
+    float* dCoef = nullptr;                        // reduction l, instance b: kCoefs floats
     int numSlots = 0;
     // energy of instance b = sum of its group slots / its norm slot + identity
     std::vector<std::vector<int>> groupSlots;
@@ -230,11 +289,10 @@ struct TrotterBatch {
     std::vector<double> identity;
     struct Red {
         int kind;                                  // 0 pairs, 1 diagonal, 2 norm
-        int b;
-        PairGroupF pg;
-        DiagGroupF dg;
+        PairShape ps;
+        DiagShape ds;
     };
-    std::vector<Red> reds;
+    std::vector<Red> reds;                         // one launch each, over all instances
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long runs = 0;
@@ -249,10 +307,12 @@ void freeDevice(TrotterBatch* b) {
     b->graph = nullptr;
     if (b->images) cudaFree(b->images);
     if (b->dInit) cudaFree(b->dInit);
+    if (b->dCoef) cudaFree(b->dCoef);
     if (b->dResults) cudaFree(b->dResults);
     if (b->hResults) cudaFreeHost(b->hResults);
     b->images = nullptr;
     b->dInit = nullptr;
+    b->dCoef = nullptr;
     b->dResults = nullptr;
     b->hResults = nullptr;
     b->compiled = false;
@@ -349,79 +409,102 @@ bool compileBatch(TrotterBatch* b) {
         if ((x | z) == 0) identityTerms.push_back((int)t);
         else groups[x].push_back((int)t);
     }
+    // one reduction launch per group (chunk), shared masks, coefficients per
+    // instance in the same order
     b->reds.clear();
-    b->groupSlots.assign(B, {});
-    b->normSlot.assign(B, 0);
     b->identity.assign(B, 0.0);
-    for (int k = 0; k < B; ++k) {
-        const Instance& in = b->inst[k];
-        for (int t : identityTerms) b->identity[k] += in.coeffs[t];
-        for (auto& g : groups) {
-            const uint64_t x = g.first;
-            if (x == 0) {
-                // diagonal terms, bucketed by their low 3 mask bits
-                for (size_t c0 = 0; c0 < g.second.size(); c0 += kMaxDiag) {
-                    TrotterBatch::Red r{};
-                    r.kind = 1;
-                    r.b = k;
-                    int m = 0;
-                    const size_t c1 = std::min(g.second.size(), c0 + kMaxDiag);
-                    for (int bk = 0; bk < kDiagItem; ++bk) {
-                        r.dg.off[bk] = m;
-                        for (size_t u = c0; u < c1; ++u) {
-                            const int t = g.second[u];
-                            if ((int)(yzOf[t] & (kDiagItem - 1)) == bk) {
-                                r.dg.zh[m] = yzOf[t] & ~(uint64_t)(kDiagItem - 1);
-                                r.dg.c[m++] = (float)in.coeffs[t];
-                            }
+    for (int k = 0; k < B; ++k)
+        for (int t : identityTerms) b->identity[k] += b->inst[k].coeffs[t];
+    std::vector<float> coef;                       // [reduction][instance][kCoefs]
+    auto addRed = [&](const TrotterBatch::Red& r, const std::vector<std::vector<float>>& perInst) {
+        b->reds.push_back(r);
+        for (int k = 0; k < B; ++k) {
+            std::vector<float> c(kCoefs, 0.f);
+            std::copy(perInst[k].begin(), perInst[k].end(), c.begin());
+            coef.insert(coef.end(), c.begin(), c.end());
+        }
+    };
+    for (auto& g : groups) {
+        const uint64_t x = g.first;
+        if (x == 0) {
+            // diagonal terms, bucketed by their low 3 mask bits
+            for (size_t c0 = 0; c0 < g.second.size(); c0 += kCoefs) {
+                TrotterBatch::Red r{};
+                r.kind = 1;
+                std::vector<int> order;
+                const size_t c1 = std::min(g.second.size(), c0 + kCoefs);
+                for (int bk = 0; bk < kDiagItem; ++bk) {
+                    r.ds.off[bk] = (int)order.size();
+                    for (size_t u = c0; u < c1; ++u) {
+                        const int t = g.second[u];
+                        if ((int)(yzOf[t] & (kDiagItem - 1)) == bk) {
+                            r.ds.zh[order.size()] = yzOf[t] & ~(uint64_t)(kDiagItem - 1);
+                            order.push_back(t);
                         }
                     }
-                    r.dg.off[kDiagItem] = m;
-                    b->groupSlots[k].push_back((int)b->reds.size());
-                    b->reds.push_back(r);
                 }
-                continue;
+                r.ds.off[kDiagItem] = (int)order.size();
+                std::vector<std::vector<float>> per(B);
+                for (int k = 0; k < B; ++k)
+                    for (int t : order) per[k].push_back((float)b->inst[k].coeffs[t]);
+                addRed(r, per);
             }
-            std::vector<PauliTerm> terms;
-            for (int t : g.second) terms.push_back(PauliTerm{yzOf[t], nYOf[t], in.coeffs[t]});
-            std::vector<std::pair<uint64_t, double>> A, Bl;
-            pauliPairTerms(x, terms, A, Bl);
-            for (size_t a0 = 0, b0 = 0; a0 < A.size() || b0 < Bl.size();) {
-                TrotterBatch::Red r{};
-                r.kind = 0;
-                r.b = k;
-                r.pg.xmask = x;
-                r.pg.low = __builtin_ctzll(x);
-                for (; a0 < A.size() && r.pg.nA < kMaxTerms; ++a0, ++r.pg.nA) {
-                    r.pg.mA[r.pg.nA] = A[a0].first;
-                    r.pg.cA[r.pg.nA] = (float)A[a0].second;
-                }
-                for (; b0 < Bl.size() && r.pg.nB < kMaxTerms; ++b0, ++r.pg.nB) {
-                    r.pg.mB[r.pg.nB] = Bl[b0].first;
-                    r.pg.cB[r.pg.nB] = (float)Bl[b0].second;
-                }
-                b->groupSlots[k].push_back((int)b->reds.size());
-                b->reds.push_back(r);
-            }
+            continue;
         }
+        // the A / B lists depend on the masks only, so they line up across
+        // instances
+        std::vector<std::vector<std::pair<uint64_t, double>>> A(B), Bl(B);
+        for (int k = 0; k < B; ++k) {
+            std::vector<PauliTerm> terms;
+            for (int t : g.second) terms.push_back(PauliTerm{yzOf[t], nYOf[t], b->inst[k].coeffs[t]});
+            pauliPairTerms(x, terms, A[k], Bl[k]);
+        }
+        for (size_t a0 = 0, b0 = 0; a0 < A[0].size() || b0 < Bl[0].size();) {
+            TrotterBatch::Red r{};
+            r.kind = 0;
+            r.ps.xmask = x;
+            r.ps.low = __builtin_ctzll(x);
+            const size_t a1 = std::min(A[0].size(), a0 + kMaxTerms), b1 = std::min(Bl[0].size(), b0 + kMaxTerms);
+            r.ps.nA = (int)(a1 - a0);
+            r.ps.nB = (int)(b1 - b0);
+            for (size_t u = a0; u < a1; ++u) r.ps.mA[u - a0] = A[0][u].first;
+            for (size_t u = b0; u < b1; ++u) r.ps.mB[u - b0] = Bl[0][u].first;
+            std::vector<std::vector<float>> per(B, std::vector<float>(kCoefs, 0.f));
+            for (int k = 0; k < B; ++k) {
+                for (size_t u = a0; u < a1; ++u) per[k][u - a0] = (float)A[k][u].second;
+                for (size_t u = b0; u < b1; ++u) per[k][kMaxTerms + u - b0] = (float)Bl[k][u].second;
+            }
+            addRed(r, per);
+            a0 = a1;
+            b0 = b1;
+        }
+    }
+    const int groupReds = (int)b->reds.size();
+    {
         TrotterBatch::Red r{};
         r.kind = 2;
-        r.b = k;
-        b->normSlot[k] = (int)b->reds.size();
-        b->reds.push_back(r);
+        addRed(r, std::vector<std::vector<float>>(B));
     }
-    b->numSlots = (int)b->reds.size();
+    b->numSlots = (int)b->reds.size() * B;
+    b->groupSlots.assign(B, {});
+    b->normSlot.assign(B, 0);
+    for (int k = 0; k < B; ++k) {
+        for (int l = 0; l < groupReds; ++l) b->groupSlots[k].push_back(l * B + k);
+        b->normSlot[k] = groupReds * B + k;
+    }
     // device side
     cudaStream_t st = stream();
     std::vector<long long> init(B);
     for (int k = 0; k < B; ++k) init[k] = b->inst[k].init;
     if (QG_CUDA(cudaMalloc(&b->images, host.size() * sizeof(float)), kFn) ||
         QG_CUDA(cudaMalloc(&b->dInit, B * sizeof(long long)), kFn) ||
+        QG_CUDA(cudaMalloc(&b->dCoef, coef.size() * sizeof(float)), kFn) ||
         QG_CUDA(cudaMalloc(&b->dResults, 2 * (size_t)b->numSlots * sizeof(double)), kFn) ||
         QG_CUDA(cudaMallocHost(&b->hResults, 2 * (size_t)b->numSlots * sizeof(double)), kFn))
         return false;
     if (QG_CUDA(cudaMemcpyAsync(b->images, host.data(), host.size() * sizeof(float), cudaMemcpyHostToDevice, st), kFn) ||
         QG_CUDA(cudaMemcpyAsync(b->dInit, init.data(), B * sizeof(long long), cudaMemcpyHostToDevice, st), kFn) ||
+        QG_CUDA(cudaMemcpyAsync(b->dCoef, coef.data(), coef.size() * sizeof(float), cudaMemcpyHostToDevice, st), kFn) ||
         QG_CUDA(cudaStreamSynchronize(st), kFn))
         return false;
     b->compiled = true;
@@ -443,21 +526,25 @@ bool queueRun(TrotterBatch* b, cudaStream_t st) {
             invalidQuESTInputError("A pass of the Trotter batch could not be launched on the tensor cores.", kFn);
             return false;
         }
-    for (int s = 0; s < b->numSlots; ++s) {
-        const TrotterBatch::Red& r = b->reds[s];
-        const float* re = b->re + (uint64_t)r.b * dim;
-        const float* im = b->im + (uint64_t)r.b * dim;
-        double* out = b->dResults + 2 * s;
-        if (r.kind == 0) {
-            const uint64_t items = dim / 2;
-            kReduce<<<reduceGrid(items), red::kThreads, 0, st>>>(PairsF32{re, im, r.pg}, items, b->partials, b->counter, out);
-        } else {
-            const uint64_t items = dim / kDiagItem;
-            if (r.kind == 1)
-                kReduce<<<reduceGrid(items), red::kThreads, 0, st>>>(DiagF32{re, im, r.dg}, items, b->partials, b->counter, out);
-            else
-                kReduce<<<reduceGrid(items), red::kThreads, 0, st>>>(NormBatchF32{re, im}, items, b->partials, b->counter, out);
-        }
+    // one launch per reduction over all instances: blockIdx.y = instance
+    const int B = b->B;
+    for (size_t l = 0; l < b->reds.size(); ++l) {
+        const TrotterBatch::Red& r = b->reds[l];
+        const float* coef = b->dCoef + l * (size_t)B * kCoefs;
+        double* out = b->dResults + 2 * l * (size_t)B;
+        const uint64_t items = r.kind == 0 ? dim / 2 : dim / kDiagItem;
+        const unsigned bx = (unsigned)std::max<uint64_t>(
+            1, std::min<uint64_t>({(uint64_t)kMaxBlocksPerInst, (items + red::kThreads - 1) / red::kThreads,
+                                   std::max<uint64_t>(1, 8ull * (uint64_t)numSMs() / (uint64_t)B)}));
+        const dim3 grid(bx, (unsigned)B);
+        if (r.kind == 0)
+            kReduceBatch<<<grid, red::kThreads, 0, st>>>(PairsF32{b->re, b->im, dim, r.ps, coef}, items, b->partials,
+                                                         b->counters, out);
+        else if (r.kind == 1)
+            kReduceBatch<<<grid, red::kThreads, 0, st>>>(DiagF32{b->re, b->im, dim, r.ds, coef}, items, b->partials,
+                                                         b->counters, out);
+        else
+            kReduceBatch<<<grid, red::kThreads, 0, st>>>(NormF32b{b->re, b->im, dim}, items, b->partials, b->counters, out);
         if (launchFailed(kFn)) return false;
     }
     return !QG_CUDA(cudaMemcpyAsync(b->hResults, b->dResults, 2 * (size_t)b->numSlots * sizeof(double),
@@ -485,7 +572,7 @@ void* quest_gb300_trotterBatchCreate(int numQubits, int numInstances) {
     const size_t all = ((size_t)1 << numQubits) * (size_t)numInstances;
     if (QG_CUDA(cudaMalloc(&b->re, all * sizeof(float)), fn) || QG_CUDA(cudaMalloc(&b->im, all * sizeof(float)), fn) ||
         QG_CUDA(cudaMalloc(&b->errFlag, sizeof(int)), fn) ||
-        QG_CUDA(cudaMalloc(&b->partials, (2 * qg::kMaxReduceBlocks + 8) * sizeof(double)), fn)) {
+        QG_CUDA(cudaMalloc(&b->partials, (size_t)numInstances * (qg::kMaxBlocksPerInst + 1) * sizeof(double)), fn)) {
         if (b->re) cudaFree(b->re);
         if (b->im) cudaFree(b->im);
         if (b->errFlag) cudaFree(b->errFlag);
@@ -493,8 +580,8 @@ void* quest_gb300_trotterBatchCreate(int numQubits, int numInstances) {
         delete b;
         return nullptr;
     }
-    b->counter = reinterpret_cast<unsigned int*>(b->partials + 2 * qg::kMaxReduceBlocks);
-    cudaMemsetAsync(b->counter, 0, sizeof(unsigned int), qg::stream());
+    b->counters = reinterpret_cast<unsigned int*>(b->partials + (size_t)numInstances * qg::kMaxBlocksPerInst);
+    cudaMemsetAsync(b->counters, 0, numInstances * sizeof(unsigned int), qg::stream());
     return b;
 }
 
