@@ -678,6 +678,10 @@ int quest_gb300_trotterBatchCopyState(void* batch, int instance, Qureg dst) {
         invalidQuESTInputError("Invalid Trotter batch instance or destination register.", fn);
         return -1;
     }
+    if (b->runs == 0 || !b->compiled) {
+        invalidQuESTInputError("The Trotter batch has no state to copy: run it first.", fn);
+        return -1;
+    }
     qg::captureDiscard(dst.deviceStateVec.real);
     const uint64_t dim = 1ull << b->n;
     cudaStream_t st = qg::stream();
@@ -685,7 +689,7 @@ int quest_gb300_trotterBatchCopyState(void* batch, int instance, Qureg dst) {
     // batch): the copy restores the start state's norm, 1, from the norm the
     // last run measured
     double scale = 1.0;
-    if (b->runs > 0 && b->hResults) {
+    if (b->hResults) {
         const double norm = b->hResults[2 * b->normSlot[instance]];
         if (norm > 0) scale = 1.0 / std::sqrt(norm);
     }

@@ -87,6 +87,10 @@ def test_batch_rejects_instances_of_other_shapes(gpulib, library_errors):
     h0, h1 = L.pauli_hamil(c0, k0), L.pauli_hamil(c1, k1)
     assert lib.quest_gb300_trotterBatchSetInstance(b, 0, h0, 1.0, 1, 2, 0) == 0
     assert lib.quest_gb300_trotterBatchSetInstance(b, 1, h1, 1.0, 1, 2, 0) == 0
+    q = L.create(n)
+    assert lib.quest_gb300_trotterBatchCopyState(b, 0, q) == -1                          # nothing run yet
+    assert any("run it first" in m for _, m in library_errors), list(library_errors)
+    library_errors.clear()
     assert lib.quest_gb300_trotterBatchRun(b, None) == -1
     assert any("share Pauli strings" in m for _, m in library_errors), list(library_errors)
     library_errors.clear()
@@ -95,6 +99,9 @@ def test_batch_rejects_instances_of_other_shapes(gpulib, library_errors):
     library_errors.clear()
     assert lib.quest_gb300_trotterBatchSetInstance(b, 1, h0, 0.5, 1, 2, 3) == 0             # same shape
     assert lib.quest_gb300_trotterBatchRun(b, None) == 0
+    assert lib.quest_gb300_trotterBatchCopyState(b, 1, q) == 0
+    assert abs(L.lib.calcTotalProb(q) - 1) < 1e-6
+    L.destroy(q)
     lib.quest_gb300_trotterBatchDestroy(b)
     lib.destroyPauliHamil(h0)
     lib.destroyPauliHamil(h1)
