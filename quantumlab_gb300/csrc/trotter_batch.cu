@@ -104,13 +104,14 @@ struct PairsF32x4 {
         return (double)acc;
     }
 };
-constexpr int kDiagItem = 8;
-struct DiagShape {                   // x = 0: terms bucketed by their 3 low mask bits
+constexpr int kDiagItem = 16;
+struct DiagShape {                   // x = 0: terms bucketed by their 4 low mask bits
     int off[kDiagItem + 1];
     uint64_t zh[kCoefs];
 };
-// sum over 8 amplitudes of |psi|^2 sum_t c_t (-1)^popc(j & z_t), through the
-// Walsh-Hadamard transform of the 8 probabilities (as in reduce.cu), in FP32
+// sum over 16 amplitudes of |psi|^2 sum_t c_t (-1)^popc(j & z_t), through the
+// Walsh-Hadamard transform of the 16 probabilities (as in reduce.cu, which
+// takes 8), in FP32: a term then costs one signed addition per 16 amplitudes
 struct DiagF32 {
     const float *re, *im;
     uint64_t dim;
@@ -121,11 +122,15 @@ struct DiagF32 {
         const float* r = re + (uint64_t)b * dim + base;
         const float* m = im + (uint64_t)b * dim + base;
         const float* c = coef + b * kCoefs;
-        const float4 r0 = *reinterpret_cast<const float4*>(r), r1 = *reinterpret_cast<const float4*>(r + 4);
-        const float4 m0 = *reinterpret_cast<const float4*>(m), m1 = *reinterpret_cast<const float4*>(m + 4);
-        float p[kDiagItem] = {fmaf(r0.x, r0.x, m0.x * m0.x), fmaf(r0.y, r0.y, m0.y * m0.y), fmaf(r0.z, r0.z, m0.z * m0.z),
-                              fmaf(r0.w, r0.w, m0.w * m0.w), fmaf(r1.x, r1.x, m1.x * m1.x), fmaf(r1.y, r1.y, m1.y * m1.y),
-                              fmaf(r1.z, r1.z, m1.z * m1.z), fmaf(r1.w, r1.w, m1.w * m1.w)};
+        float p[kDiagItem];
+#pragma unroll
+        for (int h = 0; h < kDiagItem / 4; ++h) {
+            const float4 a = *reinterpret_cast<const float4*>(r + 4 * h), q = *reinterpret_cast<const float4*>(m + 4 * h);
+            p[4 * h] = fmaf(a.x, a.x, q.x * q.x);
+            p[4 * h + 1] = fmaf(a.y, a.y, q.y * q.y);
+            p[4 * h + 2] = fmaf(a.z, a.z, q.z * q.z);
+            p[4 * h + 3] = fmaf(a.w, a.w, q.w * q.w);
+        }
 #pragma unroll
         for (int sb = 1; sb < kDiagItem; sb <<= 1)
 #pragma unroll
@@ -560,7 +565,8 @@ bool queueRun(TrotterBatch* b, cudaStream_t st) {
         const TrotterBatch::Red& r = b->reds[l];
         const float* coef = b->dCoef + l * (size_t)B * kCoefs;
         double* out = b->dResults + 2 * l * (size_t)B;
-        const uint64_t items = r.kind == 0 ? dim / 2 : dim / kDiagItem;     // kind 3: four pairs, 8 amplitudes
+        // items: a pair (kind 0), four pairs or 8 amplitudes (kinds 3, 2), kDiagItem amplitudes (kind 1)
+        const uint64_t items = r.kind == 0 ? dim / 2 : r.kind == 1 ? dim / kDiagItem : dim / 8;
         const unsigned bx = (unsigned)std::max<uint64_t>(
             1, std::min<uint64_t>({(uint64_t)kMaxBlocksPerInst, (items + red::kThreads - 1) / red::kThreads,
                                    std::max<uint64_t>(1, 8ull * (uint64_t)numSMs() / (uint64_t)B)}));
