@@ -447,6 +447,42 @@ def run_swaps(args, rank=0, world=1):
 
 
 # ------------------------------------------------ the other configurations
+def c4_batch(L, reps=3):
+    """The 12 instances of the 64 that share the first-order, dt = 0.1 shape
+    (U = 2, 4, 8 repeating) evolved as one Trotter batch at 24 qubits: one
+    plan, one launch per pass over all 12 states, graph replay after the first
+    run, energies from the FP32 states.  Returns the energies and the time per
+    run (CUDA events over `reps` replays)."""
+    import ctypes as C
+    from quantumlab_gb300 import workloads as W
+
+    lib = L.lib
+    sites, n4, T = 12, 24, 1.0
+    inst = W.hubbard_instances(64)
+    sel = [i for i in range(64) if inst[i][1] == 0.1 and inst[i][2] == 1]
+    hb = []
+    batch = lib.quest_gb300_trotterBatchCreate(n4, len(sel))
+    for k, i in enumerate(sel):
+        U, dt, order = inst[i]
+        codes, coeffs, const = W.hubbard_terms(sites, U)
+        hb.append(L.pauli_hamil(codes, coeffs))
+        lib.quest_gb300_trotterBatchSetInstance(batch, k, hb[-1], T, order, int(round(T / dt)), W.neel_index(sites))
+    eb = (C.c_double * len(sel))()
+    t0 = time.perf_counter()
+    lib.quest_gb300_trotterBatchRun(batch, eb)                 # compile, eager run, graph capture
+    first_s = time.perf_counter() - t0
+    lib.quest_gb300_eventRecord(32)
+    for _ in range(reps):
+        lib.quest_gb300_trotterBatchRun(batch, eb)
+    lib.quest_gb300_eventRecord(33)
+    batch_ms = lib.quest_gb300_eventElapsedMs(32, 33) / max(1, reps)
+    npb = lib.quest_gb300_trotterBatchNumPasses(batch)
+    lib.quest_gb300_trotterBatchDestroy(batch)
+    for h in hb:
+        lib.destroyPauliHamil(h)
+    return {"sel": sel, "energies": list(eb), "batch_ms": batch_ms, "passes": npb, "first_s": first_s}
+
+
 def run_configs(args):
     """Secondary lines for the configurations the headline does not cover
     (their parity is in tests/): C1 the 20-qubit plain FP64 circuit (GPU
@@ -566,31 +602,8 @@ def run_configs(args):
         L.destroy(q)
     lib.destroyPauliHamil(h25)
     L.destroy(ws)
-    # Batched: the 12 instances of the 64 that share the first-order, dt = 0.1
-    # shape (U = 2, 4, 8 repeating) evolve together (one plan, one launch per
-    # pass over all 12 states, graph replay), energies from the FP32 states.
-    sel = [i for i in range(64) if inst[i][1] == 0.1 and inst[i][2] == 1]
-    hb = []
-    batch = lib.quest_gb300_trotterBatchCreate(n4, len(sel))
-    for k, i in enumerate(sel):
-        U, dt, order = inst[i]
-        codes, coeffs, const = W.hubbard_terms(sites, U)
-        hb.append(L.pauli_hamil(codes, coeffs))
-        lib.quest_gb300_trotterBatchSetInstance(batch, k, hb[-1], T, order, int(round(T / dt)), W.neel_index(sites))
-    eb = (C.c_double * len(sel))()
-    t0 = time.perf_counter()
-    lib.quest_gb300_trotterBatchRun(batch, eb)                 # compile, eager run, graph capture
-    first_s = time.perf_counter() - t0
-    reps_b = 3
-    lib.quest_gb300_eventRecord(32)
-    for _ in range(reps_b):
-        lib.quest_gb300_trotterBatchRun(batch, eb)
-    lib.quest_gb300_eventRecord(33)
-    batch_ms = lib.quest_gb300_eventElapsedMs(32, 33) / reps_b
-    npb = lib.quest_gb300_trotterBatchNumPasses(batch)
-    lib.quest_gb300_trotterBatchDestroy(batch)
-    for h in hb:
-        lib.destroyPauliHamil(h)
+    bat = c4_batch(L, reps=3)
+    sel, eb, batch_ms, npb, first_s = bat["sel"], bat["energies"], bat["batch_ms"], bat["passes"], bat["first_s"]
     same = [r for r in rows if r["dt"] == 0.1 and r["order"] == 1]
     plain1 = sum(r["plain_ms"] for r in same) / len(same)
     capt1 = sum(r["captured_ms"] for r in same) / len(same)
@@ -690,6 +703,8 @@ def main():
     ap.add_argument("--swap-vectors", type=int, default=4096)
     ap.add_argument("--swap-sample", type=int, default=6)
     ap.add_argument("--no-configs", action="store_true", help="skip the configuration 1/3/4 lines")
+    ap.add_argument("--c4-batch-only", action="store_true",
+                    help="only the batched Trotter run of configuration 4 (12 instances, 24 qubits); for profiling")
     args = ap.parse_args()
     rank, world, local = dist_info()
     os.environ.setdefault("QUEST_GB300_DEVICE", str(local))
@@ -697,6 +712,11 @@ def main():
         out = run_reference(args, rank, world)
         if out is not None:
             print(json.dumps(out), flush=True)
+        return
+    if args.c4_batch_only:
+        import quantumlab_gb300 as qg
+        bat = c4_batch(qg.load(), reps=args.steps)
+        print(json.dumps({"c4_batch": {k: v for k, v in bat.items() if k != "sel"}}), flush=True)
         return
     out = run_gpu(args, rank, world)
     if not args.no_swap:
