@@ -51,6 +51,12 @@ int quest_gb300_planAddControlledPhaseShift(void* plan, int qubit1, int qubit2, 
 int quest_gb300_planSetBeamWidth(void* plan, int width);
 /* Compile; returns the number of passes, or -1. */
 int quest_gb300_planCompile(void* plan);
+/* Compile `plan` with the passes of the compiled plan `structure`, without a
+ * search: the same circuit with other angles (a variational loop, another
+ * Hamiltonian instance).  The gate lists must match gate by gate in qubits,
+ * and each gate of `plan` must be diagonal on at least the qubits where the
+ * structure's gate is.  Returns the number of passes, or -1. */
+int quest_gb300_planCompileLike(void* plan, void* structure);
 int quest_gb300_planNumGates(void* plan);
 /* Copy pass i (targets ascending, FP64 matrix); returns k or -1. */
 int quest_gb300_planPass(void* plan, int i, int* targets, double* re, double* im);

@@ -556,6 +556,15 @@ int quest_gb300_planCompile(void* plan) {
     return p->compiled ? (int)p->passes.size() : -1;
 }
 
+int quest_gb300_planCompileLike(void* plan, void* structure) {
+    FusedPlan* p = P(plan);
+    const FusedPlan* s = P(structure);
+    if (!p || !s || p == s) return -1;
+    if (p->device && p->deviceFree) p->deviceFree(p->device);
+    p->device = nullptr;
+    return qg::compilePlanLike(*p, *s) ? (int)p->passes.size() : -1;
+}
+
 int quest_gb300_planNumGates(void* plan) { return P(plan) ? (int)P(plan)->gates.size() : -1; }
 
 int quest_gb300_planPass(void* plan, int i, int* targets, double* re, double* im) {

@@ -203,6 +203,7 @@ SIGNATURES = {
     "quest_gb300_setTensorCoreKernel": (None, [_I]),
     "quest_gb300_setCapture": (_I, [_Q, _I]),
     "quest_gb300_hostMirrorPinned": (_I, [_Q]),
+    "quest_gb300_planCompileLike": (_I, [C.c_void_p, C.c_void_p]),
     "quest_gb300_trotterBatchCreate": (C.c_void_p, [_I, _I]),
     "quest_gb300_trotterBatchSetInstance": (_I, [C.c_void_p, _I, PauliHamil, C.c_double, _I, _I, C.c_longlong]),
     "quest_gb300_trotterBatchRun": (_I, [C.c_void_p, _P(C.c_double)]),

@@ -185,3 +185,47 @@ def test_invalid_gates_rejected(lib):
     assert lib.quest_gb300_planAddControlledNot(p, 1, 4) == -1
     lib.quest_gb300_planDestroy(p)
     assert lib.quest_gb300_planCreate(4, 7) is None
+
+
+def test_compile_like_reuses_the_passes_with_new_angles(lib):
+    """planCompileLike: the same circuit with other angles takes the passes of
+    a compiled plan without a search, and its pass products still reproduce
+    the new circuit exactly; a circuit of another shape is refused."""
+    L = lib
+    L.quest_gb300_planCompileLike.argtypes = [C.c_void_p, C.c_void_p]
+    n, kmax = 9, 4
+    ops_a = W.c2_circuit(n=n, layers=4, seed=21)
+    # the same gates on the same qubits, other angles
+    ops_b = [op if op[0] != "cu" else (op[0], op[1]) + tuple(np.roll(op[2:], 1)) for op in ops_a]
+    ops_b = [op if op[0] != "cp" else (op[0], op[1], op[2], op[3] + 0.7) for op in ops_b]
+
+    def build(ops):
+        p = L.quest_gb300_planCreate(n, kmax)
+        for op in ops:
+            if op[0] == "cu":
+                assert L.quest_gb300_planAddCompactUnitary(p, *op[1:]) == 0
+            elif op[0] == "cx":
+                assert L.quest_gb300_planAddControlledNot(p, op[1], op[2]) == 0
+            elif op[0] == "cp":
+                assert L.quest_gb300_planAddControlledPhaseShift(p, op[1], op[2], op[3]) == 0
+        return p
+
+    pa, pb = build(ops_a), build(ops_b)
+    na = L.quest_gb300_planCompile(pa)
+    assert na > 0
+    assert L.quest_gb300_planCompileLike(pb, pa) == na
+    psi = np.zeros(1 << n, dtype=complex)
+    psi[0] = 1
+    for i in range(na):
+        t = (C.c_int * 6)()
+        re, im = np.zeros(4096), np.zeros(4096)
+        k = L.quest_gb300_planPass(pb, i, t, re.ctypes.data_as(C.POINTER(C.c_double)), im.ctypes.data_as(C.POINTER(C.c_double)))
+        D = 1 << k
+        psi = apply_matrix(psi, n, list(t[:k]), (re[:D * D] + 1j * im[:D * D]).reshape(D, D))
+    want = reference(n, ops_b)
+    assert np.max(np.abs(psi - want)) < 1e-12
+    # another shape: one gate fewer
+    pc = build(ops_b[:-1])
+    assert L.quest_gb300_planCompileLike(pc, pa) == -1
+    for p in (pa, pb, pc):
+        L.quest_gb300_planDestroy(p)
