@@ -38,6 +38,11 @@ struct Capture {
     void* q32 = nullptr;          // FP32 scratch register of the flushes (kept between flushes)
     long long flushes = 0, gatesApplied = 0, passesApplied = 0;
     double compileMs = 0.0;       // host time spent planning the flushes
+    // The last searched plan (gates and passes, no device copy).  A flush of
+    // the same circuit shape (same qubits gate by gate, at least as diagonal:
+    // a repeated circuit, or new angles) takes its passes without a search.
+    FusedPlan* shape = nullptr;
+    long long shapeReuses = 0;
 };
 
 namespace {
@@ -121,7 +126,8 @@ static void flushRecord(Capture* c, double* re, double* im) {
     plan->maxFused = std::min(g_capMaxFused, widestPass(c->n));
     plan->gates.swap(c->gates);
     const auto t0 = std::chrono::steady_clock::now();
-    compilePlan(*plan);
+    const bool reused = c->shape && c->shape->maxFused == plan->maxFused && compilePlanLike(*plan, *c->shape);
+    if (!reused) compilePlan(*plan);
     c->compileMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (!plan->compiled) {
         invalidQuESTInputError("The captured gates could not be fused.", "captureFlush");
@@ -134,7 +140,17 @@ static void flushRecord(Capture* c, double* re, double* im) {
     c->gatesApplied += (long long)plan->gates.size();
     c->passesApplied += (long long)plan->passes.size();
     c->flushes += 1;
-    quest_gb300_planDestroy(plan);
+    if (reused) {
+        c->shapeReuses += 1;
+        quest_gb300_planDestroy(plan);
+    } else {
+        // keep the searched plan as the shape of the next flushes
+        if (plan->device && plan->deviceFree) plan->deviceFree(plan->device);
+        plan->device = nullptr;
+        plan->passes.clear();
+        if (c->shape) quest_gb300_planDestroy(c->shape);
+        c->shape = plan;
+    }
 }
 
 void captureFlush(double* re, double* im) {
@@ -166,6 +182,7 @@ void captureDrop(const double* re) {
     }
     if (c) {
         if (c->q32) quest_gb300_destroyQuregF32(c->q32);
+        if (c->shape) quest_gb300_planDestroy(c->shape);
         delete c;
     }
 }

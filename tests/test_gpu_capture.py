@@ -241,11 +241,15 @@ def test_capture_stats_count_the_flushes(gpulib):
     assert lib.quest_gb300_setCapture(q, 1) == 0
     ops = W.c2_circuit(n=n, layers=2, seed=4)
     queued = 0
+    states = []
     for _ in range(2):
         lib.initZeroState(q)
         W.run_ops(L, q, ops)
         queued += lib.quest_gb300_capturedGates(q)
         lib.calcTotalProb(q)
+        states.append(L.amps(q).copy())
+    # the second flush takes the first one's passes (same circuit shape)
+    assert np.max(np.abs(states[0] - states[1])) < 1e-6
     assert lib.quest_gb300_captureStats(q, C.byref(f), C.byref(g), C.byref(p), C.byref(ms)) == 0
     assert f.value == 2 and g.value == queued == 2 * len(ops)
     assert 2 <= p.value <= g.value and ms.value >= 0.0
