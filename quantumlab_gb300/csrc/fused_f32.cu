@@ -166,17 +166,38 @@ __global__ void kF64toF32(const double* __restrict__ sr, const double* __restric
     }
 }
 // FP32 -> FP64, each amplitude times *scale when scale is given
+// FP32 -> FP64 by moving the fields (exact, as the conversion instruction):
+// exponent rebiased by 1023 - 127 = 896, fraction shifted by 52 - 23 = 29.
+// Zeros too; subnormals, infinities and NaNs take the conversion
+// instruction.  GB300 runs that instruction on its FP64 pipe, which made the
+// conversion of a 30-qubit state FP64-bound.
+__device__ __forceinline__ double toF64(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xFFu;
+    const uint64_t sign = (uint64_t)(u >> 31) << 63;
+    if (e != 0u && e != 0xFFu)
+        return __longlong_as_double((long long)(sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(u & 0x7FFFFFu) << 29)));
+    if ((u & 0x7FFFFFFFu) == 0u) return __longlong_as_double((long long)sign);
+    return (double)f;
+}
 __global__ void kF32toF64(const float* __restrict__ sr, const float* __restrict__ si, double* __restrict__ dr,
                           double* __restrict__ di, uint64_t n, const double* __restrict__ scale) {
     const uint64_t i = 4 * ((uint64_t)blockIdx.x * kConvThreads + threadIdx.x);
-    const double s = scale ? *scale : 1.0;
     if (i + 3 < n) {
         const float4 r = *reinterpret_cast<const float4*>(sr + i), m = *reinterpret_cast<const float4*>(si + i);
-        *reinterpret_cast<double2*>(dr + i) = make_double2(r.x * s, r.y * s);
-        *reinterpret_cast<double2*>(dr + i + 2) = make_double2(r.z * s, r.w * s);
-        *reinterpret_cast<double2*>(di + i) = make_double2(m.x * s, m.y * s);
-        *reinterpret_cast<double2*>(di + i + 2) = make_double2(m.z * s, m.w * s);
+        double2 a = make_double2(toF64(r.x), toF64(r.y)), b = make_double2(toF64(r.z), toF64(r.w));
+        double2 c = make_double2(toF64(m.x), toF64(m.y)), d = make_double2(toF64(m.z), toF64(m.w));
+        if (scale) {
+            const double s = *scale;
+            a.x *= s; a.y *= s; b.x *= s; b.y *= s;
+            c.x *= s; c.y *= s; d.x *= s; d.y *= s;
+        }
+        *reinterpret_cast<double2*>(dr + i) = a;
+        *reinterpret_cast<double2*>(dr + i + 2) = b;
+        *reinterpret_cast<double2*>(di + i) = c;
+        *reinterpret_cast<double2*>(di + i + 2) = d;
     } else {
+        const double s = scale ? *scale : 1.0;
         for (uint64_t j = i; j < n; ++j) {
             dr[j] = (double)sr[j] * s;
             di[j] = (double)si[j] * s;
