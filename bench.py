@@ -45,12 +45,16 @@ def peaks():
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling during the timed region.  The samples go to
+    $QUEST_GB300_CLOCKS_DIR (default: the system temporary directory); the
+    bench line carries their summary."""
 
     def __init__(self, index: int = 0):
+        import tempfile
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        out_dir = os.environ.get("QUEST_GB300_CLOCKS_DIR", tempfile.gettempdir())
+        self.path = os.path.join(out_dir, f"quest_gb300_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
