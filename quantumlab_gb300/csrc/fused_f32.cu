@@ -40,6 +40,7 @@ struct QuregF32 {
 // tensor-core applier (fused_tc.cu): 1 applied, 0 not a tensor-core pass, -1 launch failed
 int applyPassTCIndexed(QuregF32& q, const FusedPass& p, const void* devPlan, size_t index, cudaStream_t st);
 void* uploadPlanTC(const FusedPlan& plan);
+bool tcImagesFit(const void* devPlan);
 void freePlanTC(void* d);
 int tcErrorFlag(const void* devPlan);
 int tcPassNorms(const void* devPlan, size_t index, double* out3);
@@ -436,6 +437,10 @@ int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPas
     if (!p->compiled) {
         invalidQuESTInputError("The fusion plan could not be compiled.", "applyPlanF32");
         return -1;
+    }
+    if (p->device && !qg::tcImagesFit(p->device)) {      // built for another precision or kernel
+        p->deviceFree(p->device);
+        p->device = nullptr;
     }
     if (!p->device) {
         p->device = qg::uploadPlanTC(*p);

@@ -36,7 +36,7 @@
 // Products.  A pass matrix is built in split real/imaginary planes.  Each
 // absorbed gate multiplies on from the left, using only its nonzero entries.
 // The inner loop runs over the D matrix columns.  Once the search has fixed
-// the passes, their products are independent and are shared among up to 8
+// the passes, their products are independent and are shared among up to 16
 // host threads.
 #include "fused_plan.h"
 #include "quest_gb300.h"
@@ -395,7 +395,7 @@ void compilePlan(FusedPlan& plan) {
         for (size_t i; (i = nextPass.fetch_add(1)) < np;) buildPass(plan, sets[i], members[i], plan.passes[i]);
     };
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const unsigned nt = (unsigned)std::min<size_t>({(size_t)std::min(hw, 8u), np, 1 + plan.gates.size() / 64});
+    const unsigned nt = (unsigned)std::min<size_t>({(size_t)std::min(hw, 16u), np, 1 + plan.gates.size() / 64});
     std::vector<std::thread> pool;
     for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
     work();
@@ -424,7 +424,7 @@ bool compilePlanLike(FusedPlan& plan, const FusedPlan& structure) {
             buildPass(plan, plan.passSets[i], plan.passMembers[i], plan.passes[i]);
     };
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const unsigned nt = (unsigned)std::min<size_t>({(size_t)std::min(hw, 8u), np, 1 + plan.gates.size() / 64});
+    const unsigned nt = (unsigned)std::min<size_t>({(size_t)std::min(hw, 16u), np, 1 + plan.gates.size() / 64});
     std::vector<std::thread> pool;
     for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
     work();

@@ -976,6 +976,7 @@ struct DevicePlan {
     // per pass: 1 if its matrix is unitary to 1e-10.  Only the drift of a
     // unitary pass is corrected; a non-unitary pass changes the norm on purpose.
     std::vector<char> unitary;
+    int parts = 0;          // the image parts built (kPart*)
 };
 
 // Canonical no-swizzle K-major image of an N x K operand (rows r, K index j):
@@ -1190,12 +1191,22 @@ static size_t imageFloats(int k) {
     const size_t tf32Compact = (k == 6) ? 2 * 3 * D * D : 0;
     return (2 * full + (3 * bEntries + 1) / 2 + tf32Compact + 3) & ~(size_t)3;     // 16-byte multiple
 }
-static void buildImage(const FusedPass& pass, float* img) {
+// Parts of an image: what the split-TF32 pipelined kernels read (the full
+// real form at k <= 5, the compact form at k = 6), what the split-BF16 ones
+// read, and the full TF32 form at every k for the direct-load kernel.
+constexpr int kPartTF32 = 1, kPartBF16 = 2, kPartDirect = 4;
+static void buildImage(const FusedPass& pass, float* img, int parts) {
     const int k = (int)pass.targets.size();
     const int D = 1 << k, K = 2 * D, N = 2 * D;
+    const bool full = (parts & kPartDirect) || ((parts & kPartTF32) && k <= 5);
+    const bool compact = (parts & kPartTF32) && k == 6;
     // real form [[Re, -Im], [Im, Re]] as B = Gr (rows r = output index, K index j)
-    std::vector<float> hi((size_t)N * K), lo((size_t)N * K);
-    for (int r = 0; r < N; ++r)
+    std::vector<float> hi, lo;
+    if (full || compact) {
+        hi.resize((size_t)N * K);
+        lo.resize((size_t)N * K);
+    }
+    for (int r = 0; r < N && (full || compact); ++r)
         for (int j = 0; j < K; ++j) {
             const cplx g = pass.m[(size_t)(r % D) * D + (j % D)];
             double v;
@@ -1207,15 +1218,17 @@ static void buildImage(const FusedPass& pass, float* img) {
         }
     // then the three BF16 parts of the pipelined kernel: the real form, or
     // at k = 6 the compact form [-Im G; Re G; Im G] (3D rows, D K columns)
-    const size_t full = (size_t)N * K;
+    const size_t fullN = (size_t)N * K;
     const int bRows = (k == 6) ? 3 * D : N, bK = (k == 6) ? D : K;
     const size_t bEntries = (size_t)bRows * bK;
-    packKMajor(hi, N, K, img);
-    packKMajor(lo, N, K, img + full);
-    uint16_t* bh = reinterpret_cast<uint16_t*>(img + 2 * full);
+    if (full) {
+        packKMajor(hi, N, K, img);
+        packKMajor(lo, N, K, img + fullN);
+    }
+    uint16_t* bh = reinterpret_cast<uint16_t*>(img + 2 * fullN);
     uint16_t* bl = bh + bEntries;
     uint16_t* bll = bl + bEntries;
-    for (int r = 0; r < bRows; ++r)
+    for (int r = 0; r < bRows && (parts & kPartBF16); ++r)
         for (int j = 0; j < bK; ++j) {
             // k = 6: rows 0..D-1 take the (r, D + j) entries of the real form
             // (-Im), rows D..3D-1 the (r - D, j) entries (Re, then Im)
@@ -1230,7 +1243,7 @@ static void buildImage(const FusedPass& pass, float* img) {
             bl[at] = l;
             bll[at] = hostBF16RN((float)(r1 - (double)bf16Value(l)));
         }
-    if (k == 6) {
+    if (compact) {
         // the compact TF32 form for the split-TF32 pipelined kernel
         std::vector<float> ch((size_t)3 * D * D), cl((size_t)3 * D * D);
         for (int r = 0; r < 3 * D; ++r)
@@ -1239,16 +1252,25 @@ static void buildImage(const FusedPass& pass, float* img) {
                 ch[(size_t)r * D + j] = hi[(size_t)rr * K + jj];
                 cl[(size_t)r * D + j] = lo[(size_t)rr * K + jj];
             }
-        float* const tc = img + 2 * full + (3 * bEntries + 1) / 2;
+        float* const tc = img + 2 * fullN + (3 * bEntries + 1) / 2;
         packKMajor(ch, 3 * D, D, tc);
         packKMajor(cl, 3 * D, D, tc + (size_t)3 * D * D);
     }
 }
 
-// Operand images of every tensor-core pass, built on up to 8 host threads
-// and uploaded in one allocation and one copy.
+// the image parts the kernels of the current precision and kernel choice read
+static int currentParts() {
+    return (g_tcPrecision == kPrecBF16 ? kPartBF16 : kPartTF32) | (g_tcVersion == 1 ? kPartDirect : 0);
+}
+
+// Operand images of every tensor-core pass: the parts the current precision
+// and kernel choice read (tcImagesFit tells when they no longer suffice),
+// built on up to 16 host threads and uploaded in one allocation and one copy.
+// A 6-qubit image holds ~300 KB; building all of its parts took ~0.4 ms of
+// host time, most of a small register's flush.
 void* uploadPlanTC(const FusedPlan& plan) {
     DevicePlan* dp = new DevicePlan();
+    dp->parts = currentParts();
     if (cudaMalloc(&dp->errFlag, sizeof(int)) != cudaSuccess) {
         cudaGetLastError();
         delete dp;
@@ -1274,9 +1296,9 @@ void* uploadPlanTC(const FusedPlan& plan) {
     std::atomic<size_t> next{0};
     auto work = [&]() {
         for (size_t i; (i = next.fetch_add(1)) < np;)
-            if (offset[i + 1] > offset[i]) buildImage(plan.passes[i], host.data() + offset[i]);
+            if (offset[i + 1] > offset[i]) buildImage(plan.passes[i], host.data() + offset[i], dp->parts);
     };
-    const unsigned nt = (unsigned)std::min<size_t>({(size_t)8, (size_t)std::max(1u, std::thread::hardware_concurrency()), np});
+    const unsigned nt = (unsigned)std::min<size_t>({(size_t)16, (size_t)std::max(1u, std::thread::hardware_concurrency()), np});
     std::vector<std::thread> pool;
     for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
     work();
@@ -1295,7 +1317,13 @@ void* uploadPlanTC(const FusedPlan& plan) {
 // The tensor-core operands of one pass, as uploadPlanTC lays them out: the
 // number of floats, and the image itself.
 size_t tcImageFloats(int k) { return imageFloats(k); }
-void tcBuildImage(const FusedPass& pass, float* img) { buildImage(pass, img); }
+void tcBuildImage(const FusedPass& pass, float* img) { buildImage(pass, img, currentParts()); }
+// whether a plan's images hold the parts the current precision and kernel
+// choice read (else the caller uploads the plan again)
+bool tcImagesFit(const void* devPlan) {
+    const DevicePlan* dp = reinterpret_cast<const DevicePlan*>(devPlan);
+    return dp && (currentParts() & ~dp->parts) == 0;
+}
 
 void freePlanTC(void* h) {
     DevicePlan* dp = reinterpret_cast<DevicePlan*>(h);

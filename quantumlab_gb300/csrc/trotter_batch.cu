@@ -417,7 +417,7 @@ bool compileBatch(TrotterBatch* b) {
                 tcBuildImage(widenTo4(plans[k].passes[p], n), host.data() + b->imgOffset[p] + k * b->imgStride[p]);
             }
         };
-        const unsigned nt = (unsigned)std::min<size_t>({(size_t)8, (size_t)std::max(1u, std::thread::hardware_concurrency()), jobs});
+        const unsigned nt = (unsigned)std::min<size_t>({(size_t)16, (size_t)std::max(1u, std::thread::hardware_concurrency()), jobs});
         std::vector<std::thread> pool;
         for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
         work();
