@@ -37,6 +37,26 @@ def swap_test_cost(dim_log2: np.ndarray) -> np.ndarray:
     return np.ldexp(1.0, 2 * np.asarray(dim_log2, dtype=np.int64) + 1)
 
 
+def trotter_instance_cost(steps: Sequence[int], order: Sequence[int]) -> np.ndarray:
+    """Relative cost of a Trotter instance (same register size): its fused
+    passes grow with the Pauli exponentials, steps x 1 at first order and
+    steps x 2 at second (the symmetrised product applies every term twice)."""
+    steps = np.asarray(steps, dtype=np.float64)
+    order = np.asarray(order, dtype=np.int64)
+    return steps * np.where(order == 1, 1.0, 2.0)
+
+
+def trotter_batches(shapes: Sequence[tuple], indices: Sequence[int]) -> list:
+    """Group a rank's Trotter instances into batches of one shape: the
+    instances of a batch (quest_gb300_trotterBatch*) must share Pauli strings,
+    order and steps.  `shapes[i]` is instance i's shape key; returns lists of
+    instance indices, in order of first appearance."""
+    groups: dict = {}
+    for i in indices:
+        groups.setdefault(shapes[i], []).append(int(i))
+    return list(groups.values())
+
+
 def gather_to_rank0(indices: np.ndarray, values: np.ndarray, total: int, world: int):
     """Assemble the per-unit results of all ranks into one array on rank 0
     (None on the others).  world == 1 needs no process group."""

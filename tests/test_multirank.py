@@ -65,3 +65,28 @@ def test_shards_partition_the_units():
         assert np.array_equal(allidx, np.arange(len(costs)))
         loads = [costs[p].sum() for p in parts]
         assert max(loads) - min(loads) <= costs.max()
+
+
+@pytest.mark.parametrize("world", [2, 4])
+def test_trotter_instances_shard_into_same_shape_batches(world):
+    """The 64 Fermi-Hubbard instances of configuration 4 are dealt to ranks by
+    cost; each rank's share falls into batches of one shape (order and step
+    count), which is what a Trotter batch accepts."""
+    from quantumlab_gb300 import workloads as W
+    from quantumlab_gb300.sharding import shard_units, trotter_batches, trotter_instance_cost
+
+    inst = W.hubbard_instances(64)
+    steps = [int(round(1.0 / dt)) for _, dt, _ in inst]
+    order = [o for _, _, o in inst]
+    cost = trotter_instance_cost(steps, order)
+    shapes = [(o, s) for o, s in zip(order, steps)]
+    seen = []
+    loads = []
+    for rank in range(world):
+        mine = shard_units(cost, world, rank)
+        loads.append(cost[mine].sum())
+        for batch in trotter_batches(shapes, mine):
+            assert len({shapes[i] for i in batch}) == 1
+            seen += batch
+    assert sorted(seen) == list(range(64))
+    assert max(loads) - min(loads) <= cost.max()
