@@ -23,14 +23,7 @@
 #ifndef QUEST_H
 #define QUEST_H
 
-#ifndef QuEST_PREC
-#define QuEST_PREC 2
-#endif
-#if QuEST_PREC != 2
-#error "this library is built for QuEST_PREC=2 (qreal = double) only"
-#endif
-typedef double qreal;
-#define REAL_EPS 1e-13
+#include "QuEST_precision.h"
 
 #ifndef M_PI
 #define M_PI 3.1415926535897932384626433832795028841971
@@ -48,6 +41,12 @@ void invalidQuESTInputError(const char* errMsg, const char* errFunc);
 /* ---- value types (reference QuEST.h:87-400; layouts must match) ---- */
 enum phaseGateType {SIGMA_Z = 0, S_GATE = 1, T_GATE = 2};
 enum pauliOpType {PAULI_I = 0, PAULI_X = 1, PAULI_Y = 2, PAULI_Z = 3};
+enum phaseFunc {
+    NORM = 0, SCALED_NORM = 1, INVERSE_NORM = 2, SCALED_INVERSE_NORM = 3, SCALED_INVERSE_SHIFTED_NORM = 4,
+    PRODUCT = 5, SCALED_PRODUCT = 6, INVERSE_PRODUCT = 7, SCALED_INVERSE_PRODUCT = 8,
+    DISTANCE = 9, SCALED_DISTANCE = 10, INVERSE_DISTANCE = 11, SCALED_INVERSE_DISTANCE = 12,
+    SCALED_INVERSE_SHIFTED_DISTANCE = 13};
+enum bitEncoding {UNSIGNED = 0, TWOS_COMPLEMENT = 1};
 
 typedef struct {
     char* buffer;
@@ -224,17 +223,69 @@ qreal calcExpecPauliProd(Qureg qureg, int* targetQubits, enum pauliOpType* pauli
 qreal calcExpecPauliSum(Qureg qureg, enum pauliOpType* allPauliCodes, qreal* termCoeffs, int numSumTerms, Qureg workspace);
 qreal calcExpecPauliHamil(Qureg qureg, PauliHamil hamil, Qureg workspace);
 
-/* ---- decoherence (QuEST.c:1259-1310) ---- */
+/* ---- decoherence (QuEST.c:1259-1322; reference QuEST.h:3620-3850) ---- */
 void mixDephasing(Qureg qureg, int targetQubit, qreal prob);
 void mixDepolarising(Qureg qureg, int targetQubit, qreal prob);
 void mixDamping(Qureg qureg, int targetQubit, qreal prob);
 void mixDensityMatrix(Qureg combineQureg, qreal prob, Qureg otherQureg);
+void mixTwoQubitDephasing(Qureg qureg, int qubit1, int qubit2, qreal prob);      /* QuEST.c:1269 */
+void mixTwoQubitDepolarising(Qureg qureg, int qubit1, int qubit2, qreal prob);   /* QuEST.c:1300 */
+void mixPauli(Qureg qureg, int targetQubit, qreal probX, qreal probY, qreal probZ);   /* QuEST.c:1312 */
 
 /* ---- QASM recording: accepted and ignored (QuEST.c:92-113) ---- */
 void startRecordingQASM(Qureg qureg);
 void stopRecordingQASM(Qureg qureg);
 void clearRecordedQASM(Qureg qureg);
 void printRecordedQASM(Qureg qureg);
+void writeRecordedQASMToFile(Qureg qureg, char* filename);
+
+/* ---- reports (reference QuEST.h:1317-1358; plain-text output) ---- */
+void reportState(Qureg qureg);
+void reportStateToScreen(Qureg qureg, QuESTEnv env, int reportRank);
+void reportQuregParams(Qureg qureg);
+void reportPauliHamil(PauliHamil hamil);
+
+/* ---- the rest of the reference API (QuEST.h:800-6900).  These are exported
+ * so that any program written against QuEST 3.4 links; QuantumLab calls none
+ * of them.  Each reports "unsupported" through invalidQuESTInputError and
+ * returns a zeroed value where it has one. ---- */
+void mixKrausMap(Qureg qureg, int target, ComplexMatrix2* ops, int numOps);
+void mixTwoQubitKrausMap(Qureg qureg, int target1, int target2, ComplexMatrix4* ops, int numOps);
+void mixMultiQubitKrausMap(Qureg qureg, int* targets, int numTargets, ComplexMatrixN* ops, int numOps);
+void mixNonTPKrausMap(Qureg qureg, int target, ComplexMatrix2* ops, int numOps);
+void mixNonTPTwoQubitKrausMap(Qureg qureg, int target1, int target2, ComplexMatrix4* ops, int numOps);
+void mixNonTPMultiQubitKrausMap(Qureg qureg, int* targets, int numTargets, ComplexMatrixN* ops, int numOps);
+void applyPauliSum(Qureg inQureg, enum pauliOpType* allPauliCodes, qreal* termCoeffs, int numSumTerms, Qureg outQureg);
+void applyPauliHamil(Qureg inQureg, PauliHamil hamil, Qureg outQureg);
+void applyMultiControlledMatrixN(Qureg qureg, int* ctrls, int numCtrls, int* targs, int numTargs, ComplexMatrixN u);
+void applyProjector(Qureg qureg, int qubit, int outcome);
+void applyQFT(Qureg qureg, int* qubits, int numQubits);
+void applyFullQFT(Qureg qureg);
+void applyPhaseFunc(Qureg qureg, int* qubits, int numQubits, enum bitEncoding encoding, qreal* coeffs, qreal* exponents, int numTerms);
+void applyPhaseFuncOverrides(Qureg qureg, int* qubits, int numQubits, enum bitEncoding encoding, qreal* coeffs, qreal* exponents, int numTerms, long long int* overrideInds, qreal* overridePhases, int numOverrides);
+void applyMultiVarPhaseFunc(Qureg qureg, int* qubits, int* numQubitsPerReg, int numRegs, enum bitEncoding encoding, qreal* coeffs, qreal* exponents, int* numTermsPerReg);
+void applyMultiVarPhaseFuncOverrides(Qureg qureg, int* qubits, int* numQubitsPerReg, int numRegs, enum bitEncoding encoding, qreal* coeffs, qreal* exponents, int* numTermsPerReg, long long int* overrideInds, qreal* overridePhases, int numOverrides);
+void applyNamedPhaseFunc(Qureg qureg, int* qubits, int* numQubitsPerReg, int numRegs, enum bitEncoding encoding, enum phaseFunc functionNameCode);
+void applyNamedPhaseFuncOverrides(Qureg qureg, int* qubits, int* numQubitsPerReg, int numRegs, enum bitEncoding encoding, enum phaseFunc functionNameCode, long long int* overrideInds, qreal* overridePhases, int numOverrides);
+void applyParamNamedPhaseFunc(Qureg qureg, int* qubits, int* numQubitsPerReg, int numRegs, enum bitEncoding encoding, enum phaseFunc functionNameCode, qreal* params, int numParams);
+void applyParamNamedPhaseFuncOverrides(Qureg qureg, int* qubits, int* numQubitsPerReg, int numRegs, enum bitEncoding encoding, enum phaseFunc functionNameCode, qreal* params, int numParams, long long int* overrideInds, qreal* overridePhases, int numOverrides);
+DiagonalOp createDiagonalOp(int numQubits, QuESTEnv env);
+DiagonalOp createDiagonalOpFromPauliHamilFile(char* fn, QuESTEnv env);
+void destroyDiagonalOp(DiagonalOp op, QuESTEnv env);
+void syncDiagonalOp(DiagonalOp op);
+void initDiagonalOp(DiagonalOp op, qreal* real, qreal* imag);
+void initDiagonalOpFromPauliHamil(DiagonalOp op, PauliHamil hamil);
+void setDiagonalOpElems(DiagonalOp op, long long int startInd, qreal* real, qreal* imag, long long int numElems);
+void applyDiagonalOp(Qureg qureg, DiagonalOp op);
+Complex calcExpecDiagonalOp(Qureg qureg, DiagonalOp op);
+PauliHamil createPauliHamilFromFile(char* fn);
+#ifndef __cplusplus
+/* C only, as in the reference (QuEST.h:776-802, 5687-5733): the matrices are
+ * variable-length 2D arrays of 2^numQubits columns.  Implemented. */
+void initComplexMatrixN(ComplexMatrixN m, qreal real[][1 << m.numQubits], qreal imag[][1 << m.numQubits]);
+ComplexMatrixN bindArraysToStackComplexMatrixN(int numQubits, qreal re[][1 << numQubits], qreal im[][1 << numQubits],
+                                               qreal** reStorage, qreal** imStorage);
+#endif
 
 #ifdef __cplusplus
 }

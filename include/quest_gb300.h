@@ -177,15 +177,18 @@ int quest_gb300_initProductState(Qureg qureg, int numRegs, const int* regQubits,
 int quest_gb300_sampleMeasurements(Qureg qureg, const int* qubits, int numQubits, int numShots, int* outcomes);
 
 /* ---- batched Trotter instances ----------------------------------------------
- * B Hamiltonian instances on n = 11..34 qubits that share Pauli strings,
- * Trotter order and repetitions (coefficients, time and the classical start
- * state may differ) evolve together: one fusion plan (searched on instance 0,
- * reused with each instance's FP64 products), one tensor-core launch per
- * fused pass over all B FP32 states, and a CUDA graph replayed after the
- * first run.  The gates are QuEST's applyTrotterCircuit(hamil, time, order,
- * reps) from initClassicalState(init).  Energies are <H> / <psi|psi> of each
- * final FP32 state (FP32 products, FP64 sums).  Errors go through
- * invalidQuESTInputError; functions return 0 or -1.                          */
+ * B Hamiltonian instances of 11..numQubits qubits (numQubits <= 34) evolve
+ * together as FP32 states.  Instances that share register size, Pauli
+ * strings, Trotter order and repetitions form a class (coefficients, time and
+ * the classical start state may differ): one fusion plan per class (searched
+ * on one member, reused with each member's FP64 products) and one
+ * tensor-core launch per fused pass over all the class's states.  Classes of
+ * different step counts, orders, sizes or Hamiltonians run one after another
+ * in the same run, and after the first run the whole batch is a CUDA graph
+ * that later runs replay.  The gates are QuEST's applyTrotterCircuit(hamil,
+ * time, order, reps) from initClassicalState(init).  Energies are
+ * <H> / <psi|psi> of each final FP32 state (FP32 products, FP64 sums).
+ * Errors go through invalidQuESTInputError; functions return 0 or -1.       */
 void* quest_gb300_trotterBatchCreate(int numQubits, int numInstances);
 int quest_gb300_trotterBatchSetInstance(void* batch, int instance, PauliHamil hamil, double time, int order, int reps,
                                         long long initClassicalState);
@@ -194,8 +197,11 @@ int quest_gb300_trotterBatchRun(void* batch, double* energies);
 /* Copy instance `instance`'s final state into an FP64 register of n qubits,
  * scaled to norm 1 (the start state's) by the norm the last run measured. */
 int quest_gb300_trotterBatchCopyState(void* batch, int instance, Qureg dst);
-/* Fused passes per run (after the first run), else -1. */
+/* Fused-pass launches per run, summed over the classes (after the first
+ * run), else -1. */
 int quest_gb300_trotterBatchNumPasses(void* batch);
+/* Classes of the batch (after the first run), else -1. */
+int quest_gb300_trotterBatchNumClasses(void* batch);
 void quest_gb300_trotterBatchDestroy(void* batch);
 
 /* ---- total probability without allocating ---------------------------------
@@ -207,10 +213,13 @@ void quest_gb300_trotterBatchDestroy(void* batch);
  * cudaMalloc, cudaFree or allocating library call.  Scratch is a fixed
  * __device__ array of about 16.5 KB per GPU, so numAmps must be a power of two
  * in [2, 2^27]; larger states are rejected with an error (use calcTotalProb).
+ * Both arrays must start on a 16-byte boundary (they are read two doubles at
+ * a time); a misaligned pointer is rejected before anything is queued.
  * The result is written to *result (host or device memory) and the call
  * returns after `stream` (a cudaStream_t; NULL = legacy default stream) has
- * finished it.  The first call on a device looks up the scratch address and
- * should come before any stream capture.  All calls share the scratch: calls
+ * finished it.  The first call on a device looks up the scratch address (a
+ * failed lookup is retried by the next call) and should come before any
+ * stream capture.  All calls share the scratch: calls
  * that overlap on the GPU race.  Returns 0 on success, nonzero after
  * reporting the error through invalidQuESTInputError.                       */
 int quest_gb300_calcTotalProbNoAlloc(const double* deviceReal, const double* deviceImag, long long numAmps,

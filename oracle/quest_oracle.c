@@ -912,6 +912,92 @@ void mixDamping(Qureg q, int t, qreal prob) {                                   
         }
     }
 }
+/* mixPauli: the Kraus map {sqrt(1-pX-pY-pZ) I, sqrt(pX) X, sqrt(pY) Y,
+ * sqrt(pZ) Z} (QuEST_common.c:740-759), applied as its superoperator
+ * S = sum_k conj(K_k) (x) K_k on (row qubit t, column qubit t + N)
+ * (QuEST_common.c:590-640 populateKrausSuperOperator2 + the 2-qubit matrix
+ * pass): local index r + 2c, out = S in. */
+void mixPauli(Qureg q, int t, qreal pX, qreal pY, qreal pZ) {                    /* QuEST.c:1312 */
+    CHECK(q.isDensityMatrix, "Operation valid only for density matrices.");
+    CHECK(validTarget(q, t), "Invalid target qubit. Must be >=0 and <numQubits.");
+    CHECK(pX >= 0 && pX <= 1 && pY >= 0 && pY <= 1 && pZ >= 0 && pZ <= 1, "Probabilities must be in [0, 1].");
+    qreal none = 1 - pX - pY - pZ;
+    CHECK(pX <= none && pY <= none && pZ <= none,
+          "The probability of any X, Y or Z error cannot exceed the probability of no error.");
+    qreal f[4] = {sqrt(none), sqrt(pX), sqrt(pY), sqrt(pZ)};
+    /* K[k][r][c] as complex (re, im) */
+    qreal Kr[4][2][2] = {{{f[0], 0}, {0, f[0]}}, {{0, f[1]}, {f[1], 0}}, {{0, 0}, {0, 0}}, {{f[3], 0}, {0, -f[3]}}};
+    qreal Ki[4][2][2] = {{{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}, {{0, -f[2]}, {f[2], 0}}, {{0, 0}, {0, 0}}};
+    qreal Sr[4][4] = {{0}}, Si[4][4] = {{0}};
+    for (int k = 0; k < 4; k++)
+        for (int r = 0; r < 2; r++) for (int c = 0; c < 2; c++)
+            for (int r2 = 0; r2 < 2; r2++) for (int c2 = 0; c2 < 2; c2++) {
+                /* K[r][r2] * conj(K[c][c2]) */
+                qreal ar = Kr[k][r][r2], ai = Ki[k][r][r2], br = Kr[k][c][c2], bi = -Ki[k][c][c2];
+                Sr[r + 2 * c][r2 + 2 * c2] += ar * br - ai * bi;
+                Si[r + 2 * c][r2 + 2 * c2] += ar * bi + ai * br;
+            }
+    int s = q.numQubitsRepresented;
+    idx_t rb = 1LL << t, cb = 1LL << (t + s);
+#pragma omp parallel for schedule(static)
+    for (idx_t g = 0; g < q.numAmpsTotal / 4; g++) {
+        idx_t b = ins0(ins0(g, t), t + s);
+        idx_t ix[4] = {b, b | rb, b | cb, b | rb | cb};
+        qreal xr[4], xi[4];
+        for (int j = 0; j < 4; j++) { xr[j] = q.stateVec.real[ix[j]]; xi[j] = q.stateVec.imag[ix[j]]; }
+        for (int r = 0; r < 4; r++) {
+            qreal yr = 0, yi = 0;
+            for (int j = 0; j < 4; j++) { yr += Sr[r][j] * xr[j] - Si[r][j] * xi[j]; yi += Sr[r][j] * xi[j] + Si[r][j] * xr[j]; }
+            q.stateVec.real[ix[r]] = yr; q.stateVec.imag[ix[r]] = yi;
+        }
+    }
+}
+/* Entries whose row and column bits differ on qubit q1 or on qubit q2 are
+ * scaled by 1 - 4p/3 (QuEST.c:1269 -> QuEST_cpu.c:97-136). */
+void mixTwoQubitDephasing(Qureg q, int q1, int q2, qreal prob) {
+    CHECK(q.isDensityMatrix, "Operation valid only for density matrices.");
+    CHECK(validTarget(q, q1) && validTarget(q, q2), "Invalid target qubit. Must be >=0 and <numQubits.");
+    CHECK(q1 != q2, "The target qubits must be unique.");
+    CHECK(prob >= 0 && prob <= 1, "Probabilities must be in [0, 1].");
+    CHECK(prob <= 3 / 4.0, "The probability of a two-qubit qubit dephase error cannot exceed 3/4, which maximally mixes.");
+    qreal retain = 1 - (4 * prob) / 3.0;
+    int s = q.numQubitsRepresented;
+    idx_t m1 = (1LL << q1) | (1LL << (q1 + s)), m2 = (1LL << q2) | (1LL << (q2 + s));
+#pragma omp parallel for schedule(static)
+    for (idx_t i = 0; i < q.numAmpsTotal; i++) {
+        idx_t a = i & m1, b = i & m2;
+        if ((a != 0 && a != m1) || (b != 0 && b != m2)) { q.stateVec.real[i] *= retain; q.stateVec.imag[i] *= retain; }
+    }
+}
+/* Level l = 16p/15: every entry is scaled by 1 - l, and each of the four
+ * entries whose row and column bits agree on both qubits gains l/4 times the
+ * sum of the four (QuEST.c:1300 -> QuEST_gpu.cu:3080-3147: the dephasing
+ * launch, then the averaging launch). */
+void mixTwoQubitDepolarising(Qureg q, int q1, int q2, qreal prob) {
+    CHECK(q.isDensityMatrix, "Operation valid only for density matrices.");
+    CHECK(validTarget(q, q1) && validTarget(q, q2), "Invalid target qubit. Must be >=0 and <numQubits.");
+    CHECK(q1 != q2, "The target qubits must be unique.");
+    CHECK(prob >= 0 && prob <= 1, "Probabilities must be in [0, 1].");
+    CHECK(prob <= 15 / 16.0, "The probability of a two-qubit depolarising error cannot exceed 15/16, which maximally mixes.");
+    qreal lvl = (16 * prob) / 15.0, retain = 1 - lvl;
+    if (lvl == 0) return;
+    int s = q.numQubitsRepresented;
+    idx_t c1 = (1LL << q1) | (1LL << (q1 + s)), c2 = (1LL << q2) | (1LL << (q2 + s));
+#pragma omp parallel for schedule(static)
+    for (idx_t i = 0; i < q.numAmpsTotal; i++) {
+        idx_t a = i & c1, b = i & c2;
+        if ((a != 0 && a != c1) || (b != 0 && b != c2)) { q.stateVec.real[i] *= retain; q.stateVec.imag[i] *= retain; }
+        else if (a == 0 && b == 0) {
+            idx_t j[4] = {i, i | c1, i | c2, i | c1 | c2};
+            qreal sr = lvl * 0.25 * (q.stateVec.real[j[0]] + q.stateVec.real[j[1]] + q.stateVec.real[j[2]] + q.stateVec.real[j[3]]);
+            qreal si = lvl * 0.25 * (q.stateVec.imag[j[0]] + q.stateVec.imag[j[1]] + q.stateVec.imag[j[2]] + q.stateVec.imag[j[3]]);
+            for (int k = 0; k < 4; k++) {
+                q.stateVec.real[j[k]] = q.stateVec.real[j[k]] * retain + sr;
+                q.stateVec.imag[j[k]] = q.stateVec.imag[j[k]] * retain + si;
+            }
+        }
+    }
+}
 void mixDensityMatrix(Qureg a, qreal p, Qureg b) {                                /* QuEST_cpu.c:908 */
 #pragma omp parallel for schedule(static)
     for (idx_t i = 0; i < a.numAmpsTotal; i++) {
@@ -924,3 +1010,64 @@ void startRecordingQASM(Qureg q) { (void)q; }
 void stopRecordingQASM(Qureg q) { (void)q; }
 void clearRecordedQASM(Qureg q) { (void)q; }
 void printRecordedQASM(Qureg q) { (void)q; }
+void writeRecordedQASMToFile(Qureg q, char* f) { (void)q; (void)f; }
+void reportState(Qureg q) { (void)q; }
+void reportStateToScreen(Qureg q, QuESTEnv env, int r) { (void)q; (void)env; (void)r; }
+void reportQuregParams(Qureg q) { (void)q; }
+void reportPauliHamil(PauliHamil h) { (void)h; }
+
+/* The rest of the API: exported so that the oracle and the product export
+ * the same symbols; each reports that it is unsupported. */
+#define UNSUP() fail("This QuEST function is not supported by the GB300 library (unsupported).", __func__)
+void mixKrausMap(Qureg q, int t, ComplexMatrix2* o, int n) { (void)q; (void)t; (void)o; (void)n; UNSUP(); }
+void mixTwoQubitKrausMap(Qureg q, int a, int b, ComplexMatrix4* o, int n) { (void)q; (void)a; (void)b; (void)o; (void)n; UNSUP(); }
+void mixMultiQubitKrausMap(Qureg q, int* t, int k, ComplexMatrixN* o, int n) { (void)q; (void)t; (void)k; (void)o; (void)n; UNSUP(); }
+void mixNonTPKrausMap(Qureg q, int t, ComplexMatrix2* o, int n) { (void)q; (void)t; (void)o; (void)n; UNSUP(); }
+void mixNonTPTwoQubitKrausMap(Qureg q, int a, int b, ComplexMatrix4* o, int n) { (void)q; (void)a; (void)b; (void)o; (void)n; UNSUP(); }
+void mixNonTPMultiQubitKrausMap(Qureg q, int* t, int k, ComplexMatrixN* o, int n) { (void)q; (void)t; (void)k; (void)o; (void)n; UNSUP(); }
+void applyPauliSum(Qureg a, enum pauliOpType* c, qreal* w, int n, Qureg b) { (void)a; (void)c; (void)w; (void)n; (void)b; UNSUP(); }
+void applyPauliHamil(Qureg a, PauliHamil h, Qureg b) { (void)a; (void)h; (void)b; UNSUP(); }
+void applyMultiControlledMatrixN(Qureg q, int* c, int nc, int* t, int nt, ComplexMatrixN u) { (void)q; (void)c; (void)nc; (void)t; (void)nt; (void)u; UNSUP(); }
+void applyProjector(Qureg q, int t, int o) { (void)q; (void)t; (void)o; UNSUP(); }
+void applyQFT(Qureg q, int* t, int n) { (void)q; (void)t; (void)n; UNSUP(); }
+void applyFullQFT(Qureg q) { (void)q; UNSUP(); }
+void applyPhaseFunc(Qureg q, int* t, int n, enum bitEncoding e, qreal* c, qreal* x, int m) { (void)q; (void)t; (void)n; (void)e; (void)c; (void)x; (void)m; UNSUP(); }
+void applyPhaseFuncOverrides(Qureg q, int* t, int n, enum bitEncoding e, qreal* c, qreal* x, int m, long long* oi, qreal* op, int no) {
+    (void)q; (void)t; (void)n; (void)e; (void)c; (void)x; (void)m; (void)oi; (void)op; (void)no; UNSUP();
+}
+void applyMultiVarPhaseFunc(Qureg q, int* t, int* r, int nr, enum bitEncoding e, qreal* c, qreal* x, int* m) {
+    (void)q; (void)t; (void)r; (void)nr; (void)e; (void)c; (void)x; (void)m; UNSUP();
+}
+void applyMultiVarPhaseFuncOverrides(Qureg q, int* t, int* r, int nr, enum bitEncoding e, qreal* c, qreal* x, int* m, long long* oi, qreal* op, int no) {
+    (void)q; (void)t; (void)r; (void)nr; (void)e; (void)c; (void)x; (void)m; (void)oi; (void)op; (void)no; UNSUP();
+}
+void applyNamedPhaseFunc(Qureg q, int* t, int* r, int nr, enum bitEncoding e, enum phaseFunc f) { (void)q; (void)t; (void)r; (void)nr; (void)e; (void)f; UNSUP(); }
+void applyNamedPhaseFuncOverrides(Qureg q, int* t, int* r, int nr, enum bitEncoding e, enum phaseFunc f, long long* oi, qreal* op, int no) {
+    (void)q; (void)t; (void)r; (void)nr; (void)e; (void)f; (void)oi; (void)op; (void)no; UNSUP();
+}
+void applyParamNamedPhaseFunc(Qureg q, int* t, int* r, int nr, enum bitEncoding e, enum phaseFunc f, qreal* p, int np) {
+    (void)q; (void)t; (void)r; (void)nr; (void)e; (void)f; (void)p; (void)np; UNSUP();
+}
+void applyParamNamedPhaseFuncOverrides(Qureg q, int* t, int* r, int nr, enum bitEncoding e, enum phaseFunc f, qreal* p, int np, long long* oi, qreal* op, int no) {
+    (void)q; (void)t; (void)r; (void)nr; (void)e; (void)f; (void)p; (void)np; (void)oi; (void)op; (void)no; UNSUP();
+}
+DiagonalOp createDiagonalOp(int n, QuESTEnv env) { DiagonalOp d; memset(&d, 0, sizeof d); (void)n; (void)env; UNSUP(); return d; }
+DiagonalOp createDiagonalOpFromPauliHamilFile(char* f, QuESTEnv env) { DiagonalOp d; memset(&d, 0, sizeof d); (void)f; (void)env; UNSUP(); return d; }
+void destroyDiagonalOp(DiagonalOp d, QuESTEnv env) { (void)d; (void)env; UNSUP(); }
+void syncDiagonalOp(DiagonalOp d) { (void)d; UNSUP(); }
+void initDiagonalOp(DiagonalOp d, qreal* r, qreal* i) { (void)d; (void)r; (void)i; UNSUP(); }
+void initDiagonalOpFromPauliHamil(DiagonalOp d, PauliHamil h) { (void)d; (void)h; UNSUP(); }
+void setDiagonalOpElems(DiagonalOp d, long long s, qreal* r, qreal* i, long long n) { (void)d; (void)s; (void)r; (void)i; (void)n; UNSUP(); }
+void applyDiagonalOp(Qureg q, DiagonalOp d) { (void)q; (void)d; UNSUP(); }
+Complex calcExpecDiagonalOp(Qureg q, DiagonalOp d) { Complex z = {0, 0}; (void)q; (void)d; UNSUP(); return z; }
+PauliHamil createPauliHamilFromFile(char* f) { PauliHamil h; memset(&h, 0, sizeof h); (void)f; UNSUP(); return h; }
+void initComplexMatrixN(ComplexMatrixN m, qreal real[][1 << m.numQubits], qreal imag[][1 << m.numQubits]) {
+    int D = 1 << m.numQubits;
+    for (int r = 0; r < D; r++) for (int c = 0; c < D; c++) { m.real[r][c] = real[r][c]; m.imag[r][c] = imag[r][c]; }
+}
+ComplexMatrixN bindArraysToStackComplexMatrixN(int n, qreal re[][1 << n], qreal im[][1 << n], qreal** rs, qreal** is) {
+    ComplexMatrixN m;
+    for (int r = 0; r < (1 << n); r++) { rs[r] = re[r]; is[r] = im[r]; }
+    m.numQubits = n; m.real = rs; m.imag = is;
+    return m;
+}

@@ -80,6 +80,9 @@ const char* const E_DEFINED_ONLY_FOR_DENSMATRS = "Operation valid only for densi
 const char* const E_INVALID_PROB = "Probabilities must be in [0, 1].";
 const char* const E_INVALID_ONE_QUBIT_DEPHASE_PROB = "The probability of a single qubit dephase error cannot exceed 1/2, which maximally mixes.";
 const char* const E_INVALID_ONE_QUBIT_DEPOL_PROB = "The probability of a single qubit depolarising error cannot exceed 3/4, which maximally mixes.";
+const char* const E_INVALID_TWO_QUBIT_DEPHASE_PROB = "The probability of a two-qubit qubit dephase error cannot exceed 3/4, which maximally mixes.";
+const char* const E_INVALID_TWO_QUBIT_DEPOL_PROB = "The probability of a two-qubit depolarising error cannot exceed 15/16, which maximally mixes.";
+const char* const E_INVALID_ONE_QUBIT_PAULI_PROBS = "The probability of any X, Y or Z error cannot exceed the probability of no error.";
 const char* const E_INVALID_CONTROLS_BIT_STATE = "The state of the control qubits must be a bit sequence (0s and 1s).";
 const char* const E_INVALID_PAULI_CODE = "Invalid Pauli code. Codes must be 0 (or PAULI_I), 1 (PAULI_X), 2 (PAULI_Y) or 3 (PAULI_Z) to indicate the identity, X, Y and Z operators respectively.";
 const char* const E_INVALID_NUM_SUM_TERMS = "Invalid number of terms in the Pauli sum. The number of terms must be >0.";
@@ -93,6 +96,9 @@ const char* const E_INVALID_TROTTER_REPS = "The number of Trotter repetitions mu
 const char* const E_QUREG_NOT_ALLOCATED = "Could not allocate memory for Qureg. Possibly insufficient memory.";
 const char* const E_QUREG_NOT_ALLOCATED_ON_GPU = "Could not allocate memory for Qureg on GPU. Possibly insufficient memory.";
 const char* const E_NO_GPU = "Trying to run GPU code with no GPU available.";
+// not in the reference: functions of the QuEST API that this library exports
+// only so that programs written against the whole API link
+const char* const E_UNSUPPORTED = "This QuEST function is not supported by the GB300 library (unsupported).";
 // not in the reference: this library's dense-matrix kernel limit
 const char* const E_MATRIX_TOO_LARGE = "Matrices on more than 10 target qubits are not supported by this library.";
 
@@ -1357,6 +1363,35 @@ void mixDamping(Qureg q, int t, qreal p) {
     if (p == 0) return;                                       // QuEST_gpu.cu:3055-3056
     qg::dmDamp(svg(q), t, q.numQubitsRepresented, p);
 }
+void mixPauli(Qureg q, int t, qreal pX, qreal pY, qreal pZ) {            // QuEST.c:1312
+    const char* caller = "mixPauli";
+    if (!vDensity(q, caller) || !vTarget(q, t, caller) || !vProb(pX, caller) || !vProb(pY, caller) ||
+        !vProb(pZ, caller))
+        return;
+    const double none = 1 - pX - pY - pZ;                     // QuEST_validation.c:634-643
+    if (!REQUIRE(pX <= none && pY <= none && pZ <= none, E_INVALID_ONE_QUBIT_PAULI_PROBS)) return;
+    qg::dmPauli(svg(q), t, q.numQubitsRepresented, pX, pY, pZ);
+}
+void mixTwoQubitDephasing(Qureg q, int q1, int q2, qreal p) {             // QuEST.c:1269
+    const char* caller = "mixTwoQubitDephasing";
+    if (!vDensity(q, caller) || !vUniqueTargets(q, q1, q2, caller) || !vProb(p, caller) ||
+        !REQUIRE(p <= 3 / 4.0, E_INVALID_TWO_QUBIT_DEPHASE_PROB))
+        return;
+    if (q1 > q2) std::swap(q1, q2);
+    const double dephase = (4 * p) / 3.0;
+    if (dephase == 0) return;                                 // QuEST_gpu.cu:2939-2940
+    qg::dmTwoQubitDephase(svg(q), q1, q2, q.numQubitsRepresented, 1 - dephase);
+}
+void mixTwoQubitDepolarising(Qureg q, int q1, int q2, qreal p) {          // QuEST.c:1300
+    const char* caller = "mixTwoQubitDepolarising";
+    if (!vDensity(q, caller) || !vUniqueTargets(q, q1, q2, caller) || !vProb(p, caller) ||
+        !REQUIRE(p <= 15 / 16.0, E_INVALID_TWO_QUBIT_DEPOL_PROB))
+        return;
+    if (q1 > q2) std::swap(q1, q2);
+    const double level = (16 * p) / 15.0;
+    if (level == 0) return;                                   // QuEST_gpu.cu:3114-3115
+    qg::dmTwoQubitDepolarise(svg(q), q1, q2, q.numQubitsRepresented, level);
+}
 void mixDensityMatrix(Qureg a, qreal p, Qureg b) {                        // QuEST.c:1018
     const char* caller = "mixDensityMatrix";
     if (!vDensity(a, caller) || !vDensity(b, caller) || !vMatchDims(a, b, caller) || !vProb(p, caller)) return;
@@ -1374,5 +1409,118 @@ void startRecordingQASM(Qureg q) { (void)q; }
 void stopRecordingQASM(Qureg q) { (void)q; }
 void clearRecordedQASM(Qureg q) { (void)q; }
 void printRecordedQASM(Qureg q) { (void)q; }
+void writeRecordedQASMToFile(Qureg q, char* filename) { (void)q; (void)filename; }
+
+// ---- reports (QuEST.c:1605-1640; plain text, this library's own layout) ----
+void reportQuregParams(Qureg q) {
+    printf("QUBITS:\nNumber of qubits is %d.\nNumber of amps is %lld.\nNumber of amps per rank is %lld.\n",
+           q.numQubitsRepresented, q.numAmpsTotal, q.numAmpsPerChunk);
+}
+void reportStateToScreen(Qureg q, QuESTEnv env, int reportRank) {
+    (void)env; (void)reportRank;
+    copyStateFromGPU(q);
+    printf("Reporting state [\n");
+    for (idx_t i = 0; i < q.numAmpsTotal; ++i) printf("%.14f, %.14f\n", q.stateVec.real[i], q.stateVec.imag[i]);
+    printf("]\n");
+}
+void reportState(Qureg q) {
+    copyStateFromGPU(q);
+    FILE* f = fopen("state_rank_0.csv", "w");
+    if (!f) return;
+    fprintf(f, "real, imag\n");
+    for (idx_t i = 0; i < q.numAmpsTotal; ++i) fprintf(f, "%.14f, %.14f\n", q.stateVec.real[i], q.stateVec.imag[i]);
+    fclose(f);
+}
+void reportPauliHamil(PauliHamil h) {
+    for (int t = 0; t < h.numSumTerms; ++t) {
+        printf("%.14f\t", h.termCoeffs[t]);
+        for (int k = 0; k < h.numQubits; ++k) printf("%d ", (int)h.pauliCodes[(idx_t)t * h.numQubits + k]);
+        printf("\n");
+    }
+}
+
+// ---- the rest of the QuEST 3.4 API (reference QuEST.h): not on the
+// simulation path this library serves; each reports E_UNSUPPORTED through
+// invalidQuESTInputError and leaves its arguments untouched ----
+#define QG_UNSUPPORTED() invalidQuESTInputError(E_UNSUPPORTED, __func__)
+void mixKrausMap(Qureg, int, ComplexMatrix2*, int) { QG_UNSUPPORTED(); }
+void mixTwoQubitKrausMap(Qureg, int, int, ComplexMatrix4*, int) { QG_UNSUPPORTED(); }
+void mixMultiQubitKrausMap(Qureg, int*, int, ComplexMatrixN*, int) { QG_UNSUPPORTED(); }
+void mixNonTPKrausMap(Qureg, int, ComplexMatrix2*, int) { QG_UNSUPPORTED(); }
+void mixNonTPTwoQubitKrausMap(Qureg, int, int, ComplexMatrix4*, int) { QG_UNSUPPORTED(); }
+void mixNonTPMultiQubitKrausMap(Qureg, int*, int, ComplexMatrixN*, int) { QG_UNSUPPORTED(); }
+void applyPauliSum(Qureg, enum pauliOpType*, qreal*, int, Qureg) { QG_UNSUPPORTED(); }
+void applyPauliHamil(Qureg, PauliHamil, Qureg) { QG_UNSUPPORTED(); }
+void applyMultiControlledMatrixN(Qureg, int*, int, int*, int, ComplexMatrixN) { QG_UNSUPPORTED(); }
+void applyProjector(Qureg, int, int) { QG_UNSUPPORTED(); }
+void applyQFT(Qureg, int*, int) { QG_UNSUPPORTED(); }
+void applyFullQFT(Qureg) { QG_UNSUPPORTED(); }
+void applyPhaseFunc(Qureg, int*, int, enum bitEncoding, qreal*, qreal*, int) { QG_UNSUPPORTED(); }
+void applyPhaseFuncOverrides(Qureg, int*, int, enum bitEncoding, qreal*, qreal*, int, long long*, qreal*, int) {
+    QG_UNSUPPORTED();
+}
+void applyMultiVarPhaseFunc(Qureg, int*, int*, int, enum bitEncoding, qreal*, qreal*, int*) { QG_UNSUPPORTED(); }
+void applyMultiVarPhaseFuncOverrides(Qureg, int*, int*, int, enum bitEncoding, qreal*, qreal*, int*, long long*,
+                                     qreal*, int) {
+    QG_UNSUPPORTED();
+}
+void applyNamedPhaseFunc(Qureg, int*, int*, int, enum bitEncoding, enum phaseFunc) { QG_UNSUPPORTED(); }
+void applyNamedPhaseFuncOverrides(Qureg, int*, int*, int, enum bitEncoding, enum phaseFunc, long long*, qreal*, int) {
+    QG_UNSUPPORTED();
+}
+void applyParamNamedPhaseFunc(Qureg, int*, int*, int, enum bitEncoding, enum phaseFunc, qreal*, int) {
+    QG_UNSUPPORTED();
+}
+void applyParamNamedPhaseFuncOverrides(Qureg, int*, int*, int, enum bitEncoding, enum phaseFunc, qreal*, int,
+                                       long long*, qreal*, int) {
+    QG_UNSUPPORTED();
+}
+DiagonalOp createDiagonalOp(int, QuESTEnv) {
+    QG_UNSUPPORTED();
+    return DiagonalOp{};
+}
+DiagonalOp createDiagonalOpFromPauliHamilFile(char*, QuESTEnv) {
+    QG_UNSUPPORTED();
+    return DiagonalOp{};
+}
+void destroyDiagonalOp(DiagonalOp, QuESTEnv) { QG_UNSUPPORTED(); }
+void syncDiagonalOp(DiagonalOp) { QG_UNSUPPORTED(); }
+void initDiagonalOp(DiagonalOp, qreal*, qreal*) { QG_UNSUPPORTED(); }
+void initDiagonalOpFromPauliHamil(DiagonalOp, PauliHamil) { QG_UNSUPPORTED(); }
+void setDiagonalOpElems(DiagonalOp, long long, qreal*, qreal*, long long) { QG_UNSUPPORTED(); }
+void applyDiagonalOp(Qureg, DiagonalOp) { QG_UNSUPPORTED(); }
+Complex calcExpecDiagonalOp(Qureg, DiagonalOp) {
+    QG_UNSUPPORTED();
+    return Complex{0, 0};
+}
+PauliHamil createPauliHamilFromFile(char*) {
+    QG_UNSUPPORTED();
+    return PauliHamil{};
+}
+// C-only helpers (their reference prototypes take variable-length 2D arrays,
+// which decay to pointers to contiguous rows of 2^numQubits entries)
+void initComplexMatrixN(ComplexMatrixN m, qreal* real, qreal* imag) {
+    const char* caller = "initComplexMatrixN";
+    if (!REQUIRE(m.real != nullptr && m.imag != nullptr, E_COMPLEX_MATRIX_NOT_INIT)) return;
+    const int D = 1 << m.numQubits;
+    for (int r = 0; r < D; ++r)
+        for (int c = 0; c < D; ++c) {
+            m.real[r][c] = real[(size_t)r * D + c];
+            m.imag[r][c] = imag[(size_t)r * D + c];
+        }
+}
+ComplexMatrixN bindArraysToStackComplexMatrixN(int numQubits, qreal* re, qreal* im, qreal** reStorage,
+                                               qreal** imStorage) {
+    const int D = 1 << numQubits;
+    for (int r = 0; r < D; ++r) {
+        reStorage[r] = re + (size_t)r * D;
+        imStorage[r] = im + (size_t)r * D;
+    }
+    ComplexMatrixN m;
+    m.numQubits = numQubits;
+    m.real = reStorage;
+    m.imag = imStorage;
+    return m;
+}
 
 }  // extern "C"

@@ -307,6 +307,16 @@ bool captureChannel(SV s, int t, int N, const double S[16]) {
     }, true);
 }
 
+bool captureChannelN(SV s, uint64_t mask, const double* S) {
+    const int D = 1 << __builtin_popcountll(mask);
+    return captureGate(s, mask, [&](std::vector<cplx>& v, const Local&) {
+        std::vector<cplx> out(D, cplx(0, 0));
+        for (int r = 0; r < D; ++r)
+            for (int c = 0; c < D; ++c) out[r] += S[(size_t)D * r + c] * v[c];
+        v.swap(out);
+    }, true);
+}
+
 bool captureMatrixN(SV s, uint64_t ctrl, const int* targs, int k, const double* mr, const double* mi) {
     uint64_t tmask = 0;
     for (int i = 0; i < k; ++i) tmask |= 1ull << targs[i];

@@ -1318,6 +1318,7 @@ void* uploadPlanTC(const FusedPlan& plan) {
 // number of floats, and the image itself.
 size_t tcImageFloats(int k) { return imageFloats(k); }
 void tcBuildImage(const FusedPass& pass, float* img) { buildImage(pass, img, currentParts()); }
+int tcImageParts() { return currentParts(); }
 // whether a plan's images hold the parts the current precision and kernel
 // choice read (else the caller uploads the plan again)
 bool tcImagesFit(const void* devPlan) {

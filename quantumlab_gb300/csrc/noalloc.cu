@@ -18,16 +18,23 @@
 // accepts at most kNoAllocBlocks * kAmpsPerBlock = 2^27 amplitudes (27
 // qubits) and rejects larger states with an error.
 //
+// The kernel reads the arrays two amplitudes at a time with 16-byte loads, so
+// both pointers must be 16-byte aligned (any pointer cudaMalloc returned, and
+// any even offset into one); a misaligned pointer is rejected on the host
+// before anything is queued.
+//
 // Host code cannot use the array's name as a device address (in host code it
 // names a host-side shadow).  The device address is looked up once per
 // device, with that device current, by cudaGetSymbolAddress on the first call
-// made on that device; that first call should therefore come before any
-// stream capture.  Every call shares the one array and leaves its contents
+// made on that device (a failed lookup is not remembered: the next call tries
+// again); that first call should therefore come before any stream capture.  Every call shares the one array and leaves its contents
 // behind: the ticket that must start at zero is cleared on the stream before
 // each launch, and calls that overlap on the GPU (other streams, other host
 // threads) race on the array -- serialise them.
 #include "quest_gb300.h"
 #include "reduce_kernel.cuh"
+
+#include <stdint.h>
 
 #include <mutex>
 
@@ -54,8 +61,22 @@ struct NormPairs {             // sum |amp|^2, two consecutive amplitudes per it
 
 constexpr int kMaxDevices = 64;
 double* g_scratchAddr[kMaxDevices] = {};
-std::once_flag g_setupOnce[kMaxDevices];
-cudaError_t g_setupErr[kMaxDevices] = {};
+std::mutex g_setupMutex;
+
+// the scratch array's device address on the current device `dev`, looked up
+// on first use and kept only once the lookup has succeeded
+cudaError_t scratchAddress(int dev, double** out) {
+    std::lock_guard<std::mutex> lk(g_setupMutex);
+    if (!g_scratchAddr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+        if (e != cudaSuccess) return e;
+        if (!p) return cudaErrorInvalidSymbol;
+        g_scratchAddr[dev] = static_cast<double*>(p);
+    }
+    *out = g_scratchAddr[dev];
+    return cudaSuccess;
+}
 
 }  // namespace
 }  // namespace qg
@@ -72,6 +93,10 @@ extern "C" int quest_gb300_calcTotalProbNoAlloc(const double* deviceReal, const 
         invalidQuESTInputError("The number of amplitudes must be a power of two, at least 2.", fn);
         return 1;
     }
+    if ((reinterpret_cast<uintptr_t>(deviceReal) & 15u) != 0 || (reinterpret_cast<uintptr_t>(deviceImag) & 15u) != 0) {
+        invalidQuESTInputError("The amplitude arrays must start on a 16-byte boundary (two doubles).", fn);
+        return 1;
+    }
     if (numAmps > kMaxAmps) {
         invalidQuESTInputError("Too many amplitudes: this entry point's fixed scratch holds partial sums for at most "
                                "2^27 amplitudes (27 qubits); use calcTotalProb for larger registers.",
@@ -85,16 +110,8 @@ extern "C" int quest_gb300_calcTotalProbNoAlloc(const double* deviceReal, const 
         return 1;
     }
     // once per device, with that device current: the array's device address
-    std::call_once(g_setupOnce[dev], [dev]() {
-        void* p = nullptr;
-        g_setupErr[dev] = cudaGetSymbolAddress(&p, g_noallocScratch);
-        if (g_setupErr[dev] == cudaSuccess) g_scratchAddr[dev] = static_cast<double*>(p);
-    });
-    if (g_setupErr[dev] != cudaSuccess || !g_scratchAddr[dev]) {
-        cudaFailed(g_setupErr[dev] != cudaSuccess ? g_setupErr[dev] : cudaErrorInvalidSymbol, "cudaGetSymbolAddress", fn);
-        return 1;
-    }
-    double* partials = g_scratchAddr[dev];
+    double* partials = nullptr;
+    if (cudaFailed(scratchAddress(dev, &partials), "cudaGetSymbolAddress", fn)) return 1;
     double* res = partials + 2 * kNoAllocBlocks;
     unsigned int* ticket = reinterpret_cast<unsigned int*>(res + 2);
     cudaStream_t st = static_cast<cudaStream_t>(stream);

@@ -79,6 +79,9 @@ bool captureMatrixN(SV s, uint64_t ctrl, const int* targs, int k, const double* 
 // real 4 x 4 superoperator S on (row qubit t, column qubit t + N): local index
 // = row bit + 2 column bit, out = S in
 bool captureChannel(SV s, int t, int N, const double S[16]);
+// a channel on the qubits of `mask` (k of them, k <= 6) as its real
+// 2^k x 2^k superoperator S (row-major), local bit i = the i-th lowest qubit
+bool captureChannelN(SV s, uint64_t mask, const double* S);
 
 struct Mat2 { double r[2][2], i[2][2]; };
 
@@ -115,10 +118,14 @@ void stateWeighted(SV out, double f1r, double f1i, SV a, double f2r, double f2i,
 void stateMixDM(SV a, double p, SV b);
 void collapseSV(SV s, int target, int outcome, double renorm);
 void collapseDM(SV s, int target, int nRep, int outcome, double renorm);
-// density-matrix channels (QuEST.c:1259-1298 semantics)
+// density-matrix channels (QuEST.c:1259-1322 semantics)
 void dmDephase(SV s, int target, int nRep, double retain);
 void dmDepolarise(SV s, int target, int nRep, double level);
 void dmDamp(SV s, int target, int nRep, double prob);
+void dmPauli(SV s, int target, int nRep, double pX, double pY, double pZ);
+// q1 < q2 (QuEST.c:1269, 1300: ensureIndsIncrease)
+void dmTwoQubitDephase(SV s, int q1, int q2, int nRep, double retain);
+void dmTwoQubitDepolarise(SV s, int q1, int q2, int nRep, double level);
 
 // ---- reductions (reduce.cu) -------------------------------------------------
 // All return their value through the pinned host slot after a stream sync.

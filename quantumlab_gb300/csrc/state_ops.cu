@@ -1,5 +1,5 @@
 // state_ops.cu -- initialisation, elementwise combinations, measurement
-// collapse and the single-qubit density-matrix channels (FP64, sm_103a).
+// collapse and the density-matrix channels (FP64, sm_103a).
 //
 // Channel semantics follow Code/QuEST340/QuEST/src/QuEST.c:1259-1298 and the
 // GPU kernels of QuEST_gpu.cu:2868-3078: the reference runs depolarising and
@@ -8,6 +8,8 @@
 // {rho[.0..0.], rho[.0..1.], rho[.1..0.], rho[.1..1.]} (row bit t, column bit
 // t+N), with the same per-entry arithmetic.
 #include "qg_internal.h"
+
+#include <type_traits>
 
 namespace qg {
 namespace {
@@ -167,6 +169,22 @@ struct Damp {
     }
 };
 
+// Pauli channel (1 - pX - pY - pZ) rho + pX X rho X + pY Y rho Y + pZ Z rho Z
+// (QuEST.c:1312, QuEST_common.c:740-759, which applies it as the Kraus
+// superoperator of those four operators): the diagonal pair exchanges weight
+// pX + pY, the off-diagonal pair keeps 1 - pX - pY - 2 pZ and exchanges pX - pY.
+struct PauliMix {
+    double diagKeep, diagSwap, offKeep, offSwap;
+    __device__ __forceinline__ void operator()(double& r00, double& i00, double& r01, double& i01, double& r10,
+                                               double& i10, double& r11, double& i11) const {
+        const double a = r00, b = i00, c = r01, d = i01;
+        r00 = diagKeep * a + diagSwap * r11; i00 = diagKeep * b + diagSwap * i11;
+        r11 = diagKeep * r11 + diagSwap * a; i11 = diagKeep * i11 + diagSwap * b;
+        r01 = offKeep * c + offSwap * r10; i01 = offKeep * d + offSwap * i10;
+        r10 = offKeep * r10 + offSwap * c; i10 = offKeep * i10 + offSwap * d;
+    }
+};
+
 // row bit t >= 1: two consecutive groups per thread with double2 loads
 template <class Op>
 __global__ void __launch_bounds__(kThreads) kChannelVec(double* __restrict__ re, double* __restrict__ im, int t, int N,
@@ -208,6 +226,108 @@ void launchChannel(SV s, int t, int N, const Op& op, const char* caller) {
     else
         kChannelT0<Op><<<blocksFor(nGroups), kThreads, 0, stream()>>>(s.re, s.im, N, nGroups, op);
     launchFailed(caller);
+}
+
+// Two-qubit channels on a density matrix (QuEST_gpu.cu:2912-2978, 3080-3147).
+// A group is the 16 entries that differ only in the bits b[0] < b[1] < b[2] <
+// b[3] = (q1, q2, q1 + N, q2 + N); local index j has bit i = bit b[i].  The
+// four entries whose row and column bits agree on both qubits (j = 0, 5, 10,
+// 15) become diagRetain x + mix (sum of the four); the other twelve are
+// scaled by retain.  Dephasing: retain = 1 - 4p/3, diagRetain = 1, no mix.
+// Depolarising: retain = diagRetain = 1 - l, mix = l/4, l = 16p/15 (the
+// reference's dephase launch followed by its averaging launch, in one pass).
+// V = 2: two consecutive groups per thread with 16-byte accesses (b[0] >= 1).
+struct TwoQubitBits {
+    int b[4];
+};
+template <int V, bool MIX>
+__global__ void __launch_bounds__(kThreads) kTwoQubitChannel(double* __restrict__ re, double* __restrict__ im,
+                                                             const TwoQubitBits tb, uint64_t nThreads, double retain,
+                                                             double diagRetain, double mix) {
+    typedef typename std::conditional<V == 2, double2, double>::type vec;
+    const uint64_t k = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (k >= nThreads) return;
+    uint64_t base = k * V;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) base = ((base >> tb.b[i]) << (tb.b[i] + 1)) | (base & ((1ull << tb.b[i]) - 1ull));
+    auto at = [&](int j) {
+        uint64_t o = base;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) o |= (uint64_t)((j >> i) & 1) << tb.b[i];
+        return o;
+    };
+    if (MIX) {
+        const int dj[4] = {0, 5, 10, 15};
+        vec r[4], m[4];
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+            r[d] = *reinterpret_cast<const vec*>(re + at(dj[d]));
+            m[d] = *reinterpret_cast<const vec*>(im + at(dj[d]));
+        }
+        if constexpr (V == 2) {
+            const double sx = mix * (r[0].x + r[1].x + r[2].x + r[3].x), sy = mix * (r[0].y + r[1].y + r[2].y + r[3].y);
+            const double tx = mix * (m[0].x + m[1].x + m[2].x + m[3].x), ty = mix * (m[0].y + m[1].y + m[2].y + m[3].y);
+#pragma unroll
+            for (int d = 0; d < 4; ++d) {
+                r[d].x = r[d].x * diagRetain + sx; r[d].y = r[d].y * diagRetain + sy;
+                m[d].x = m[d].x * diagRetain + tx; m[d].y = m[d].y * diagRetain + ty;
+            }
+        } else {
+            const double sx = mix * (r[0] + r[1] + r[2] + r[3]), tx = mix * (m[0] + m[1] + m[2] + m[3]);
+#pragma unroll
+            for (int d = 0; d < 4; ++d) {
+                r[d] = r[d] * diagRetain + sx;
+                m[d] = m[d] * diagRetain + tx;
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+            *reinterpret_cast<vec*>(re + at(dj[d])) = r[d];
+            *reinterpret_cast<vec*>(im + at(dj[d])) = m[d];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        if (j == 0 || j == 5 || j == 10 || j == 15) continue;
+        const uint64_t o = at(j);
+        vec r = *reinterpret_cast<const vec*>(re + o), m = *reinterpret_cast<const vec*>(im + o);
+        if constexpr (V == 2) {
+            r.x *= retain; r.y *= retain; m.x *= retain; m.y *= retain;
+        } else {
+            r *= retain; m *= retain;
+        }
+        *reinterpret_cast<vec*>(re + o) = r;
+        *reinterpret_cast<vec*>(im + o) = m;
+    }
+}
+
+template <bool MIX>
+void launchTwoQubitChannel(SV s, int q1, int q2, int N, double retain, double diagRetain, double mix,
+                           const char* caller) {
+    const TwoQubitBits tb{{q1, q2, q1 + N, q2 + N}};
+    const uint64_t nGroups = 1ull << (s.n - 4);
+    if (q1 >= 1)
+        kTwoQubitChannel<2, MIX><<<blocksFor(nGroups / 2), kThreads, 0, stream()>>>(s.re, s.im, tb, nGroups / 2,
+                                                                                  retain, diagRetain, mix);
+    else
+        kTwoQubitChannel<1, MIX><<<blocksFor(nGroups), kThreads, 0, stream()>>>(s.re, s.im, tb, nGroups, retain,
+                                                                               diagRetain, mix);
+    launchFailed(caller);
+}
+
+// the 16 x 16 superoperator of a two-qubit channel on the local qubits
+// (q1, q2, q1 + N, q2 + N), for the op-stream capture
+void twoQubitSuperop(double retain, double diagRetain, double mix, double S[256]) {
+    for (int i = 0; i < 256; ++i) S[i] = 0;
+    for (int j = 0; j < 16; ++j) {
+        const bool diag = (j == 0 || j == 5 || j == 10 || j == 15);
+        if (!diag) {
+            S[17 * j] = retain;
+            continue;
+        }
+        for (int c : {0, 5, 10, 15}) S[16 * j + c] = mix;
+        S[17 * j] += diagRetain;
+    }
 }
 
 }  // namespace
@@ -324,6 +444,30 @@ void dmDepolarise(SV s, int t, int N, double level) {
     const double S[16] = {d, 0, 0, x, 0, o, 0, 0, 0, 0, o, 0, x, 0, 0, d};
     if (s.cap && captureChannel(s, t, N, S)) return;
     launchChannel(s, t, N, Depolarise{level}, "mixDepolarising");
+}
+void dmPauli(SV s, int t, int N, double pX, double pY, double pZ) {
+    const PauliMix op{1 - pX - pY, pX + pY, 1 - pX - pY - 2 * pZ, pX - pY};
+    const double S[16] = {op.diagKeep, 0, 0, op.diagSwap, 0, op.offKeep, op.offSwap, 0,
+                          0, op.offSwap, op.offKeep, 0, op.diagSwap, 0, 0, op.diagKeep};
+    if (s.cap && captureChannel(s, t, N, S)) return;
+    launchChannel(s, t, N, op, "mixPauli");
+}
+void dmTwoQubitDephase(SV s, int q1, int q2, int N, double retain) {
+    if (s.cap) {
+        double S[256];
+        twoQubitSuperop(retain, 1.0, 0.0, S);
+        if (captureChannelN(s, (1ull << q1) | (1ull << q2) | (1ull << (q1 + N)) | (1ull << (q2 + N)), S)) return;
+    }
+    launchTwoQubitChannel<false>(s, q1, q2, N, retain, 1.0, 0.0, "mixTwoQubitDephasing");
+}
+void dmTwoQubitDepolarise(SV s, int q1, int q2, int N, double level) {
+    const double retain = 1 - level, mix = level * 0.25;
+    if (s.cap) {
+        double S[256];
+        twoQubitSuperop(retain, retain, mix, S);
+        if (captureChannelN(s, (1ull << q1) | (1ull << q2) | (1ull << (q1 + N)) | (1ull << (q2 + N)), S)) return;
+    }
+    launchTwoQubitChannel<true>(s, q1, q2, N, retain, retain, mix, "mixTwoQubitDepolarising");
 }
 void dmDamp(SV s, int t, int N, double p) {
     const double o = sqrt(1 - p);

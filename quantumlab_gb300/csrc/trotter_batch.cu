@@ -3,24 +3,26 @@
 //
 // QuantumLab's Fermi-Hubbard studies run one Trotter circuit per Hamiltonian
 // instance (QuEST.c:1079 applyTrotterCircuit -> QuEST_common.c:762-844 per
-// instance, then calcExpecPauliSum, QuEST_common.c:506-533).  Instances that
-// share the Pauli strings, order and repetitions but differ in coefficients
-// and time give circuits of the same shape with other angles.  A batch holds
-// B such instances as FP32 states of n qubits, side by side in one
-// allocation, and runs them together:
-//   * the fusion planner compiles instance 0's gate stream; every other
-//     instance takes the same passes with its own FP64 products
-//     (compilePlanLike), so the planner runs once;
-//   * each pass is one launch of the tensor-core applier over all B states
-//     (the CTAs are shared out among the states, each state's CTAs load that
-//     state's operands); passes narrower than 4 qubits are widened with
-//     identity factors so that every pass runs on the tensor cores;
+// instance, then calcExpecPauliSum, QuEST_common.c:506-533).  A batch holds B
+// instances as FP32 states and runs them together.  Instances that share the
+// register size, Pauli strings, order and repetitions form a class: their
+// circuits have the same shape with other angles.  Instances of different
+// step counts, orders, register sizes or Hamiltonians sit in one batch as
+// different classes:
+//   * per class, the fusion planner compiles one member's gate stream; every
+//     other member takes the same passes with its own FP64 products
+//     (compilePlanLike), so the planner runs once per class;
+//   * each pass is one launch of the tensor-core applier over all the class's
+//     states (the CTAs are shared out among the states, each state's CTAs
+//     load that state's operands); passes narrower than 4 qubits are widened
+//     with identity factors so that every pass runs on the tensor cores;
 //   * the energies <H_b> are reduced from the FP32 states (FP32 products per
-//     amplitude pair, FP64 sums), divided by each state's norm, which also
-//     removes the norm drift of the FP32 passes to first order;
-//   * after the first run the whole sequence (initial states, passes,
-//     reductions, the copy of the results to pinned host memory) is a CUDA
-//     graph that later runs replay.
+//     amplitude pair, FP64 sums), one launch per term group over the class's
+//     states, divided by each state's norm, which also removes the norm drift
+//     of the FP32 passes to first order;
+//   * after the first run the whole sequence (every class's initial states,
+//     passes and reductions, and the copy of the results to pinned host
+//     memory) is one CUDA graph that later runs replay.
 #include "fused_plan.h"
 #include "qg_internal.h"
 #include "quest_gb300.h"
@@ -32,12 +34,14 @@
 #include <cstring>
 #include <map>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 namespace qg {
 
 size_t tcImageFloats(int k);
 void tcBuildImage(const FusedPass& pass, float* img);
+int tcImageParts();
 bool applyPassTCBatch(float* re, float* im, int n, const FusedPass& pass, const float* images, size_t imageStride,
                       int batch, int* errFlag, cudaStream_t st);
 
@@ -227,6 +231,7 @@ __global__ void kBatchToF64(const float* __restrict__ sr, const float* __restric
 }
 
 struct Instance {
+    int n = 0;                       // qubits
     std::vector<int> codes;          // numTerms x n, QuEST pauliOpType values
     std::vector<double> coeffs;
     double time = 0.0;
@@ -298,34 +303,51 @@ FusedPass widenTo4(const FusedPass& p, int n) {
     return w;
 }
 
+// The energy reductions of one class: one launch each over the class's
+// instances (blockIdx.y = instance).
+struct Red {
+    int kind;                                      // 0 pairs, 3 pairs by four, 1 diagonal, 2 norm
+    PairShape ps;
+    DiagShape ds;
+};
+
+// Instances that share register size, Pauli strings, order and repetitions:
+// one fusion plan, one launch per pass over all of them.
+struct TrotterClass {
+    int n = 0;
+    std::vector<int> members;                      // instance indices, in batch order
+    size_t stateOffset = 0;                        // floats into re / im of member 0's planes
+    int posBase = 0;                               // first row of partials / counters / dInit
+    int slotBase = 0;                              // first result slot
+    size_t coefOffset = 0;                         // floats into dCoef
+    std::vector<FusedPass> shape;                  // per pass: the targets (member 0's pass)
+    std::vector<size_t> imgOffset, imgStride;      // per pass, in floats into images
+    std::vector<Red> reds;
+    // energy of member m = sum of its group slots / its norm slot + identity
+    std::vector<std::vector<int>> groupSlots;
+    std::vector<int> normSlot;
+    std::vector<double> identity;
+};
+
 }  // namespace
 
 struct TrotterBatch {
-    int n = 0, B = 0;
-    float *re = nullptr, *im = nullptr;
+    int maxQubits = 0, B = 0;
     std::vector<Instance> inst;
     bool compiled = false;
-    std::vector<FusedPass> shape;                  // per pass: the targets (instance 0's pass)
-    std::vector<size_t> imgOffset, imgStride;      // per pass, in floats
+    int parts = 0;                                 // operand image parts built (tcImageParts)
+    std::vector<TrotterClass> classes;
+    std::vector<int> classOf, posOf;               // per instance: its class, its place in it
+    float *re = nullptr, *im = nullptr;            // every class's states, class after class
     float* images = nullptr;
     long long* dInit = nullptr;
     int* errFlag = nullptr;
     double* partials = nullptr;                    // per instance kMaxBlocksPerInst block partials
     unsigned int* counters = nullptr;              // per instance last-block tickets
-    double* dResults = nullptr;                    // slot l * B + b: reduction l of instance b
+    double* dResults = nullptr;                    // per class: slot slotBase + l * size + m
     double* hResults = nullptr;                    // pinned
-    float* dCoef = nullptr;                        // reduction l, instance b: kCoefs floats
+    float* dCoef = nullptr;                        // per class, reduction l, member m: kCoefs floats
     int numSlots = 0;
-    // energy of instance b = sum of its group slots / its norm slot + identity
-    std::vector<std::vector<int>> groupSlots;
-    std::vector<int> normSlot;
-    std::vector<double> identity;
-    struct Red {
-        int kind;                                  // 0 pairs, 3 pairs by four, 1 diagonal, 2 norm
-        PairShape ps;
-        DiagShape ds;
-    };
-    std::vector<Red> reds;                         // one launch each, over all instances
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long runs = 0;
@@ -338,93 +360,28 @@ void freeDevice(TrotterBatch* b) {
     if (b->graph) cudaGraphDestroy(b->graph);
     b->exec = nullptr;
     b->graph = nullptr;
-    if (b->images) cudaFree(b->images);
-    if (b->dInit) cudaFree(b->dInit);
-    if (b->dCoef) cudaFree(b->dCoef);
-    if (b->dResults) cudaFree(b->dResults);
+    for (void* p : {(void*)b->re, (void*)b->im, (void*)b->images, (void*)b->dInit, (void*)b->dCoef, (void*)b->dResults})
+        if (p) cudaFree(p);
     if (b->hResults) cudaFreeHost(b->hResults);
+    b->re = b->im = nullptr;
     b->images = nullptr;
     b->dInit = nullptr;
     b->dCoef = nullptr;
     b->dResults = nullptr;
     b->hResults = nullptr;
+    b->classes.clear();
     b->compiled = false;
+    b->runs = 0;
 }
 
 const char* kFn = "quest_gb300_trotterBatchRun";
 
-bool compileBatch(TrotterBatch* b) {
-    const int n = b->n, B = b->B;
-    const Instance& i0 = b->inst[0];
-    for (int k = 0; k < B; ++k) {
-        const Instance& in = b->inst[k];
-        if (!in.set) {
-            invalidQuESTInputError("Every instance of the Trotter batch must be set before it runs.", kFn);
-            return false;
-        }
-        if (in.codes != i0.codes || in.order != i0.order || in.reps != i0.reps) {
-            invalidQuESTInputError("The instances of a Trotter batch must share Pauli strings, order and repetitions.", kFn);
-            return false;
-        }
-    }
-    // gate streams and plans: instance 0 searched, the others reuse its passes
-    std::vector<FusedPlan> plans(B);
-    for (int k = 0; k < B; ++k) {
-        FusedPlan& p = plans[k];
-        p.numQubits = n;
-        p.maxFused = widestPass(n);
-        for (int r = 0; r < b->inst[k].reps; ++r)
-            trotterTerms(b->inst[k], n, b->inst[k].time / b->inst[k].reps, b->inst[k].order, p.gates);
-    }
-    compilePlan(plans[0]);
-    bool ok = plans[0].compiled;
-    {
-        std::atomic<int> next{1};
-        std::atomic<bool> good{true};
-        auto work = [&]() {
-            for (int k; (k = next.fetch_add(1)) < B;)
-                if (!compilePlanLike(plans[k], plans[0])) good = false;
-        };
-        const unsigned nt = (unsigned)std::min<int>(8, std::max(1, B - 1));
-        std::vector<std::thread> pool;
-        for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
-        if (ok) work();
-        for (auto& t : pool) t.join();
-        ok = ok && good;
-    }
-    if (!ok) {
-        invalidQuESTInputError("The Trotter circuits of the batch could not be fused with one pass structure.", kFn);
-        return false;
-    }
-    const size_t np = plans[0].passes.size();
-    b->shape.clear();
-    b->imgOffset.assign(np, 0);
-    b->imgStride.assign(np, 0);
-    size_t total = 0;
-    for (size_t p = 0; p < np; ++p) {
-        b->shape.push_back(widenTo4(plans[0].passes[p], n));
-        b->imgStride[p] = tcImageFloats((int)b->shape[p].targets.size());
-        b->imgOffset[p] = total;
-        total += b->imgStride[p] * (size_t)B;
-    }
-    std::vector<float> host(std::max<size_t>(total, 4));
-    {
-        std::atomic<size_t> next{0};
-        const size_t jobs = np * (size_t)B;
-        auto work = [&]() {
-            for (size_t j; (j = next.fetch_add(1)) < jobs;) {
-                const size_t p = j / B, k = j % B;
-                tcBuildImage(widenTo4(plans[k].passes[p], n), host.data() + b->imgOffset[p] + k * b->imgStride[p]);
-            }
-        };
-        const unsigned nt = (unsigned)std::min<size_t>({(size_t)16, (size_t)std::max(1u, std::thread::hardware_concurrency()), jobs});
-        std::vector<std::thread> pool;
-        for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
-        work();
-        for (auto& t : pool) t.join();
-    }
-    // the energy reductions: Pauli strings grouped by X/Y mask (one read of
-    // the state per group), plus the norm
+// The energy reductions of class c (Pauli strings grouped by X/Y mask, one
+// read of a state per group, plus the norm), with the coefficients of every
+// member appended to coef ([reduction][member][kCoefs]).
+void buildReductions(const TrotterBatch* b, TrotterClass& c, std::vector<float>& coef) {
+    const int n = c.n, M = (int)c.members.size();
+    const Instance& i0 = b->inst[c.members[0]];
     std::map<uint64_t, std::vector<int>> groups;   // x -> term indices
     std::vector<uint64_t> yzOf(i0.coeffs.size());
     std::vector<int> nYOf(i0.coeffs.size());
@@ -432,37 +389,34 @@ bool compileBatch(TrotterBatch* b) {
     for (size_t t = 0; t < i0.coeffs.size(); ++t) {
         uint64_t x = 0, y = 0, z = 0;
         for (int q = 0; q < n; ++q) {
-            const int c = i0.codes[t * n + q];
-            if (c == PAULI_X) x |= 1ull << q;
-            if (c == PAULI_Y) { x |= 1ull << q; y |= 1ull << q; }
-            if (c == PAULI_Z) z |= 1ull << q;
+            const int cd = i0.codes[t * n + q];
+            if (cd == PAULI_X) x |= 1ull << q;
+            if (cd == PAULI_Y) { x |= 1ull << q; y |= 1ull << q; }
+            if (cd == PAULI_Z) z |= 1ull << q;
         }
         yzOf[t] = y | z;
         nYOf[t] = __builtin_popcountll(y);
         if ((x | z) == 0) identityTerms.push_back((int)t);
         else groups[x].push_back((int)t);
     }
-    // one reduction launch per group (chunk), shared masks, coefficients per
-    // instance in the same order
-    b->reds.clear();
-    b->identity.assign(B, 0.0);
-    for (int k = 0; k < B; ++k)
-        for (int t : identityTerms) b->identity[k] += b->inst[k].coeffs[t];
-    std::vector<float> coef;                       // [reduction][instance][kCoefs]
-    auto addRed = [&](const TrotterBatch::Red& r, const std::vector<std::vector<float>>& perInst) {
-        b->reds.push_back(r);
-        for (int k = 0; k < B; ++k) {
-            std::vector<float> c(kCoefs, 0.f);
-            std::copy(perInst[k].begin(), perInst[k].end(), c.begin());
-            coef.insert(coef.end(), c.begin(), c.end());
+    c.reds.clear();
+    c.identity.assign(M, 0.0);
+    for (int m = 0; m < M; ++m)
+        for (int t : identityTerms) c.identity[m] += b->inst[c.members[m]].coeffs[t];
+    auto addRed = [&](const Red& r, const std::vector<std::vector<float>>& perMember) {
+        c.reds.push_back(r);
+        for (int m = 0; m < M; ++m) {
+            std::vector<float> v(kCoefs, 0.f);
+            if (!perMember.empty()) std::copy(perMember[m].begin(), perMember[m].end(), v.begin());
+            coef.insert(coef.end(), v.begin(), v.end());
         }
     };
     for (auto& g : groups) {
         const uint64_t x = g.first;
         if (x == 0) {
-            // diagonal terms, bucketed by their low 3 mask bits
+            // diagonal terms, bucketed by their low mask bits
             for (size_t c0 = 0; c0 < g.second.size(); c0 += kCoefs) {
-                TrotterBatch::Red r{};
+                Red r{};
                 r.kind = 1;
                 std::vector<int> order;
                 const size_t c1 = std::min(g.second.size(), c0 + kCoefs);
@@ -477,23 +431,23 @@ bool compileBatch(TrotterBatch* b) {
                     }
                 }
                 r.ds.off[kDiagItem] = (int)order.size();
-                std::vector<std::vector<float>> per(B);
-                for (int k = 0; k < B; ++k)
-                    for (int t : order) per[k].push_back((float)b->inst[k].coeffs[t]);
+                std::vector<std::vector<float>> per(M);
+                for (int m = 0; m < M; ++m)
+                    for (int t : order) per[m].push_back((float)b->inst[c.members[m]].coeffs[t]);
                 addRed(r, per);
             }
             continue;
         }
         // the A / B lists depend on the masks only, so they line up across
-        // instances
-        std::vector<std::vector<std::pair<uint64_t, double>>> A(B), Bl(B);
-        for (int k = 0; k < B; ++k) {
+        // the members
+        std::vector<std::vector<std::pair<uint64_t, double>>> A(M), Bl(M);
+        for (int m = 0; m < M; ++m) {
             std::vector<PauliTerm> terms;
-            for (int t : g.second) terms.push_back(PauliTerm{yzOf[t], nYOf[t], b->inst[k].coeffs[t]});
-            pauliPairTerms(x, terms, A[k], Bl[k]);
+            for (int t : g.second) terms.push_back(PauliTerm{yzOf[t], nYOf[t], b->inst[c.members[m]].coeffs[t]});
+            pauliPairTerms(x, terms, A[m], Bl[m]);
         }
         for (size_t a0 = 0, b0 = 0; a0 < A[0].size() || b0 < Bl[0].size();) {
-            TrotterBatch::Red r{};
+            Red r{};
             r.kind = (x & 3) ? 0 : 3;                  // 3: four contiguous pairs per item
             r.ps.xmask = x;
             r.ps.low = __builtin_ctzll(x);
@@ -502,36 +456,148 @@ bool compileBatch(TrotterBatch* b) {
             r.ps.nB = (int)(b1 - b0);
             for (size_t u = a0; u < a1; ++u) r.ps.mA[u - a0] = A[0][u].first;
             for (size_t u = b0; u < b1; ++u) r.ps.mB[u - b0] = Bl[0][u].first;
-            std::vector<std::vector<float>> per(B, std::vector<float>(kCoefs, 0.f));
-            for (int k = 0; k < B; ++k) {
-                for (size_t u = a0; u < a1; ++u) per[k][u - a0] = (float)A[k][u].second;
-                for (size_t u = b0; u < b1; ++u) per[k][kMaxTerms + u - b0] = (float)Bl[k][u].second;
+            std::vector<std::vector<float>> per(M, std::vector<float>(kCoefs, 0.f));
+            for (int m = 0; m < M; ++m) {
+                for (size_t u = a0; u < a1; ++u) per[m][u - a0] = (float)A[m][u].second;
+                for (size_t u = b0; u < b1; ++u) per[m][kMaxTerms + u - b0] = (float)Bl[m][u].second;
             }
             addRed(r, per);
             a0 = a1;
             b0 = b1;
         }
     }
-    const int groupReds = (int)b->reds.size();
-    {
-        TrotterBatch::Red r{};
-        r.kind = 2;
-        addRed(r, std::vector<std::vector<float>>(B));
+    const int groupReds = (int)c.reds.size();
+    Red norm{};
+    norm.kind = 2;
+    addRed(norm, {});
+    c.groupSlots.assign(M, {});
+    c.normSlot.assign(M, 0);
+    for (int m = 0; m < M; ++m) {
+        for (int l = 0; l < groupReds; ++l) c.groupSlots[m].push_back(c.slotBase + l * M + m);
+        c.normSlot[m] = c.slotBase + groupReds * M + m;
     }
-    b->numSlots = (int)b->reds.size() * B;
-    b->groupSlots.assign(B, {});
-    b->normSlot.assign(B, 0);
+}
+
+// Run fn(j) for j in [0, jobs) on up to `threads` host threads.
+template <class F>
+void parallelFor(size_t jobs, unsigned threads, F fn) {
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+        for (size_t j; (j = next.fetch_add(1)) < jobs;) fn(j);
+    };
+    const unsigned nt = (unsigned)std::max<size_t>(1, std::min<size_t>(threads, jobs));
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+}
+
+bool compileBatch(TrotterBatch* b) {
+    const int B = b->B;
+    for (int k = 0; k < B; ++k)
+        if (!b->inst[k].set) {
+            invalidQuESTInputError("Every instance of the Trotter batch must be set before it runs.", kFn);
+            return false;
+        }
+    // classes: instances of one register size, Pauli strings, order and
+    // repetitions, in order of first appearance
+    b->classes.clear();
+    b->classOf.assign(B, -1);
+    b->posOf.assign(B, -1);
     for (int k = 0; k < B; ++k) {
-        for (int l = 0; l < groupReds; ++l) b->groupSlots[k].push_back(l * B + k);
-        b->normSlot[k] = groupReds * B + k;
+        const Instance& in = b->inst[k];
+        int c = 0;
+        for (; c < (int)b->classes.size(); ++c) {
+            const Instance& r = b->inst[b->classes[c].members[0]];
+            if (r.n == in.n && r.order == in.order && r.reps == in.reps && r.codes == in.codes) break;
+        }
+        if (c == (int)b->classes.size()) {
+            b->classes.emplace_back();
+            b->classes.back().n = in.n;
+        }
+        b->classOf[k] = c;
+        b->posOf[k] = (int)b->classes[c].members.size();
+        b->classes[c].members.push_back(k);
     }
+    const int C = (int)b->classes.size();
+    // gate streams; each class's member 0 searched (classes in parallel), the
+    // other members reuse its passes with their own FP64 products
+    std::vector<std::vector<FusedPlan>> plans(C);
+    for (int c = 0; c < C; ++c) {
+        TrotterClass& cl = b->classes[c];
+        plans[c].resize(cl.members.size());
+        for (size_t m = 0; m < cl.members.size(); ++m) {
+            const Instance& in = b->inst[cl.members[m]];
+            FusedPlan& p = plans[c][m];
+            p.numQubits = cl.n;
+            p.maxFused = widestPass(cl.n);
+            for (int r = 0; r < in.reps; ++r) trotterTerms(in, cl.n, in.time / in.reps, in.order, p.gates);
+        }
+    }
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    parallelFor((size_t)C, std::min(hw, 8u), [&](size_t c) { compilePlan(plans[c][0]); });
+    std::vector<std::pair<int, int>> likeJobs;
+    for (int c = 0; c < C; ++c)
+        for (size_t m = 1; m < plans[c].size(); ++m) likeJobs.emplace_back(c, (int)m);
+    std::atomic<bool> good{true};
+    for (int c = 0; c < C; ++c) good = good && plans[c][0].compiled;
+    if (good)
+        parallelFor(likeJobs.size(), std::min(hw, 8u), [&](size_t j) {
+            if (!compilePlanLike(plans[likeJobs[j].first][likeJobs[j].second], plans[likeJobs[j].first][0]))
+                good = false;
+        });
+    if (!good) {
+        invalidQuESTInputError("The Trotter circuits of the batch could not be fused with one pass structure.", kFn);
+        return false;
+    }
+    // layout: states, image offsets, result slots and rows, class after class
+    size_t stateFloats = 0, imgTotal = 0;
+    int pos = 0, slots = 0;
+    std::vector<float> coef;                       // [class][reduction][member][kCoefs]
+    for (int c = 0; c < C; ++c) {
+        TrotterClass& cl = b->classes[c];
+        const size_t M = cl.members.size();
+        cl.stateOffset = stateFloats;
+        stateFloats += ((size_t)1 << cl.n) * M;
+        cl.posBase = pos;
+        pos += (int)M;
+        const size_t np = plans[c][0].passes.size();
+        cl.shape.clear();
+        cl.imgOffset.assign(np, 0);
+        cl.imgStride.assign(np, 0);
+        for (size_t p = 0; p < np; ++p) {
+            cl.shape.push_back(widenTo4(plans[c][0].passes[p], cl.n));
+            cl.imgStride[p] = tcImageFloats((int)cl.shape[p].targets.size());
+            cl.imgOffset[p] = imgTotal;
+            imgTotal += cl.imgStride[p] * M;
+        }
+        cl.slotBase = slots;
+        cl.coefOffset = coef.size();
+        buildReductions(b, cl, coef);
+        slots += (int)(cl.reds.size() * M);
+    }
+    b->numSlots = slots;
+    // operand images of every (class, pass, member), on host threads
+    b->parts = tcImageParts();
+    std::vector<float> host(std::max<size_t>(imgTotal, 4));
+    std::vector<std::tuple<int, int, int>> imgJobs;            // class, pass, member
+    for (int c = 0; c < C; ++c)
+        for (size_t p = 0; p < b->classes[c].shape.size(); ++p)
+            for (size_t m = 0; m < b->classes[c].members.size(); ++m) imgJobs.emplace_back(c, (int)p, (int)m);
+    parallelFor(imgJobs.size(), std::min(hw, 16u), [&](size_t j) {
+        const int c = std::get<0>(imgJobs[j]), p = std::get<1>(imgJobs[j]), m = std::get<2>(imgJobs[j]);
+        const TrotterClass& cl = b->classes[c];
+        tcBuildImage(widenTo4(plans[c][m].passes[p], cl.n), host.data() + cl.imgOffset[p] + m * cl.imgStride[p]);
+    });
     // device side
     cudaStream_t st = stream();
     std::vector<long long> init(B);
-    for (int k = 0; k < B; ++k) init[k] = b->inst[k].init;
-    if (QG_CUDA(cudaMalloc(&b->images, host.size() * sizeof(float)), kFn) ||
+    for (int k = 0; k < B; ++k) init[b->classes[b->classOf[k]].posBase + b->posOf[k]] = b->inst[k].init;
+    if (QG_CUDA(cudaMalloc(&b->re, stateFloats * sizeof(float)), kFn) ||
+        QG_CUDA(cudaMalloc(&b->im, stateFloats * sizeof(float)), kFn) ||
+        QG_CUDA(cudaMalloc(&b->images, host.size() * sizeof(float)), kFn) ||
         QG_CUDA(cudaMalloc(&b->dInit, B * sizeof(long long)), kFn) ||
-        QG_CUDA(cudaMalloc(&b->dCoef, coef.size() * sizeof(float)), kFn) ||
+        QG_CUDA(cudaMalloc(&b->dCoef, std::max<size_t>(1, coef.size()) * sizeof(float)), kFn) ||
         QG_CUDA(cudaMalloc(&b->dResults, 2 * (size_t)b->numSlots * sizeof(double)), kFn) ||
         QG_CUDA(cudaMallocHost(&b->hResults, 2 * (size_t)b->numSlots * sizeof(double)), kFn))
         return false;
@@ -544,45 +610,53 @@ bool compileBatch(TrotterBatch* b) {
     return true;
 }
 
-// the run's work, queued on `st` (the library stream, or a capture stream)
+// the run's work, queued on `st` (the library stream, or a capture stream):
+// class after class, its states' initialisation, its passes (one launch each
+// over the class's states) and its reductions (one launch each over the
+// class's states), then one copy of every result to pinned host memory
 bool queueRun(TrotterBatch* b, cudaStream_t st) {
-    const uint64_t dim = 1ull << b->n, all = dim * (uint64_t)b->B;
-    if (QG_CUDA(cudaMemsetAsync(b->errFlag, 0, sizeof(int), st), kFn) ||
-        QG_CUDA(cudaMemsetAsync(b->re, 0, all * sizeof(float), st), kFn) ||
-        QG_CUDA(cudaMemsetAsync(b->im, 0, all * sizeof(float), st), kFn))
-        return false;
-    kBatchClassical<<<(b->B + 127) / 128, 128, 0, st>>>(b->re, dim, b->dInit, b->B);
-    if (launchFailed(kFn)) return false;
-    for (size_t p = 0; p < b->shape.size(); ++p)
-        if (!applyPassTCBatch(b->re, b->im, b->n, b->shape[p], b->images + b->imgOffset[p], b->imgStride[p], b->B,
-                              b->errFlag, st)) {
-            invalidQuESTInputError("A pass of the Trotter batch could not be launched on the tensor cores.", kFn);
+    if (QG_CUDA(cudaMemsetAsync(b->errFlag, 0, sizeof(int), st), kFn)) return false;
+    for (const TrotterClass& cl : b->classes) {
+        const int M = (int)cl.members.size();
+        const uint64_t dim = 1ull << cl.n, all = dim * (uint64_t)M;
+        float* re = b->re + cl.stateOffset;
+        float* im = b->im + cl.stateOffset;
+        if (QG_CUDA(cudaMemsetAsync(re, 0, all * sizeof(float), st), kFn) ||
+            QG_CUDA(cudaMemsetAsync(im, 0, all * sizeof(float), st), kFn))
             return false;
-        }
-    // one launch per reduction over all instances: blockIdx.y = instance
-    const int B = b->B;
-    for (size_t l = 0; l < b->reds.size(); ++l) {
-        const TrotterBatch::Red& r = b->reds[l];
-        const float* coef = b->dCoef + l * (size_t)B * kCoefs;
-        double* out = b->dResults + 2 * l * (size_t)B;
-        // items: a pair (kind 0), four pairs or 8 amplitudes (kinds 3, 2), kDiagItem amplitudes (kind 1)
-        const uint64_t items = r.kind == 0 ? dim / 2 : r.kind == 1 ? dim / kDiagItem : dim / 8;
-        const unsigned bx = (unsigned)std::max<uint64_t>(
-            1, std::min<uint64_t>({(uint64_t)kMaxBlocksPerInst, (items + red::kThreads - 1) / red::kThreads,
-                                   std::max<uint64_t>(1, 8ull * (uint64_t)numSMs() / (uint64_t)B)}));
-        const dim3 grid(bx, (unsigned)B);
-        if (r.kind == 0)
-            kReduceBatch<<<grid, red::kThreads, 0, st>>>(PairsF32{b->re, b->im, dim, r.ps, coef}, items, b->partials,
-                                                         b->counters, out);
-        else if (r.kind == 3)
-            kReduceBatch<<<grid, red::kThreads, 0, st>>>(PairsF32x4{b->re, b->im, dim, r.ps, coef}, items, b->partials,
-                                                         b->counters, out);
-        else if (r.kind == 1)
-            kReduceBatch<<<grid, red::kThreads, 0, st>>>(DiagF32{b->re, b->im, dim, r.ds, coef}, items, b->partials,
-                                                         b->counters, out);
-        else
-            kReduceBatch<<<grid, red::kThreads, 0, st>>>(NormF32b{b->re, b->im, dim}, items, b->partials, b->counters, out);
+        kBatchClassical<<<(M + 127) / 128, 128, 0, st>>>(re, dim, b->dInit + cl.posBase, M);
         if (launchFailed(kFn)) return false;
+        for (size_t p = 0; p < cl.shape.size(); ++p)
+            if (!applyPassTCBatch(re, im, cl.n, cl.shape[p], b->images + cl.imgOffset[p], cl.imgStride[p], M,
+                                  b->errFlag, st)) {
+                invalidQuESTInputError("A pass of the Trotter batch could not be launched on the tensor cores.", kFn);
+                return false;
+            }
+        double* partials = b->partials + (size_t)cl.posBase * kMaxBlocksPerInst;
+        unsigned int* counters = b->counters + cl.posBase;
+        for (size_t l = 0; l < cl.reds.size(); ++l) {
+            const Red& r = cl.reds[l];
+            const float* coef = b->dCoef + cl.coefOffset + l * (size_t)M * kCoefs;
+            double* out = b->dResults + 2 * ((size_t)cl.slotBase + l * (size_t)M);
+            // items: a pair (kind 0), four pairs or 8 amplitudes (kinds 3, 2), kDiagItem amplitudes (kind 1)
+            const uint64_t items = r.kind == 0 ? dim / 2 : r.kind == 1 ? dim / kDiagItem : dim / 8;
+            const unsigned bx = (unsigned)std::max<uint64_t>(
+                1, std::min<uint64_t>({(uint64_t)kMaxBlocksPerInst, (items + red::kThreads - 1) / red::kThreads,
+                                       std::max<uint64_t>(1, 8ull * (uint64_t)numSMs() / (uint64_t)M)}));
+            const dim3 grid(bx, (unsigned)M);
+            if (r.kind == 0)
+                kReduceBatch<<<grid, red::kThreads, 0, st>>>(PairsF32{re, im, dim, r.ps, coef}, items, partials,
+                                                             counters, out);
+            else if (r.kind == 3)
+                kReduceBatch<<<grid, red::kThreads, 0, st>>>(PairsF32x4{re, im, dim, r.ps, coef}, items, partials,
+                                                             counters, out);
+            else if (r.kind == 1)
+                kReduceBatch<<<grid, red::kThreads, 0, st>>>(DiagF32{re, im, dim, r.ds, coef}, items, partials,
+                                                             counters, out);
+            else
+                kReduceBatch<<<grid, red::kThreads, 0, st>>>(NormF32b{re, im, dim}, items, partials, counters, out);
+            if (launchFailed(kFn)) return false;
+        }
     }
     return !QG_CUDA(cudaMemcpyAsync(b->hResults, b->dResults, 2 * (size_t)b->numSlots * sizeof(double),
                                     cudaMemcpyDeviceToHost, st), kFn);
@@ -603,15 +677,11 @@ void* quest_gb300_trotterBatchCreate(int numQubits, int numInstances) {
         return nullptr;
     }
     TrotterBatch* b = new TrotterBatch();
-    b->n = numQubits;
+    b->maxQubits = numQubits;
     b->B = numInstances;
     b->inst.resize(numInstances);
-    const size_t all = ((size_t)1 << numQubits) * (size_t)numInstances;
-    if (QG_CUDA(cudaMalloc(&b->re, all * sizeof(float)), fn) || QG_CUDA(cudaMalloc(&b->im, all * sizeof(float)), fn) ||
-        QG_CUDA(cudaMalloc(&b->errFlag, sizeof(int)), fn) ||
+    if (QG_CUDA(cudaMalloc(&b->errFlag, sizeof(int)), fn) ||
         QG_CUDA(cudaMalloc(&b->partials, (size_t)numInstances * (qg::kMaxBlocksPerInst + 1) * sizeof(double)), fn)) {
-        if (b->re) cudaFree(b->re);
-        if (b->im) cudaFree(b->im);
         if (b->errFlag) cudaFree(b->errFlag);
         if (b->partials) cudaFree(b->partials);
         delete b;
@@ -630,14 +700,14 @@ int quest_gb300_trotterBatchSetInstance(void* batch, int instance, PauliHamil ha
         invalidQuESTInputError("Invalid Trotter batch or instance index.", fn);
         return -1;
     }
-    if (hamil.numQubits != b->n || hamil.numSumTerms < 1 || !hamil.pauliCodes || !hamil.termCoeffs ||
-        !(order == 1 || (order >= 2 && order % 2 == 0)) || reps < 1 || initClassicalState < 0 ||
-        initClassicalState >= (1ll << b->n)) {
+    if (hamil.numQubits < 11 || hamil.numQubits > b->maxQubits || hamil.numSumTerms < 1 || !hamil.pauliCodes ||
+        !hamil.termCoeffs || !(order == 1 || (order >= 2 && order % 2 == 0)) || reps < 1 || initClassicalState < 0 ||
+        initClassicalState >= (1ll << hamil.numQubits)) {
         invalidQuESTInputError("Invalid Hamiltonian, order, repetitions or initial state for the Trotter batch.", fn);
         return -1;
     }
     qg::Instance& in = b->inst[instance];
-    in.codes.resize((size_t)hamil.numSumTerms * b->n);
+    in.codes.resize((size_t)hamil.numSumTerms * hamil.numQubits);
     for (size_t i = 0; i < in.codes.size(); ++i) {
         const int c = (int)hamil.pauliCodes[i];
         if (c < 0 || c > 3) {
@@ -646,12 +716,14 @@ int quest_gb300_trotterBatchSetInstance(void* batch, int instance, PauliHamil ha
         }
         in.codes[i] = c;
     }
+    in.n = hamil.numQubits;
     in.coeffs.assign(hamil.termCoeffs, hamil.termCoeffs + hamil.numSumTerms);
     in.time = time;
     in.order = order;
     in.reps = reps;
     in.init = initClassicalState;
     in.set = true;
+    cudaStreamSynchronize(qg::stream());
     qg::freeDevice(b);                               // recompiled at the next run
     return 0;
 }
@@ -660,6 +732,11 @@ int quest_gb300_trotterBatchRun(void* batch, double* energies) {
     const char* fn = "quest_gb300_trotterBatchRun";
     TrotterBatch* b = reinterpret_cast<TrotterBatch*>(batch);
     if (!b) return -1;
+    // images built for another precision or kernel choice are rebuilt
+    if (b->compiled && (qg::tcImageParts() & ~b->parts) != 0) {
+        cudaStreamSynchronize(qg::stream());
+        qg::freeDevice(b);
+    }
     if (!b->compiled && !qg::compileBatch(b)) {
         qg::freeDevice(b);
         return -1;
@@ -680,10 +757,12 @@ int quest_gb300_trotterBatchRun(void* batch, double* energies) {
     }
     if (energies)
         for (int k = 0; k < b->B; ++k) {
+            const qg::TrotterClass& cl = b->classes[b->classOf[k]];
+            const int m = b->posOf[k];
             double e = 0.0;
-            for (int s : b->groupSlots[k]) e += b->hResults[2 * s];
-            const double norm = b->hResults[2 * b->normSlot[k]];
-            energies[k] = (norm > 0 ? e / norm : 0.0) + b->identity[k];
+            for (int s : cl.groupSlots[m]) e += b->hResults[2 * s];
+            const double norm = b->hResults[2 * cl.normSlot[m]];
+            energies[k] = (norm > 0 ? e / norm : 0.0) + cl.identity[m];
         }
     if (!b->exec) {
         // later runs replay the same work as one graph
@@ -710,8 +789,7 @@ int quest_gb300_trotterBatchRun(void* batch, double* energies) {
 int quest_gb300_trotterBatchCopyState(void* batch, int instance, Qureg dst) {
     const char* fn = "quest_gb300_trotterBatchCopyState";
     TrotterBatch* b = reinterpret_cast<TrotterBatch*>(batch);
-    if (!b || instance < 0 || instance >= b->B || dst.isDensityMatrix || dst.numQubitsRepresented != b->n ||
-        !dst.deviceStateVec.real) {
+    if (!b || instance < 0 || instance >= b->B || dst.isDensityMatrix || !dst.deviceStateVec.real) {
         invalidQuESTInputError("Invalid Trotter batch instance or destination register.", fn);
         return -1;
     }
@@ -719,26 +797,39 @@ int quest_gb300_trotterBatchCopyState(void* batch, int instance, Qureg dst) {
         invalidQuESTInputError("The Trotter batch has no state to copy: run it first.", fn);
         return -1;
     }
+    const qg::TrotterClass& cl = b->classes[b->classOf[instance]];
+    const int m = b->posOf[instance];
+    if (dst.numQubitsRepresented != cl.n) {
+        invalidQuESTInputError("The destination register's size differs from the instance's.", fn);
+        return -1;
+    }
     qg::captureDiscard(dst.deviceStateVec.real);
-    const uint64_t dim = 1ull << b->n;
+    const uint64_t dim = 1ull << cl.n;
     cudaStream_t st = qg::stream();
     // the FP32 passes drift the norm by ~1e-7 each (no correction inside a
     // batch): the copy restores the start state's norm, 1, from the norm the
     // last run measured
     double scale = 1.0;
-    if (b->hResults) {
-        const double norm = b->hResults[2 * b->normSlot[instance]];
-        if (norm > 0) scale = 1.0 / std::sqrt(norm);
-    }
-    qg::kBatchToF64<<<4 * qg::numSMs(), 256, 0, st>>>(b->re + instance * dim, b->im + instance * dim,
-                                                      dst.deviceStateVec.real, dst.deviceStateVec.imag, dim, scale);
+    const double norm = b->hResults[2 * cl.normSlot[m]];
+    if (norm > 0) scale = 1.0 / std::sqrt(norm);
+    const size_t off = cl.stateOffset + (size_t)m * dim;
+    qg::kBatchToF64<<<4 * qg::numSMs(), 256, 0, st>>>(b->re + off, b->im + off, dst.deviceStateVec.real,
+                                                      dst.deviceStateVec.imag, dim, scale);
     if (qg::launchFailed(fn)) return -1;
     return QG_CUDA(cudaStreamSynchronize(st), fn) ? -1 : 0;
 }
 
 int quest_gb300_trotterBatchNumPasses(void* batch) {
     TrotterBatch* b = reinterpret_cast<TrotterBatch*>(batch);
-    return b && b->compiled ? (int)b->shape.size() : -1;
+    if (!b || !b->compiled) return -1;
+    size_t passes = 0;
+    for (const qg::TrotterClass& cl : b->classes) passes += cl.shape.size();
+    return (int)passes;
+}
+
+int quest_gb300_trotterBatchNumClasses(void* batch) {
+    TrotterBatch* b = reinterpret_cast<TrotterBatch*>(batch);
+    return b && b->compiled ? (int)b->classes.size() : -1;
 }
 
 void quest_gb300_trotterBatchDestroy(void* batch) {
@@ -746,8 +837,6 @@ void quest_gb300_trotterBatchDestroy(void* batch) {
     if (!b) return;
     cudaStreamSynchronize(qg::stream());
     qg::freeDevice(b);
-    if (b->re) cudaFree(b->re);
-    if (b->im) cudaFree(b->im);
     if (b->errFlag) cudaFree(b->errFlag);
     if (b->partials) cudaFree(b->partials);
     delete b;

@@ -166,6 +166,9 @@ SIGNATURES = {
     "mixDepolarising": (None, [_Q, _I, _D]),
     "mixDamping": (None, [_Q, _I, _D]),
     "mixDensityMatrix": (None, [_Q, _D, _Q]),
+    "mixPauli": (None, [_Q, _I, _D, _D, _D]),
+    "mixTwoQubitDephasing": (None, [_Q, _I, _I, _D]),
+    "mixTwoQubitDepolarising": (None, [_Q, _I, _I, _D]),
     # extensions (include/quest_gb300.h)
     "quest_gb300_stream": (C.c_void_p, []),
     "quest_gb300_launchCount": (c_ll, []),
@@ -209,6 +212,7 @@ SIGNATURES = {
     "quest_gb300_trotterBatchRun": (_I, [C.c_void_p, _P(C.c_double)]),
     "quest_gb300_trotterBatchCopyState": (_I, [C.c_void_p, _I, _Q]),
     "quest_gb300_trotterBatchNumPasses": (_I, [C.c_void_p]),
+    "quest_gb300_trotterBatchNumClasses": (_I, [C.c_void_p]),
     "quest_gb300_trotterBatchDestroy": (None, [C.c_void_p]),
     "quest_gb300_captureStats": (_I, [_Q, _P(C.c_longlong), _P(C.c_longlong), _P(C.c_longlong), _P(C.c_double)]),
     "quest_gb300_sampleMeasurements": (_I, [_Q, _P(_I), _I, _I, _P(_I)]),

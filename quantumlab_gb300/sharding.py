@@ -39,22 +39,13 @@ def swap_test_cost(dim_log2: np.ndarray) -> np.ndarray:
 
 def trotter_instance_cost(steps: Sequence[int], order: Sequence[int]) -> np.ndarray:
     """Relative cost of a Trotter instance (same register size): its fused
-    passes grow with the Pauli exponentials, steps x 1 at first order and
-    steps x 2 at second (the symmetrised product applies every term twice)."""
+    passes grow with the Pauli exponentials applied, steps x the exponentials
+    per step.  Per step, order 1 applies every term once and order 2 twice
+    (the symmetrised product); order 2k applies five order-(2k-2) products
+    (QuEST_common.c:800-820), so 2 x 5^(k-1) times."""
     steps = np.asarray(steps, dtype=np.float64)
     order = np.asarray(order, dtype=np.int64)
-    return steps * np.where(order == 1, 1.0, 2.0)
-
-
-def trotter_batches(shapes: Sequence[tuple], indices: Sequence[int]) -> list:
-    """Group a rank's Trotter instances into batches of one shape: the
-    instances of a batch (quest_gb300_trotterBatch*) must share Pauli strings,
-    order and steps.  `shapes[i]` is instance i's shape key; returns lists of
-    instance indices, in order of first appearance."""
-    groups: dict = {}
-    for i in indices:
-        groups.setdefault(shapes[i], []).append(int(i))
-    return list(groups.values())
+    return steps * np.where(order == 1, 1.0, 2.0 * np.power(5.0, np.maximum(order // 2 - 1, 0)))
 
 
 def gather_to_rank0(indices: np.ndarray, values: np.ndarray, total: int, world: int):

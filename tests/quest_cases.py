@@ -171,6 +171,26 @@ def decoherence_ops(rng: R, n: int):
     return out
 
 
+def channel2_ops(rng: R, n: int):
+    """The channels QuantumLab's density-matrix simulator adds
+    (QLSimulatorDensityMatrix.cpp:136-150): mixPauli on every qubit, and the
+    two-qubit dephasing and depolarising channels on every ordered pair."""
+    out = []
+    for t in range(n):
+        px, py = rng.u(0, 0.25), rng.u(0, 0.2)
+        out.append((f"mixPauli[{t}]", [["mixPauli", t, px, py, rng.u(0, 0.2)]]))
+    out.append(("mixPauli[bound]", [["mixPauli", 0, 0.25, 0.25, 0.25]]))
+    for a in range(n):
+        for b in range(n):
+            if a != b:
+                out.append((f"mixTwoQubitDephasing[{a},{b}]", [["mixTwoQubitDephasing", a, b, rng.u(0, 0.75)]]))
+                out.append((f"mixTwoQubitDepolarising[{a},{b}]",
+                            [["mixTwoQubitDepolarising", a, b, rng.u(0, 15 / 16)]]))
+    out.append(("mixTwoQubitDepolarising[max]", [["mixTwoQubitDepolarising", 0, n - 1, 15 / 16]]))
+    out.append(("mixTwoQubitDephasing[p=0]", [["mixTwoQubitDephasing", 1, 0, 0.0]]))
+    return out
+
+
 def probes_for(n: int, density: bool, rng: R):
     p = [["calcTotalProb"]]
     for t in range(n):
@@ -223,14 +243,28 @@ def build_cases(seed: int = 20261203):
             cases.append({"name": f"{kind}{n}:measure:seed{s}", "density": density, "n": n, "init": "random",
                           "ops": [["seedQuEST", [1000 + s, 77]]] + [["measure", t] for t in range(n)],
                           "probes": [["calcTotalProb"]]})
+    # the two-qubit and Pauli channels, on density matrices of 2, 3 and 4
+    # qubits (own random stream: the cases above keep their inputs)
+    rng2 = R(seed + 1)
+    for n in (2, 3, 4):
+        for name, seq in channel2_ops(rng2, n):
+            cases.append({"name": f"dm{n}:{name}", "density": True, "n": n, "init": "random", "ops": seq,
+                          "probes": [], "stream": 2})
     # random initial states are stored explicitly
     for c in cases:
+        if c.get("stream") == 2:
+            continue
         if c["init"] == "random":
             nsv = 2 * c["n"] if c["density"] else c["n"]
             c["state"] = [cplx(z) for z in rng.state(c["n"])]          # pure state; DM mixes it with |+><+|
             c["mix"] = rng.u(0.2, 0.8)
             _ = nsv
         c["other"] = [cplx(z) for z in rng.state(c["n"])]
+    for c in cases:
+        if c.get("stream") == 2:
+            c["state"] = [cplx(z) for z in rng2.state(c["n"])]
+            c["mix"] = rng2.u(0.2, 0.8)
+            c["other"] = [cplx(z) for z in rng2.state(c["n"])]
     return cases
 
 
@@ -340,6 +374,10 @@ def apply(L, q, other, op):
         lib.initClassicalState(q, a[0])
     elif f in ("mixDephasing", "mixDepolarising", "mixDamping"):
         getattr(lib, f)(q, a[0], a[1])
+    elif f == "mixPauli":
+        lib.mixPauli(q, a[0], a[1], a[2], a[3])
+    elif f in ("mixTwoQubitDephasing", "mixTwoQubitDepolarising"):
+        getattr(lib, f)(q, a[0], a[1], a[2])
     elif f == "mixDensityMatrix":
         lib.mixDensityMatrix(q, a[0], other)
     elif f == "collapseToOutcome":

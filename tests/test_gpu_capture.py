@@ -131,6 +131,40 @@ def test_capture_density_matrix_and_channels(gpulib):
     L.destroy(cap)
 
 
+def test_capture_pauli_and_two_qubit_channels(gpulib):
+    """mixPauli (a 4 x 4 superoperator on (t, t + N)) and the two-qubit
+    dephasing and depolarising channels (16 x 16 on (q1, q2, q1 + N, q2 + N))
+    are queued like the one-qubit channels and fused with the gates."""
+    L = gpulib
+    lib = L.lib
+    n = 6
+    rng = np.random.default_rng(9)
+    direct = L.create(n, density=True)
+    cap = L.create(n, density=True)
+    lib.quest_gb300_setCapture(cap, 1)
+    for q in (direct, cap):
+        lib.initZeroState(q)
+    for layer in range(3):
+        angles = rng.uniform(0, 2 * np.pi, size=n)
+        probs = rng.uniform(0, 0.1, size=(n, 5))
+        for q in (direct, cap):
+            for t in range(n):
+                lib.rotateY(q, t, angles[t])
+            for t in range(layer % 2, n - 1, 2):
+                lib.controlledNot(q, t, t + 1)
+            for t in range(n):
+                lib.mixPauli(q, t, probs[t, 0], probs[t, 1], probs[t, 2])
+                lib.mixTwoQubitDephasing(q, t, (t + 2) % n, probs[t, 3])
+                lib.mixTwoQubitDepolarising(q, (t + 3) % n, t, probs[t, 4])
+    assert lib.quest_gb300_capturedGates(cap) > 3 * n * 3
+    a, b = L.amps(direct), L.amps(cap)
+    assert np.max(np.abs(a - b)) <= 1e-5
+    assert abs(lib.calcTotalProb(cap) - 1) < 1e-9
+    assert abs(lib.calcPurity(cap) / lib.calcPurity(direct) - 1) < 1e-6
+    L.destroy(direct)
+    L.destroy(cap)
+
+
 def test_capture_drops_queue_on_overwrite_and_off_flushes(gpulib):
     L = gpulib
     lib = L.lib

@@ -106,6 +106,40 @@ def test_validation_messages_match_reference(gpulib):
     L.destroy(q)
 
 
+def test_channel_validation_and_unsupported_api(gpulib):
+    """The two-qubit and Pauli channels check their input as the reference
+    does (QuEST_validation.c:457-461, 609-643); the API outside the
+    simulation path reports "unsupported"; neither touches the state."""
+    L = gpulib
+    assert L.capture_errors()
+    d = L.create(3, True)
+    L.lib.initPlusState(d)
+    before = L.amps(d).copy()
+    L.errors.clear()
+    L.lib.mixTwoQubitDephasing(d, 1, 1, 0.1)
+    L.lib.mixTwoQubitDephasing(d, 0, 1, 0.8)
+    L.lib.mixTwoQubitDepolarising(d, 0, 3, 0.1)
+    L.lib.mixTwoQubitDepolarising(d, 0, 1, 0.95)
+    L.lib.mixPauli(d, 0, 0.3, 0.3, 0.1)
+    L.lib.mixPauli(d, 0, -0.1, 0, 0)
+    L.lib.applyFullQFT(d)
+    msgs = [m for _, m in L.errors]
+    assert msgs[:6] == ["The target qubits must be unique.",
+                        "The probability of a two-qubit qubit dephase error cannot exceed 3/4, which maximally mixes.",
+                        "Invalid target qubit. Must be >=0 and <numQubits.",
+                        "The probability of a two-qubit depolarising error cannot exceed 15/16, which maximally mixes.",
+                        "The probability of any X, Y or Z error cannot exceed the probability of no error.",
+                        "Probabilities must be in [0, 1]."]
+    assert "unsupported" in msgs[6] and L.errors[6][0] == "applyFullQFT"
+    assert np.array_equal(L.amps(d), before)
+    q = L.create(3)
+    L.errors.clear()
+    L.lib.mixPauli(q, 0, 0.1, 0.1, 0.1)
+    assert [m for _, m in L.errors] == ["Operation valid only for density matrices."]
+    L.destroy(q)
+    L.destroy(d)
+
+
 def test_host_mirror_is_page_locked(gpulib):
     """createQureg page-locks its host mirror (cudaMallocHost), so that
     copyStateToGPU / copyStateFromGPU run at the host link's speed; the query

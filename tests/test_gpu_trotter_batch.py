@@ -74,33 +74,90 @@ def test_batch_matches_each_instance_alone(gpulib, library_errors, sites, order,
     assert not library_errors
 
 
-def test_batch_rejects_instances_of_other_shapes(gpulib, library_errors):
-    """Instances must share Pauli strings, order and repetitions."""
+def _check_instance(L, b, i, sites, U, time, order, reps, energy, q=None):
+    """Instance i of the batch against applyTrotterCircuit run alone in FP64."""
+    want, e_want, scale = plain_run(L, sites, U, time, order, reps)
+    own = q is None
+    if own:
+        q = L.create(2 * sites)
+    assert L.lib.quest_gb300_trotterBatchCopyState(b, i, q) == 0
+    got = L.amps(q)
+    if own:
+        L.destroy(q)
+    f = abs(np.vdot(want, got)) ** 2 / (np.vdot(got, got).real * np.vdot(want, want).real)
+    err = np.max(np.abs(got - want))
+    assert 1 - f <= 1e-6 and err <= 1e-5, (i, 1 - f, err)
+    assert abs(energy - e_want) <= 1e-5 * scale, (i, energy, e_want)
+    return 1 - f, abs(energy - e_want) / scale
+
+
+def test_batch_of_uneven_instances(gpulib, library_errors):
+    """Instances of different Trotter orders, step counts (repetitions),
+    Hamiltonians and register sizes run in one batch: they fall into classes
+    of one shape each, and every instance matches its own plain FP64 run; the
+    graph replay gives the same energies."""
+    L = gpulib
+    lib = L.lib
+    # (sites, U, time, order, reps): orders 1/2/4, 2..6 steps, 6 and 7 sites
+    spec = [(6, 2.0, 1.0, 1, 2), (6, 4.0, 1.0, 2, 3), (6, 8.0, 0.5, 1, 6), (7, 2.0, 1.0, 2, 2),
+            (6, 4.0, 1.0, 1, 2), (6, 2.0, 0.7, 4, 1), (7, 4.0, 1.0, 2, 2), (6, 8.0, 1.0, 2, 3)]
+    b = lib.quest_gb300_trotterBatchCreate(14, len(spec))
+    assert b
+    hams = []
+    for i, (sites, U, time, order, reps) in enumerate(spec):
+        codes, coeffs, _ = W.hubbard_terms(sites, U)
+        hams.append(L.pauli_hamil(codes, coeffs))
+        assert lib.quest_gb300_trotterBatchSetInstance(b, i, hams[-1], time, order, reps, W.neel_index(sites)) == 0
+    e1 = (C.c_double * len(spec))()
+    assert lib.quest_gb300_trotterBatchRun(b, e1) == 0, list(library_errors)
+    # classes: (6 sites, o1, 2 reps) x2, (6, o2, 3) x2, (6, o1, 6), (7, o2, 2) x2, (6, o4, 1)
+    assert lib.quest_gb300_trotterBatchNumClasses(b) == 5
+    e2 = (C.c_double * len(spec))()
+    assert lib.quest_gb300_trotterBatchRun(b, e2) == 0
+    assert list(e1) == list(e2)
+    for i, (sites, U, time, order, reps) in enumerate(spec):
+        dF, dE = _check_instance(L, b, i, sites, U, time, order, reps, e1[i])
+        print(f"instance {i} {spec[i]}: 1-F={dF:.2e}, |dE|/sum|c|={dE:.2e}")
+    lib.quest_gb300_trotterBatchDestroy(b)
+    for h in hams:
+        lib.destroyPauliHamil(h)
+    assert not library_errors
+
+
+def test_batch_checks_and_precision_switch(gpulib, library_errors):
+    """CopyState needs a run and a register of the instance's size; changing
+    the tensor-core precision between runs rebuilds the batch's operands for
+    the new kernels."""
     L = gpulib
     lib = L.lib
     sites = 6
     n = 2 * sites
     b = lib.quest_gb300_trotterBatchCreate(n, 2)
     c0, k0, _ = W.hubbard_terms(sites, 2.0)
-    c1, k1, _ = W.hubbard_terms(sites - 1, 2.0)
-    c1 = np.concatenate([c1, np.zeros((len(c1), 2), dtype=c1.dtype)], axis=1)   # other strings, same width
-    h0, h1 = L.pauli_hamil(c0, k0), L.pauli_hamil(c1, k1)
-    assert lib.quest_gb300_trotterBatchSetInstance(b, 0, h0, 1.0, 1, 2, 0) == 0
-    assert lib.quest_gb300_trotterBatchSetInstance(b, 1, h1, 1.0, 1, 2, 0) == 0
+    h0 = L.pauli_hamil(c0, k0)
+    assert lib.quest_gb300_trotterBatchSetInstance(b, 0, h0, 1.0, 1, 2, W.neel_index(sites)) == 0
+    assert lib.quest_gb300_trotterBatchSetInstance(b, 1, h0, 1.0, 2, 2, W.neel_index(sites)) == 0
     q = L.create(n)
     assert lib.quest_gb300_trotterBatchCopyState(b, 0, q) == -1                          # nothing run yet
     assert any("run it first" in m for _, m in library_errors), list(library_errors)
     library_errors.clear()
-    assert lib.quest_gb300_trotterBatchRun(b, None) == -1
-    assert any("share Pauli strings" in m for _, m in library_errors), list(library_errors)
+    c1, k1, _ = W.hubbard_terms(7, 2.0)
+    h1 = L.pauli_hamil(c1, k1)
+    assert lib.quest_gb300_trotterBatchSetInstance(b, 0, h1, 1.0, 1, 2, 0) == -1         # wider than the batch
     library_errors.clear()
-    assert lib.quest_gb300_trotterBatchSetInstance(b, 1, h0, 1.0, 2, 2, 0) == 0             # other order
-    assert lib.quest_gb300_trotterBatchRun(b, None) == -1
-    library_errors.clear()
-    assert lib.quest_gb300_trotterBatchSetInstance(b, 1, h0, 0.5, 1, 2, 3) == 0             # same shape
-    assert lib.quest_gb300_trotterBatchRun(b, None) == 0
-    assert lib.quest_gb300_trotterBatchCopyState(b, 1, q) == 0
-    assert abs(L.lib.calcTotalProb(q) - 1) < 1e-6
+    before = lib.quest_gb300_getTensorCorePrecision()
+    e = (C.c_double * 2)()
+    try:
+        for prec in (0, 1, 0):
+            assert lib.quest_gb300_setTensorCorePrecision(prec) == 0
+            assert lib.quest_gb300_trotterBatchRun(b, e) == 0, list(library_errors)
+            for i, order in enumerate((1, 2)):
+                _check_instance(L, b, i, sites, 2.0, 1.0, order, 2, e[i], q)
+    finally:
+        lib.quest_gb300_setTensorCorePrecision(before)
+    small = L.create(n - 2)
+    assert lib.quest_gb300_trotterBatchCopyState(b, 0, small) == -1
+    L.destroy(small)
     L.destroy(q)
     lib.quest_gb300_trotterBatchDestroy(b)
     lib.destroyPauliHamil(h0)

@@ -68,25 +68,31 @@ def test_shards_partition_the_units():
 
 
 @pytest.mark.parametrize("world", [2, 4])
-def test_trotter_instances_shard_into_same_shape_batches(world):
+def test_trotter_instances_shard_by_cost(world):
     """The 64 Fermi-Hubbard instances of configuration 4 are dealt to ranks by
-    cost; each rank's share falls into batches of one shape (order and step
-    count), which is what a Trotter batch accepts."""
+    cost (a rank then runs its share as one Trotter batch, whatever the
+    orders and step counts); the loads differ by at most one instance."""
     from quantumlab_gb300 import workloads as W
-    from quantumlab_gb300.sharding import shard_units, trotter_batches, trotter_instance_cost
+    from quantumlab_gb300.sharding import shard_units, trotter_instance_cost
 
     inst = W.hubbard_instances(64)
     steps = [int(round(1.0 / dt)) for _, dt, _ in inst]
     order = [o for _, _, o in inst]
     cost = trotter_instance_cost(steps, order)
-    shapes = [(o, s) for o, s in zip(order, steps)]
-    seen = []
-    loads = []
+    seen, loads = [], []
     for rank in range(world):
         mine = shard_units(cost, world, rank)
         loads.append(cost[mine].sum())
-        for batch in trotter_batches(shapes, mine):
-            assert len({shapes[i] for i in batch}) == 1
-            seen += batch
+        seen += list(mine)
     assert sorted(seen) == list(range(64))
     assert max(loads) - min(loads) <= cost.max()
+
+
+def test_trotter_cost_counts_the_exponentials():
+    """Exponentials per step: 1 at order 1, 2 at order 2, 10 at order 4
+    (five second-order products), 50 at order 6."""
+    from quantumlab_gb300.sharding import trotter_instance_cost
+    assert list(trotter_instance_cost([10, 10, 10, 10], [1, 2, 4, 6])) == [10.0, 20.0, 100.0, 500.0]
+    costs = trotter_instance_cost([3, 3, 3, 3], [4, 1, 1, 1])
+    parts = [sharding.shard_units(costs, 2, r) for r in range(2)]
+    assert sorted(len(p) for p in parts) == [1, 3]          # the order-4 instance alone on one rank
