@@ -62,14 +62,25 @@ int quest_gb300_planNumGates(void* plan);
 int quest_gb300_planPass(void* plan, int i, int* targets, double* re, double* im);
 
 /* ---- autotuner -------------------------------------------------------------
- * Per-pass cost table (ms) by width k and target layout (a target below qubit
- * 5 or not) for registers of numQubits qubits, measured on a scratch FP32
- * register and cached as JSON ($QUEST_GB300_TUNE_CACHE, default
- * ~/.cache/quest_gb300_tune.json).  planCompileTuned compiles the plan at
- * every width in [minK, maxK] and keeps the fastest predicted one.          */
+ * No counterpart in the reference.  autotune measures, for registers of
+ * numQubits qubits at the current tensor-core precision, the time of one pass
+ * of every width k = 1..6 in every target layout class (0: every target at or
+ * above qubit 5; 1: a target below 5; 2: qubits 0 and 1 both targets) on a
+ * scratch FP32 register.  Each class that runs on the tensor cores is timed
+ * with every pipelined kernel variant (2: two loader groups on alternate
+ * chunks + one epilogue group; 3: one + one; 4: one + two; 5: two loader
+ * groups splitting each chunk + two epilogue groups) and the fastest is used
+ * for that class from then on (setKernelTuning(0) returns to the fixed
+ * defaults).  The table is cached as JSON ($QUEST_GB300_TUNE_CACHE, default
+ * ~/.cache/quest_gb300_tune.json) and loaded by the first autotune call.
+ * planCompileTuned compiles the plan at every width in [minK, maxK] and keeps
+ * the fastest predicted one.  tunedKernel returns the chosen variant of a
+ * class (0 if untuned) and its measured time per pass.                      */
 int quest_gb300_autotune(int numQubits);
 double quest_gb300_planPredictMs(void* plan);
 int quest_gb300_planCompileTuned(void* plan, int minK, int maxK);
+int quest_gb300_tunedKernel(int numQubits, int k, int layout, double* msPerPass);
+void quest_gb300_setKernelTuning(int on);
 
 /* ---- FP32 registers of the fused engine ----------------------------------
  * A state vector of 2^numQubits FP32 complex amplitudes (SoA) on the
@@ -127,6 +138,12 @@ double quest_gb300_compareF32(void* qureg32, Qureg reference, double* maxAmpErr)
 void* quest_gb300_swapTestBatchCreate(const double* vectors, const long long* offsets, const int* dimLog2,
                                       int numVectors, const int* idxA, const int* idxB, int numTests);
 int quest_gb300_swapTestBatchRun(void* batch, double* p0Out);
+/* Autotune the batch's kernel: time every pairing of CTAs per SM (2, 3, 4)
+ * and shared-memory threshold (states of up to 2^9, 2^11 or 2^13 amplitudes
+ * kept in shared memory, larger ones in a global arena), keep the fastest and
+ * capture the graph again with it.  Writes the choice, its time per run and
+ * the default's (4 CTAs per SM, 2^13) in ms; returns 0 or -1. */
+int quest_gb300_swapTestBatchTune(void* batch, int* ctasPerSM, int* smemAmps, double* msBest, double* msDefault);
 void quest_gb300_swapTestBatchDestroy(void* batch);
 
 /* ---- op-stream capture ------------------------------------------------------
@@ -150,7 +167,9 @@ int quest_gb300_capturedGates(Qureg qureg);
  * them (any pointer may be null).  Returns 0, or -1 when capture is off. */
 int quest_gb300_captureStats(Qureg qureg, long long* flushes, long long* gatesApplied, long long* passesApplied,
                              double* compileMs);
-/* widest fused pass of the flushes, 1..6 (default 6) */
+/* widest fused pass of the flushes, 1..6 (default 6); 0: the autotuner picks
+ * the width of each searched plan (planCompileTuned over 4..6; the first such
+ * flush of a register size measures its cost table) */
 void quest_gb300_setCaptureFusion(int maxFusedQubits);
 
 /* ---- amplitude-encoded product states ------------------------------------------

@@ -1,13 +1,17 @@
-// autotune.cpp -- fusion-width autotuner of the FP32 fused engine (host C++).
-// No counterpart in the reference.
+// autotune.cpp -- autotuner of the FP32 fused engine (host C++).  No
+// counterpart in the reference.
 //
 // The cost of a fused pass depends on its width k, on the applier that runs
-// it (SIMT for k <= 3, tensor cores for k = 4..6) and on whether one of its
-// targets is a low qubit (< 5), which selects the staging tensor-core kernel.
-// The tuner times one synthetic pass of every (k, layout) class on a scratch
-// FP32 register of the requested size, keeps the table in memory and in a
-// small JSON cache file, and picks for a plan the width k in {minK..maxK}
-// whose compiled pass list has the lowest predicted time.
+// it (SIMT for k <= 3, tensor cores for k = 4..6), on its target layout (all
+// targets at or above qubit 5; a target below 5; qubits 0 and 1 both
+// targets) and, on the tensor cores, on the pipeline shape of the kernel (how
+// many loader and epilogue warp groups, whether the loaders split each
+// K-chunk).  The tuner times one synthetic pass of every (k, layout) class on
+// a scratch FP32 register of the requested size, each tensor-core class with
+// every pipeline variant, keeps the fastest variant per class (the launcher
+// uses it from then on) and the per-pass times in memory and in a small JSON
+// cache file, and picks for a plan the width k in {minK..maxK} whose compiled
+// pass list has the lowest predicted time.
 #include "fused_plan.h"
 #include "qg_internal.h"
 #include "quest_gb300.h"
@@ -25,15 +29,24 @@
 #include <string>
 #include <vector>
 
+namespace qg {
+int tuneLayout(const FusedPass& pass);
+void setTunedKernel(int n, int prec, int k, int layout, int version);
+void setKernelTrial(int version);
+void setKernelTuning(bool on);
+}  // namespace qg
+
 namespace {
 
+// per (register size, operand precision): ms per pass and the tensor-core
+// variant chosen, indexed [k][layout] (qg::tuneLayout); 0 = not measured
 struct CostTable {
-    // ms per pass, indexed [k][lowTarget]; 0 = not measured
-    double ms[7][2] = {};
+    double ms[7][3] = {};
+    int ver[7][3] = {};
 };
 
 std::mutex g_tuneMutex;
-std::map<int, CostTable> g_tables;   // by register size n
+std::map<std::pair<int, int>, CostTable> g_tables;
 
 std::string cachePath() {
     if (const char* e = getenv("QUEST_GB300_TUNE_CACHE")) return e;
@@ -41,7 +54,8 @@ std::string cachePath() {
     return std::string(home ? home : "/tmp") + "/.cache/quest_gb300_tune.json";
 }
 
-// cache format: {"n": {"k,low": ms, ...}, ...} -- one flat object per size
+// cache format: one flat object, "n<n>_p<prec>_k<k>_l<layout>": ms and
+// "n<n>_p<prec>_k<k>_l<layout>_v": variant
 void loadCache() {
     FILE* f = fopen(cachePath().c_str(), "r");
     if (!f) return;
@@ -55,11 +69,18 @@ void loadCache() {
         const size_t end = s.find('"', pos + 1);
         if (end == std::string::npos) break;
         const std::string key = s.substr(pos + 1, end - pos - 1);
-        int n = 0, k = 0, low = 0;
-        double ms = 0;
-        if (sscanf(key.c_str(), "n%d_k%d_low%d", &n, &k, &low) == 3 && k >= 1 && k <= 6 && (low == 0 || low == 1) &&
-            sscanf(s.c_str() + end + 1, " : %lf", &ms) == 1 && ms > 0)
-            g_tables[n].ms[k][low] = ms;
+        int n = 0, prec = 0, k = 0, lay = 0, chars = 0;
+        double v = 0;
+        if (sscanf(key.c_str(), "n%d_p%d_k%d_l%d%n", &n, &prec, &k, &lay, &chars) == 4 && k >= 1 && k <= 6 &&
+            lay >= 0 && lay < 3 && (prec == 0 || prec == 1) && sscanf(s.c_str() + end + 1, " : %lf", &v) == 1 && v > 0) {
+            CostTable& t = g_tables[{n, prec}];
+            if (key.compare(chars, std::string::npos, "_v") == 0) {
+                t.ver[k][lay] = (int)v;
+                qg::setTunedKernel(n, prec, k, lay, (int)v);
+            } else if ((size_t)chars == key.size()) {
+                t.ms[k][lay] = v;
+            }
+        }
         pos = end + 1;
     }
 }
@@ -78,11 +99,15 @@ void saveCache() {
     bool first = true;
     for (auto& kv : g_tables)
         for (int k = 1; k <= 6; ++k)
-            for (int low = 0; low < 2; ++low)
-                if (kv.second.ms[k][low] > 0) {
-                    fprintf(f, "%s  \"n%d_k%d_low%d\": %.6f", first ? "" : ",\n", kv.first, k, low, kv.second.ms[k][low]);
+            for (int lay = 0; lay < 3; ++lay) {
+                const int n = kv.first.first, prec = kv.first.second;
+                if (kv.second.ms[k][lay] > 0) {
+                    fprintf(f, "%s  \"n%d_p%d_k%d_l%d\": %.6f", first ? "" : ",\n", n, prec, k, lay, kv.second.ms[k][lay]);
                     first = false;
                 }
+                if (kv.second.ver[k][lay] > 0)
+                    fprintf(f, ",\n  \"n%d_p%d_k%d_l%d_v\": %d", n, prec, k, lay, kv.second.ver[k][lay]);
+            }
     fprintf(f, "\n}\n");
     fclose(f);
 }
@@ -114,57 +139,118 @@ double timePass(void* q32, int n, const std::vector<int>& t) {
     return ms[1];
 }
 
+// targets of a synthetic pass of width k in layout class `lay` on n qubits
+// (empty if the class does not exist there)
+std::vector<int> layoutTargets(int n, int k, int lay) {
+    std::vector<int> t;
+    if (lay == 2) {
+        if (k < 2) return {};
+        t = {0, 1};
+    } else if (lay == 1) {
+        t = {2};
+    }
+    // the rest spread over the high qubits (>= 5), two apart from the top
+    for (int q = n - 1; (int)t.size() < k && q >= 5; q -= 2) t.push_back(q);
+    for (int q = 5; (int)t.size() < k && q < n; ++q)
+        if (std::find(t.begin(), t.end(), q) == t.end()) t.push_back(q);
+    std::sort(t.begin(), t.end());
+    t.erase(std::unique(t.begin(), t.end()), t.end());
+    if ((int)t.size() != k) return {};
+    return t;
+}
+
+int layoutOf(const std::vector<int>& targets) {
+    if (targets.size() >= 2 && targets[0] == 0 && targets[1] == 1) return 2;
+    return targets[0] < 5 ? 1 : 0;
+}
+
 }  // namespace
 
 extern "C" {
 
 // Measure (or load from the cache) the per-pass cost table for registers of
-// numQubits qubits.  Returns 0 on success.
+// numQubits qubits at the current tensor-core precision.  For every width k
+// and target layout class that runs on the tensor cores, each pipelined
+// variant (loader / epilogue warp-group counts and chunk split: versions 2
+// to 5) is timed and the fastest becomes that class's kernel from then on.
+// Returns 0 on success.
 int quest_gb300_autotune(int numQubits) {
+    if (numQubits < 1 || numQubits > 40) return -1;
     std::lock_guard<std::mutex> lk(g_tuneMutex);
     std::call_once(g_loaded, loadCache);
-    CostTable& t = g_tables[numQubits];
+    const int prec = quest_gb300_getTensorCorePrecision();
+    CostTable& t = g_tables[{numQubits, prec}];
+    auto wanted = [&](int k, int lay) {
+        if (k > numQubits || (k == 6 && numQubits < 13)) return false;    // 6-qubit passes need n >= k + 7
+        return !layoutTargets(numQubits, k, lay).empty();
+    };
     bool missing = false;
     for (int k = 1; k <= 6; ++k)
-        for (int low = 0; low < 2; ++low)
-            if (k <= numQubits - (low ? 0 : 5) && !(k == 6 && numQubits < 13) && !(t.ms[k][low] > 0)) missing = true;
+        for (int lay = 0; lay < 3; ++lay)
+            if (wanted(k, lay) && !(t.ms[k][lay] > 0)) missing = true;
     if (!missing) return 0;
     void* q32 = quest_gb300_createQuregF32(numQubits);
     if (!q32) return -1;
-    for (int k = 1; k <= 6 && k <= numQubits; ++k)
-        for (int low = 0; low < 2; ++low) {
-            if (t.ms[k][low] > 0) continue;
-            if (k == 6 && numQubits < 13) continue;       // 6-qubit passes need the tensor-core applier (n >= k + 7)
-            std::vector<int> targ;
-            if (low) {
-                for (int i = 0; i < k; ++i) targ.push_back(i * 2 < numQubits ? i * 2 : i);    // includes qubit 0
-            } else {
-                if (numQubits - k < 5) continue;
-                for (int i = 0; i < k; ++i) targ.push_back(numQubits - 1 - 2 * i >= 5 ? numQubits - 1 - 2 * i : 5 + i);
+    quest_gb300_initZeroStateF32(q32);
+    for (int k = 1; k <= 6; ++k)
+        for (int lay = 0; lay < 3; ++lay) {
+            if (!wanted(k, lay) || t.ms[k][lay] > 0) continue;
+            const std::vector<int> targ = layoutTargets(numQubits, k, lay);
+            const bool tc = k >= 4 && numQubits >= k + 7;
+            if (!tc) {
+                t.ms[k][lay] = timePass(q32, numQubits, targ);
+                continue;
             }
-            std::sort(targ.begin(), targ.end());
-            targ.erase(std::unique(targ.begin(), targ.end()), targ.end());
-            if ((int)targ.size() != k) continue;
-            t.ms[k][low] = timePass(q32, numQubits, targ);
+            double best = 0;
+            int bestV = 0;
+            for (int v = 2; v <= 5; ++v) {
+                qg::setKernelTrial(v);
+                const double ms = timePass(q32, numQubits, targ);
+                if (ms > 0 && (bestV == 0 || ms < best)) {
+                    best = ms;
+                    bestV = v;
+                }
+            }
+            qg::setKernelTrial(0);
+            t.ms[k][lay] = best;
+            t.ver[k][lay] = bestV;
+            qg::setTunedKernel(numQubits, prec, k, lay, bestV);
         }
     quest_gb300_destroyQuregF32(q32);
     saveCache();
     return 0;
 }
 
+// The tensor-core variant the tuner chose for passes of width k in target
+// layout class `layout` (0: every target >= 5; 1: a target below 5; 2:
+// targets include qubits 0 and 1) on numQubits qubits at the current
+// precision, and its time per pass; 0 when that class is not tuned.
+int quest_gb300_tunedKernel(int numQubits, int k, int layout, double* msPerPass) {
+    std::lock_guard<std::mutex> lk(g_tuneMutex);
+    if (k < 1 || k > 6 || layout < 0 || layout > 2) return 0;
+    auto it = g_tables.find({numQubits, quest_gb300_getTensorCorePrecision()});
+    if (it == g_tables.end()) return 0;
+    if (msPerPass) *msPerPass = it->second.ms[k][layout];
+    return it->second.ver[k][layout];
+}
+
+// Use the tuned variants (on, the default once a table is loaded) or the
+// fixed per-width defaults (off).
+void quest_gb300_setKernelTuning(int on) { qg::setKernelTuning(on != 0); }
+
 // Predicted time (ms) of a compiled plan from the cost table (autotune first).
 double quest_gb300_planPredictMs(void* plan) {
     qg::FusedPlan* p = reinterpret_cast<qg::FusedPlan*>(plan);
     if (!p || !p->compiled) return -1;
     std::lock_guard<std::mutex> lk(g_tuneMutex);
-    auto it = g_tables.find(p->numQubits);
+    auto it = g_tables.find({p->numQubits, quest_gb300_getTensorCorePrecision()});
     if (it == g_tables.end()) return -1;
     double total = 0;
     for (const auto& pass : p->passes) {
         const int k = (int)pass.targets.size();
-        const int low = pass.targets[0] < 5 ? 1 : 0;
-        double c = it->second.ms[k][low];
-        if (!(c > 0)) c = it->second.ms[k][1 - low];
+        const int lay = layoutOf(pass.targets);
+        double c = it->second.ms[k][lay];
+        for (int alt = 0; alt < 3 && !(c > 0); ++alt) c = it->second.ms[k][alt];
         if (!(c > 0)) return -1;
         total += c;
     }

@@ -38,9 +38,9 @@ namespace qg {
 namespace {
 
 constexpr int kSwapThreads = 256;
-constexpr int kSwapCtasPerSM = 4;
+constexpr int kSwapCtasPerSM = 4;        // the most CTAs per SM (launch bounds); the default
 constexpr int kAreaFloats = (kSwapThreads / 32) * 32 * 33;   // 8 transpose tiles (33.8 KB)
-constexpr int kSmemAmps = 8192;          // pass A/B in shared memory up to 2^13 amplitudes (d <= 6)
+constexpr int kSmemAmps = 8192;          // default: pass A/B in shared memory up to 2^13 amplitudes (d <= 6)
 static_assert(kSmemAmps <= kAreaFloats, "a small state must fit the tile area");
 constexpr int kMaxD = 10;
 constexpr double kInvSqrt2 = 0.70710678118654752440;
@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(kSwapThreads, kSwapCtasPerSM) kSwapTests(const
                                                                            const SwapJob* __restrict__ jobs, int numJobs,
                                                                            unsigned int* __restrict__ ticket,
                                                                            float* __restrict__ arena, size_t arenaPerCta,
-                                                                           double* __restrict__ out) {
+                                                                           double* __restrict__ out, int smemAmps) {
     __shared__ __align__(16) float su[1 << kMaxD];
     __shared__ float sv[1 << kMaxD];
     // the whole state of a small test, or the warps' 32 x 33 transpose tiles
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(kSwapThreads, kSwapCtasPerSM) kSwapTests(const
         }
         __syncthreads();
         double total = 0.0;
-        if (2 * half <= (uint64_t)kSmemAmps) {
+        if (2 * half <= (uint64_t)smemAmps) {
             // ---- small state, in shared memory
             float* phi = area;
             for (uint32_t idx = threadIdx.x; idx < half; idx += kSwapThreads) {
@@ -159,19 +159,52 @@ struct SwapBatch {
     SwapJob* jobs = nullptr;
     unsigned int* ticket = nullptr;
     float* arena = nullptr;
-    size_t arenaPerCta = 0;
+    size_t arenaPerCta = 0;           // floats per CTA of the arena (for up to kSwapCtasPerSM CTAs per SM)
     double* out = nullptr;
-    int grid = 0;
+    int maxD = 1;
+    int ctasPerSM = kSwapCtasPerSM;   // tunable: 1 .. kSwapCtasPerSM
+    int smemAmps = kSmemAmps;         // tunable: states of at most this many amplitudes stay in shared memory
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     double* hostOut = nullptr;        // pinned
 };
 
+void dropGraph(SwapBatch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
+// the run's work on `st`: reset the ticket, the persistent kernel, results to
+// pinned host memory
+void queueSwaps(SwapBatch* b, cudaStream_t st) {
+    cudaMemsetAsync(b->ticket, 0, sizeof(unsigned int), st);
+    kSwapTests<<<numSMs() * b->ctasPerSM, kSwapThreads, 0, st>>>(b->pool, b->jobs, b->numTests, b->ticket, b->arena,
+                                                                  b->arenaPerCta, b->out, b->smemAmps);
+    cudaMemcpyAsync(b->hostOut, b->out, b->numTests * sizeof(double), cudaMemcpyDeviceToHost, st);
+}
+
+// (re)capture the graph for the current parameters
+bool captureSwaps(SwapBatch* b, const char* fn) {
+    dropGraph(b);
+    cudaStream_t cap = nullptr;
+    if (QG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), fn)) return false;
+    bool ok = !QG_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), fn);
+    if (ok) {
+        queueSwaps(b, cap);
+        ok = !QG_CUDA(cudaStreamEndCapture(cap, &b->graph), fn);
+    }
+    if (ok) ok = !QG_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0), fn);
+    cudaStreamDestroy(cap);
+    if (!ok) dropGraph(b);
+    return ok;
+}
+
 void freeBatch(SwapBatch* b) {
     if (!b) return;
     cudaStreamSynchronize(stream());
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->graph) cudaGraphDestroy(b->graph);
+    dropGraph(b);
     cudaFree(b->pool);
     cudaFree(b->jobs);
     cudaFree(b->ticket);
@@ -219,9 +252,12 @@ void* quest_gb300_swapTestBatchCreate(const double* vectors, const long long* of
     std::stable_sort(jobs.begin(), jobs.end(), [](const SwapJob& x, const SwapJob& y) { return x.d > y.d; });
     SwapBatch* b = new SwapBatch();
     b->numTests = numTests;
-    b->grid = qg::numSMs() * qg::kSwapCtasPerSM;
-    const size_t arenaNeed = (2ull << (2 * maxD)) > (size_t)qg::kSmemAmps ? (2ull << (2 * maxD)) : 0;
+    b->maxD = maxD;
+    // an arena slice per CTA for every state that may leave shared memory
+    // (any state above the smallest tunable threshold)
+    const size_t arenaNeed = (2ull << (2 * maxD)) > 512 ? (2ull << (2 * maxD)) : 0;
     b->arenaPerCta = arenaNeed;
+    const size_t maxGrid = (size_t)qg::numSMs() * qg::kSwapCtasPerSM;
     std::vector<float> pool32(poolLen);
     for (long long i = 0; i < poolLen; ++i) pool32[i] = (float)vectors[i];
     cudaStream_t st = qg::stream();
@@ -230,34 +266,63 @@ void* quest_gb300_swapTestBatchCreate(const double* vectors, const long long* of
         QG_CUDA(cudaMalloc(&b->ticket, sizeof(unsigned int)), fn) ||
         QG_CUDA(cudaMalloc(&b->out, numTests * sizeof(double)), fn) ||
         QG_CUDA(cudaMallocHost(&b->hostOut, numTests * sizeof(double)), fn) ||
-        (arenaNeed && QG_CUDA(cudaMalloc(&b->arena, arenaNeed * b->grid * sizeof(float)), fn))) {
+        (arenaNeed && QG_CUDA(cudaMalloc(&b->arena, arenaNeed * maxGrid * sizeof(float)), fn))) {
         qg::freeBatch(b);
         return nullptr;
     }
     QG_CUDA(cudaMemcpyAsync(b->pool, pool32.data(), poolLen * sizeof(float), cudaMemcpyHostToDevice, st), fn);
     QG_CUDA(cudaMemcpyAsync(b->jobs, jobs.data(), numTests * sizeof(SwapJob), cudaMemcpyHostToDevice, st), fn);
     QG_CUDA(cudaStreamSynchronize(st), fn);
-    // capture: reset ticket, the persistent kernel, results to pinned host
-    cudaStream_t cap = nullptr;
-    if (QG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), fn)) {
-        qg::freeBatch(b);
-        return nullptr;
-    }
-    bool ok = !QG_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), fn);
-    if (ok) {
-        cudaMemsetAsync(b->ticket, 0, sizeof(unsigned int), cap);
-        qg::kSwapTests<<<b->grid, qg::kSwapThreads, 0, cap>>>(b->pool, b->jobs, numTests, b->ticket, b->arena,
-                                                               b->arenaPerCta, b->out);
-        cudaMemcpyAsync(b->hostOut, b->out, numTests * sizeof(double), cudaMemcpyDeviceToHost, cap);
-        ok = !QG_CUDA(cudaStreamEndCapture(cap, &b->graph), fn);
-    }
-    if (ok) ok = !QG_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0), fn);
-    cudaStreamDestroy(cap);
-    if (!ok) {
+    if (!qg::captureSwaps(b, fn)) {
         qg::freeBatch(b);
         return nullptr;
     }
     return b;
+}
+
+// Time the batch with every pairing of CTAs per SM (2, 3, 4) and
+// shared-memory threshold (states of up to 2^9, 2^11 or 2^13 amplitudes stay
+// in shared memory: d <= 4, 5 or 6), two runs each, keep the fastest and
+// capture the graph again with it.  Writes the choice, its time and the time
+// of the default (4 CTAs per SM, 2^13) in ms; returns 0 or -1.
+int quest_gb300_swapTestBatchTune(void* batch, int* ctasPerSM, int* smemAmps, double* msBest, double* msDefault) {
+    SwapBatch* b = reinterpret_cast<SwapBatch*>(batch);
+    const char* fn = "quest_gb300_swapTestBatchTune";
+    if (!b) return -1;
+    cudaStream_t st = qg::stream();
+    cudaEvent_t e0, e1;
+    if (QG_CUDA(cudaEventCreate(&e0), fn) || QG_CUDA(cudaEventCreate(&e1), fn)) return -1;
+    double best = -1, dflt = -1;
+    int bestC = qg::kSwapCtasPerSM, bestS = qg::kSmemAmps;
+    for (int c = 2; c <= qg::kSwapCtasPerSM; ++c)
+        for (int sm : {512, 2048, 8192}) {
+            b->ctasPerSM = c;
+            b->smemAmps = sm;
+            qg::queueSwaps(b, st);                    // warm-up
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < 2; ++r) qg::queueSwaps(b, st);
+            cudaEventRecord(e1, st);
+            if (QG_CUDA(cudaEventSynchronize(e1), fn)) return -1;
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            const double per = ms / 2.0;
+            if (c == qg::kSwapCtasPerSM && sm == qg::kSmemAmps) dflt = per;
+            if (best < 0 || per < best) {
+                best = per;
+                bestC = c;
+                bestS = sm;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->ctasPerSM = bestC;
+    b->smemAmps = bestS;
+    if (!qg::captureSwaps(b, fn)) return -1;
+    if (ctasPerSM) *ctasPerSM = bestC;
+    if (smemAmps) *smemAmps = bestS;
+    if (msBest) *msBest = best;
+    if (msDefault) *msDefault = dflt;
+    return 0;
 }
 
 // Replay the batch's graph on the library stream and write P(anc = 0) of

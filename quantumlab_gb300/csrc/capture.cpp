@@ -50,7 +50,10 @@ namespace {
 std::mutex g_capMutex;
 std::unordered_map<const double*, Capture*> g_caps;
 int g_capDefault = -1;            // -1: not read from the environment yet
-int g_capMaxFused = 6;
+int g_capMaxFused = 6;            // 0: the autotuner picks the width per searched plan
+
+// the widest pass a flush of an n-qubit register may fuse
+int capWidest(int n) { return g_capMaxFused == 0 ? widestPass(n) : std::min(g_capMaxFused, widestPass(n)); }
 
 int defaultMode() {
     if (g_capDefault < 0) {
@@ -123,11 +126,19 @@ static void flushRecord(Capture* c, double* re, double* im) {
     quest_gb300_copyFromQureg(c->q32, view);
     FusedPlan* plan = new FusedPlan();
     plan->numQubits = c->n;
-    plan->maxFused = std::min(g_capMaxFused, widestPass(c->n));
+    const bool tuned = g_capMaxFused == 0;
+    plan->maxFused = tuned && c->shape ? c->shape->maxFused : capWidest(c->n);
     plan->gates.swap(c->gates);
     const auto t0 = std::chrono::steady_clock::now();
     const bool reused = c->shape && c->shape->maxFused == plan->maxFused && compilePlanLike(*plan, *c->shape);
-    if (!reused) compilePlan(*plan);
+    if (!reused) {
+        // autotuned: the width with the lowest predicted time (the cost table
+        // of this register size is measured by the first such flush)
+        if (!tuned || quest_gb300_planCompileTuned(plan, std::min(4, capWidest(c->n)), capWidest(c->n)) < 0) {
+            plan->maxFused = capWidest(c->n);
+            compilePlan(*plan);
+        }
+    }
     c->compileMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (!plan->compiled) {
         invalidQuESTInputError("The captured gates could not be fused.", "captureFlush");
@@ -197,7 +208,7 @@ static bool captureGate(SV s, uint64_t mask, const std::function<void(std::vecto
     Capture* c = reinterpret_cast<Capture*>(s.cap);
     const Local l = localOf(mask);
     const int k = (int)l.qubits.size();
-    if (k < 1 || k > std::min(g_capMaxFused, widestPass(c->n))) {
+    if (k < 1 || k > capWidest(c->n)) {
         flushRecord(c, s.re, s.im);
         return false;
     }
@@ -397,9 +408,10 @@ int quest_gb300_captureStats(Qureg q, long long* flushes, long long* gatesApplie
     return 0;
 }
 
-/* Largest fused pass width used by flushes (1..6, default 6). */
+/* Largest fused pass width used by flushes (1..6, default 6); 0: the
+ * autotuner picks the width of each searched plan. */
 void quest_gb300_setCaptureFusion(int maxFusedQubits) {
-    if (maxFusedQubits >= 1 && maxFusedQubits <= 6) qg::g_capMaxFused = maxFusedQubits;
+    if (maxFusedQubits >= 0 && maxFusedQubits <= 6) qg::g_capMaxFused = maxFusedQubits;
 }
 
 }  // extern "C"

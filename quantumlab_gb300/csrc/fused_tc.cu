@@ -13,10 +13,14 @@
 //
 // Two kernels:
 //   * kApplyTC2 (the default; "pipelined kernel" below): warp-specialised and
-//     persistent, split-BF16 operands.  X = Xh + Xl (two BF16 parts, ~2^-17)
-//     and Gr = Gh + Gl + Gll (three BF16 parts, ~2^-24); Out = Xh.Gh + Xl.Gh
-//     + Xh.Gl + Xh.Gll accumulated in FP32 by kind::f16 MMAs, which run at
-//     twice the TF32 rate;
+//     persistent, with one of two operand forms (setTensorCorePrecision):
+//       - 3-term split-TF32, the default: X = Xh + Xl and Gr = Gh + Gl in
+//         TF32 parts, Out = Xh.Gh + Xl.Gh + Xh.Gl accumulated in FP32 by
+//         kind::tf32 MMAs;
+//       - 4-term split-BF16: X = Xh + Xl (two BF16 parts, ~2^-17) and
+//         Gr = Gh + Gl + Gll (three BF16 parts, ~2^-24), Out = Xh.Gh + Xl.Gh
+//         + Xh.Gl + Xh.Gll accumulated in FP32 by kind::f16 MMAs, which run
+//         at twice the TF32 rate;
 //   * kApplyTC (setTensorCoreKernel(1)): the direct-load kernel, split-TF32.
 //     Each thread owns one tile column and loads its 2D values straight from
 //     global memory (the 32 lanes of a warp read 32 consecutive amplitudes),
@@ -1180,6 +1184,12 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
 bool g_tcEnabled = true;
 int g_tcPrecision = kPrecTF32;   // operands of the pipelined kernel
 int g_tcVersion = 0;      // 0: per pass by target layout; 1, 2, 3: force one kernel
+int g_tcTrial = 0;        // autotuner: the pipelined variant being timed (0: none)
+bool g_tcTuning = true;   // use the tuned variant of a pass class when there is one
+// tuned pipelined variant (2..5, 0 = none) by register size, precision,
+// width k and target layout (tuneLayout)
+constexpr int kTuneMaxN = 40;
+int g_tcTuned[kTuneMaxN + 1][2][7][3] = {};
 
 }  // namespace
 
@@ -1376,10 +1386,33 @@ void tcNoteSimtPass(void* devPlan, size_t index) {
 //   * 6 qubits: kernel 5 (2.7-3.0).  Kernels 2 and 4 are each a few percent
 //     faster on some target sets.  Choosing by target set came to the same
 //     total over the 30-qubit circuit (297.4 against 296.3 ms).
+// A pass's target layout class for the tuner: 2 when qubits 0 and 1 are both
+// targets (the 16-byte column variant), 1 when another target is below qubit
+// 5, 0 when every target is at or above qubit 5.
+int tuneLayout(const FusedPass& pass) {
+    if (pass.targets.size() >= 2 && pass.targets[0] == 0 && pass.targets[1] == 1) return 2;
+    return pass.targets[0] < 5 ? 1 : 0;
+}
+void setTunedKernel(int n, int prec, int k, int layout, int version) {
+    if (n >= 0 && n <= kTuneMaxN && (prec == 0 || prec == 1) && k >= 4 && k <= 6 && layout >= 0 && layout < 3)
+        g_tcTuned[n][prec][k][layout] = (version >= 2 && version <= 5) ? version : 0;
+}
+int tunedKernel(int n, int prec, int k, int layout) {
+    if (n < 0 || n > kTuneMaxN || (prec != 0 && prec != 1) || k < 4 || k > 6 || layout < 0 || layout > 2) return 0;
+    return g_tcTuned[n][prec][k][layout];
+}
+void setKernelTrial(int version) { g_tcTrial = (version >= 2 && version <= 5) ? version : 0; }
+void setKernelTuning(bool on) { g_tcTuning = on; }
+
 int tcKernelFor(const FusedPass& pass, int n) {
     const int k = (int)pass.targets.size();
     if (!g_tcEnabled || k < 4 || k > 6 || n < k + 7) return 0;
     if (g_tcVersion != 0) return g_tcVersion;
+    if (g_tcTrial != 0) return g_tcTrial;
+    if (g_tcTuning) {
+        const int v = tunedKernel(n, g_tcPrecision, k, tuneLayout(pass));
+        if (v) return v;
+    }
     if (g_tcPrecision == kPrecTF32) return k == 4 ? 3 : k == 5 ? 2 : 5;
     const bool high = pass.targets[0] >= 5;
     if (k == 5) return 5;

@@ -192,6 +192,8 @@ SIGNATURES = {
     "quest_gb300_autotune": (_I, [_I]),
     "quest_gb300_planPredictMs": (qreal, [C.c_void_p]),
     "quest_gb300_planCompileTuned": (_I, [C.c_void_p, _I, _I]),
+    "quest_gb300_tunedKernel": (_I, [_I, _I, _I, _P(qreal)]),
+    "quest_gb300_setKernelTuning": (None, [_I]),
     "quest_gb300_createQuregF32": (C.c_void_p, [_I]),
     "quest_gb300_destroyQuregF32": (None, [C.c_void_p]),
     "quest_gb300_initZeroStateF32": (None, [C.c_void_p]),
@@ -223,6 +225,7 @@ SIGNATURES = {
     "quest_gb300_swapTestBatchCreate": (C.c_void_p, [_P(qreal), _P(c_ll), _P(_I), _I, _P(_I), _P(_I), _I]),
     "quest_gb300_swapTestBatchRun": (_I, [C.c_void_p, _P(qreal)]),
     "quest_gb300_swapTestBatchDestroy": (None, [C.c_void_p]),
+    "quest_gb300_swapTestBatchTune": (_I, [C.c_void_p, _P(_I), _P(_I), _P(qreal), _P(qreal)]),
     "quest_gb300_calcTotalProbNoAlloc": (_I, [C.c_void_p, C.c_void_p, c_ll, _P(qreal), C.c_void_p]),
     "quest_gb300_calcTotalProbF32": (qreal, [C.c_void_p]),
     "quest_gb300_calcProbOfOutcomeF32": (qreal, [C.c_void_p, _I, _I]),

@@ -233,3 +233,59 @@ def test_autotuned_plan_matches_and_predicts(gpulib, tmp_path, monkeypatch):
     L.lib.quest_gb300_planDestroy(p)
     L.lib.quest_gb300_destroyQuregF32(q32)
     L.destroy(q64)
+
+
+def test_autotune_picks_kernel_variants(gpulib, tmp_path, monkeypatch):
+    """autotune times every pipelined variant of each tensor-core pass class
+    and keeps the fastest; the plan gives the same state with the tuned
+    variants and with the fixed defaults; the cache records the choices."""
+    L = gpulib
+    lib = L.lib
+    cache = tmp_path / "tune.json"
+    monkeypatch.setenv("QUEST_GB300_TUNE_CACHE", str(cache))
+    n = 17
+    assert lib.quest_gb300_autotune(n) == 0
+    ms = C.c_double(0)
+    for k in (4, 5, 6):
+        for layout in (0, 1, 2):
+            v = lib.quest_gb300_tunedKernel(n, k, layout, C.byref(ms))
+            assert 2 <= v <= 5 and ms.value > 0, (k, layout, v)
+    text = cache.read_text()
+    assert f'"n{n}_p0_k6_l2_v"' in text or f'"n{n}_p1_k6_l2_v"' in text
+    ops = W.c2_circuit(n=n, layers=6, seed=5)
+    p = L.plan(n, 6, ops)
+    states = []
+    for tuning in (1, 0):
+        lib.quest_gb300_setKernelTuning(tuning)
+        q32 = lib.quest_gb300_createQuregF32(n)
+        assert lib.quest_gb300_applyPlanF32(q32, p) == 0
+        states.append(L.amps_f32(q32, n))
+        lib.quest_gb300_destroyQuregF32(q32)
+    lib.quest_gb300_setKernelTuning(1)
+    a, b = states
+    assert np.max(np.abs(a - b)) < 1e-5
+    lib.quest_gb300_planDestroy(p)
+
+
+def test_capture_with_autotuned_width(gpulib, tmp_path, monkeypatch):
+    """setCaptureFusion(0): each searched flush plan takes the width the
+    autotuner predicts fastest; the result matches the direct FP64 calls."""
+    L = gpulib
+    lib = L.lib
+    monkeypatch.setenv("QUEST_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+    n = 16
+    ops = W.c2_circuit(n=n, layers=5, seed=21)
+    direct, cap = L.create(n), L.create(n)
+    lib.quest_gb300_setCaptureFusion(0)
+    try:
+        lib.quest_gb300_setCapture(cap, 1)
+        for q in (direct, cap):
+            lib.initZeroState(q)
+            W.run_ops(L, q, ops)
+        a, b = L.amps(direct), L.amps(cap)
+    finally:
+        lib.quest_gb300_setCaptureFusion(6)
+    f = abs(np.vdot(a, b)) ** 2
+    assert 1 - f <= 1e-6 and np.max(np.abs(a - b)) <= 1e-5
+    L.destroy(direct)
+    L.destroy(cap)

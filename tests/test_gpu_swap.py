@@ -70,3 +70,31 @@ def test_swap_batch_matches_per_gate_circuit(gpulib, oracle):
             p_gate = W.swap_test_plain(lib, regs[key], u, v, d)
             assert abs(p_gate - (1 + np.dot(u, v) ** 2) / 2) < 1e-12
             assert abs(out[k] - p_gate) < 1e-6
+
+
+def test_swap_batch_tuning_keeps_results(gpulib):
+    """swapTestBatchTune tries every CTAs-per-SM / shared-memory threshold
+    pairing, keeps the fastest, and the batch still matches the closed form
+    (sizes on both sides of every threshold: d = 2 .. 8)."""
+    L = gpulib
+    rng = np.random.default_rng(11)
+    vecs = []
+    for d in range(2, 9):
+        for _ in range(3):
+            v = rng.normal(size=1 << d)
+            vecs.append(v / np.linalg.norm(v))
+    dims = np.array([int(np.log2(len(v))) for v in vecs], dtype=np.int32)
+    offsets = np.cumsum([0] + [len(v) for v in vecs[:-1]]).astype(np.int64)
+    pool = np.concatenate(vecs)
+    pairs = [(a, b) for a in range(len(vecs)) for b in range(len(vecs)) if dims[a] == dims[b]]
+    ia = np.array([a for a, _ in pairs], dtype=np.int32)
+    ib = np.array([b for _, b in pairs], dtype=np.int32)
+    h = make_batch(L, pool, offsets, dims, ia, ib)
+    c, s, best, dflt = C.c_int(0), C.c_int(0), C.c_double(0), C.c_double(0)
+    assert L.lib.quest_gb300_swapTestBatchTune(h, C.byref(c), C.byref(s), C.byref(best), C.byref(dflt)) == 0
+    assert 2 <= c.value <= 4 and s.value in (512, 2048, 8192) and 0 < best.value <= dflt.value
+    out = np.zeros(len(ia))
+    assert L.lib.quest_gb300_swapTestBatchRun(h, out.ctypes.data_as(C.POINTER(C.c_double))) == 0
+    want = np.array([(1 + np.dot(vecs[a], vecs[b]) ** 2) / 2 for a, b in pairs])
+    assert np.max(np.abs(out - want)) < 1e-6
+    L.lib.quest_gb300_swapTestBatchDestroy(h)
