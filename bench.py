@@ -278,6 +278,45 @@ def run_gpu(args, rank, world):
     else:
         one_minus_f = max_amp_err = None
 
+    # ---- the plain path's double-float mode, and one plain gate alone ----
+    plain_df = None
+    gate_roof = None
+    if not args.skip_plain:
+        qdf = L.create(n)
+        lib.quest_gb300_setPlainArithmetic(1)
+        lib.initZeroState(qdf)
+        run_plain_step(L, qdf, ops)
+        lib.calcTotalProb(qdf)
+        lib.initZeroState(qdf)
+        lib.quest_gb300_eventRecord(10)
+        run_plain_step(L, qdf, ops)
+        lib.calcTotalProb(qdf)
+        lib.quest_gb300_eventRecord(11)
+        df_ms = lib.quest_gb300_eventElapsedMs(10, 11)
+        ip = lib.calcInnerProduct(q64, qdf)
+        plain_df = {"ms_per_circuit": round(df_ms, 1), "gbs": round(alg_bytes / (df_ms / 1e3) / 1e9, 1),
+                    "speedup_vs_fp64": round(plain_ms / df_ms, 2),
+                    "one_minus_fidelity_vs_fp64": 1 - (ip.real ** 2 + ip.imag ** 2),
+                    "total_prob": lib.calcTotalProb(qdf),
+                    "mode": "quest_gb300_setPlainArithmetic(1): general 2x2 gates in double-float on the FP32 pipes"}
+        # one compactUnitary on qubit 10 of the 30-qubit state (no controls):
+        # 32 B per amplitude (read + write of the FP64 complex state)
+        from quantumlab_gb300.quest import Complex
+        gate_roof = {}
+        a_, b_ = Complex(0.6, 0.0), Complex(0.0, 0.8)
+        for mode, name in ((0, "fp64"), (1, "double_float")):
+            lib.quest_gb300_setPlainArithmetic(mode)
+            lib.compactUnitary(qdf, 10, a_, b_)
+            lib.quest_gb300_eventRecord(12)
+            for _ in range(8):
+                lib.compactUnitary(qdf, 10, a_, b_)
+            lib.quest_gb300_eventRecord(13)
+            gms = lib.quest_gb300_eventElapsedMs(12, 13) / 8
+            gate_roof[name] = {"kernel": "kPairVec<" + ("OpCompact" if mode == 0 else "OpMatrix2DF") + ">",
+                               "avg_launch_ms": round(gms, 4), "achieved_gbs": round((1 << n) * 32 / gms / 1e6, 1)}
+        lib.quest_gb300_setPlainArithmetic(0)
+        L.destroy(qdf)
+
     # ---- the same plan with the pipelined kernel's other operands ---------
     # (3-term split-TF32 is the default; 4-term split-BF16 is the other)
     other = None
@@ -380,6 +419,13 @@ def run_gpu(args, rank, world):
         e2e_prob = e2e_step()
     e2e_s = barrier_max((time.perf_counter() - t0) / e2e_steps, world)
     split = [x / e2e_steps for x in split]
+    # the same device->host copy again with nothing in between: whether a slow
+    # copy in the steps is the copy itself or the state the step left
+    d2h_repeat = []
+    for _ in range(3):
+        t = time.perf_counter()
+        lib.copyStateFromGPU(q64)
+        d2h_repeat.append(round((time.perf_counter() - t) * 1e3, 1))
     lib.quest_gb300_setCapture(q64, 0)
     # what the host link gave this process: whether both host mirrors are
     # page-locked, and plain 1 GiB copies between pinned and device memory
@@ -391,6 +437,9 @@ def run_gpu(args, rank, world):
     lib.quest_gb300_planDestroy(plan)
 
     peak, peak_kind = peaks()
+    if gate_roof:
+        for g in gate_roof.values():
+            g["frac"] = round(g["achieved_gbs"] / peak, 4)
     achieved = pass_bytes / (dom_avg / 1e3) / 1e9
     if other:
         other["dominant_kernel_frac"] = round(pass_bytes / (other["dominant_kernel_avg_ms"] / 1e3) / 1e9 / peak, 4)
@@ -426,6 +475,8 @@ def run_gpu(args, rank, world):
         "autotune": autotune,
         "plain_fp64": ({"ms_per_circuit": round(plain_ms, 1), "gbs": round(alg_bytes / (plain_ms / 1e3) / 1e9, 1),
                         "launches": len(ops)} if plain_ms else None),
+        "plain_double_float": plain_df,
+        "plain_gate_30q": gate_roof,
         "speedup_fused_vs_plain": round(plain_ms / ms_step, 2) if plain_ms else None,
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
@@ -441,7 +492,8 @@ def run_gpu(args, rank, world):
                 "split_ms": {"h2d_initStateFromAmps": round(split[0] * 1e3, 1),
                              "gates_and_flush": round(split[1] * 1e3, 1),
                              "d2h_copyStateFromGPU": round(split[2] * 1e3, 1)},
-                "d2h_ms_each_step": d2h_each, "host_mirrors_pinned": mirrors_pinned, "link_probe_1GiB": link},
+                "d2h_ms_each_step": d2h_each, "d2h_ms_repeated_alone": d2h_repeat,
+                "host_mirrors_pinned": mirrors_pinned, "link_probe_1GiB": link},
         "gpu_launches": int(launches // max(1, args.steps)),
         "gpu_launches_timed_region": int(launches),
         "total_prob_fp32": total32,
@@ -606,6 +658,12 @@ def run_configs(args):
     q = L.create(n1)
     c1(L, q)
     ms1 = statistics.median([gpu_ms(lambda: c1(L, q))[0] for _ in range(3)])
+    amps_fp64 = L.amps(q).copy()
+    lib.quest_gb300_setPlainArithmetic(1)
+    c1(L, q)
+    ms1df = statistics.median([gpu_ms(lambda: c1(L, q))[0] for _ in range(3)])
+    err1df = float(np.max(np.abs(L.amps(q) - amps_fp64)))
+    lib.quest_gb300_setPlainArithmetic(0)
     L.destroy(q)
     Lc, kind = cpu_library()
     qc = Lc.create(n1)
@@ -614,6 +672,7 @@ def run_configs(args):
     cpu1 = (time.perf_counter() - t0) * 1e3
     Lc.destroy(qc)
     out["c1_plain_fp64_20q"] = {"gates": len(ops1), "gpu_ms": round(ms1, 2), "gpu_gbs": round(alg1 / ms1 / 1e6, 1),
+                                "gpu_ms_double_float": round(ms1df, 2), "double_float_max_amp_err_vs_fp64": err1df,
                                 "cpu_ms": round(cpu1, 1), "cpu_kind": kind, "cpu_cores": os.cpu_count(),
                                 "speedup_gpu_vs_cpu": round(cpu1 / ms1, 1)}
     # ---- C3 ----

@@ -61,6 +61,22 @@ int quest_gb300_planNumGates(void* plan);
 /* Copy pass i (targets ascending, FP64 matrix); returns k or -1. */
 int quest_gb300_planPass(void* plan, int i, int* targets, double* re, double* im);
 
+/* ---- arithmetic of the plain path ------------------------------------------
+ * No counterpart in the reference.  GB300 runs FP64 fused multiply-adds at
+ * about 1/70 of its FP32 rate, so the plain path's general 2 x 2 gates
+ * (compactUnitary and the rotations, unitary and its controlled forms,
+ * hadamard) are bound by the FP64 pipe, not by HBM.  Mode 1 computes them in
+ * double-float arithmetic on the FP32 and integer pipes: each double is split
+ * into two floats by integer field operations (2^-47 relative), products are
+ * exact through FMA, sums compensated (TwoSum), and the result is packed back
+ * into the double's fields; the state stays FP64 in memory.  A gate's result
+ * is then within a few 2^-47 of FP64, relative to its largest term.  Doubles
+ * below 2^-126 in magnitude are flushed to 0 and those of 2^128 and above
+ * are not representable.  Mode 0, exact FP64, is the default.  Returns 0, or
+ * -1 for an unknown mode. */
+int quest_gb300_setPlainArithmetic(int mode);
+int quest_gb300_getPlainArithmetic(void);
+
 /* ---- autotuner -------------------------------------------------------------
  * No counterpart in the reference.  autotune measures, for registers of
  * numQubits qubits at the current tensor-core precision, the time of one pass

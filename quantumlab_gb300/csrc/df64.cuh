@@ -1,0 +1,178 @@
+// df64.cuh -- double-float arithmetic for the plain path's pair gates.
+//
+// GB300 executes FP64 at ~1.6 fused multiply-adds per clock per SM and
+// converts between double and float at the same rate, against ~117 FP32
+// FMAs (measured).  A general 2 x 2 complex gate needs 8 FP64 multiply-adds
+// per amplitude, so in FP64 it runs at a quarter of HBM bandwidth.  This
+// header restates the update in double-float (DF) form on the FP32 and
+// integer pipes:
+//   * a double x becomes hi + lo, two floats, by integer field operations
+//     (no FP64 instruction): hi is x truncated to 24 significant bits, lo the
+//     remaining 29 bits rounded to 24, so |x - (hi + lo)| <= 2^-47 |x|;
+//   * products are exact through the FMA (Dekker's TwoProduct in its FMA
+//     form: p = a b, e = fma(a, b, -p)) and sums through Knuth's TwoSum;
+//     the dot product of four DF terms follows the compensated scheme of
+//     Ogita, Rump and Oishi (Dot2, SIAM J. Sci. Comput. 26, 2005), with the
+//     cross terms a_hi b_lo + a_lo b_hi added to the error sum;
+//   * the DF result goes back to a double by integer field operations: the
+//     high float's fields placed in the double, the low float added as an
+//     integer number of the double's units (truncated below one unit).
+// Range: doubles with 2^-126 <= |x| < 2^128 keep 2^-47 relative precision
+// down to |x| ~ 2^-102 (then the low part leaves the float range); smaller
+// magnitudes become 0, an absolute error below 2^-126.
+// The result of a gate is within a few 2^-47 of the FP64 result, relative to
+// the largest term.
+//
+// The functions compile for the device and, for the CPU unit test of the
+// field manipulations (tests/test_df64.py), for the host.
+#pragma once
+
+#include <stdint.h>
+#include <string.h>
+
+#if defined(__CUDACC__)
+#define QG_DF_HD __host__ __device__ __forceinline__
+#else
+#define QG_DF_HD inline
+#endif
+
+namespace qg {
+namespace df {
+
+QG_DF_HD uint32_t f2u(float f) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(f);
+#else
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+QG_DF_HD float u2f(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+QG_DF_HD void d2words(double d, uint32_t& hi, uint32_t& lo) {
+#if defined(__CUDA_ARCH__)
+    hi = (uint32_t)__double2hiint(d);
+    lo = (uint32_t)__double2loint(d);
+#else
+    uint64_t u;
+    memcpy(&u, &d, 8);
+    hi = (uint32_t)(u >> 32);
+    lo = (uint32_t)u;
+#endif
+}
+QG_DF_HD double words2d(uint32_t hi, uint32_t lo) {
+#if defined(__CUDA_ARCH__)
+    return __hiloint2double((int)hi, (int)lo);
+#else
+    const uint64_t u = ((uint64_t)hi << 32) | lo;
+    double d;
+    memcpy(&d, &u, 8);
+    return d;
+#endif
+}
+QG_DF_HD float fmaF(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return __builtin_fmaf(a, b, c);
+#endif
+}
+
+struct F2 {
+    float h, l;
+};
+
+// double -> hi + lo (integer field operations only)
+QG_DF_HD F2 fromDouble(double x) {
+    uint32_t hi, lo;
+    d2words(x, hi, lo);
+    const uint32_t e = (hi >> 20) & 0x7FFu;             // biased exponent
+    const uint32_t sign = hi & 0x80000000u;
+    // (hi, lo) << 3: the exponent's low 9 bits at 23..31 and the top 23
+    // fraction bits below; rebiasing by 896 = 1023 - 127 is the same modulo
+    // 2^9 for every exponent of the float range
+    const uint32_t fs = (hi << 3) | (lo >> 29);
+    const uint32_t hb = (fs - (896u << 23)) | sign;
+    // the remaining 29 fraction bits, rounded to 23 below a leading one
+    // worth 2^(E - 23): L = 2^(E-23) (1 + f), lo = L - 2^(E-23) exactly
+    const uint32_t expPart = (fs & 0xFF800000u) - (407u << 23);   // (e - 919) << 23 modulo 2^32
+    const uint32_t mant = ((lo & 0x1FFFFFFFu) + 32u) >> 6;
+    const float l = u2f(expPart + mant) - u2f(expPart);
+    F2 r;
+    r.h = e >= 897u ? u2f(hb) : u2f(sign);              // |x| < 2^-126: 0
+    r.l = e >= 920u ? u2f(f2u(l) | sign) : 0.f;         // low part below 2^-103: 0
+    return r;
+}
+
+// hi + lo (|lo| below one ulp of hi, as fromDouble and dot4 give) ->
+// double, truncated below one unit of the double
+QG_DF_HD double toDouble(F2 v) {
+    const uint32_t fh = f2u(v.h), fl = f2u(v.l);
+    const uint32_t ah = fh & 0x7FFFFFFFu;
+    if (ah < 0x00800000u) return words2d(fh & 0x80000000u, 0u);    // 0 (or below the float range)
+    const uint32_t eh = ah >> 23, el = (fl >> 23) & 0xFFu;
+    uint32_t hi = ((ah >> 3) + (896u << 20)) | (fh & 0x80000000u);
+    uint32_t lo = fh << 29;
+    // lo in units of the double's last place 2^(Eh - 52): ml 2^t with ml its
+    // 24-bit significand (no leading one when lo is subnormal, whose
+    // exponent field 0 stands for 1) and t = El - Eh + 29 <= 6
+    const uint32_t ml = (fl & 0x7FFFFFu) | (el != 0u ? 0x800000u : 0u);
+    const int t = (int)(el != 0u ? el : 1u) - (int)eh + 29;
+    const bool neg = ((fh ^ fl) & 0x80000000u) != 0;
+    // subtracting from a power of two crosses into the binade below, whose
+    // unit is half as large
+    const int tt = t + ((neg && (ah & 0x7FFFFFu) == 0u) ? 1 : 0);
+    const uint32_t d = tt >= 0 ? (tt >= 32 ? 0u : ml << tt) : (tt <= -32 ? 0u : ml >> -tt);
+    const uint64_t w = ((uint64_t)hi << 32) | lo;
+    const uint64_t r = neg ? w - d : w + d;
+    return words2d((uint32_t)(r >> 32), (uint32_t)r);
+}
+
+// Knuth's TwoSum: s + err = a + b exactly
+QG_DF_HD void twoSum(float a, float b, float& s, float& err) {
+    s = a + b;
+    const float bb = s - a;
+    err = (a - (s - bb)) + (b - bb);
+}
+
+// sum_k c_k x_k over four DF terms, as a DF result (Dot2 with the cross
+// terms): the high products are summed by TwoSum, their rounding errors,
+// the products' FMA errors and the cross terms go to the error sum
+QG_DF_HD F2 dot4(const F2 c[4], const F2 x[4]) {
+    float p = c[0].h * x[0].h;
+    float s = fmaF(c[0].h, x[0].h, -p);
+    s = fmaF(c[0].h, x[0].l, s);
+    s = fmaF(c[0].l, x[0].h, s);
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+        const float h = c[k].h * x[k].h;
+        const float r = fmaF(c[k].h, x[k].h, -h);
+        float q;
+        twoSum(p, h, p, q);
+        s = fmaF(c[k].h, x[k].l, s);
+        s = fmaF(c[k].l, x[k].h, s);
+        s += q + r;
+    }
+    F2 out;
+    twoSum(p, s, out.h, out.l);                         // |s| may exceed |p| when the terms cancel
+    return out;
+}
+
+// a double as a DF constant (host side: exact split by rounding)
+inline F2 splitConst(double c) {
+    F2 r;
+    r.h = (float)c;
+    r.l = (float)(c - (double)r.h);
+    return r;
+}
+
+}  // namespace df
+}  // namespace qg

@@ -102,6 +102,9 @@ void gateRotateZ(SV s, uint64_t ctrl, uint64_t targ, double angle);
 // conj!=0 applies the elementwise conjugate operator.
 void gatePauliRotation(SV s, uint64_t ctrl, uint64_t xmask, uint64_t ymask, uint64_t zmask, double angle, int conj);
 void gateSwap(SV s, int q1, int q2);
+// plain-path arithmetic of the general 2 x 2 gates: 0 FP64, 1 double-float
+bool setPlainArithmetic(int mode);
+int plainArithmetic();
 // Dense 2^k x 2^k (k <= 6) on targets (targs[0] = least significant matrix bit).
 // mr/mi row-major host arrays.
 void gateMatrixN(SV s, uint64_t ctrl, const int* targs, int k, const double* mr, const double* mi);

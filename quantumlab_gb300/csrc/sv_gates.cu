@@ -12,6 +12,7 @@
 // inserted bit is bit 0, consecutive k give consecutive i0, so one thread
 // takes k = 2t, 2t+1 and moves them with double2 loads (kVec).  When the
 // partner bit is bit 0 the pair itself is adjacent (kAdj).  Otherwise kScalar.
+#include "df64.cuh"
 #include "qg_internal.h"
 
 #include <algorithm>
@@ -73,6 +74,37 @@ struct OpCompact {
         li = br * b + bi * a + ar * d - ai * c;
     }
 };
+
+// The 2 x 2 update in double-float form (df64.cuh), for the plain path's
+// double-float mode (quest_gb300_setPlainArithmetic(1)): each output is a
+// compensated four-term dot product of DF coefficients and the DF parts of
+// the inputs, on the FP32 and integer pipes.  coef[o] holds the four
+// coefficients of output o (ur, ui, lr, li) against inputs (a, b, c, d) =
+// (ur, ui, lr, li) for the real outputs and (b, a, d, c) for the imaginary
+// ones, signs included.
+struct OpMatrix2DF {
+    df::F2 coef[4][4];
+    __device__ __forceinline__ void operator()(double& ur, double& ui, double& lr, double& li) const {
+        const df::F2 a = df::fromDouble(ur), b = df::fromDouble(ui), c = df::fromDouble(lr), d = df::fromDouble(li);
+        const df::F2 re4[4] = {a, b, c, d}, im4[4] = {b, a, d, c};
+        ur = df::toDouble(df::dot4(coef[0], re4));
+        ui = df::toDouble(df::dot4(coef[1], im4));
+        lr = df::toDouble(df::dot4(coef[2], re4));
+        li = df::toDouble(df::dot4(coef[3], im4));
+    }
+};
+OpMatrix2DF matrix2DF(const Mat2& m) {
+    OpMatrix2DF op;
+    const double k[4][4] = {{m.r[0][0], -m.i[0][0], m.r[0][1], -m.i[0][1]},
+                            {m.r[0][0], m.i[0][0], m.r[0][1], m.i[0][1]},
+                            {m.r[1][0], -m.i[1][0], m.r[1][1], -m.i[1][1]},
+                            {m.r[1][0], m.i[1][0], m.r[1][1], m.i[1][1]}};
+    for (int o = 0; o < 4; ++o)
+        for (int j = 0; j < 4; ++j) op.coef[o][j] = df::splitConst(k[o][j]);
+    return op;
+}
+// 0: exact FP64 (the default); 1: double-float for the general 2 x 2 gates
+int g_plainArith = 0;
 
 // QuEST_gpu.cu:1771-1826
 struct OpHadamard {
@@ -328,13 +360,21 @@ void gateMatrix2(SV s, int target, uint64_t ctrl, uint64_t flip, const Mat2& u) 
         const double ur[4] = {u.r[0][0], u.r[0][1], u.r[1][0], u.r[1][1]}, ui[4] = {u.i[0][0], u.i[0][1], u.i[1][0], u.i[1][1]};
         if (capturePair(s, target, ctrl, flip, ur, ui)) return;
     }
-    launchPair(s, ctrl, ctrl & ~flip, 1ull << target, OpMatrix2{u}, "unitary");
+    if (g_plainArith == 1) launchPair(s, ctrl, ctrl & ~flip, 1ull << target, matrix2DF(u), "unitary");
+    else launchPair(s, ctrl, ctrl & ~flip, 1ull << target, OpMatrix2{u}, "unitary");
 }
 
 void gateCompact(SV s, int target, uint64_t ctrl, double ar, double ai, double br, double bi) {   // QuEST_gpu.cu:838, 905
     if (s.cap) {
         const double ur[4] = {ar, -br, br, ar}, ui[4] = {ai, bi, bi, -ai};     // [alpha, -conj(beta); beta, conj(alpha)]
         if (capturePair(s, target, ctrl, 0, ur, ui)) return;
+    }
+    if (g_plainArith == 1) {
+        Mat2 m;                                            // [alpha, -conj(beta); beta, conj(alpha)]
+        m.r[0][0] = ar; m.i[0][0] = ai; m.r[0][1] = -br; m.i[0][1] = bi;
+        m.r[1][0] = br; m.i[1][0] = bi; m.r[1][1] = ar; m.i[1][1] = -ai;
+        launchPair(s, ctrl, ctrl, 1ull << target, matrix2DF(m), "compactUnitary");
+        return;
     }
     launchPair(s, ctrl, ctrl, 1ull << target, OpCompact{ar, ai, br, bi}, "compactUnitary");
 }
@@ -345,8 +385,21 @@ void gateHadamard(SV s, int target) {                                           
         const double ur[4] = {f, f, f, -f}, ui[4] = {0, 0, 0, 0};
         if (capturePair(s, target, 0, 0, ur, ui)) return;
     }
+    if (g_plainArith == 1) {
+        const double f = 0.70710678118654752440;
+        Mat2 m{{{f, f}, {f, -f}}, {{0, 0}, {0, 0}}};
+        launchPair(s, 0, 0, 1ull << target, matrix2DF(m), "hadamard");
+        return;
+    }
     launchPair(s, 0, 0, 1ull << target, OpHadamard{0.70710678118654752440}, "hadamard");
 }
+
+bool setPlainArithmetic(int mode) {
+    if (mode != 0 && mode != 1) return false;
+    g_plainArith = mode;
+    return true;
+}
+int plainArithmetic() { return g_plainArith; }
 
 void gateNot(SV s, uint64_t ctrl, uint64_t targMask) {                               // QuEST_gpu.cu:1354, 1867, 1912
     if (s.cap && captureNot(s, ctrl, targMask)) return;
@@ -450,3 +503,12 @@ void gateMatrixN(SV s, uint64_t ctrl, const int* targs, int k, const double* mr,
 }
 
 }  // namespace qg
+
+extern "C" {
+/* Arithmetic of the plain path's general 2 x 2 gates (compactUnitary and the
+ * rotations built on it, unitary and its controlled forms, hadamard): 0 =
+ * exact FP64 (the default), 1 = double-float on the FP32 and integer pipes
+ * (df64.cuh).  Returns 0, or -1 for an unknown mode. */
+int quest_gb300_setPlainArithmetic(int mode) { return qg::setPlainArithmetic(mode) ? 0 : -1; }
+int quest_gb300_getPlainArithmetic(void) { return qg::plainArithmetic(); }
+}

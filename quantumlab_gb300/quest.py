@@ -194,6 +194,8 @@ SIGNATURES = {
     "quest_gb300_planCompileTuned": (_I, [C.c_void_p, _I, _I]),
     "quest_gb300_tunedKernel": (_I, [_I, _I, _I, _P(qreal)]),
     "quest_gb300_setKernelTuning": (None, [_I]),
+    "quest_gb300_setPlainArithmetic": (_I, [_I]),
+    "quest_gb300_getPlainArithmetic": (_I, []),
     "quest_gb300_createQuregF32": (C.c_void_p, [_I]),
     "quest_gb300_destroyQuregF32": (None, [C.c_void_p]),
     "quest_gb300_initZeroStateF32": (None, [C.c_void_p]),

@@ -189,3 +189,47 @@ def test_many_term_pauli_sum_vs_oracle(gpulib, oracle, density):
         L.destroy(ws)
         L.destroy(q)
     assert abs(vals[0] - vals[1]) < 1e-10 * np.sum(np.abs(coeffs)), vals
+
+
+@pytest.fixture
+def double_float(gpulib):
+    """The plain path's double-float mode for the general 2 x 2 gates, reset
+    to exact FP64 afterwards."""
+    assert gpulib.lib.quest_gb300_setPlainArithmetic(1) == 0
+    yield gpulib
+    gpulib.lib.quest_gb300_setPlainArithmetic(0)
+
+
+def test_double_float_mode_catalogue(double_float, golden):
+    """Every catalogue case with the general 2 x 2 gates in double-float
+    arithmetic against the reference's FP64 outputs, at the plain path's
+    tolerance (1e-12 x the case's largest amplitude)."""
+    cases, amps, _ = golden
+    failures = []
+    for i, case in enumerate(cases):
+        a, results, probes = QC.run_case(double_float, case)
+        try:
+            check_case(case, a, results, probes, amps[f"case{i}"])
+        except AssertionError as e:
+            failures.append(str(e))
+    assert not failures, f"{len(failures)} failing cases:\n" + "\n".join(failures[:40])
+
+
+def test_double_float_mode_circuit_vs_oracle(double_float, oracle):
+    """The 20-qubit, 40-layer plain circuit (800 compactUnitary, 380 CNOT) in
+    double-float mode against the oracle's FP64: every amplitude within
+    1e-12 x max|amp|, total probability and P(q = 1) within 1e-12."""
+    L = double_float
+    n = 20
+    ops = W.c1_circuit(n=n, layers=40, seed=1)
+    res = []
+    for lib in (L, oracle):
+        q = lib.create(n)
+        W.run_ops(lib, q, ops)
+        res.append((lib.amps(q).copy(), lib.lib.calcTotalProb(q), [lib.lib.calcProbOfOutcome(q, t, 1) for t in range(n)]))
+        lib.destroy(q)
+    (ag, tg, pg), (ao, to, po) = res
+    err = float(np.max(np.abs(ag - ao)))
+    print(f"double-float 20q/40 layers: max|d amp| = {err:.3e} (max|amp| {np.max(np.abs(ao)):.3e})")
+    assert err <= 1e-12 * float(np.max(np.abs(ao)))
+    assert abs(tg - to) < 1e-12 and np.max(np.abs(np.array(pg) - np.array(po))) < 1e-12
