@@ -166,6 +166,15 @@ def run_gpu(args, rank, world):
     lib = L.lib
     n, k = args.qubits, args.fusion
     ops = W.c2_circuit(n=n, layers=args.layers, seed=2)
+    # the end-to-end input (|0..0> in FP64) lives in a register's pinned host
+    # mirror, allocated and written before anything is timed, as an
+    # application that loops over circuits would hold it
+    src = L.create(n)
+    src_re = np.ctypeslib.as_array(src.stateVec.real, shape=(1 << n,))
+    src_im = np.ctypeslib.as_array(src.stateVec.imag, shape=(1 << n,))
+    src_re[:] = 0.0
+    src_im[:] = 0.0
+    src_re[0] = 1.0
     alg_bytes = W.algorithmic_bytes(ops, n)
     pass_bytes = 2 * (1 << n) * 8                   # one fused pass: read + write the FP32 state
 
@@ -294,10 +303,11 @@ def run_gpu(args, rank, world):
         lib.quest_gb300_eventRecord(11)
         df_ms = lib.quest_gb300_eventElapsedMs(10, 11)
         ip = lib.calcInnerProduct(q64, qdf)
+        n64, ndf = lib.calcTotalProb(q64), lib.calcTotalProb(qdf)
         plain_df = {"ms_per_circuit": round(df_ms, 1), "gbs": round(alg_bytes / (df_ms / 1e3) / 1e9, 1),
                     "speedup_vs_fp64": round(plain_ms / df_ms, 2),
-                    "one_minus_fidelity_vs_fp64": 1 - (ip.real ** 2 + ip.imag ** 2),
-                    "total_prob": lib.calcTotalProb(qdf),
+                    "one_minus_fidelity_vs_fp64": 1 - (ip.real ** 2 + ip.imag ** 2) / (n64 * ndf),
+                    "total_prob": ndf, "total_prob_err_vs_fp64": abs(ndf - n64),
                     "mode": "quest_gb300_setPlainArithmetic(1): general 2x2 gates in double-float on the FP32 pipes"}
         # one compactUnitary on qubit 10 of the 30-qubit state (no controls):
         # 32 B per amplitude (read + write of the FP64 complex state)
@@ -381,15 +391,9 @@ def run_gpu(args, rank, world):
     # calcTotalProb, then copyStateFromGPU of every amplitude into the
     # register's host mirror.  Op-stream capture is on for the register, so
     # the gate calls are queued and applied by the fused FP32 engine at
-    # calcTotalProb.  One untimed warm-up step (FP32 scratch, plan upload).
+    # calcTotalProb.  Two untimed warm-up steps (FP32 scratch, plan upload).
     lib.quest_gb300_destroyQuregF32(q32)
     q32 = None
-    src = L.create(n)                                  # its pinned host mirror holds the input
-    src_re = np.ctypeslib.as_array(src.stateVec.real, shape=(1 << n,))
-    src_im = np.ctypeslib.as_array(src.stateVec.imag, shape=(1 << n,))
-    src_re[:] = 0.0
-    src_im[:] = 0.0
-    src_re[0] = 1.0
     lib.quest_gb300_setCapture(q64, 1)
 
     split = [0.0, 0.0, 0.0]                            # host -> device, gates + flush, device -> host
@@ -409,10 +413,11 @@ def run_gpu(args, rank, world):
         d2h_each.append(round((t3 - t2) * 1e3, 1))
         return p
 
-    e2e_step()
+    for _ in range(2):                                 # untimed warm-up steps
+        e2e_step()
     split[:] = [0.0, 0.0, 0.0]
     d2h_each.clear()
-    e2e_steps = max(1, min(args.steps, 2))
+    e2e_steps = max(1, min(args.steps, 3))
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):

@@ -7,8 +7,9 @@
 // header restates the update in double-float (DF) form on the FP32 and
 // integer pipes:
 //   * a double x becomes hi + lo, two floats, by integer field operations
-//     (no FP64 instruction): hi is x truncated to 24 significant bits, lo the
-//     remaining 29 bits rounded to 24, so |x - (hi + lo)| <= 2^-47 |x|;
+//     and one integer-to-float conversion (no FP64 instruction): hi is x
+//     rounded to 24 significant bits, lo the signed remainder rounded to 24,
+//     so |x - (hi + lo)| <= 2^-48 |x|;
 //   * products are exact through the FMA (Dekker's TwoProduct in its FMA
 //     form: p = a b, e = fma(a, b, -p)) and sums through Knuth's TwoSum;
 //     the dot product of four DF terms follows the compensated scheme of
@@ -17,10 +18,10 @@
 //   * the DF result goes back to a double by integer field operations: the
 //     high float's fields placed in the double, the low float added as an
 //     integer number of the double's units (truncated below one unit).
-// Range: doubles with 2^-126 <= |x| < 2^128 keep 2^-47 relative precision
-// down to |x| ~ 2^-102 (then the low part leaves the float range); smaller
+// Range: doubles with 2^-126 <= |x| < 2^128 keep 2^-48 relative precision
+// down to |x| ~ 2^-74 (then the low part leaves the float range); smaller
 // magnitudes become 0, an absolute error below 2^-126.
-// The result of a gate is within a few 2^-47 of the FP64 result, relative to
+// The result of a gate is within a few 2^-48 of the FP64 result, relative to
 // the largest term.
 //
 // The functions compile for the device and, for the CPU unit test of the
@@ -86,30 +87,69 @@ QG_DF_HD float fmaF(float a, float b, float c) {
 #endif
 }
 
+// Products and sums that must stay rounded as written: the compiler would
+// otherwise contract p + a * b into one FMA, which breaks the error-free
+// transformations below
+QG_DF_HD float mulR(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+QG_DF_HD float addR(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+QG_DF_HD float subR(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+
 struct F2 {
     float h, l;
 };
 
-// double -> hi + lo (integer field operations only)
+QG_DF_HD float i2f(int32_t v) {
+#if defined(__CUDA_ARCH__)
+    return __int2float_rn(v);
+#else
+    return (float)v;
+#endif
+}
+
+// double -> hi + lo (integer field operations and one integer-to-float
+// conversion; no FP64 instruction): hi is x rounded to 24 significant bits,
+// lo the signed remainder (at most 29 bits) rounded to 24
 QG_DF_HD F2 fromDouble(double x) {
     uint32_t hi, lo;
     d2words(x, hi, lo);
     const uint32_t e = (hi >> 20) & 0x7FFu;             // biased exponent
     const uint32_t sign = hi & 0x80000000u;
-    // (hi, lo) << 3: the exponent's low 9 bits at 23..31 and the top 23
+    // round the 52-bit fraction at bit 29 (a carry may reach the exponent)
+    const uint32_t lo2 = lo + (1u << 28);
+    const uint32_t hi2 = hi + (lo2 < lo ? 1u : 0u);
+    // (hi2, lo2) << 3: the exponent's low 9 bits at 23..31 and the top 23
     // fraction bits below; rebiasing by 896 = 1023 - 127 is the same modulo
     // 2^9 for every exponent of the float range
-    const uint32_t fs = (hi << 3) | (lo >> 29);
-    const uint32_t hb = (fs - (896u << 23)) | sign;
-    // the remaining 29 fraction bits, rounded to 23 below a leading one
-    // worth 2^(E - 23): L = 2^(E-23) (1 + f), lo = L - 2^(E-23) exactly
-    const uint32_t expPart = (fs & 0xFF800000u) - (407u << 23);   // (e - 919) << 23 modulo 2^32
-    const uint32_t mant = ((lo & 0x1FFFFFFFu) + 32u) >> 6;
-    const float l = u2f(expPart + mant) - u2f(expPart);
-    F2 r;
-    r.h = e >= 897u ? u2f(hb) : u2f(sign);              // |x| < 2^-126: 0
-    r.l = e >= 920u ? u2f(f2u(l) | sign) : 0.f;         // low part below 2^-103: 0
-    return r;
+    const uint32_t fs = (hi2 << 3) | (lo2 >> 29);
+    const uint32_t hb = ((fs - (896u << 23)) & 0x7FFFFFFFu) | sign;
+    // the remainder x - hi in units of 2^(E - 52): the low 29 fraction bits
+    // as a signed 29-bit number (negative when hi was rounded up)
+    const int32_t r = (int32_t)(lo << 3) >> 3;
+    // 2^(E - 52) as a float: (e - 948) << 23 from the original exponent
+    const uint32_t scale = ((((hi << 3) | (lo >> 29)) & 0xFF800000u) - (436u << 23));
+    const float l = mulR(i2f(r), u2f(scale));
+    F2 f;
+    f.h = e >= 897u ? u2f(hb) : u2f(sign);              // |x| < 2^-126: 0
+    f.l = e >= 949u ? u2f(f2u(l) ^ sign) : 0.f;         // remainder below the float range: 0
+    return f;
 }
 
 // hi + lo (|lo| below one ulp of hi, as fromDouble and dot4 give) ->
@@ -138,28 +178,28 @@ QG_DF_HD double toDouble(F2 v) {
 
 // Knuth's TwoSum: s + err = a + b exactly
 QG_DF_HD void twoSum(float a, float b, float& s, float& err) {
-    s = a + b;
-    const float bb = s - a;
-    err = (a - (s - bb)) + (b - bb);
+    s = addR(a, b);
+    const float bb = subR(s, a);
+    err = addR(subR(a, subR(s, bb)), subR(b, bb));
 }
 
 // sum_k c_k x_k over four DF terms, as a DF result (Dot2 with the cross
 // terms): the high products are summed by TwoSum, their rounding errors,
 // the products' FMA errors and the cross terms go to the error sum
 QG_DF_HD F2 dot4(const F2 c[4], const F2 x[4]) {
-    float p = c[0].h * x[0].h;
+    float p = mulR(c[0].h, x[0].h);
     float s = fmaF(c[0].h, x[0].h, -p);
     s = fmaF(c[0].h, x[0].l, s);
     s = fmaF(c[0].l, x[0].h, s);
 #pragma unroll
     for (int k = 1; k < 4; ++k) {
-        const float h = c[k].h * x[k].h;
+        const float h = mulR(c[k].h, x[k].h);
         const float r = fmaF(c[k].h, x[k].h, -h);
         float q;
         twoSum(p, h, p, q);
         s = fmaF(c[k].h, x[k].l, s);
         s = fmaF(c[k].l, x[k].h, s);
-        s += q + r;
+        s = addR(s, addR(q, r));
     }
     F2 out;
     twoSum(p, s, out.h, out.l);                         // |s| may exceed |p| when the terms cancel

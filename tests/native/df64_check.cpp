@@ -12,7 +12,7 @@ using namespace qg::df;
 int main() {
     std::mt19937_64 rng(20261204);
     std::uniform_real_distribution<double> u(-1, 1);
-    // double -> DF: relative error for |x| >= 2^-102, absolute below
+    // double -> DF: relative error for |x| >= 2^-73, absolute below
     double inRel = 0, inAbsSmall = 0, outRel = 0;
     long loTooBig = 0;
     for (int i = 0; i < 2000000; ++i) {
@@ -20,7 +20,7 @@ int main() {
         const F2 f = fromDouble(x);
         const long double back = (long double)f.h + (long double)f.l;
         const double err = (double)std::fabs(back - (long double)x);
-        if (std::fabs(x) >= std::ldexp(1.0, -102)) inRel = std::max(inRel, err / std::fabs(x));
+        if (std::fabs(x) >= std::ldexp(1.0, -73)) inRel = std::max(inRel, err / std::fabs(x));
         else inAbsSmall = std::max(inAbsSmall, err);
         if (!(std::fabs(f.l) <= std::ldexp(std::fabs(f.h), -23))) ++loTooBig;      // below one ulp of hi
         // DF -> double: the double nearest below |hi + lo| (truncation)

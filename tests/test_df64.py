@@ -23,8 +23,8 @@ def test_df64_bounds(tmp_path):
     assert out.returncode == 0, out.stderr
     v = {k: float(x) for k, x in (line.split() for line in out.stdout.strip().splitlines())}
     print(v)
-    assert v["in_rel"] <= 2.0 ** -47                 # hi: 24 bits truncated, lo: 29 bits rounded to 24
-    assert v["in_abs_small"] <= 2.0 ** -126          # below 2^-102 the low part is dropped
+    assert v["in_rel"] <= 2.0 ** -48                 # hi and the signed remainder each rounded to 24 bits
+    assert v["in_abs_small"] <= 2.0 ** -97           # below 2^-73 the low part is dropped
     assert v["lo_not_below_ulp"] == 0
     assert v["out_rel"] <= 2.0 ** -52                # truncation below one unit of the double
     assert v["pow2_rel"] <= 2.0 ** -52               # subtraction across a power of two

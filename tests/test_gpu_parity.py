@@ -233,3 +233,29 @@ def test_double_float_mode_circuit_vs_oracle(double_float, oracle):
     print(f"double-float 20q/40 layers: max|d amp| = {err:.3e} (max|amp| {np.max(np.abs(ao)):.3e})")
     assert err <= 1e-12 * float(np.max(np.abs(ao)))
     assert abs(tg - to) < 1e-12 and np.max(np.abs(np.array(pg) - np.array(po))) < 1e-12
+
+
+def test_lab_channels_on_a_larger_density_matrix(gpulib, oracle):
+    """mixPauli and the two-qubit dephasing / depolarising channels on a
+    7-qubit density matrix (a 14-qubit vector: the 16-byte form of the
+    two-qubit kernel runs whenever the lower qubit is not 0), every ordered
+    pair of a few qubits, against the oracle to 1e-12."""
+    n = 7
+    rng = np.random.default_rng(23)
+    ops = W.c3_circuit(nq=n, layers=2, seed=8)
+    res = []
+    for L in (gpulib, oracle):
+        d = L.create(n, True)
+        L.lib.initZeroState(d)
+        W.run_ops(L, d, ops)
+        r = np.random.default_rng(5)
+        for q1, q2 in [(0, 1), (1, 0), (2, 6), (6, 3), (4, 5), (5, 2)]:
+            L.lib.mixTwoQubitDephasing(d, q1, q2, float(r.uniform(0, 0.75)))
+            L.lib.mixTwoQubitDepolarising(d, q2, q1, float(r.uniform(0, 15 / 16)))
+            L.lib.mixPauli(d, q1, float(r.uniform(0, 0.2)), float(r.uniform(0, 0.2)), float(r.uniform(0, 0.2)))
+        res.append((L.amps(d).copy(), L.lib.calcTotalProb(d), L.lib.calcPurity(d)))
+        L.destroy(d)
+    (ag, tg, pg), (ao, to, po) = res
+    assert np.max(np.abs(ag - ao)) <= 1e-12 * max(1.0, float(np.max(np.abs(ao))))
+    assert abs(tg - to) < 1e-12 and abs(pg - po) < 1e-12
+    _ = rng
