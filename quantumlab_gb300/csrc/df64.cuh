@@ -15,9 +15,10 @@
 //     the dot product of four DF terms follows the compensated scheme of
 //     Ogita, Rump and Oishi (Dot2, SIAM J. Sci. Comput. 26, 2005), with the
 //     cross terms a_hi b_lo + a_lo b_hi added to the error sum;
-//   * the DF result goes back to a double by integer field operations: the
-//     high float's fields placed in the double, the low float added as an
-//     integer number of the double's units (truncated below one unit).
+//   * the DF result goes back to a double by field operations: the high
+//     float's fields placed in the double, the low float scaled to the
+//     double's unit and converted to an integer (rounded to nearest), added
+//     to the bit pattern.
 // Range: doubles with 2^-126 <= |x| < 2^128 keep 2^-48 relative precision
 // down to |x| ~ 2^-74 (then the low part leaves the float range); smaller
 // magnitudes become 0, an absolute error below 2^-126.
@@ -130,7 +131,7 @@ QG_DF_HD float i2f(int32_t v) {
 QG_DF_HD F2 fromDouble(double x) {
     uint32_t hi, lo;
     d2words(x, hi, lo);
-    const uint32_t e = (hi >> 20) & 0x7FFu;             // biased exponent
+    const uint32_t ex = hi & 0x7FF00000u;                // biased exponent << 20
     const uint32_t sign = hi & 0x80000000u;
     // round the 52-bit fraction at bit 29 (a carry may reach the exponent)
     const uint32_t lo2 = lo + (1u << 28);
@@ -144,36 +145,44 @@ QG_DF_HD F2 fromDouble(double x) {
     // as a signed 29-bit number (negative when hi was rounded up)
     const int32_t r = (int32_t)(lo << 3) >> 3;
     // 2^(E - 52) as a float: (e - 948) << 23 from the original exponent
-    const uint32_t scale = ((((hi << 3) | (lo >> 29)) & 0xFF800000u) - (436u << 23));
+    // (modulo 2^32, as above)
+    const uint32_t scale = (ex << 3) - (948u << 23);
     const float l = mulR(i2f(r), u2f(scale));
     F2 f;
-    f.h = e >= 897u ? u2f(hb) : u2f(sign);              // |x| < 2^-126: 0
-    f.l = e >= 949u ? u2f(f2u(l) ^ sign) : 0.f;         // remainder below the float range: 0
+    f.h = ex >= (897u << 20) ? u2f(hb) : u2f(sign);     // |x| < 2^-126: 0
+    f.l = ex >= (949u << 20) ? u2f(f2u(l) ^ sign) : 0.f;   // remainder below the float range: 0
     return f;
 }
 
+QG_DF_HD int32_t f2iRn(float f) {
+#if defined(__CUDA_ARCH__)
+    return __float2int_rn(f);
+#else
+    return (int32_t)__builtin_lrintf(f);
+#endif
+}
+
 // hi + lo (|lo| below one ulp of hi, as fromDouble and dot4 give) ->
-// double, truncated below one unit of the double
+// double, rounded to nearest: the high float's fields placed in the double,
+// then lo, scaled to units of the double's last place 2^(Eh - 52) by an
+// exact power-of-two product and converted to an integer, added to the
+// magnitude's bit pattern (|lo| < 2^29 units)
 QG_DF_HD double toDouble(F2 v) {
-    const uint32_t fh = f2u(v.h), fl = f2u(v.l);
-    const uint32_t ah = fh & 0x7FFFFFFFu;
-    if (ah < 0x00800000u) return words2d(fh & 0x80000000u, 0u);    // 0 (or below the float range)
-    const uint32_t eh = ah >> 23, el = (fl >> 23) & 0xFFu;
-    uint32_t hi = ((ah >> 3) + (896u << 20)) | (fh & 0x80000000u);
-    uint32_t lo = fh << 29;
-    // lo in units of the double's last place 2^(Eh - 52): ml 2^t with ml its
-    // 24-bit significand (no leading one when lo is subnormal, whose
-    // exponent field 0 stands for 1) and t = El - Eh + 29 <= 6
-    const uint32_t ml = (fl & 0x7FFFFFu) | (el != 0u ? 0x800000u : 0u);
-    const int t = (int)(el != 0u ? el : 1u) - (int)eh + 29;
-    const bool neg = ((fh ^ fl) & 0x80000000u) != 0;
+    const uint32_t fh = f2u(v.h);
+    const uint32_t ah = fh & 0x7FFFFFFFu, sh = fh & 0x80000000u;
+    const uint32_t hi = ((ah >> 3) + (896u << 20)) | sh;
+    const uint32_t lo = fh << 29;
+    // lo against the magnitude: its sign flipped when hi is negative
+    const float lm = u2f(f2u(v.l) ^ sh);
     // subtracting from a power of two crosses into the binade below, whose
-    // unit is half as large
-    const int tt = t + ((neg && (ah & 0x7FFFFFu) == 0u) ? 1 : 0);
-    const uint32_t d = tt >= 0 ? (tt >= 32 ? 0u : ml << tt) : (tt <= -32 ? 0u : ml >> -tt);
-    const uint64_t w = ((uint64_t)hi << 32) | lo;
-    const uint64_t r = neg ? w - d : w + d;
-    return words2d((uint32_t)(r >> 32), (uint32_t)r);
+    // unit is half as large: scale by 2^(53 - Eh) instead of 2^(52 - Eh)
+    const bool down = (ah & 0x7FFFFFu) == 0u && lm < 0.f;
+    const uint32_t scaleBits = ((down ? 307u : 306u) << 23) - (ah & 0x7F800000u);
+    const int32_t d = f2iRn(mulR(lm, u2f(scaleBits)));
+    const uint64_t w = (((uint64_t)hi << 32) | lo) + (uint64_t)(int64_t)d;
+    // hi below 2^-75 (its unit would leave the float range) or zero: hi alone
+    if (ah < (52u << 23)) return ah < 0x00800000u ? words2d(sh, 0u) : words2d(hi, lo);
+    return words2d((uint32_t)(w >> 32), (uint32_t)w);
 }
 
 // Knuth's TwoSum: s + err = a + b exactly

@@ -26,7 +26,7 @@ def test_df64_bounds(tmp_path):
     assert v["in_rel"] <= 2.0 ** -48                 # hi and the signed remainder each rounded to 24 bits
     assert v["in_abs_small"] <= 2.0 ** -97           # below 2^-73 the low part is dropped
     assert v["lo_not_below_ulp"] == 0
-    assert v["out_rel"] <= 2.0 ** -52                # truncation below one unit of the double
-    assert v["pow2_rel"] <= 2.0 ** -52               # subtraction across a power of two
+    assert v["out_rel"] <= 2.0 ** -53                # rounded to the nearest double
+    assert v["pow2_rel"] <= 2.0 ** -53               # subtraction across a power of two
     assert v["dot4_rel_to_largest_term"] <= 2.0 ** -42       # four inputs at 2^-47 each, sums compensated
     assert v["exact_cases"] == 1
