@@ -199,32 +199,31 @@ def run_gpu(args, rank, world):
     kk = [lib.quest_gb300_planPass(plan, i, None, None, None) for i in range(npass)]
     q32 = lib.quest_gb300_createQuregF32(n)
 
-    def fused_step(per_pass=False):
+    def fused_step():
         lib.quest_gb300_initZeroStateF32(q32)
-        if not per_pass:
-            lib.quest_gb300_applyPlanF32(q32, plan)
-        else:
-            for i in range(npass):
-                lib.quest_gb300_eventRecord(100 + 2 * i)
-                lib.quest_gb300_applyPlanF32Range(q32, plan, i, 1)
-                lib.quest_gb300_eventRecord(101 + 2 * i)
-        total = lib.quest_gb300_calcTotalProbF32(q32)
-        return total, ([lib.quest_gb300_eventElapsedMs(100 + 2 * i, 101 + 2 * i) for i in range(npass)] if per_pass else [])
+        lib.quest_gb300_applyPlanF32(q32, plan)
+        return lib.quest_gb300_calcTotalProbF32(q32), None
 
     for _ in range(args.warmup):
         fused_step()
     barrier(world)
     launches0 = lib.quest_gb300_launchCount()
     pass_ms = [0.0] * npass
+    pt = (C.c_double * max(1, npass))()
+    # each pass's duration from CUDA events the library records around it on
+    # its stream, inside the timed steps (no extra host calls between passes)
+    lib.quest_gb300_setPassEvents(1)
     with Clocks(int(os.environ.get("LOCAL_RANK", 0))) as clk:
         lib.quest_gb300_eventRecord(0)
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            total32, pm = fused_step(per_pass=True)
-            pass_ms = [a + b for a, b in zip(pass_ms, pm)]
+            total32, _ = fused_step()                  # ends with a synchronising FP64 reduction
+            lib.quest_gb300_passTimesMs(pt, npass)
+            pass_ms = [a + pt[i] for i, a in enumerate(pass_ms)]
         lib.quest_gb300_eventRecord(1)
         ms = lib.quest_gb300_eventElapsedMs(0, 1)
         wall = time.perf_counter() - t0
+    lib.quest_gb300_setPassEvents(0)
     launches = lib.quest_gb300_launchCount() - launches0
     ms_step = barrier_max(ms / args.steps, world)
     value = world * alg_bytes / (ms_step / 1e3) / 1e9
@@ -334,11 +333,14 @@ def run_gpu(args, rank, world):
     if lib.quest_gb300_setTensorCorePrecision(1 - prec) == 0:
         fused_step()                                   # warm-up
         tf_pass = [0.0] * npass
+        lib.quest_gb300_setPassEvents(1)
         lib.quest_gb300_eventRecord(4)
         for _ in range(args.steps):
-            _, pm = fused_step(per_pass=True)
-            tf_pass = [a + b for a, b in zip(tf_pass, pm)]
+            fused_step()
+            lib.quest_gb300_passTimesMs(pt, npass)
+            tf_pass = [a + pt[i] for i, a in enumerate(tf_pass)]
         lib.quest_gb300_eventRecord(5)
+        lib.quest_gb300_setPassEvents(0)
         tf_ms = lib.quest_gb300_eventElapsedMs(4, 5) / args.steps
         tf_dom = sum(tf_pass[i] for i in dom_idx) / args.steps / max(1, len(dom_idx))
         other = {"ms_per_circuit": round(tf_ms, 2), "gbs": round(alg_bytes / (tf_ms / 1e3) / 1e9, 1),

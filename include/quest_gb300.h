@@ -61,6 +61,14 @@ int quest_gb300_planNumGates(void* plan);
 /* Copy pass i (targets ascending, FP64 matrix); returns k or -1. */
 int quest_gb300_planPass(void* plan, int i, int* targets, double* re, double* im);
 
+/* Per-pass timing: with setPassEvents(1), applyPlanF32 records a CUDA event
+ * pair on the library stream around each pass; passTimesMs writes the
+ * durations (ms) of the passes of the last application (-1 for a pass not
+ * recorded) once the stream has passed them, and returns the number of
+ * passes. */
+void quest_gb300_setPassEvents(int on);
+int quest_gb300_passTimesMs(double* out, int maxPasses);
+
 /* ---- arithmetic of the plain path ------------------------------------------
  * No counterpart in the reference.  GB300 runs FP64 fused multiply-adds at
  * about 1/70 of its FP32 rate, so the plain path's general 2 x 2 gates

@@ -426,6 +426,28 @@ void quest_gb300_copyStateToHostF32(void* h, double* re, double* im) {
     QG_CUDA(cudaStreamSynchronize(st), "copyStateToHostF32");
 }
 
+// Per-pass timing of plan applications (quest_gb300_setPassEvents): a CUDA
+// event pair around every pass of the last application, recorded on the
+// library stream from inside the pass loop.
+namespace {
+bool g_passEvents = false;
+std::vector<cudaEvent_t> g_passEv;       // start, end of pass i at 2 i, 2 i + 1
+std::vector<char> g_passRecorded;        // pass i of the last application was recorded
+}  // namespace
+
+extern "C" void quest_gb300_setPassEvents(int on) { g_passEvents = on != 0; }
+
+extern "C" int quest_gb300_passTimesMs(double* out, int maxPasses) {
+    const int n = (int)g_passRecorded.size();
+    if (!out) return n;
+    for (int i = 0; i < n && i < maxPasses; ++i) {
+        float ms = 0.f;
+        out[i] = (g_passRecorded[i] && cudaEventElapsedTime(&ms, g_passEv[2 * i], g_passEv[2 * i + 1]) == cudaSuccess)
+                     ? (double)ms : -1.0;
+    }
+    return n;
+}
+
 int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPasses) {
     QuregF32* q = qg::Q(h);
     qg::FusedPlan* p = reinterpret_cast<qg::FusedPlan*>(plan);
@@ -456,19 +478,33 @@ int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPas
     if (firstPass == 0) qg::tcBeginPlan(p->device, p->passes.size());
     qg::tcBeginRange(p->device);
     bool usedTC = false;
+    if (g_passEvents) {
+        while ((int)g_passEv.size() < 2 * total) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) break;
+            g_passEv.push_back(e);
+        }
+        if (firstPass == 0) g_passRecorded.assign(total, 0);
+    }
     for (int i = firstPass; i < last; ++i) {
         const qg::FusedPass& pass = p->passes[i];
+        const bool timed = g_passEvents && (int)g_passEv.size() >= 2 * total && i < (int)g_passRecorded.size();
+        if (timed) cudaEventRecord(g_passEv[2 * i], st);
         const int tc = qg::applyPassTCIndexed(*q, pass, p->device, (size_t)i, st);
         if (tc < 0) return -1;
-        if (tc > 0) {
+        if (tc == 0) {
+            if (!qg::applyPassSimt(*q, pass, st)) {
+                invalidQuESTInputError("fused pass on more than 5 qubits needs the tensor-core applier", "applyPlanF32");
+                return -1;
+            }
+            qg::tcNoteSimtPass(p->device, (size_t)i);
+        } else {
             usedTC = true;
-            continue;
         }
-        if (!qg::applyPassSimt(*q, pass, st)) {
-            invalidQuESTInputError("fused pass on more than 5 qubits needs the tensor-core applier", "applyPlanF32");
-            return -1;
+        if (timed) {
+            cudaEventRecord(g_passEv[2 * i + 1], st);
+            g_passRecorded[i] = 1;
         }
-        qg::tcNoteSimtPass(p->device, (size_t)i);
     }
     if (usedTC && qg::g_checkTC && last == total) {
         const int e = qg::tcErrorFlag(p->device);

@@ -195,6 +195,8 @@ SIGNATURES = {
     "quest_gb300_tunedKernel": (_I, [_I, _I, _I, _P(qreal)]),
     "quest_gb300_setKernelTuning": (None, [_I]),
     "quest_gb300_setPlainArithmetic": (_I, [_I]),
+    "quest_gb300_setPassEvents": (None, [_I]),
+    "quest_gb300_passTimesMs": (_I, [_P(qreal), _I]),
     "quest_gb300_getPlainArithmetic": (_I, []),
     "quest_gb300_createQuregF32": (C.c_void_p, [_I]),
     "quest_gb300_destroyQuregF32": (None, [C.c_void_p]),

@@ -289,3 +289,30 @@ def test_capture_with_autotuned_width(gpulib, tmp_path, monkeypatch):
     assert 1 - f <= 1e-6 and np.max(np.abs(a - b)) <= 1e-5
     L.destroy(direct)
     L.destroy(cap)
+
+
+def test_pass_events_time_every_pass(gpulib):
+    """setPassEvents(1): applyPlanF32 records an event pair around each pass;
+    passTimesMs returns one positive duration per pass of the last
+    application, summing to no more than the whole application."""
+    L = gpulib
+    lib = L.lib
+    n = 18
+    p = L.plan(n, 6, W.c2_circuit(n=n, layers=4, seed=3))
+    npass = lib.quest_gb300_planCompile(p)
+    q32 = lib.quest_gb300_createQuregF32(n)
+    lib.quest_gb300_applyPlanF32(q32, p)                      # warm-up (upload)
+    lib.quest_gb300_setPassEvents(1)
+    try:
+        lib.quest_gb300_eventRecord(40)
+        assert lib.quest_gb300_applyPlanF32(q32, p) == 0
+        lib.quest_gb300_eventRecord(41)
+        whole = lib.quest_gb300_eventElapsedMs(40, 41)
+        out = (C.c_double * npass)()
+        assert lib.quest_gb300_passTimesMs(out, npass) == npass
+        times = list(out)
+        assert all(t > 0 for t in times) and sum(times) <= whole * 1.01
+    finally:
+        lib.quest_gb300_setPassEvents(0)
+    lib.quest_gb300_destroyQuregF32(q32)
+    lib.quest_gb300_planDestroy(p)
