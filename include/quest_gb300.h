@@ -235,6 +235,15 @@ int quest_gb300_sampleMeasurements(Qureg qureg, const int* qubits, int numQubits
 void* quest_gb300_trotterBatchCreate(int numQubits, int numInstances);
 int quest_gb300_trotterBatchSetInstance(void* batch, int instance, PauliHamil hamil, double time, int order, int reps,
                                         long long initClassicalState);
+/* Set instance `instance` to an explicit circuit instead: the gates recorded
+ * in `plan` (planCreate(numQubits, ...) + planAdd*; 11 <= numQubits <= the
+ * batch's), applied from initClassicalState(init); its "energy" is the
+ * expectation of `hamil` (numSumTerms = 0: none, reported as 0).  Instances
+ * with the same register size, gate qubits gate by gate and Hamiltonian
+ * strings share a class (one search, one launch per pass); an instance whose
+ * gates cannot take its class's passes is given its own. */
+int quest_gb300_trotterBatchSetCircuit(void* batch, int instance, void* plan, PauliHamil hamil,
+                                       long long initClassicalState);
 /* Evolve every instance; energies (may be null): B doubles. */
 int quest_gb300_trotterBatchRun(void* batch, double* energies);
 /* Copy instance `instance`'s final state into an FP64 register of n qubits,

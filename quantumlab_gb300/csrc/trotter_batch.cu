@@ -4,7 +4,10 @@
 // QuantumLab's Fermi-Hubbard studies run one Trotter circuit per Hamiltonian
 // instance (QuEST.c:1079 applyTrotterCircuit -> QuEST_common.c:762-844 per
 // instance, then calcExpecPauliSum, QuEST_common.c:506-533).  A batch holds B
-// instances as FP32 states and runs them together.  Instances that share the
+// instances as FP32 states and runs them together.  An instance is a Trotter
+// circuit or an explicit circuit (the gates of a fusion plan, e.g. one
+// circuit shape with other parameters per instance), each with the Pauli sum
+// whose expectation the run reports.  Instances that share the
 // register size, Pauli strings, order and repetitions form a class: their
 // circuits have the same shape with other angles.  Instances of different
 // step counts, orders, register sizes or Hamiltonians sit in one batch as
@@ -231,6 +234,8 @@ __global__ void kBatchToF64(const float* __restrict__ sr, const float* __restric
 }
 
 struct Instance {
+    bool circuit = false;            // an explicit gate list instead of a Trotter circuit
+    std::vector<FusedGate> gates;    // (circuit) its gates, in order
     int n = 0;                       // qubits
     std::vector<int> codes;          // numTerms x n, QuEST pauliOpType values
     std::vector<double> coeffs;
@@ -503,57 +508,93 @@ bool compileBatch(TrotterBatch* b) {
             invalidQuESTInputError("Every instance of the Trotter batch must be set before it runs.", kFn);
             return false;
         }
-    // classes: instances of one register size, Pauli strings, order and
-    // repetitions, in order of first appearance
+    // classes: instances of one register size, measured Pauli strings and
+    // circuit shape (Trotter order and repetitions, or the qubits of every
+    // gate of an explicit circuit), in order of first appearance
+    auto sameShape = [](const Instance& r, const Instance& in) {
+        if (r.n != in.n || r.circuit != in.circuit || r.codes != in.codes) return false;
+        if (!in.circuit) return r.order == in.order && r.reps == in.reps;
+        if (r.gates.size() != in.gates.size()) return false;
+        for (size_t g = 0; g < r.gates.size(); ++g)
+            if (r.gates[g].qubits != in.gates[g].qubits) return false;
+        return true;
+    };
     b->classes.clear();
-    b->classOf.assign(B, -1);
-    b->posOf.assign(B, -1);
+    std::vector<int> leaderOf(B, -1);
     for (int k = 0; k < B; ++k) {
         const Instance& in = b->inst[k];
         int c = 0;
-        for (; c < (int)b->classes.size(); ++c) {
-            const Instance& r = b->inst[b->classes[c].members[0]];
-            if (r.n == in.n && r.order == in.order && r.reps == in.reps && r.codes == in.codes) break;
-        }
+        for (; c < (int)b->classes.size(); ++c)
+            if (sameShape(b->inst[b->classes[c].members[0]], in)) break;
         if (c == (int)b->classes.size()) {
             b->classes.emplace_back();
             b->classes.back().n = in.n;
         }
-        b->classOf[k] = c;
-        b->posOf[k] = (int)b->classes[c].members.size();
         b->classes[c].members.push_back(k);
+        leaderOf[k] = b->classes[c].members[0];
     }
-    const int C = (int)b->classes.size();
-    // gate streams; each class's member 0 searched (classes in parallel), the
-    // other members reuse its passes with their own FP64 products
-    std::vector<std::vector<FusedPlan>> plans(C);
-    for (int c = 0; c < C; ++c) {
-        TrotterClass& cl = b->classes[c];
-        plans[c].resize(cl.members.size());
-        for (size_t m = 0; m < cl.members.size(); ++m) {
-            const Instance& in = b->inst[cl.members[m]];
-            FusedPlan& p = plans[c][m];
-            p.numQubits = cl.n;
-            p.maxFused = widestPass(cl.n);
-            for (int r = 0; r < in.reps; ++r) trotterTerms(in, cl.n, in.time / in.reps, in.order, p.gates);
-        }
+    // gate streams; every class's first member is searched (classes in
+    // parallel), the others reuse its passes with their own FP64 products.
+    // Passes are at most min(6, n - 7) qubits wide, the tensor-core limit.
+    std::vector<FusedPlan> plan(B);
+    for (int k = 0; k < B; ++k) {
+        const Instance& in = b->inst[k];
+        FusedPlan& p = plan[k];
+        p.numQubits = in.n;
+        p.maxFused = std::min(widestPass(in.n), in.n - 7);
+        if (in.circuit) p.gates = in.gates;
+        else
+            for (int r = 0; r < in.reps; ++r) trotterTerms(in, in.n, in.time / in.reps, in.order, p.gates);
     }
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    parallelFor((size_t)C, std::min(hw, 8u), [&](size_t c) { compilePlan(plans[c][0]); });
-    std::vector<std::pair<int, int>> likeJobs;
-    for (int c = 0; c < C; ++c)
-        for (size_t m = 1; m < plans[c].size(); ++m) likeJobs.emplace_back(c, (int)m);
-    std::atomic<bool> good{true};
-    for (int c = 0; c < C; ++c) good = good && plans[c][0].compiled;
-    if (good)
-        parallelFor(likeJobs.size(), std::min(hw, 8u), [&](size_t j) {
-            if (!compilePlanLike(plans[likeJobs[j].first][likeJobs[j].second], plans[likeJobs[j].first][0]))
-                good = false;
-        });
-    if (!good) {
-        invalidQuESTInputError("The Trotter circuits of the batch could not be fused with one pass structure.", kFn);
-        return false;
+    std::vector<int> leaders, others;
+    for (const TrotterClass& cl : b->classes) {
+        leaders.push_back(cl.members[0]);
+        for (size_t m = 1; m < cl.members.size(); ++m) others.push_back(cl.members[m]);
     }
+    parallelFor(leaders.size(), std::min(hw, 8u), [&](size_t i) { compilePlan(plan[leaders[i]]); });
+    for (int l : leaders)
+        if (!plan[l].compiled) {
+            invalidQuESTInputError("A circuit of the batch could not be fused.", kFn);
+            return false;
+        }
+    std::vector<char> like(B, 1);
+    parallelFor(others.size(), std::min(hw, 8u),
+                [&](size_t i) { like[others[i]] = compilePlanLike(plan[others[i]], plan[leaderOf[others[i]]]) ? 1 : 0; });
+    // a member whose gates cannot take its class's passes (an explicit
+    // circuit with a gate less diagonal than the leader's) gets a class and a
+    // search of its own
+    std::vector<int> alone;
+    for (int o : others)
+        if (!like[o]) alone.push_back(o);
+    parallelFor(alone.size(), std::min(hw, 8u), [&](size_t i) { compilePlan(plan[alone[i]]); });
+    for (int o : alone)
+        if (!plan[o].compiled) {
+            invalidQuESTInputError("A circuit of the batch could not be fused.", kFn);
+            return false;
+        }
+    if (!alone.empty()) {
+        for (TrotterClass& cl : b->classes) {
+            std::vector<int> keep;
+            for (int k : cl.members)
+                if (like[k]) keep.push_back(k);
+            cl.members.swap(keep);
+        }
+        for (int o : alone) {
+            b->classes.emplace_back();
+            b->classes.back().n = b->inst[o].n;
+            b->classes.back().members.push_back(o);
+        }
+    }
+    b->classOf.assign(B, -1);
+    b->posOf.assign(B, -1);
+    for (int c = 0; c < (int)b->classes.size(); ++c)
+        for (size_t m = 0; m < b->classes[c].members.size(); ++m) {
+            b->classOf[b->classes[c].members[m]] = c;
+            b->posOf[b->classes[c].members[m]] = (int)m;
+        }
+    const int C = (int)b->classes.size();
+    auto planOf = [&](int c, size_t m) -> FusedPlan& { return plan[b->classes[c].members[m]]; };
     // layout: states, image offsets, result slots and rows, class after class
     size_t stateFloats = 0, imgTotal = 0;
     int pos = 0, slots = 0;
@@ -565,12 +606,12 @@ bool compileBatch(TrotterBatch* b) {
         stateFloats += ((size_t)1 << cl.n) * M;
         cl.posBase = pos;
         pos += (int)M;
-        const size_t np = plans[c][0].passes.size();
+        const size_t np = planOf(c, 0).passes.size();
         cl.shape.clear();
         cl.imgOffset.assign(np, 0);
         cl.imgStride.assign(np, 0);
         for (size_t p = 0; p < np; ++p) {
-            cl.shape.push_back(widenNarrow(plans[c][0].passes[p], cl.n));
+            cl.shape.push_back(widenNarrow(planOf(c, 0).passes[p], cl.n));
             cl.imgStride[p] = tcImageFloats((int)cl.shape[p].targets.size());
             cl.imgOffset[p] = imgTotal;
             imgTotal += cl.imgStride[p] * M;
@@ -591,7 +632,7 @@ bool compileBatch(TrotterBatch* b) {
     parallelFor(imgJobs.size(), std::min(hw, 16u), [&](size_t j) {
         const int c = std::get<0>(imgJobs[j]), p = std::get<1>(imgJobs[j]), m = std::get<2>(imgJobs[j]);
         const TrotterClass& cl = b->classes[c];
-        tcBuildImage(widenNarrow(plans[c][m].passes[p], cl.n), host.data() + cl.imgOffset[p] + m * cl.imgStride[p]);
+        tcBuildImage(widenNarrow(planOf(c, m).passes[p], cl.n), host.data() + cl.imgOffset[p] + m * cl.imgStride[p]);
     });
     // device side
     cudaStream_t st = stream();
@@ -720,11 +761,59 @@ int quest_gb300_trotterBatchSetInstance(void* batch, int instance, PauliHamil ha
         }
         in.codes[i] = c;
     }
+    in.circuit = false;
+    in.gates.clear();
     in.n = hamil.numQubits;
     in.coeffs.assign(hamil.termCoeffs, hamil.termCoeffs + hamil.numSumTerms);
     in.time = time;
     in.order = order;
     in.reps = reps;
+    in.init = initClassicalState;
+    in.set = true;
+    cudaStreamSynchronize(qg::stream());
+    qg::freeDevice(b);                               // recompiled at the next run
+    return 0;
+}
+
+int quest_gb300_trotterBatchSetCircuit(void* batch, int instance, void* plan, PauliHamil hamil,
+                                       long long initClassicalState) {
+    const char* fn = "quest_gb300_trotterBatchSetCircuit";
+    TrotterBatch* b = reinterpret_cast<TrotterBatch*>(batch);
+    const qg::FusedPlan* p = reinterpret_cast<const qg::FusedPlan*>(plan);
+    if (!b || instance < 0 || instance >= b->B || !p) {
+        invalidQuESTInputError("Invalid batch, instance index or plan.", fn);
+        return -1;
+    }
+    const int n = p->numQubits;
+    if (n < 11 || n > b->maxQubits || initClassicalState < 0 || initClassicalState >= (1ll << n)) {
+        invalidQuESTInputError("Invalid register size or initial state for the batch.", fn);
+        return -1;
+    }
+    if (hamil.numSumTerms > 0 && (hamil.numQubits != n || !hamil.pauliCodes || !hamil.termCoeffs)) {
+        invalidQuESTInputError("The measured Hamiltonian must act on the circuit's qubits.", fn);
+        return -1;
+    }
+    qg::Instance& in = b->inst[instance];
+    in.codes.clear();
+    in.coeffs.clear();
+    if (hamil.numSumTerms > 0) {
+        in.codes.resize((size_t)hamil.numSumTerms * n);
+        for (size_t i = 0; i < in.codes.size(); ++i) {
+            const int c = (int)hamil.pauliCodes[i];
+            if (c < 0 || c > 3) {
+                invalidQuESTInputError("Invalid Pauli code in the measured Hamiltonian.", fn);
+                return -1;
+            }
+            in.codes[i] = c;
+        }
+        in.coeffs.assign(hamil.termCoeffs, hamil.termCoeffs + hamil.numSumTerms);
+    }
+    in.circuit = true;
+    in.gates = p->gates;
+    in.n = n;
+    in.time = 0.0;
+    in.order = 1;
+    in.reps = 1;
     in.init = initClassicalState;
     in.set = true;
     cudaStreamSynchronize(qg::stream());

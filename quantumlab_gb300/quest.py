@@ -216,6 +216,7 @@ SIGNATURES = {
     "quest_gb300_trotterBatchCreate": (C.c_void_p, [_I, _I]),
     "quest_gb300_trotterBatchSetInstance": (_I, [C.c_void_p, _I, PauliHamil, C.c_double, _I, _I, C.c_longlong]),
     "quest_gb300_trotterBatchRun": (_I, [C.c_void_p, _P(C.c_double)]),
+    "quest_gb300_trotterBatchSetCircuit": (_I, [C.c_void_p, _I, C.c_void_p, PauliHamil, C.c_longlong]),
     "quest_gb300_trotterBatchCopyState": (_I, [C.c_void_p, _I, _Q]),
     "quest_gb300_trotterBatchNumPasses": (_I, [C.c_void_p]),
     "quest_gb300_trotterBatchNumClasses": (_I, [C.c_void_p]),

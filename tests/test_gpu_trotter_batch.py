@@ -162,3 +162,71 @@ def test_batch_checks_and_precision_switch(gpulib, library_errors):
     lib.quest_gb300_trotterBatchDestroy(b)
     lib.destroyPauliHamil(h0)
     lib.destroyPauliHamil(h1)
+
+
+def _with_new_angles(ops, seed):
+    """The same circuit shape (gates on the same qubits) with other angles."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for op in ops:
+        if op[0] == "cu":
+            v = rng.normal(size=4)
+            v /= np.linalg.norm(v)
+            out.append(("cu", op[1], *v))
+        elif op[0] == "cp":
+            out.append(("cp", op[1], op[2], float(rng.uniform(0, 2 * np.pi))))
+        else:
+            out.append(op)
+    return out
+
+
+def test_batch_of_explicit_circuits(gpulib, library_errors):
+    """Explicit circuits (fusion-plan gate lists) share a batch with a Trotter
+    instance: three 13-qubit circuits of one shape with other angles (one
+    class), two 14-qubit ones of another shape, each measured against a
+    random Pauli sum; every instance matches the same calls run directly in
+    FP64 (state and expectation)."""
+    L = gpulib
+    lib = L.lib
+    rng = np.random.default_rng(31)
+    base13 = W.c2_circuit(n=13, layers=4, seed=40)
+    base14 = W.c2_circuit(n=14, layers=3, seed=41)
+    circuits = [(13, base13), (13, _with_new_angles(base13, 1)), (13, _with_new_angles(base13, 2)),
+                (14, base14), (14, _with_new_angles(base14, 3))]
+    sites, U = 6, 4.0
+    b = lib.quest_gb300_trotterBatchCreate(14, len(circuits) + 1)
+    hams, plans, sums = [], [], []
+    for i, (n, ops) in enumerate(circuits):
+        codes = rng.integers(0, 4, size=(12, n)).astype(np.int32)
+        coeffs = rng.normal(size=12)
+        sums.append((codes, coeffs))
+        hams.append(L.pauli_hamil(codes, coeffs))
+        plans.append(L.plan(n, 6, ops))
+        assert lib.quest_gb300_trotterBatchSetCircuit(b, i, plans[-1], hams[-1], 5 * i) == 0
+    tc, tk, _ = W.hubbard_terms(sites, U)
+    hams.append(L.pauli_hamil(tc, tk))
+    assert lib.quest_gb300_trotterBatchSetInstance(b, len(circuits), hams[-1], 1.0, 1, 3, W.neel_index(sites)) == 0
+    e = (C.c_double * (len(circuits) + 1))()
+    assert lib.quest_gb300_trotterBatchRun(b, e) == 0, list(library_errors)
+    assert lib.quest_gb300_trotterBatchNumClasses(b) == 3
+    for i, (n, ops) in enumerate(circuits):
+        q, ws = L.create(n), L.create(n)
+        L.lib.initClassicalState(q, 5 * i)
+        W.run_ops(L, q, ops)
+        want = L.amps(q).copy()
+        codes, coeffs = sums[i]
+        e_want = L.calcExpecPauliSum(q, codes, coeffs, ws)
+        assert lib.quest_gb300_trotterBatchCopyState(b, i, q) == 0
+        got = L.amps(q)
+        f = abs(np.vdot(want, got)) ** 2 / (np.vdot(got, got).real * np.vdot(want, want).real)
+        assert 1 - f <= 1e-6 and np.max(np.abs(got - want)) <= 1e-5, (i, 1 - f)
+        assert abs(e[i] - e_want) <= 1e-5 * np.sum(np.abs(coeffs)), (i, e[i], e_want)
+        L.destroy(ws)
+        L.destroy(q)
+    _check_instance(L, b, len(circuits), sites, U, 1.0, 1, 3, e[len(circuits)])
+    lib.quest_gb300_trotterBatchDestroy(b)
+    for p in plans:
+        lib.quest_gb300_planDestroy(p)
+    for h in hams:
+        lib.destroyPauliHamil(h)
+    assert not library_errors
