@@ -183,9 +183,9 @@ def _with_new_angles(ops, seed):
 def test_batch_of_explicit_circuits(gpulib, library_errors):
     """Explicit circuits (fusion-plan gate lists) share a batch with a Trotter
     instance: three 13-qubit circuits of one shape with other angles (one
-    class), two 14-qubit ones of another shape, each measured against a
-    random Pauli sum; every instance matches the same calls run directly in
-    FP64 (state and expectation)."""
+    class), two 14-qubit ones of another shape, each measured against Pauli
+    strings shared by its size with its own coefficients; every instance
+    matches the same calls run directly in FP64 (state and expectation)."""
     L = gpulib
     lib = L.lib
     rng = np.random.default_rng(31)
@@ -196,8 +196,9 @@ def test_batch_of_explicit_circuits(gpulib, library_errors):
     sites, U = 6, 4.0
     b = lib.quest_gb300_trotterBatchCreate(14, len(circuits) + 1)
     hams, plans, sums = [], [], []
+    strings = {n: rng.integers(0, 4, size=(12, n)).astype(np.int32) for n in (13, 14)}   # one set per size
     for i, (n, ops) in enumerate(circuits):
-        codes = rng.integers(0, 4, size=(12, n)).astype(np.int32)
+        codes = strings[n]
         coeffs = rng.normal(size=12)
         sums.append((codes, coeffs))
         hams.append(L.pauli_hamil(codes, coeffs))
