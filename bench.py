@@ -166,22 +166,8 @@ def run_gpu(args, rank, world):
     lib = L.lib
     n, k = args.qubits, args.fusion
     ops = W.c2_circuit(n=n, layers=args.layers, seed=2)
-    # the end-to-end input lives in a register's pinned host mirror, made
-    # before anything is timed, as an application that loops over circuits
-    # would hold it: a seeded random product state (every amplitude nonzero,
-    # no two host pages alike), prepared on the device and copied out once.
-    # (A buffer of identical pages -- |0..0> is almost all zeros -- was seen
-    # to be merged by the host while idle on this pool's virtual machines,
-    # after which device->host copies into it slowed from 90 ms to 2 s.)
+    # the register whose pinned host mirror holds the end-to-end input
     src = L.create(n)
-    lib.initPlusState(src)
-    rng_in = np.random.default_rng(2024)
-    from quantumlab_gb300.quest import Complex as _Cx
-    for t in range(n):
-        v = rng_in.normal(size=4)
-        v /= np.linalg.norm(v)
-        lib.compactUnitary(src, t, _Cx(v[0], v[1]), _Cx(v[2], v[3]))
-    lib.copyStateFromGPU(src)
     alg_bytes = W.algorithmic_bytes(ops, n)
     pass_bytes = 2 * (1 << n) * 8                   # one fused pass: read + write the FP32 state
 
@@ -403,6 +389,20 @@ def run_gpu(args, rank, world):
     # calcTotalProb.  Two untimed warm-up steps (FP32 scratch, plan upload).
     lib.quest_gb300_destroyQuregF32(q32)
     q32 = None
+    # The input, prepared just before the steps as an application looping
+    # over circuits would produce it: a seeded random product state (every
+    # amplitude nonzero, no two host pages alike), made on the device and
+    # copied into src's pinned mirror.  (Pinned buffers left untouched for a
+    # minute were measured copying at a fraction of the link's rate on a
+    # virtual machine whose host reclaims idle guest pages.)
+    lib.initPlusState(src)
+    rng_in = np.random.default_rng(2024)
+    from quantumlab_gb300.quest import Complex as _Cx
+    for t in range(n):
+        v = rng_in.normal(size=4)
+        v /= np.linalg.norm(v)
+        lib.compactUnitary(src, t, _Cx(v[0], v[1]), _Cx(v[2], v[3]))
+    lib.copyStateFromGPU(src)
     lib.quest_gb300_setCapture(q64, 1)
 
     split = [0.0, 0.0, 0.0]                            # host -> device, gates + flush, device -> host
