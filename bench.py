@@ -166,8 +166,6 @@ def run_gpu(args, rank, world):
     lib = L.lib
     n, k = args.qubits, args.fusion
     ops = W.c2_circuit(n=n, layers=args.layers, seed=2)
-    # the register whose pinned host mirror holds the end-to-end input
-    src = L.create(n)
     alg_bytes = W.algorithmic_bytes(ops, n)
     pass_bytes = 2 * (1 << n) * 8                   # one fused pass: read + write the FP32 state
 
@@ -389,6 +387,13 @@ def run_gpu(args, rank, world):
     # calcTotalProb.  Two untimed warm-up steps (FP32 scratch, plan upload).
     lib.quest_gb300_destroyQuregF32(q32)
     q32 = None
+    # The end-to-end registers, created just before their steps as an
+    # application allocates its registers and then loops over circuits: src
+    # (whose pinned host mirror holds the input) and qe (the lab's register).
+    L.destroy(q64)
+    q64 = None
+    src = L.create(n)
+    qe = L.create(n)
     # The input, prepared just before the steps as an application looping
     # over circuits would produce it: a seeded random product state (every
     # amplitude nonzero, no two host pages alike), made on the device and
@@ -403,19 +408,19 @@ def run_gpu(args, rank, world):
         v /= np.linalg.norm(v)
         lib.compactUnitary(src, t, _Cx(v[0], v[1]), _Cx(v[2], v[3]))
     lib.copyStateFromGPU(src)
-    lib.quest_gb300_setCapture(q64, 1)
+    lib.quest_gb300_setCapture(qe, 1)
 
     split = [0.0, 0.0, 0.0]                            # host -> device, gates + flush, device -> host
     d2h_each = []
 
     def e2e_step():
         t = time.perf_counter()
-        lib.initStateFromAmps(q64, src.stateVec.real, src.stateVec.imag)
+        lib.initStateFromAmps(qe, src.stateVec.real, src.stateVec.imag)
         t1 = time.perf_counter()
-        run_plain_step(L, q64, ops)
-        p = lib.calcTotalProb(q64)
+        run_plain_step(L, qe, ops)
+        p = lib.calcTotalProb(qe)
         t2 = time.perf_counter()
-        lib.copyStateFromGPU(q64)
+        lib.copyStateFromGPU(qe)
         t3 = time.perf_counter()
         for i, d in enumerate((t1 - t, t2 - t1, t3 - t2)):
             split[i] += d
@@ -438,16 +443,16 @@ def run_gpu(args, rank, world):
     d2h_repeat = []
     for _ in range(3):
         t = time.perf_counter()
-        lib.copyStateFromGPU(q64)
+        lib.copyStateFromGPU(qe)
         d2h_repeat.append(round((time.perf_counter() - t) * 1e3, 1))
-    lib.quest_gb300_setCapture(q64, 0)
+    lib.quest_gb300_setCapture(qe, 0)
     # what the host link gave this process: whether both host mirrors are
     # page-locked, and plain 1 GiB copies between pinned and device memory
-    mirrors_pinned = [lib.quest_gb300_hostMirrorPinned(src) == 1, lib.quest_gb300_hostMirrorPinned(q64) == 1]
+    mirrors_pinned = [lib.quest_gb300_hostMirrorPinned(src) == 1, lib.quest_gb300_hostMirrorPinned(qe) == 1]
     link = link_probe()
     state_bytes = (1 << n) * 16
     L.destroy(src)
-    L.destroy(q64)
+    L.destroy(qe)
     lib.quest_gb300_planDestroy(plan)
 
     peak, peak_kind = peaks()
