@@ -169,6 +169,79 @@ def run_gpu(args, rank, world):
     alg_bytes = W.algorithmic_bytes(ops, n)
     pass_bytes = 2 * (1 << n) * 8                   # one fused pass: read + write the FP32 state
 
+    # ---- end to end through the QuEST C ABI with host buffers ------------
+    # The lab's call pattern, unchanged: initStateFromAmps from pinned host
+    # FP64 arrays, every gate of the circuit as one QuEST API call,
+    # calcTotalProb, then copyStateFromGPU of every amplitude into the
+    # register's host mirror.  Op-stream capture is on for the register, so
+    # the gate calls are queued and applied by the fused FP32 engine at
+    # calcTotalProb.  Two untimed warm-up steps (FP32 scratch, plan upload).
+    # The end-to-end registers: src (whose pinned host mirror holds the
+    # input) and qe (the lab's register).  This runs first, before the
+    # other arms load the GPU, as an application that only loops over
+    # circuits would run.
+    src = L.create(n)
+    qe = L.create(n)
+    # The input, prepared just before the steps as an application looping
+    # over circuits would produce it: a seeded random product state (every
+    # amplitude nonzero, no two host pages alike), made on the device and
+    # copied into src's pinned mirror.  (Pinned buffers left untouched for a
+    # minute were measured copying at a fraction of the link's rate on a
+    # virtual machine whose host reclaims idle guest pages.)
+    lib.initPlusState(src)
+    rng_in = np.random.default_rng(2024)
+    from quantumlab_gb300.quest import Complex as _Cx
+    for t in range(n):
+        v = rng_in.normal(size=4)
+        v /= np.linalg.norm(v)
+        lib.compactUnitary(src, t, _Cx(v[0], v[1]), _Cx(v[2], v[3]))
+    lib.copyStateFromGPU(src)
+    lib.quest_gb300_setCapture(qe, 1)
+
+    split = [0.0, 0.0, 0.0]                            # host -> device, gates + flush, device -> host
+    d2h_each = []
+
+    def e2e_step():
+        t = time.perf_counter()
+        lib.initStateFromAmps(qe, src.stateVec.real, src.stateVec.imag)
+        t1 = time.perf_counter()
+        run_plain_step(L, qe, ops)
+        p = lib.calcTotalProb(qe)
+        t2 = time.perf_counter()
+        lib.copyStateFromGPU(qe)
+        t3 = time.perf_counter()
+        for i, d in enumerate((t1 - t, t2 - t1, t3 - t2)):
+            split[i] += d
+        d2h_each.append(round((t3 - t2) * 1e3, 1))
+        return p
+
+    for _ in range(2):                                 # untimed warm-up steps
+        e2e_step()
+    split[:] = [0.0, 0.0, 0.0]
+    d2h_each.clear()
+    e2e_steps = max(1, min(args.steps, 3))
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_prob = e2e_step()
+    e2e_s = barrier_max((time.perf_counter() - t0) / e2e_steps, world)
+    split = [x / e2e_steps for x in split]
+    # the same device->host copy again with nothing in between: whether a slow
+    # copy in the steps is the copy itself or the state the step left
+    d2h_repeat = []
+    for _ in range(3):
+        t = time.perf_counter()
+        lib.copyStateFromGPU(qe)
+        d2h_repeat.append(round((time.perf_counter() - t) * 1e3, 1))
+    lib.quest_gb300_setCapture(qe, 0)
+    # what the host link gave this process: whether both host mirrors are
+    # page-locked, and plain 1 GiB copies between pinned and device memory
+    mirrors_pinned = [lib.quest_gb300_hostMirrorPinned(src) == 1, lib.quest_gb300_hostMirrorPinned(qe) == 1]
+    link = link_probe()
+    state_bytes = (1 << n) * 16
+    L.destroy(src)
+    L.destroy(qe)
+
     # ---- fused FP32 engine (the headline) --------------------------------
     prec = 0 if args.precision == "tf32" else 1
     pname = "split-TF32" if prec == 0 else "split-BF16"
@@ -378,82 +451,9 @@ def run_gpu(args, rank, world):
             widths[str(kw)] = entry
             lib.quest_gb300_planDestroy(pw)
 
-    # ---- end to end through the QuEST C ABI with host buffers ------------
-    # The lab's call pattern, unchanged: initStateFromAmps from pinned host
-    # FP64 arrays (|0..0>), every gate of the circuit as one QuEST API call,
-    # calcTotalProb, then copyStateFromGPU of every amplitude into the
-    # register's host mirror.  Op-stream capture is on for the register, so
-    # the gate calls are queued and applied by the fused FP32 engine at
-    # calcTotalProb.  Two untimed warm-up steps (FP32 scratch, plan upload).
-    lib.quest_gb300_destroyQuregF32(q32)
-    q32 = None
-    # The end-to-end registers, created just before their steps as an
-    # application allocates its registers and then loops over circuits: src
-    # (whose pinned host mirror holds the input) and qe (the lab's register).
-    L.destroy(q64)
-    q64 = None
-    src = L.create(n)
-    qe = L.create(n)
-    # The input, prepared just before the steps as an application looping
-    # over circuits would produce it: a seeded random product state (every
-    # amplitude nonzero, no two host pages alike), made on the device and
-    # copied into src's pinned mirror.  (Pinned buffers left untouched for a
-    # minute were measured copying at a fraction of the link's rate on a
-    # virtual machine whose host reclaims idle guest pages.)
-    lib.initPlusState(src)
-    rng_in = np.random.default_rng(2024)
-    from quantumlab_gb300.quest import Complex as _Cx
-    for t in range(n):
-        v = rng_in.normal(size=4)
-        v /= np.linalg.norm(v)
-        lib.compactUnitary(src, t, _Cx(v[0], v[1]), _Cx(v[2], v[3]))
-    lib.copyStateFromGPU(src)
-    lib.quest_gb300_setCapture(qe, 1)
-
-    split = [0.0, 0.0, 0.0]                            # host -> device, gates + flush, device -> host
-    d2h_each = []
-
-    def e2e_step():
-        t = time.perf_counter()
-        lib.initStateFromAmps(qe, src.stateVec.real, src.stateVec.imag)
-        t1 = time.perf_counter()
-        run_plain_step(L, qe, ops)
-        p = lib.calcTotalProb(qe)
-        t2 = time.perf_counter()
-        lib.copyStateFromGPU(qe)
-        t3 = time.perf_counter()
-        for i, d in enumerate((t1 - t, t2 - t1, t3 - t2)):
-            split[i] += d
-        d2h_each.append(round((t3 - t2) * 1e3, 1))
-        return p
-
-    for _ in range(2):                                 # untimed warm-up steps
-        e2e_step()
-    split[:] = [0.0, 0.0, 0.0]
-    d2h_each.clear()
-    e2e_steps = max(1, min(args.steps, 3))
-    barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_prob = e2e_step()
-    e2e_s = barrier_max((time.perf_counter() - t0) / e2e_steps, world)
-    split = [x / e2e_steps for x in split]
-    # the same device->host copy again with nothing in between: whether a slow
-    # copy in the steps is the copy itself or the state the step left
-    d2h_repeat = []
-    for _ in range(3):
-        t = time.perf_counter()
-        lib.copyStateFromGPU(qe)
-        d2h_repeat.append(round((time.perf_counter() - t) * 1e3, 1))
-    lib.quest_gb300_setCapture(qe, 0)
-    # what the host link gave this process: whether both host mirrors are
-    # page-locked, and plain 1 GiB copies between pinned and device memory
-    mirrors_pinned = [lib.quest_gb300_hostMirrorPinned(src) == 1, lib.quest_gb300_hostMirrorPinned(qe) == 1]
-    link = link_probe()
-    state_bytes = (1 << n) * 16
-    L.destroy(src)
-    L.destroy(qe)
     lib.quest_gb300_planDestroy(plan)
+    lib.quest_gb300_destroyQuregF32(q32)
+    L.destroy(q64)
 
     peak, peak_kind = peaks()
     if gate_roof:
