@@ -144,6 +144,15 @@ void quest_gb300_setTensorCoreKernel(int version);
  * Xh.Gll).  Both accumulate in FP32.  Returns 0, or -1 for another mode. */
 int quest_gb300_setTensorCorePrecision(int mode);
 int quest_gb300_getTensorCorePrecision(void);
+/* How the pipelined tensor-core kernels stage state tiles in shared memory:
+ * 0 = 16-byte cp.async copies by every loader lane (the default); 1 = TMA
+ * bulk copies (cp.async.bulk), one 128-byte row of a tile per copy, completing
+ * on an mbarrier.  Both give identical results; on the 30-qubit random
+ * circuit a 6-qubit pass takes 2.83 ms with 0 and 3.77 ms with 1 (split-TF32),
+ * because 128-byte copies keep the TMA unit far below the HBM rate.  Returns
+ * 0, or -1 for another mode. */
+int quest_gb300_setTensorCoreStaging(int mode);
+int quest_gb300_getTensorCoreStaging(void);
 double quest_gb300_calcTotalProbF32(void* qureg32);
 double quest_gb300_calcProbOfOutcomeF32(void* qureg32, int measureQubit, int outcome);
 /* 1 - |<ref|q>|^2 / (<ref|ref><q|q>) against an FP64 state vector; writes the

@@ -52,6 +52,8 @@ void setTensorCoresEnabled(bool on);
 void setTensorCoreKernel(int version);
 bool setTensorCorePrecision(int mode);
 int tensorCorePrecision();
+bool setTensorCoreStaging(int mode);
+int tensorCoreStaging();
 bool tensorCoresEnabled();
 int tcKernelFor(const FusedPass& pass, int n);
 float* f32re(QuregF32& q) { return q.re; }
@@ -546,6 +548,8 @@ void quest_gb300_setTensorCores(int enabled) { qg::setTensorCoresEnabled(enabled
 void quest_gb300_setTensorCoreKernel(int version) { qg::setTensorCoreKernel(version); }
 int quest_gb300_setTensorCorePrecision(int mode) { return qg::setTensorCorePrecision(mode) ? 0 : -1; }
 int quest_gb300_getTensorCorePrecision(void) { return qg::tensorCorePrecision(); }
+int quest_gb300_setTensorCoreStaging(int mode) { return qg::setTensorCoreStaging(mode) ? 0 : -1; }
+int quest_gb300_getTensorCoreStaging(void) { return qg::tensorCoreStaging(); }
 
 double quest_gb300_calcTotalProbF32(void* h) {
     QuregF32* q = qg::Q(h);

@@ -92,6 +92,20 @@ __device__ __forceinline__ void bulkG2S(void* dst, const void* src, uint32_t byt
                  : "memory");
 }
 
+// order this thread's generic-proxy accesses of shared memory before later
+// async-proxy (bulk copy) accesses
+__device__ __forceinline__ void fenceProxyAsync() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// one test of a phase (acquire); true when the phase with the parity completed
+__device__ __forceinline__ bool mbarTest(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smemAddr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
 // 16-byte asynchronous copy global -> shared (no register staging, L1
 // bypassed); completion is tracked per thread by commit groups
 __device__ __forceinline__ void cpAsync16(float* dst, const float* src) {
@@ -596,8 +610,12 @@ struct TileWalker {
 };
 
 // CV = 4: the targets include qubits 0 and 1, and columns are read and
-// written as 16-byte words (see colWords4)
-template <int KQ, int LG, int EG, int LS, int PR, int CV>
+// written as 16-byte words (see colWords4).
+// ST: how the loaders stage a chunk.  0: 16-byte cp.async per lane (commit
+// groups); 1: TMA bulk copies, one 128-byte row (32 positions, contiguous in
+// global memory and in the padded shared layout) per lane and part,
+// completing on one mbarrier per warp and row stage.
+template <int KQ, int LG, int EG, int LS, int PR, int CV, int ST>
 __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* __restrict__ re, float* __restrict__ im,
                                                                   const float* __restrict__ gImage, uint64_t numTiles,
                                                                   int* __restrict__ errFlag, const NormLinks nl,
@@ -636,6 +654,8 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
     float* xs = reinterpret_cast<float*>(gh + S::NGP * kGW);   // [loader group][warp][stage][part][R]
     float* es = xs + (size_t)XST * LG * 4 * PPG * R;     // [epilogue group][warp][R]
     __shared__ __align__(8) uint64_t barG, fullB[NST], emptyB[NST], dFullB[2], dEmptyB[2];
+    constexpr int kStageBars = ST == 1 ? 4 * LG * XST : 1;
+    __shared__ __align__(8) uint64_t stageB[kStageBars];   // bulk staging: [loader warp][row stage]
     __shared__ uint32_t tmemBase;
     __shared__ volatile int abortF;
 
@@ -652,6 +672,8 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                 mbarInit(&dFullB[b], 1);
                 mbarInit(&dEmptyB[b], 128);
             }
+            if (ST == 1)
+                for (int b = 0; b < kStageBars; ++b) mbarInit(&stageB[b], 1);
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
         tmemAlloc(&tmemBase, kCols);
@@ -684,28 +706,51 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         // consecutive amplitudes: one 16-byte copy to pad(q); a warp's copy
         // reads four 128-byte lines.
         TileWalker<KQ> walk;
-        auto issue = [&](uint32_t sc, float* buf) {
+        // bulk staging: lane l < ROWS copies row l of each part, region
+        // indices 32 l .. 32 l + 31 (qubits 0..4 are region bits 0..4, so a
+        // row is 128 contiguous bytes in global memory; in the padded layout
+        // it starts at pad(32 l), a 16-byte boundary)
+        constexpr int ROWS = PART / 32;
+        static_assert(ROWS <= 32 && ROWS / 4 <= V4P, "one row per lane");
+        const uint64_t rowA = p.laneOff[8 * (lane & 3)];
+        uint64_t* const wbar = stageB + (ST == 1 ? (g * 4 + rw) * XST : 0);
+        auto issue = [&](uint32_t sc, float* buf, int stage) {
             const uint64_t tile = cta + (uint64_t)(sc / NCH) * ncta;
             const int ch = sc % NCH;
-            const uint64_t tb = walk.at(p, tile) + laneA;
+            if constexpr (ST == 1) {
+                const uint64_t tb = walk.at(p, tile) + rowA;
+                if (lane == 0) mbarExpectTx(&wbar[stage], (uint32_t)(PPG * ROWS * 128));
+                if (lane < ROWS) {
 #pragma unroll
-            for (int pp = 0; pp < PPG; ++pp) {
-                const int pt = p0 + pp;
-                const float* const src = (S::plane(ch, pt) == 0 ? re : im) + tb;
-                float* const dst = buf + pp * R + rowBase;
+                    for (int pp = 0; pp < PPG; ++pp) {
+                        const int pt = p0 + pp;
+                        const int m = ((KQ == 6) ? V4P * S::half(ch, pt) : 0) + (lane >> 2);
+                        const float* const src = (S::plane(ch, pt) == 0 ? re : im) + tb + p.warpOff[rw][m];
+                        bulkG2S(buf + pp * R + padIdx(32u * lane), src, 128u, &wbar[stage]);
+                    }
+                }
+            } else {
+                const uint64_t tb = walk.at(p, tile) + laneA;
 #pragma unroll
-                for (int mm = 0; mm < V4P; ++mm) {
-                    const int m = ((KQ == 6) ? V4P * S::half(ch, pt) : 0) + mm;
-                    cpAsync16(dst + padIdx(128u * mm), src + p.warpOff[rw][m]);
+                for (int pp = 0; pp < PPG; ++pp) {
+                    const int pt = p0 + pp;
+                    const float* const src = (S::plane(ch, pt) == 0 ? re : im) + tb;
+                    float* const dst = buf + pp * R + rowBase;
+#pragma unroll
+                    for (int mm = 0; mm < V4P; ++mm) {
+                        const int m = ((KQ == 6) ? V4P * S::half(ch, pt) : 0) + mm;
+                        cpAsync16(dst + padIdx(128u * mm), src + p.warpOff[rw][m]);
+                    }
                 }
             }
         };
-        // XST chunks in flight ahead of the split (one commit group each)
+        // XST chunks in flight ahead of the split (cp.async: one commit group each)
         for (int st = 0; st < XST; ++st) {
-            if ((uint32_t)st < nMine) issue(s0 + st * sStep, wbuf + (size_t)st * PPG * R);
-            cpAsyncCommit();
+            if ((uint32_t)st < nMine) issue(s0 + st * sStep, wbuf + (size_t)st * PPG * R, st);
+            if (ST == 0) cpAsyncCommit();
         }
         bool ok = true;
+        uint32_t stopAt = nMine;                             // bulk staging: first chunk not waited for
         for (uint32_t idx = 0; idx < nMine; ++idx) {
             const uint32_t sq = s0 + idx * sStep;
             // TMEM stage b of chunk sq; its previous use was chunk sq - NST
@@ -714,10 +759,21 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
             float* const xr = wbuf + (size_t)(idx % XST) * PPG * R;
             if (u > 0 && !warpWaitOrAbort(&emptyB[b], (u - 1) & 1, &abortF, lane)) {
                 ok = false;
+                stopAt = idx;
                 break;
             }
-            cpAsyncWait<XST - 1>();                          // this lane's copies of the chunk landed
-            __syncwarp();                                    // ... and every lane's
+            if constexpr (ST == 1) {
+                const uint32_t par = (idx / XST) & 1u;
+                if (!warpWaitOrAbort(&wbar[idx % XST], par, &abortF, lane)) {
+                    ok = false;
+                    stopAt = idx;
+                    break;
+                }
+                mbarTest(&wbar[idx % XST], par);                 // every lane acquires the landed rows
+            } else {
+                cpAsyncWait<XST - 1>();                          // this lane's copies of the chunk landed
+                __syncwarp();                                    // ... and every lane's
+            }
             // this group's K entries of the stage: [p0 JP, (p0 + PPG) JP); EPW per column
             constexpr int EPW = BF ? 2 : 1;
             const uint32_t aH = tmem + laneSel + b * kStageCols + p0 * JP / EPW;
@@ -784,11 +840,21 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
             tmemWaitSt();
             fenceBefore();
             mbarArrive(&fullB[b]);
+            if (ST == 1) fenceProxyAsync();                  // column reads before the bulk refill
             __syncwarp();                                    // column reads done before the stage is refilled
-            if (idx + XST < nMine) issue(sq + XST * sStep, xr);
-            cpAsyncCommit();
+            if (idx + XST < nMine) issue(sq + XST * sStep, xr, (int)(idx % XST));
+            if (ST == 0) cpAsyncCommit();
         }
-        cpAsyncWait<0>();                                    // no copy in flight when the warp leaves
+        if constexpr (ST == 1) {
+            // no copy in flight when the warp leaves: chunks stopAt .. were issued
+            // and not waited for (bounded waits)
+            const uint32_t end = nMine < stopAt + XST ? nMine : stopAt + XST;
+            for (uint32_t c = stopAt; c < end; ++c)
+                if (lane == 0) mbarWait(&wbar[c % XST], (c / XST) & 1u);
+            __syncwarp();
+        } else {
+            cpAsyncWait<0>();                                // no copy in flight when the warp leaves
+        }
         if (!ok) {
             if (lane == 0) atomicExch(errFlag, 3);
             abortF = 1;
@@ -1066,7 +1132,7 @@ bool colWords4(const TC2Params<KQ>& p) {
 
 // batch > 1: the same pass on `batch` registers of n qubits, instStride floats
 // apart, each with its own image, imageStride floats apart
-template <int KQ, int LG, int EG, int LS, int PR, int CV = 1>
+template <int KQ, int LG, int EG, int LS, int PR, int CV = 1, int ST = 0>
 bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, const NormLinks& nl,
                cudaStream_t st, int batch = 1, uint64_t instStride = 0, uint64_t imageStride = 0) {
     using S = TC2Shape<KQ, LG, EG, LS, PR>;
@@ -1150,7 +1216,7 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
     }
     if constexpr (CV == 4) {
         if (!colWords4(p))
-            return launchTC2<KQ, LG, EG, LS, PR, 1>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride);
+            return launchTC2<KQ, LG, EG, LS, PR, 1, ST>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride);
     }
     const uint64_t numTiles = 1ull << (n - KQ - kTileBitsC);
     // one CTA per SM: a batch shares the SMs among its registers
@@ -1172,12 +1238,12 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
     }
     static bool configured = false;
     if (!configured) {
-        if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ, LG, EG, LS, PR, CV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+        if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ, LG, EG, LS, PR, CV, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "applyPlanF32"))
             return false;
         configured = true;
     }
-    kApplyTC2<KQ, LG, EG, LS, PR, CV><<<(unsigned)grid, (4 * (LG + EG) + 1) * 32, smem, st>>>(re, im, img, numTiles, errFlag, nl, p);
+    kApplyTC2<KQ, LG, EG, LS, PR, CV, ST><<<(unsigned)grid, (4 * (LG + EG) + 1) * 32, smem, st>>>(re, im, img, numTiles, errFlag, nl, p);
     return !launchFailed("applyPlanF32");
 }
 
@@ -1186,6 +1252,7 @@ int g_tcPrecision = kPrecTF32;   // operands of the pipelined kernel
 int g_tcVersion = 0;      // 0: per pass by target layout; 1, 2, 3: force one kernel
 int g_tcTrial = 0;        // autotuner: the pipelined variant being timed (0: none)
 bool g_tcTuning = true;   // use the tuned variant of a pass class when there is one
+int g_tcStaging = 0;      // loader staging of the pipelined kernels: 0 cp.async, 1 TMA bulk rows
 // tuned pipelined variant (2..5, 0 = none) by register size, precision,
 // width k and target layout (tuneLayout)
 constexpr int kTuneMaxN = 40;
@@ -1431,8 +1498,10 @@ static bool launchPassTC(int version, const FusedPass& pass, float* re, float* i
     // variant with 16-byte column words
     bool done = false;
     if (g_tcVersion == 0 && pass.targets[0] == 0 && pass.targets[1] == 1) {
-#define QG_TC2W(KQ, LG, EG, LS, PR) \
-    (done = true, launchTC2<KQ, LG, EG, LS, PR, 4>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride))
+#define QG_TC2W(KQ, LG, EG, LS, PR)                                                                                    \
+    (done = true,                                                                                                       \
+     g_tcStaging ? launchTC2<KQ, LG, EG, LS, PR, 4, 1>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride) \
+                 : launchTC2<KQ, LG, EG, LS, PR, 4, 0>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride))
         const bool tf = g_tcPrecision == kPrecTF32;
         if (tf && k == 4 && version == 3) ok = QG_TC2W(4, 1, 1, 1, kPrecTF32);
         else if (tf && k == 5 && version == 2) ok = QG_TC2W(5, 2, 1, 1, kPrecTF32);
@@ -1447,11 +1516,12 @@ static bool launchPassTC(int version, const FusedPass& pass, float* re, float* i
         // 2: two loader groups (alternate chunks) + one epilogue group; 3: one
         // + one; 4: one + two; 5: two loader groups (each half of every chunk)
         // + two epilogue groups
-#define QG_TC2P(KQ, PR)                                                                                                   \
-    (version == 2   ? launchTC2<KQ, 2, 1, 1, PR>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride)  \
-     : version == 3 ? launchTC2<KQ, 1, 1, 1, PR>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride)  \
-     : version == 4 ? launchTC2<KQ, 1, 2, 1, PR>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride)  \
-                    : launchTC2<KQ, 2, 2, 2, PR>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride))
+#define QG_TC2S(KQ, PR, ST)                                                                                                    \
+    (version == 2   ? launchTC2<KQ, 2, 1, 1, PR, 1, ST>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride)  \
+     : version == 3 ? launchTC2<KQ, 1, 1, 1, PR, 1, ST>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride)  \
+     : version == 4 ? launchTC2<KQ, 1, 2, 1, PR, 1, ST>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride)  \
+                    : launchTC2<KQ, 2, 2, 2, PR, 1, ST>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride))
+#define QG_TC2P(KQ, PR) (g_tcStaging ? QG_TC2S(KQ, PR, 1) : QG_TC2S(KQ, PR, 0))
 #define QG_TC2(KQ) (g_tcPrecision == kPrecTF32 ? QG_TC2P(KQ, kPrecTF32) : QG_TC2P(KQ, kPrecBF16))
         switch (k) {
             case 4: ok = QG_TC2(4); break;
@@ -1461,6 +1531,7 @@ static bool launchPassTC(int version, const FusedPass& pass, float* re, float* i
         }
 #undef QG_TC2
 #undef QG_TC2P
+#undef QG_TC2S
         return ok;
     }
     if (batch != 1) return false;
@@ -1552,6 +1623,12 @@ bool setTensorCorePrecision(int mode) {
     return true;
 }
 int tensorCorePrecision() { return g_tcPrecision; }
+bool setTensorCoreStaging(int mode) {
+    if (mode != 0 && mode != 1) return false;
+    g_tcStaging = mode;
+    return true;
+}
+int tensorCoreStaging() { return g_tcStaging; }
 void setTensorCoreKernel(int version) { g_tcVersion = (version >= 1 && version <= 5) ? version : 0; }
 bool tensorCoresEnabled() { return g_tcEnabled; }
 

@@ -156,6 +156,35 @@ def test_tensor_core_target_layouts(gpulib, targets, version, precision):
     L.destroy(q64)
 
 
+@pytest.mark.parametrize("version", [0, 2, 3, 4, 5])
+def test_bulk_staging_is_bit_identical(gpulib, version, precision):
+    """The pipelined kernels' TMA bulk staging (one 128-byte row per copy)
+    gives the same FP32 state, bit for bit, as 16-byte cp.async staging: a
+    random circuit at 18 qubits with passes of 4 to 6 qubits (qubits 0 and 1
+    among the targets of some), every pipelined variant."""
+    L = gpulib
+    n = 18
+    ops = W.c2_circuit(n=n, layers=6, seed=5)
+    plan = L.plan(n, 6, ops)
+    ks = [L.lib.quest_gb300_planPass(plan, i, None, None, None) for i in range(L.lib.quest_gb300_planCompile(plan))]
+    assert max(ks) == 6 and min(ks) <= 5
+    states = []
+    L.lib.quest_gb300_setTensorCoreKernel(version)
+    for staging in (0, 1):
+        assert L.lib.quest_gb300_setTensorCoreStaging(staging) == 0
+        assert L.lib.quest_gb300_getTensorCoreStaging() == staging
+        q32 = L.lib.quest_gb300_createQuregF32(n)
+        assert L.lib.quest_gb300_applyPlanF32(q32, plan) == 0
+        states.append(L.amps_f32(q32, n))
+        L.lib.quest_gb300_destroyQuregF32(q32)
+    L.lib.quest_gb300_setTensorCoreStaging(0)
+    L.lib.quest_gb300_setTensorCoreKernel(0)
+    assert L.lib.quest_gb300_setTensorCoreStaging(2) == -1
+    L.lib.quest_gb300_planDestroy(plan)
+    assert np.array_equal(states[0], states[1])
+    assert abs(np.vdot(states[1], states[1]).real - 1) < 1e-5
+
+
 @pytest.mark.parametrize("version", [0, 1, 3, 4, 5])
 def test_non_unitary_passes_keep_their_norm(gpulib, version, precision):
     """A plan mixing non-unitary and unitary dense gates on the tensor cores:
