@@ -103,6 +103,47 @@ def test_capture_matches_direct_fp64(gpulib, n):
     L.destroy(cap)
 
 
+def test_capture_matches_oracle(gpulib, oracle):
+    """Captured calls against the CPU oracle directly: the mixed circuit at
+    16 qubits (every captured gate kind, a mid-circuit read), then a noisy
+    7-qubit density matrix (gates and the three channels as superoperators)."""
+    L = gpulib
+    n = 16
+    ref = oracle.create(n)
+    oracle.lib.initZeroState(ref)
+    reads_o = []
+    mixed_circuit(oracle, ref, n, 9, reads_o)
+    cap = L.create(n)
+    assert L.lib.quest_gb300_setCapture(cap, 1) == 0
+    L.lib.initZeroState(cap)
+    reads_c = []
+    mixed_circuit(L, cap, n, 9, reads_c)
+    a, b = oracle.amps(ref), L.amps(cap)
+    f = abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real)
+    print(f"SV n={n} vs oracle: 1-F={1 - f:.2e}, max|d|={np.max(np.abs(a - b)):.2e}")
+    assert 1 - f <= 1e-6 and np.max(np.abs(a - b)) <= 1e-5
+    assert abs(reads_o[0] - reads_c[0]) < 1e-6
+    oracle.destroy(ref)
+    L.destroy(cap)
+
+    n = 7
+    ops = W.c3_circuit(nq=n, layers=2, seed=6)
+    ref = oracle.create(n, density=True)
+    oracle.lib.initZeroState(ref)
+    W.run_ops(oracle, ref, ops)
+    cap = L.create(n, density=True)
+    L.lib.quest_gb300_setCapture(cap, 1)
+    L.lib.initZeroState(cap)
+    W.run_ops(L, cap, ops)
+    a, b = oracle.amps(ref), L.amps(cap)
+    po, pc = oracle.lib.calcPurity(ref), L.lib.calcPurity(cap)
+    print(f"DM n={n} vs oracle: max|d rho|={np.max(np.abs(a - b)):.2e}, purity rel. diff {abs(pc / po - 1):.2e}")
+    assert np.max(np.abs(a - b)) <= 1e-5 and abs(pc / po - 1) < 1e-6
+    assert abs(L.lib.calcTotalProb(cap) - oracle.lib.calcTotalProb(ref)) < 1e-9
+    oracle.destroy(ref)
+    L.destroy(cap)
+
+
 def test_capture_density_matrix_and_channels(gpulib):
     """Density matrix: gates are doubled (U on t, conj U on t + N) and queued;
     dephasing, depolarising and damping are queued too, as their 4 x 4

@@ -228,6 +228,31 @@ def test_non_unitary_passes_keep_their_norm(gpulib, version, precision):
     L.destroy(q64)
 
 
+@pytest.mark.parametrize("kmax", [4, 5, 6])
+def test_fused_matches_oracle(gpulib, oracle, kmax, precision):
+    """The fused FP32 engine against the CPU oracle directly (not through
+    the plain GPU engine): the random circuit at 20 qubits, 10 layers, from
+    |0..0>; 1 - F and max |d amp| against the oracle's FP64 state."""
+    L = gpulib
+    n = 20
+    ops = W.c2_circuit(n=n, layers=10, seed=17)
+    qo = oracle.create(n)
+    W.run_ops(oracle, qo, ops)
+    ref = oracle.amps(qo).copy()
+    oracle.destroy(qo)
+    q32 = L.lib.quest_gb300_createQuregF32(n)
+    plan = L.plan(n, kmax, ops)
+    assert L.lib.quest_gb300_applyPlanF32(q32, plan) == 0
+    got = L.amps_f32(q32, n)
+    L.lib.quest_gb300_planDestroy(plan)
+    L.lib.quest_gb300_destroyQuregF32(q32)
+    ov = np.vdot(ref, got)
+    omf = 1 - abs(ov) ** 2 / (np.vdot(ref, ref).real * np.vdot(got, got).real)
+    err = float(np.max(np.abs(got - ref)))
+    print(f"n={n} k={kmax} prec={precision} vs oracle: 1-F={omf:.2e} max|d amp|={err:.2e}")
+    assert omf <= 1e-6 and err <= 1e-5
+
+
 @pytest.mark.parametrize("kmax", [4, 6])
 def test_fused_30q_headline_accuracy(gpulib, kmax, precision):
     """The 30-qubit, 20-layer circuit: fused FP32 vs plain FP64."""

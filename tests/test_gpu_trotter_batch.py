@@ -74,6 +74,39 @@ def test_batch_matches_each_instance_alone(gpulib, library_errors, sites, order,
     assert not library_errors
 
 
+def test_batch_matches_oracle(gpulib, oracle, library_errors):
+    """Batch instances against the CPU oracle's applyTrotterCircuit directly
+    (not through the plain GPU engine): 6 sites, orders 1 and 2, U = 2, 8."""
+    L = gpulib
+    lib = L.lib
+    sites, time = 6, 1.0
+    n = 2 * sites
+    inst = [(2.0, 1, 6), (8.0, 2, 3)]
+    b = lib.quest_gb300_trotterBatchCreate(n, len(inst))
+    hams = []
+    for i, (U, order, reps) in enumerate(inst):
+        codes, coeffs, _ = W.hubbard_terms(sites, U)
+        hams.append(L.pauli_hamil(codes, coeffs))
+        assert lib.quest_gb300_trotterBatchSetInstance(b, i, hams[-1], time, order, reps, W.neel_index(sites)) == 0
+    e = (C.c_double * len(inst))()
+    assert lib.quest_gb300_trotterBatchRun(b, e) == 0, list(library_errors)
+    q = L.create(n)
+    for i, (U, order, reps) in enumerate(inst):
+        want, e_want, scale = plain_run(oracle, sites, U, time, order, reps)
+        assert lib.quest_gb300_trotterBatchCopyState(b, i, q) == 0
+        got = L.amps(q)
+        f = abs(np.vdot(want, got)) ** 2 / (np.vdot(got, got).real * np.vdot(want, want).real)
+        err = np.max(np.abs(got - want))
+        print(f"U={U} order={order} reps={reps} vs oracle: 1-F={1 - f:.2e}, max|d amp|={err:.2e}, dE={e[i] - e_want:.2e}")
+        assert 1 - f <= 1e-6 and err <= 1e-5
+        assert abs(e[i] - e_want) <= 1e-5 * scale
+    L.destroy(q)
+    lib.quest_gb300_trotterBatchDestroy(b)
+    for h in hams:
+        lib.destroyPauliHamil(h)
+    assert not library_errors
+
+
 def _check_instance(L, b, i, sites, U, time, order, reps, energy, q=None):
     """Instance i of the batch against applyTrotterCircuit run alone in FP64."""
     want, e_want, scale = plain_run(L, sites, U, time, order, reps)
