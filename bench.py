@@ -261,6 +261,7 @@ def run_gpu(args, rank, world):
     npass = lib.quest_gb300_planCompile(plan)              # the chosen width's passes (same plan again)
     tc = [lib.quest_gb300_planPassUsesTensorCores(plan, i) for i in range(npass)]
     kk = [lib.quest_gb300_planPass(plan, i, None, None, None) for i in range(npass)]
+    ctl = [lib.quest_gb300_planPassControls(plan, i, None) for i in range(npass)]
     q32 = lib.quest_gb300_createQuregF32(n)
 
     def fused_step():
@@ -451,6 +452,31 @@ def run_gpu(args, rank, world):
             widths[str(kw)] = entry
             lib.quest_gb300_planDestroy(pw)
 
+    # ---- the same width without control qubits (every controlled phase of
+    # the random matching then needs both its qubits in one pass) ----------
+    without_ctl = None
+    if max(ctl) > 0:
+        p0 = L.plan(n, tuned_k, ops, controls=0)
+        np0 = lib.quest_gb300_planCompile(p0)
+
+        def step0():
+            lib.quest_gb300_initZeroStateF32(q32)
+            lib.quest_gb300_applyPlanF32(q32, p0)
+            return lib.quest_gb300_calcTotalProbF32(q32)
+
+        step0()                                        # warm-up (plan upload)
+        lib.quest_gb300_eventRecord(10)
+        for _ in range(args.steps):
+            step0()
+        lib.quest_gb300_eventRecord(11)
+        ms0 = lib.quest_gb300_eventElapsedMs(10, 11) / args.steps
+        without_ctl = {"passes": np0, "ms_per_circuit": round(ms0, 2), "gbs": round(alg_bytes / (ms0 / 1e3) / 1e9, 1)}
+        if plain_ms:
+            err = C.c_double(0)
+            without_ctl["one_minus_fidelity"] = lib.quest_gb300_compareF32(q32, q64, C.byref(err))
+            without_ctl["max_amp_err"] = err.value
+        lib.quest_gb300_planDestroy(p0)
+
     lib.quest_gb300_planDestroy(plan)
     lib.quest_gb300_destroyQuregF32(q32)
     L.destroy(q64)
@@ -478,7 +504,8 @@ def run_gpu(args, rank, world):
         "data": "synthetic (seeded Haar/CPhase-matching/CNOT-brickwork circuit)",
         "config": {"workload": f"{n}-qubit random circuit, {args.layers} layers: fused FP32 engine (k<={k}) vs plain FP64 per-gate engine",
                    "qubits": n, "layers": args.layers, "gates_per_circuit": len(ops), "fusion_max_qubits": k,
-                   "fused_passes": npass, "algorithmic_bytes_per_circuit": alg_bytes,
+                   "fusion_max_control_qubits": max(ctl), "fused_passes": npass,
+                   "algorithmic_bytes_per_circuit": alg_bytes,
                    "value_definition": "per-gate FP64 algorithmic bytes of the circuit / time per circuit",
                    "value_timed_region": ("initZeroStateF32, every fused pass of the compiled plan, FP64 total "
                                           "probability; the plan's search and FP64 products (plan_compile_s) and "
@@ -486,11 +513,13 @@ def run_gpu(args, rank, world):
                    "l2": "state 8 GiB (FP32) / 16 GiB (FP64) >> 129 MB L2, no flush needed",
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
         "fused_fp32": {"ms_per_circuit": round(ms_step, 2), "gbs": round(value, 1), "passes": npass,
+                       "controlled_passes": sum(1 for c in ctl if c > 0),
                        "plan_compile_s": round(plan_s, 3), "one_minus_fidelity": one_minus_f,
                        "max_amp_err": max_amp_err,
                        "kernels": {name: {"passes": c, "ms_per_circuit": round(t, 2)} for name, (c, t) in groups.items()}},
         ("fused_fp32_split_bf16" if prec == 0 else "fused_fp32_split_tf32"): other,
         "fused_fp32_by_width": widths or None,
+        "fused_fp32_without_control_qubits": without_ctl,
         "autotune": autotune,
         "plain_fp64": ({"ms_per_circuit": round(plain_ms, 1), "gbs": round(alg_bytes / (plain_ms / 1e3) / 1e9, 1),
                         "launches": len(ops)} if plain_ms else None),

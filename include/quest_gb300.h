@@ -49,6 +49,17 @@ int quest_gb300_planAddControlledPhaseShift(void* plan, int qubit1, int qubit2, 
 /* Sets kept per level of the pass search (1..256, default 16); wider finds
  * fewer passes on some circuits at more host time.  Returns 0 or -1. */
 int quest_gb300_planSetBeamWidth(void* plan, int width);
+/* Control qubits a pass may use (0..3; a new plan gets 3 on registers of 24
+ * qubits or more while the tensor cores are enabled, else 0; op-stream
+ * capture uses the same rule).  A pass of at least four
+ * qubits may then absorb gates that also act on qubits outside its targets,
+ * when each gate is diagonal on those qubits and each such qubit lies above
+ * the pass's tile (at least 7 non-target qubits below it): the pass applies,
+ * per amplitude, the matrix of the value of its control bits (2^controls
+ * FP64 products).  A controlled controlledPhaseShift, for instance, no longer
+ * needs both its qubits in one pass.  Controlled passes run on the
+ * tensor-core applier only.  Returns 0 or -1. */
+int quest_gb300_planSetMaxControls(void* plan, int maxControls);
 /* Compile; returns the number of passes, or -1. */
 int quest_gb300_planCompile(void* plan);
 /* Compile `plan` with the passes of the compiled plan `structure`, without a
@@ -58,8 +69,15 @@ int quest_gb300_planCompile(void* plan);
  * structure's gate is.  Returns the number of passes, or -1. */
 int quest_gb300_planCompileLike(void* plan, void* structure);
 int quest_gb300_planNumGates(void* plan);
-/* Copy pass i (targets ascending, FP64 matrix); returns k or -1. */
+/* Copy pass i (targets ascending, FP64 matrix; for a controlled pass the
+ * matrix of control value 0); returns k or -1. */
 int quest_gb300_planPass(void* plan, int i, int* targets, double* re, double* im);
+/* Control qubits of pass i (ascending) into controls (may be NULL); returns
+ * their number or -1. */
+int quest_gb300_planPassControls(void* plan, int i, int* controls);
+/* The matrix of pass i for control value `block` (bit j <-> the j-th control
+ * qubit); returns k or -1. */
+int quest_gb300_planPassBlock(void* plan, int i, int block, double* re, double* im);
 
 /* Per-pass timing: with setPassEvents(1), applyPlanF32 records a CUDA event
  * pair on the library stream around each pass; passTimesMs writes the
@@ -153,6 +171,13 @@ int quest_gb300_getTensorCorePrecision(void);
  * 0, or -1 for another mode. */
 int quest_gb300_setTensorCoreStaging(int mode);
 int quest_gb300_getTensorCoreStaging(void);
+/* Host check of the pipelined tensor-core kernel's addressing (no GPU): from
+ * the launch parameters of a pass on `targets` (ascending, 4..6) with
+ * `controls` (ascending, 0..3) on a register of numQubits <= 26 qubits, walk
+ * every CTA, tile, warp and lane as the kernel does.  Returns 0 when every
+ * amplitude is read and written exactly once, 1 when not, -1 when the pass
+ * does not fit (controls inside the tile, too few qubits). */
+int quest_gb300_checkTileCoverage(int numQubits, const int* targets, int numTargets, const int* controls, int numControls);
 double quest_gb300_calcTotalProbF32(void* qureg32);
 double quest_gb300_calcProbOfOutcomeF32(void* qureg32, int measureQubit, int outcome);
 /* 1 - |<ref|q>|^2 / (<ref|ref><q|q>) against an FP64 state vector; writes the

@@ -126,6 +126,7 @@ static void flushRecord(Capture* c, double* re, double* im) {
     quest_gb300_copyFromQureg(c->q32, view);
     FusedPlan* plan = new FusedPlan();
     plan->numQubits = c->n;
+    plan->maxControls = defaultMaxControls(c->n);
     const bool tuned = g_capMaxFused == 0;
     plan->maxFused = tuned && c->shape ? c->shape->maxFused : capWidest(c->n);
     plan->gates.swap(c->gates);

@@ -54,6 +54,7 @@ bool setTensorCorePrecision(int mode);
 int tensorCorePrecision();
 bool setTensorCoreStaging(int mode);
 int tensorCoreStaging();
+int tcCheckCoverage(int n, const std::vector<int>& targets, const std::vector<int>& controls);
 bool tensorCoresEnabled();
 int tcKernelFor(const FusedPass& pass, int n);
 float* f32re(QuregF32& q) { return q.re; }
@@ -495,6 +496,10 @@ int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPas
         const int tc = qg::applyPassTCIndexed(*q, pass, p->device, (size_t)i, st);
         if (tc < 0) return -1;
         if (tc == 0) {
+            if (!pass.controls.empty()) {
+                invalidQuESTInputError("fused pass with control qubits needs the tensor-core applier", "applyPlanF32");
+                return -1;
+            }
             if (!qg::applyPassSimt(*q, pass, st)) {
                 invalidQuESTInputError("fused pass on more than 5 qubits needs the tensor-core applier", "applyPlanF32");
                 return -1;
@@ -549,6 +554,18 @@ void quest_gb300_setTensorCoreKernel(int version) { qg::setTensorCoreKernel(vers
 int quest_gb300_setTensorCorePrecision(int mode) { return qg::setTensorCorePrecision(mode) ? 0 : -1; }
 int quest_gb300_getTensorCorePrecision(void) { return qg::tensorCorePrecision(); }
 int quest_gb300_setTensorCoreStaging(int mode) { return qg::setTensorCoreStaging(mode) ? 0 : -1; }
+
+int quest_gb300_checkTileCoverage(int numQubits, const int* targets, int numTargets, const int* controls, int numControls) {
+    if (!targets || numTargets < 4 || numTargets > 6 || numControls < 0 || numControls > 3 || (numControls && !controls))
+        return -1;
+    std::vector<int> t(targets, targets + numTargets), c(controls, controls + numControls);
+    for (size_t i = 1; i < t.size(); ++i)
+        if (t[i] <= t[i - 1]) return -1;
+    for (size_t i = 1; i < c.size(); ++i)
+        if (c[i] <= c[i - 1]) return -1;
+    if (t[0] < 0 || t.back() >= numQubits || (numControls && (c[0] < 0 || c.back() >= numQubits))) return -1;
+    return qg::tcCheckCoverage(numQubits, t, c);
+}
 int quest_gb300_getTensorCoreStaging(void) { return qg::tensorCoreStaging(); }
 
 double quest_gb300_calcTotalProbF32(void* h) {

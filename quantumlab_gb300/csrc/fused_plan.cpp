@@ -55,6 +55,7 @@ constexpr int kDepth = 1;   // multi-qubit gates per member looked at for candid
 
 struct GateInfo {
     uint64_t mask = 0;
+    uint64_t diag = 0;      // qubits on which the gate is diagonal
     int nq = 0;
     int q[6];
     int seg[6];             // segment of the gate on q[t]
@@ -96,8 +97,8 @@ bool better(const Scored& a, const Scored& b) {
 
 class Search {
   public:
-    Search(const std::vector<FusedGate>& gates, int numQubits, int kmax, int beam)
-        : nq_(numQubits), kmax_(kmax), beam_(std::max(1, beam)), g_(gates.size()), byq_(numQubits),
+    Search(const std::vector<FusedGate>& gates, int numQubits, int kmax, int beam, int maxCtl)
+        : nq_(numQubits), kmax_(kmax), beam_(std::max(1, beam)), maxCtl_(maxCtl), g_(gates.size()), byq_(numQubits),
           segStart_(numQubits), cur_(numQubits, 0), rem_(numQubits, 0), applied_(gates.size(), 0),
           stamp_(gates.size(), 0), remaining_((int)gates.size()) {
         std::vector<int> lastDiag(numQubits, 0);
@@ -105,6 +106,7 @@ class Search {
             const FusedGate& fg = gates[i];
             GateInfo& gi = g_[i];
             const uint64_t diag = diagonalQubits(fg);
+            gi.diag = diag;
             gi.nq = (int)fg.qubits.size();
             for (int t = 0; t < gi.nq; ++t) {
                 const int q = fg.qubits[t];
@@ -128,8 +130,9 @@ class Search {
     bool done() const { return remaining_ == 0; }
 
     // choose the next pass, apply its closure; returns its qubit set (0 on
-    // failure) and the absorbed gates in an allowed order
-    uint64_t next(std::vector<int>& absorbed) {
+    // failure), the absorbed gates in an allowed order and the pass's
+    // control qubits
+    uint64_t next(std::vector<int>& absorbed, uint64_t& controls) {
         std::vector<Scored> beam, cand;
         std::unordered_set<uint64_t> seen;
         for (int q = 0; q < nq_; ++q)
@@ -168,7 +171,7 @@ class Search {
             S = g_[first_].mask;
         }
         absorbed.clear();
-        closure(S, &absorbed, nullptr, true);
+        controls = closure(S, &absorbed, nullptr, true);
         return absorbed.empty() ? 0 : S;     // 0: no progress (cannot happen, see above)
     }
 
@@ -184,8 +187,13 @@ class Search {
     }
 
     // Closure of S from the current front.  With `commit` the absorbed gates
-    // are marked as run and the front moves past them.
-    void closure(uint64_t S, std::vector<int>* out, Scored* sc, bool commit) {
+    // are marked as run and the front moves past them.  With maxCtl > 0 and
+    // at least four qubits in S, a gate may also use up to maxCtl qubits
+    // outside S on which it is diagonal ("controls"): each must lie outside
+    // the pass's tile (at least 7 qubits outside S below it), so that it is
+    // constant over every tile and the pass applies one of 2^controls
+    // matrices per tile.  Returns the controls used.
+    uint64_t closure(uint64_t S, std::vector<int>* out, Scored* sc, bool commit) {
         if (++stampId_ == 0) {
             std::fill(stamp_.begin(), stamp_.end(), 0u);
             stampId_ = 1;
@@ -200,6 +208,9 @@ class Search {
             lrem[q] = rem_[q];
         }
         int multi = 0, all = 0;
+        uint64_t ctl = 0, touched = S;
+        const bool allowCtl = maxCtl_ > 0 && nS >= 4;
+        auto validCtl = [&](int c) { return c - __builtin_popcountll(S & ((1ull << c) - 1ull)) >= 7; };
         bool changed = true;
         while (changed) {
             changed = false;
@@ -213,7 +224,21 @@ class Search {
                         const int i = byq_[q][j];
                         if (applied_[i] || stamp_[i] == id) continue;
                         const GateInfo& gi = g_[i];
-                        if (gi.mask & ~S) continue;
+                        const uint64_t outside = gi.mask & ~S;
+                        if (outside) {
+                            if (!allowCtl || (outside & ~gi.diag) ||
+                                __builtin_popcountll(ctl | outside) > maxCtl_)
+                                continue;
+                            bool ok = true;
+                            for (uint64_t m = outside; m && ok; m &= m - 1) ok = validCtl(__builtin_ctzll(m));
+                            if (!ok) continue;
+                            for (uint64_t m = outside & ~touched; m; m &= m - 1) {
+                                const int c = __builtin_ctzll(m);
+                                lcur[c] = cur_[c];
+                                lrem[c] = rem_[c];
+                            }
+                            touched |= outside;
+                        }
                         bool ready = true;
                         for (int t = 0; t < gi.nq && ready; ++t) ready = gi.seg[t] == lcur[gi.q[t]];
                         if (!ready) continue;
@@ -221,6 +246,7 @@ class Search {
                         if (out) out->push_back(i);
                         ++all;
                         multi += gi.nq > 1;
+                        ctl |= outside;
                         changed = true;
                         for (int t = 0; t < gi.nq; ++t) {
                             const int x = gi.q[t];
@@ -258,17 +284,18 @@ class Search {
         }
         if (commit) {
             for (int i : *out) applied_[i] = 1;
-            for (int a = 0; a < nS; ++a) {
-                const int q = qs[a];
+            for (uint64_t m = S | ctl; m; m &= m - 1) {
+                const int q = __builtin_ctzll(m);
                 cur_[q] = lcur[q];
                 rem_[q] = lrem[q];
                 if (cur_[q] >= nseg(q)) live_ &= ~(1ull << q);
             }
             remaining_ -= all;
         }
+        return ctl;
     }
 
-    int nq_, kmax_, beam_;
+    int nq_, kmax_, beam_, maxCtl_;
     std::vector<GateInfo> g_;
     std::vector<std::vector<int>> byq_;       // gates on each qubit, program order
     std::vector<std::vector<int>> segStart_;  // per qubit: first index in byq_ of each segment, then byq_.size()
@@ -332,6 +359,9 @@ void mulGate(double* __restrict Mr, double* __restrict Mi, int D, const FusedGat
 
 }  // namespace
 
+bool tensorCoresEnabled();   // fused_tc.cu
+int defaultMaxControls(int n) { return (n >= 24 && tensorCoresEnabled()) ? 3 : 0; }
+
 bool matrixIsUnitary(const std::vector<cplx>& m, int D) {
     for (int r = 0; r < D; ++r)
         for (int c = r; c < D; ++c) {
@@ -346,24 +376,71 @@ bool matrixIsUnitary(const std::vector<cplx>& m, int D) {
     return true;
 }
 
-// product of the absorbed gates of one pass on its qubit set S
-void buildPass(const FusedPlan& plan, uint64_t S, const std::vector<int>& absorbed, FusedPass& p) {
+// The block of g (diagonal on the qubits of `ctl` it touches) for the values
+// `val` of those qubits (bit j of val <-> the j-th qubit of ctl): a gate on
+// g's other qubits.
+FusedGate controlBlock(const FusedGate& g, uint64_t ctl, uint32_t val) {
+    FusedGate sub;
+    const int m = (int)g.qubits.size();
+    uint32_t fixedMask = 0, fixedVal = 0;
+    int keep[6], nk = 0;
+    for (int b = 0; b < m; ++b) {
+        const int q = g.qubits[b];
+        if (ctl >> q & 1ull) {
+            fixedMask |= 1u << b;
+            const int j = __builtin_popcountll(ctl & ((1ull << q) - 1ull));
+            if (val >> j & 1u) fixedVal |= 1u << b;
+        } else {
+            keep[nk++] = b;
+            sub.qubits.push_back(q);
+        }
+    }
+    const int G = 1 << m, Gs = 1 << nk;
+    auto expand = [&](int r) {
+        int x = (int)fixedVal;
+        for (int t = 0; t < nk; ++t)
+            if (r >> t & 1) x |= 1 << keep[t];
+        return x;
+    };
+    sub.m.resize((size_t)Gs * Gs);
+    for (int r = 0; r < Gs; ++r)
+        for (int c = 0; c < Gs; ++c) sub.m[(size_t)r * Gs + c] = g.m[(size_t)expand(r) * G + expand(c)];
+    sub.unitary = g.unitary;
+    return sub;
+}
+
+// products of the absorbed gates of one pass on its qubit set S, one per
+// value of its control qubits `ctl`
+void buildPass(const FusedPlan& plan, uint64_t S, uint64_t ctl, const std::vector<int>& absorbed, FusedPass& p) {
     p.targets.clear();
-    for (int q = 0; q < 64; ++q)
+    p.controls.clear();
+    for (int q = 0; q < 64; ++q) {
         if (S >> q & 1) p.targets.push_back(q);
+        if (ctl >> q & 1) p.controls.push_back(q);
+    }
     const int k = (int)p.targets.size(), D = 1 << k;
+    const uint32_t nv = 1u << p.controls.size();
     int posOf[64];
     for (int b = 0; b < k; ++b) posOf[p.targets[b]] = b;
-    std::vector<double> Mr((size_t)D * D, 0.0), Mi((size_t)D * D, 0.0), tr((size_t)64 * D), ti((size_t)64 * D);
-    for (int r = 0; r < D; ++r) Mr[(size_t)r * D + r] = 1.0;
-    for (int i : absorbed) {
-        const FusedGate& g = plan.gates[i];
-        int pos[6];
-        for (size_t t = 0; t < g.qubits.size(); ++t) pos[t] = posOf[g.qubits[t]];
-        mulGate(Mr.data(), Mi.data(), D, g, pos, tr.data(), ti.data());
+    std::vector<double> Mr((size_t)D * D), Mi((size_t)D * D), tr((size_t)64 * D), ti((size_t)64 * D);
+    p.m.resize((size_t)nv * D * D);
+    for (uint32_t v = 0; v < nv; ++v) {
+        std::fill(Mr.begin(), Mr.end(), 0.0);
+        std::fill(Mi.begin(), Mi.end(), 0.0);
+        for (int r = 0; r < D; ++r) Mr[(size_t)r * D + r] = 1.0;
+        for (int i : absorbed) {
+            const FusedGate& g0 = plan.gates[i];
+            uint64_t gm = 0;
+            for (int q : g0.qubits) gm |= 1ull << q;
+            const FusedGate sub = (gm & ctl) ? controlBlock(g0, ctl, v) : FusedGate{};
+            const FusedGate& g = (gm & ctl) ? sub : g0;
+            int pos[6];
+            for (size_t t = 0; t < g.qubits.size(); ++t) pos[t] = posOf[g.qubits[t]];
+            mulGate(Mr.data(), Mi.data(), D, g, pos, tr.data(), ti.data());
+        }
+        cplx* blk = p.m.data() + (size_t)v * D * D;
+        for (size_t e = 0; e < (size_t)D * D; ++e) blk[e] = cplx(Mr[e], Mi[e]);
     }
-    p.m.resize((size_t)D * D);
-    for (size_t e = 0; e < p.m.size(); ++e) p.m[e] = cplx(Mr[e], Mi[e]);
     p.numGates = (int)absorbed.size();
     p.unitary = true;
     for (int i : absorbed) p.unitary = p.unitary && plan.gates[i].unitary;
@@ -371,28 +448,31 @@ void buildPass(const FusedPlan& plan, uint64_t S, const std::vector<int>& absorb
 
 void compilePlan(FusedPlan& plan) {
     plan.passes.clear();
-    std::vector<uint64_t> sets;
+    std::vector<uint64_t> sets, ctls;
     std::vector<std::vector<int>> members;
     {
-        Search search(plan.gates, plan.numQubits, plan.maxFused, plan.beamWidth);
+        Search search(plan.gates, plan.numQubits, plan.maxFused, plan.beamWidth, plan.maxControls);
         std::vector<int> absorbed;
+        uint64_t ctl = 0;
         while (!search.done()) {
-            sets.push_back(search.next(absorbed));
+            sets.push_back(search.next(absorbed, ctl));
             if (!sets.back()) {
                 plan.compiled = false;
                 return;
             }
+            ctls.push_back(ctl);
             members.push_back(absorbed);
         }
     }
     plan.passSets = sets;
+    plan.passControls = ctls;
     plan.passMembers = members;
     // the pass products are independent: a few host threads share them
     const size_t np = sets.size();
     plan.passes.resize(np);
     std::atomic<size_t> nextPass{0};
     auto work = [&]() {
-        for (size_t i; (i = nextPass.fetch_add(1)) < np;) buildPass(plan, sets[i], members[i], plan.passes[i]);
+        for (size_t i; (i = nextPass.fetch_add(1)) < np;) buildPass(plan, sets[i], ctls[i], members[i], plan.passes[i]);
     };
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     const unsigned nt = (unsigned)std::min<size_t>({(size_t)std::min(hw, 16u), np, 1 + plan.gates.size() / 64});
@@ -415,13 +495,14 @@ bool compilePlanLike(FusedPlan& plan, const FusedPlan& structure) {
         if ((db & ~da) != 0) return false;
     }
     plan.passSets = structure.passSets;
+    plan.passControls = structure.passControls;
     plan.passMembers = structure.passMembers;
     const size_t np = plan.passSets.size();
     plan.passes.resize(np);
     std::atomic<size_t> nextPass{0};
     auto work = [&]() {
         for (size_t i; (i = nextPass.fetch_add(1)) < np;)
-            buildPass(plan, plan.passSets[i], plan.passMembers[i], plan.passes[i]);
+            buildPass(plan, plan.passSets[i], plan.passControls[i], plan.passMembers[i], plan.passes[i]);
     };
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     const unsigned nt = (unsigned)std::min<size_t>({(size_t)std::min(hw, 16u), np, 1 + plan.gates.size() / 64});
@@ -492,6 +573,7 @@ void* quest_gb300_planCreate(int numQubits, int maxFusedQubits) {
     FusedPlan* p = new FusedPlan();
     p->numQubits = numQubits;
     p->maxFused = std::min(maxFusedQubits, qg::widestPass(numQubits));
+    p->maxControls = qg::defaultMaxControls(numQubits);
     return p;
 }
 
@@ -547,6 +629,23 @@ int quest_gb300_planSetBeamWidth(void* plan, int width) {
     return 0;
 }
 
+int quest_gb300_planSetMaxControls(void* plan, int maxControls) {
+    FusedPlan* p = P(plan);
+    if (!p || maxControls < 0 || maxControls > 3) return -1;
+    p->maxControls = maxControls;
+    p->compiled = false;
+    return 0;
+}
+
+int quest_gb300_planPassControls(void* plan, int i, int* controls) {
+    FusedPlan* p = P(plan);
+    if (!p || !p->compiled || i < 0 || i >= (int)p->passes.size()) return -1;
+    const qg::FusedPass& s = p->passes[i];
+    if (controls)
+        for (size_t j = 0; j < s.controls.size(); ++j) controls[j] = s.controls[j];
+    return (int)s.controls.size();
+}
+
 int quest_gb300_planCompile(void* plan) {
     FusedPlan* p = P(plan);
     if (!p) return -1;
@@ -575,11 +674,24 @@ int quest_gb300_planPass(void* plan, int i, int* targets, double* re, double* im
     if (targets)
         for (int b = 0; b < k; ++b) targets[b] = s.targets[b];
     if (re && im)
-        for (size_t e = 0; e < s.m.size(); ++e) {
+        for (size_t e = 0; e < ((size_t)1 << (2 * k)); ++e) {     // block 0 (all control bits 0)
             re[e] = s.m[e].real();
             im[e] = s.m[e].imag();
         }
     return k;
+}
+
+int quest_gb300_planPassBlock(void* plan, int i, int block, double* re, double* im) {
+    FusedPlan* p = P(plan);
+    if (!p || !p->compiled || i < 0 || i >= (int)p->passes.size() || !re || !im) return -1;
+    const qg::FusedPass& s = p->passes[i];
+    const size_t DD = (size_t)1 << (2 * s.targets.size());
+    if (block < 0 || (size_t)block >= ((size_t)1 << s.controls.size())) return -1;
+    for (size_t e = 0; e < DD; ++e) {
+        re[e] = s.m[block * DD + e].real();
+        im[e] = s.m[block * DD + e].imag();
+    }
+    return (int)s.targets.size();
 }
 
 }  // extern "C"

@@ -23,7 +23,12 @@ struct FusedGate {
 
 struct FusedPass {
     std::vector<int> targets;  // ascending; matrix bit b <-> targets[b]
-    std::vector<cplx> m;       // row-major D x D, D = 2^targets.size()
+    // Control qubits (ascending; none unless the plan allows them): qubits
+    // outside the targets on which every absorbed gate that touches them is
+    // diagonal.  The pass applies, to each amplitude, the matrix of the value
+    // c of its control bits (bit j of c <-> controls[j]).
+    std::vector<int> controls;
+    std::vector<cplx> m;       // 2^controls.size() row-major D x D blocks (block c), D = 2^targets.size()
     int numGates = 0;
     bool unitary = false;      // every absorbed gate is unitary
 };
@@ -32,11 +37,13 @@ struct FusedPlan {
     int numQubits = 0;
     int maxFused = 4;
     int beamWidth = 16;         // sets kept per level of the pass search
+    int maxControls = 0;        // control qubits a pass may use (0..3; see FusedPass)
     std::vector<FusedGate> gates;
     std::vector<FusedPass> passes;
     // the search's result: per pass its qubit set and the indices of the
     // gates it absorbs, in an allowed order (compilePlanLike reuses them)
     std::vector<uint64_t> passSets;
+    std::vector<uint64_t> passControls;
     std::vector<std::vector<int>> passMembers;
     bool compiled = false;
     // device copy of the per-pass FP32 (and split-TF32) operands, built on
@@ -49,6 +56,12 @@ struct FusedPlan {
 // need the tensor-core applier (n >= 13: a tile is 2^(6+7) amplitudes), the
 // SIMT applier takes up to five.
 inline int widestPass(int n) { return n >= 13 ? 6 : (n < 5 ? n : 5); }
+
+// Control qubits a new plan on n qubits may use: 3 from 24 qubits up while
+// the tensor cores are enabled (controlled passes run only there; below 24
+// qubits the extra operand images cost more host time than the passes they
+// save), else 0.
+int defaultMaxControls(int n);
 
 // |m m^+ - I| <= 1e-12 entrywise for a row-major D x D matrix.
 bool matrixIsUnitary(const std::vector<cplx>& m, int D);

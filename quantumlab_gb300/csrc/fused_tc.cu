@@ -481,7 +481,8 @@ struct TC2Params {
     uint64_t laneOff[32];                 // amplitude offset of region index 4 lane
     uint32_t colLane[32];                 // pad(in-part index of the group bits of lane l)
     uint32_t colJ[1 << KQ];               // pad(in-part index of the position bits of matrix index j)
-    int insI[KQ + kTileBitsC];            // ascending qubits of I
+    int insI[KQ + kTileBitsC + 3];        // ascending qubits of I and of the controls (zero in a tile base)
+    int numIns;                           // entries of insI
     int runBits;                          // I contains qubits [0, runBits)
     uint64_t outMask;                     // the qubits outside I (where tile index bits go)
     uint64_t gridStep;                    // the tile base offset of ctasPerInst tiles
@@ -493,6 +494,15 @@ struct TC2Params {
     uint32_t ctasPerInst;
     uint64_t instStride;
     uint64_t imageStride;
+    // Controlled passes: 2^ctrlBits matrices, one per value c of the control
+    // qubits (outside I and outside the tile bases).  The CTAs of a register
+    // come in 2^ctrlBits groups of ctasPerInst; group c runs the amplitudes
+    // whose control bits are c, ctrlOff[c] amplitudes into the register (c
+    // deposited into the control qubits), with operand image block c,
+    // ctrlImageStride floats after block c - 1.
+    uint32_t ctrlBits;
+    uint64_t ctrlOff[8];
+    uint64_t ctrlImageStride;
 };
 
 // Operand precision of kApplyTC2: 3-term split-TF32 or 4-term split-BF16.
@@ -580,10 +590,10 @@ __device__ __forceinline__ bool warpWaitOrAbort(uint64_t* bar, uint32_t parity, 
 // amplitude offset of the first amplitude of a tile: the tile index bits go,
 // in order, to the qubits outside I
 template <int KQ>
-__device__ __forceinline__ uint64_t tileBase(const TC2Params<KQ>& p, uint64_t tile) {
+__host__ __device__ __forceinline__ uint64_t tileBase(const TC2Params<KQ>& p, uint64_t tile) {
     uint64_t tb = tile << p.runBits;
 #pragma unroll 1
-    for (int b = p.runBits; b < KQ + kTileBitsC; ++b) {
+    for (int b = p.runBits; b < p.numIns; ++b) {
         const int s = p.insI[b];
         tb = ((tb >> s) << (s + 1)) | (tb & ((1ull << s) - 1ull));
     }
@@ -596,7 +606,7 @@ __device__ __forceinline__ uint64_t tileBase(const TC2Params<KQ>& p, uint64_t ti
 template <int KQ>
 struct TileWalker {
     uint64_t tile = ~0ull, base = 0;
-    __device__ __forceinline__ uint64_t at(const TC2Params<KQ>& p, uint64_t t) {
+    __host__ __device__ __forceinline__ uint64_t at(const TC2Params<KQ>& p, uint64_t t) {
         if (tile == ~0ull || t < tile) {
             base = tileBase(p, t);
             tile = t;
@@ -622,13 +632,15 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                                                                   const __grid_constant__ TC2Params<KQ> p) {
     using S = TC2Shape<KQ, LG, EG, LS, PR>;
     constexpr bool BF = (PR == kPrecBF16);
-    // this CTA's register of a batch, and its place among that register's CTAs
+    // this CTA's register of a batch and control value, and its place among
+    // the CTAs of that pair
     const uint32_t cta = blockIdx.x % p.ctasPerInst, ncta = p.ctasPerInst;
     {
-        const uint64_t inst = blockIdx.x / p.ctasPerInst;
-        re += inst * p.instStride;
-        im += inst * p.instStride;
-        gImage += inst * p.imageStride;
+        const uint64_t u = blockIdx.x / p.ctasPerInst;
+        const uint64_t inst = u >> p.ctrlBits, cv = u & ((1u << p.ctrlBits) - 1u);
+        re += inst * p.instStride + p.ctrlOff[cv];
+        im += inst * p.instStride + p.ctrlOff[cv];
+        gImage += inst * p.imageStride + cv * p.ctrlImageStride;
     }
     constexpr int D = S::D, N = S::N;
     constexpr int NCH = S::NCH, KC = S::KC, PART = S::PART, R = S::R, PPG = S::PPG, XST = S::XST, NST = S::NST;
@@ -1130,20 +1142,28 @@ bool colWords4(const TC2Params<KQ>& p) {
     return true;
 }
 
-// batch > 1: the same pass on `batch` registers of n qubits, instStride floats
-// apart, each with its own image, imageStride floats apart
-template <int KQ, int LG, int EG, int LS, int PR, int CV = 1, int ST = 0>
-bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, const NormLinks& nl,
-               cudaStream_t st, int batch = 1, uint64_t instStride = 0, uint64_t imageStride = 0) {
-    using S = TC2Shape<KQ, LG, EG, LS, PR>;
-    constexpr int D = S::D, K = S::K, N = S::N, PART = S::PART;
-    constexpr int V4 = S::TILE / 512;
-    const size_t smem = S::smemBytes;
-    // the pass image: full TF32 hi, lo (k <= 5: the split-TF32 operands), the
-    // three BF16 parts, then at k = 6 the compact TF32 hi, lo
-    if (PR == kPrecBF16) img += (size_t)2 * N * K;
-    else if (KQ == 6) img += (size_t)2 * N * K + (size_t)3 * S::GE / 2;
-    TC2Params<KQ> p{};
+// floats of one operand image of a k-qubit pass (one matrix block; the
+// layouts are described at buildImageBlock)
+static size_t imageFloats(int k) {
+    if (k < 4 || k > 6) return 0;
+    const size_t D = (size_t)1 << k, full = 4 * D * D;
+    const size_t bEntries = (k == 6) ? 3 * D * D : full;
+    const size_t tf32Compact = (k == 6) ? 2 * 3 * D * D : 0;
+    return (2 * full + (3 * bEntries + 1) / 2 + tf32Compact + 3) & ~(size_t)3;     // 16-byte multiple
+}
+
+// Launch parameters of kApplyTC2 for a pass of KQ qubits on `batch`
+// registers of n qubits (instStride floats apart, each with its own image,
+// imageStride floats apart): the tile layout tables, the tiles per register
+// and control value, and the grid.  False when the pass does not fit.
+template <int KQ>
+bool tc2Params(int n, const FusedPass& pass, int batch, uint64_t instStride, uint64_t imageStride, TC2Params<KQ>& p,
+               uint64_t& numTiles, uint64_t& grid) {
+    constexpr int D = 1 << KQ;
+    constexpr int TILE = 1 << (KQ + kTileBitsC);
+    constexpr int PART = (KQ == 6) ? TILE / 8 : TILE / 4;     // as TC2Shape
+    constexpr int V4 = TILE / 512;
+    p = TC2Params<KQ>{};
     // I = targets + the 7 lowest other qubits (ascending); tile position b <-> qubit I[b]
     uint64_t tmask = 0;
     for (int b = 0; b < KQ; ++b) tmask |= 1ull << pass.targets[b];
@@ -1157,10 +1177,17 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
     for (int q = 0; q < n; ++q)
         if (imask >> q & 1ull) I[ni++] = q;
     if (ni != KQ + kTileBitsC) return false;
+    // control qubits: outside I (so constant over every tile), at most three
+    uint64_t cmask = 0;
+    for (int c : pass.controls) cmask |= 1ull << c;
+    const int nctl = (int)pass.controls.size();
+    if (nctl > 3 || (cmask & imask) || (nctl && (cmask >> n) != 0)) return false;
     int run = 0;
     while (run < ni && I[run] == run) ++run;
     p.runBits = run;
-    for (int b = 0; b < ni; ++b) p.insI[b] = I[b];
+    p.numIns = 0;
+    for (int q = 0; q < n; ++q)
+        if ((imask | cmask) >> q & 1ull) p.insI[p.numIns++] = q;
     for (uint32_t h = 0; h < (1u << (ni - run)); ++h) {
         uint64_t a = 0;
         for (int i = 0; i < ni - run; ++i)
@@ -1214,18 +1241,24 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
             if (j >> b & 1) v |= 1u << posOf[pass.targets[b]];
         p.colJ[j] = padIdx(compress(v) % PART);
     }
-    if constexpr (CV == 4) {
-        if (!colWords4(p))
-            return launchTC2<KQ, LG, EG, LS, PR, 1, ST>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride);
-    }
-    const uint64_t numTiles = 1ull << (n - KQ - kTileBitsC);
-    // one CTA per SM: a batch shares the SMs among its registers
-    const uint64_t ctas = std::min<uint64_t>(numTiles, std::max<uint64_t>(1, (uint64_t)numSMs() / (uint64_t)std::max(1, batch)));
-    const uint64_t grid = ctas * (uint64_t)std::max(1, batch);
-    p.outMask = ~imask;
+    // tiles per register and control value
+    numTiles = 1ull << (n - KQ - kTileBitsC - nctl);
+    // one CTA per SM: a batch and the control values share the SMs
+    const uint64_t groups = (uint64_t)std::max(1, batch) << nctl;
+    const uint64_t ctas = std::min<uint64_t>(numTiles, std::max<uint64_t>(1, (uint64_t)numSMs() / groups));
+    grid = ctas * groups;
+    p.outMask = ~imask & ~cmask;
     p.ctasPerInst = (uint32_t)ctas;
     p.instStride = instStride;
     p.imageStride = imageStride;
+    p.ctrlBits = (uint32_t)nctl;
+    for (uint32_t c = 0; c < (1u << nctl); ++c) {
+        uint64_t off = 0;
+        for (int j = 0; j < nctl; ++j)
+            if (c >> j & 1u) off |= 1ull << pass.controls[j];
+        p.ctrlOff[c] = off;
+    }
+    p.ctrlImageStride = imageFloats(KQ);
     {
         // gridStep = ctas deposited into the qubits outside I
         uint64_t dep = 0, src = ctas;
@@ -1236,6 +1269,29 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
             }
         p.gridStep = dep;
     }
+    return true;
+}
+
+// batch > 1: the same pass on `batch` registers of n qubits, instStride floats
+// apart, each with its own image, imageStride floats apart
+template <int KQ, int LG, int EG, int LS, int PR, int CV = 1, int ST = 0>
+bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, const NormLinks& nl,
+               cudaStream_t st, int batch = 1, uint64_t instStride = 0, uint64_t imageStride = 0) {
+    using S = TC2Shape<KQ, LG, EG, LS, PR>;
+    constexpr int K = S::K, N = S::N;
+    static_assert(S::PART == ((KQ == 6) ? S::TILE / 8 : S::TILE / 4), "part layout of tc2Params");
+    const size_t smem = S::smemBytes;
+    TC2Params<KQ> p;
+    uint64_t numTiles = 0, grid = 0;
+    if (!tc2Params<KQ>(n, pass, batch, instStride, imageStride, p, numTiles, grid)) return false;
+    if constexpr (CV == 4) {
+        if (!colWords4(p))
+            return launchTC2<KQ, LG, EG, LS, PR, 1, ST>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride);
+    }
+    // the pass image: full TF32 hi, lo (k <= 5: the split-TF32 operands), the
+    // three BF16 parts, then at k = 6 the compact TF32 hi, lo
+    if (PR == kPrecBF16) img += (size_t)2 * N * K;
+    else if (KQ == 6) img += (size_t)2 * N * K + (size_t)3 * S::GE / 2;
     static bool configured = false;
     if (!configured) {
         if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ, LG, EG, LS, PR, CV, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -1260,21 +1316,15 @@ int g_tcTuned[kTuneMaxN + 1][2][7][3] = {};
 
 }  // namespace
 
-// the images of one pass (layouts above); buildImage writes imageFloats(k) floats
-static size_t imageFloats(int k) {
-    if (k < 4 || k > 6) return 0;
-    const size_t D = (size_t)1 << k, full = 4 * D * D;
-    const size_t bEntries = (k == 6) ? 3 * D * D : full;
-    const size_t tf32Compact = (k == 6) ? 2 * 3 * D * D : 0;
-    return (2 * full + (3 * bEntries + 1) / 2 + tf32Compact + 3) & ~(size_t)3;     // 16-byte multiple
-}
 // Parts of an image: what the split-TF32 pipelined kernels read (the full
 // real form at k <= 5, the compact form at k = 6), what the split-BF16 ones
 // read, and the full TF32 form at every k for the direct-load kernel.
 constexpr int kPartTF32 = 1, kPartBF16 = 2, kPartDirect = 4;
-static void buildImage(const FusedPass& pass, float* img, int parts) {
+// the image of one matrix block of a pass (block c: control value c)
+static void buildImageBlock(const FusedPass& pass, int block, float* img, int parts) {
     const int k = (int)pass.targets.size();
     const int D = 1 << k, K = 2 * D, N = 2 * D;
+    const cplx* const M = pass.m.data() + (size_t)block * D * D;
     const bool full = (parts & kPartDirect) || ((parts & kPartTF32) && k <= 5);
     const bool compact = (parts & kPartTF32) && k == 6;
     // real form [[Re, -Im], [Im, Re]] as B = Gr (rows r = output index, K index j)
@@ -1285,7 +1335,7 @@ static void buildImage(const FusedPass& pass, float* img, int parts) {
     }
     for (int r = 0; r < N && (full || compact); ++r)
         for (int j = 0; j < K; ++j) {
-            const cplx g = pass.m[(size_t)(r % D) * D + (j % D)];
+            const cplx g = M[(size_t)(r % D) * D + (j % D)];
             double v;
             if (r < D) v = (j < D) ? g.real() : -g.imag();
             else v = (j < D) ? g.imag() : g.real();
@@ -1310,7 +1360,7 @@ static void buildImage(const FusedPass& pass, float* img, int parts) {
             // k = 6: rows 0..D-1 take the (r, D + j) entries of the real form
             // (-Im), rows D..3D-1 the (r - D, j) entries (Re, then Im)
             const int rr = (k == 6 && r >= D) ? r - D : r, jj = (k == 6 && r < D) ? D + j : j;
-            const cplx g = pass.m[(size_t)(rr % D) * D + (jj % D)];
+            const cplx g = M[(size_t)(rr % D) * D + (jj % D)];
             const double v = (rr < D) ? ((jj < D) ? g.real() : -g.imag()) : ((jj < D) ? g.imag() : g.real());
             const uint16_t h = hostBF16RN((float)v);
             const double r1 = v - (double)bf16Value(h);
@@ -1333,6 +1383,12 @@ static void buildImage(const FusedPass& pass, float* img, int parts) {
         packKMajor(ch, 3 * D, D, tc);
         packKMajor(cl, 3 * D, D, tc + (size_t)3 * D * D);
     }
+}
+
+// the images of every matrix block of a pass, imageFloats(k) floats apart
+static void buildImage(const FusedPass& pass, float* img, int parts) {
+    const size_t stride = imageFloats((int)pass.targets.size());
+    for (size_t b = 0; b < ((size_t)1 << pass.controls.size()); ++b) buildImageBlock(pass, (int)b, img + b * stride, parts);
 }
 
 // the image parts the kernels of the current precision and kernel choice read
@@ -1364,8 +1420,8 @@ void* uploadPlanTC(const FusedPlan& plan) {
         const FusedPass& pass = plan.passes[i];
         const int k = (int)pass.targets.size();
         dp->unitary.push_back(pass.unitary ? 1 : 0);
-        const bool tc = k >= 4 && k <= 6 && plan.numQubits >= k + 7;
-        offset[i + 1] = offset[i] + (tc ? imageFloats(k) : 0);
+        const bool tc = k >= 4 && k <= 6 && plan.numQubits >= k + 7 + (int)pass.controls.size();
+        offset[i + 1] = offset[i] + (tc ? imageFloats(k) << pass.controls.size() : 0);
     }
     dp->images.assign(np, nullptr);
     if (offset[np] == 0) return dp;
@@ -1394,7 +1450,7 @@ void* uploadPlanTC(const FusedPlan& plan) {
 // The tensor-core operands of one pass, as uploadPlanTC lays them out: the
 // number of floats, and the image itself.
 size_t tcImageFloats(int k) { return imageFloats(k); }
-void tcBuildImage(const FusedPass& pass, float* img) { buildImage(pass, img, currentParts()); }
+void tcBuildImage(const FusedPass& pass, float* img) { buildImageBlock(pass, 0, img, currentParts()); }
 int tcImageParts() { return currentParts(); }
 // whether a plan's images hold the parts the current precision and kernel
 // choice read (else the caller uploads the plan again)
@@ -1471,9 +1527,8 @@ int tunedKernel(int n, int prec, int k, int layout) {
 void setKernelTrial(int version) { g_tcTrial = (version >= 2 && version <= 5) ? version : 0; }
 void setKernelTuning(bool on) { g_tcTuning = on; }
 
-int tcKernelFor(const FusedPass& pass, int n) {
+static int tcKernelChoice(const FusedPass& pass, int n) {
     const int k = (int)pass.targets.size();
-    if (!g_tcEnabled || k < 4 || k > 6 || n < k + 7) return 0;
     if (g_tcVersion != 0) return g_tcVersion;
     if (g_tcTrial != 0) return g_tcTrial;
     if (g_tcTuning) {
@@ -1485,6 +1540,69 @@ int tcKernelFor(const FusedPass& pass, int n) {
     if (k == 5) return 5;
     if (k == 4) return high ? 2 : 5;
     return 5;
+}
+int tcKernelFor(const FusedPass& pass, int n) {
+    const int k = (int)pass.targets.size(), nc = (int)pass.controls.size();
+    if (!g_tcEnabled || k < 4 || k > 6 || n < k + 7 + nc) return 0;
+    const int v = tcKernelChoice(pass, n);
+    return (nc && v == 1) ? 5 : v;          // the direct-load kernel takes no control qubits
+}
+
+// Host model of the global accesses of kApplyTC2 for one pass on one
+// register of n qubits, from the same launch parameters and tile walk: every
+// CTA (register group, control value), every tile of its sequence (with the
+// loaders' step, one tile group, and the epilogue's, two groups), every warp,
+// lane, 128-position block m and the 4 amplitudes of a 16-byte access.
+// Counts the accesses per amplitude; -1 when an address falls outside the
+// register or the pass does not fit.
+template <int KQ>
+int tc2Coverage(int n, const FusedPass& pass, int groups, std::vector<uint8_t>& count) {
+    TC2Params<KQ> p;
+    uint64_t numTiles = 0, grid = 0;
+    if (!tc2Params<KQ>(n, pass, 1, 0, 0, p, numTiles, grid)) return -1;
+    constexpr int V4 = (1 << (KQ + kTileBitsC)) / 512;
+    const uint64_t size = 1ull << n;
+    count.assign(size, 0);
+    for (uint64_t b = 0; b < grid; ++b) {
+        const uint64_t cta = b % p.ctasPerInst, u = b / p.ctasPerInst;
+        if ((u >> p.ctrlBits) != 0) return -1;
+        const uint64_t off = p.ctrlOff[u & ((1u << p.ctrlBits) - 1u)];
+        for (int g = 0; g < groups; ++g) {
+            TileWalker<KQ> walk;
+            for (uint64_t t = cta + (uint64_t)g * p.ctasPerInst; t < numTiles; t += (uint64_t)groups * p.ctasPerInst) {
+                const uint64_t base = walk.at(p, t);
+                for (int rw = 0; rw < 4; ++rw)
+                    for (int lane = 0; lane < 32; ++lane)
+                        for (int m = 0; m < V4; ++m)
+                            for (int e = 0; e < 4; ++e) {
+                                const uint64_t a = off + base + p.laneOff[lane] + p.warpOff[rw][m] + (uint64_t)e;
+                                if (a >= size) return -1;
+                                if (count[a] < 255) ++count[a];
+                            }
+            }
+        }
+    }
+    return 0;
+}
+
+// 0 when a pass on `targets` (ascending) with `controls` reads and writes
+// every amplitude of an n-qubit register exactly once (both tile walks of
+// tc2Coverage), 1 when it does not, -1 when it does not fit or n > 26
+int tcCheckCoverage(int n, const std::vector<int>& targets, const std::vector<int>& controls) {
+    const int k = (int)targets.size();
+    if (n > 26 || k < 4 || k > 6 || controls.size() > 3) return -1;
+    FusedPass pass;
+    pass.targets = targets;
+    pass.controls = controls;
+    std::vector<uint8_t> cnt;
+    for (int groups = 1; groups <= 2; ++groups) {
+        const int rc = k == 4 ? tc2Coverage<4>(n, pass, groups, cnt)
+                              : k == 5 ? tc2Coverage<5>(n, pass, groups, cnt) : tc2Coverage<6>(n, pass, groups, cnt);
+        if (rc) return -1;
+        for (uint8_t v : cnt)
+            if (v != 1) return 1;
+    }
+    return 0;
 }
 
 // Launch tensor-core kernel `version` (tcKernelFor) for a pass of k = 4..6

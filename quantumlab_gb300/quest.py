@@ -183,10 +183,14 @@ SIGNATURES = {
     "quest_gb300_planAddControlledNot": (_I, [C.c_void_p, _I, _I]),
     "quest_gb300_planAddControlledPhaseShift": (_I, [C.c_void_p, _I, _I, _D]),
     "quest_gb300_planSetBeamWidth": (_I, [C.c_void_p, _I]),
+    "quest_gb300_planSetMaxControls": (_I, [C.c_void_p, _I]),
+    "quest_gb300_planPassControls": (_I, [C.c_void_p, _I, _P(_I)]),
+    "quest_gb300_planPassBlock": (_I, [C.c_void_p, _I, _I, _P(qreal), _P(qreal)]),
     "quest_gb300_setTensorCorePrecision": (_I, [_I]),
     "quest_gb300_getTensorCorePrecision": (_I, []),
     "quest_gb300_setTensorCoreStaging": (_I, [_I]),
     "quest_gb300_getTensorCoreStaging": (_I, []),
+    "quest_gb300_checkTileCoverage": (_I, [_I, _P(_I), _I, _P(_I), _I]),
     "quest_gb300_planPassNorms": (_I, [C.c_void_p, _I, C.POINTER(C.c_double)]),
     "quest_gb300_planCompile": (_I, [C.c_void_p]),
     "quest_gb300_planNumGates": (_I, [C.c_void_p]),
@@ -419,11 +423,15 @@ class QuESTLibrary:
         return self.lib.calcExpecPauliProd(q, _ints(ts), _ints(ps), len(ts), ws)
 
     # ---- fused FP32 engine (include/quest_gb300.h) ----------------------------
-    def plan(self, n: int, kmax: int, ops) -> int:
-        """Record workloads-style ops into a fusion plan and compile it."""
+    def plan(self, n: int, kmax: int, ops, controls: Optional[int] = None) -> int:
+        """Record workloads-style ops into a fusion plan and compile it
+        (`controls`: the plan's control-qubit limit, else the library's
+        default for n)."""
         p = self.lib.quest_gb300_planCreate(n, kmax)
         if not p:
             raise ValueError("invalid plan parameters")
+        if controls is not None and self.lib.quest_gb300_planSetMaxControls(p, controls) != 0:
+            raise ValueError("invalid control limit")
         for op in ops:
             k = op[0]
             if k == "cu":

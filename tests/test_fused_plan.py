@@ -25,13 +25,19 @@ def lib():
     L.quest_gb300_planSetBeamWidth.argtypes = [C.c_void_p, C.c_int]
     L.quest_gb300_planCompile.argtypes = [C.c_void_p]
     L.quest_gb300_planPass.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.quest_gb300_planSetMaxControls.argtypes = [C.c_void_p, C.c_int]
+    L.quest_gb300_planPassControls.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)]
+    L.quest_gb300_planPassBlock.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     return L
 
 
-def make_plan(L, n, kmax, ops, beam=None):
+def make_plan(L, n, kmax, ops, beam=None, controls=None):
+    """Compile; returns [(targets, matrix)], or with `controls` (the plan's
+    control limit) [(targets, control qubits, [matrix per control value])]."""
     p = L.quest_gb300_planCreate(n, kmax)
     if beam is not None:
         assert L.quest_gb300_planSetBeamWidth(p, beam) == 0
+    assert L.quest_gb300_planSetMaxControls(p, controls or 0) == 0
     for op in ops:
         if op[0] == "m":                          # ("m", qubits, matrix)
             re = np.ascontiguousarray(op[2].real.ravel())
@@ -53,7 +59,17 @@ def make_plan(L, n, kmax, ops, beam=None):
         im = np.zeros(4096)
         k = L.quest_gb300_planPass(p, i, t, re.ctypes.data_as(C.POINTER(C.c_double)), im.ctypes.data_as(C.POINTER(C.c_double)))
         D = 1 << k
-        passes.append((list(t[:k]), (re[:D * D] + 1j * im[:D * D]).reshape(D, D)))
+        if controls is None:
+            passes.append((list(t[:k]), (re[:D * D] + 1j * im[:D * D]).reshape(D, D)))
+            continue
+        cq = (C.c_int * 3)()
+        nc = L.quest_gb300_planPassControls(p, i, cq)
+        blocks = []
+        for b in range(1 << nc):
+            assert L.quest_gb300_planPassBlock(p, i, b, re.ctypes.data_as(C.POINTER(C.c_double)),
+                                               im.ctypes.data_as(C.POINTER(C.c_double))) == k
+            blocks.append((re[:D * D] + 1j * im[:D * D]).reshape(D, D))
+        passes.append((list(t[:k]), list(cq[:nc]), blocks))
     L.quest_gb300_planDestroy(p)
     return passes
 
@@ -73,6 +89,10 @@ def apply_matrix(psi, n, targets, m):
 def reference(n, ops):
     psi = np.zeros(1 << n, dtype=complex)
     psi[0] = 1
+    return reference_from(psi, n, ops)
+
+
+def reference_from(psi, n, ops):
     for op in ops:
         if op[0] == "cu":
             a, b = complex(op[2], op[3]), complex(op[4], op[5])
@@ -177,6 +197,68 @@ def test_plan_pass_count_brickwork(lib):
     ops = W.c1_circuit(n=20, layers=40, seed=1)
     # 1180 gates; merging in program order took 85 passes
     assert len(make_plan(lib, 20, 6, ops)) <= 45
+
+
+def apply_controlled(psi, n, targets, controls, blocks):
+    """block c acts on the amplitudes whose control bits are c (bit j <->
+    controls[j]); it moves amplitudes only across target bits"""
+    idx = np.arange(1 << n)
+    val = np.zeros(1 << n, dtype=np.int64)
+    for j, q in enumerate(controls):
+        val |= ((idx >> q) & 1) << j
+    out = np.zeros_like(psi)
+    for c, m in enumerate(blocks):
+        sel = val == c
+        out[sel] = apply_matrix(psi, n, targets, m)[sel]
+    return out
+
+
+@pytest.mark.parametrize("kmax,maxctl,kind", [(6, 3, "c2"), (6, 1, "c2"), (5, 2, "c2"), (4, 3, "c2"),
+                                              (6, 3, "mixed"), (5, 3, "mixed")])
+def test_controlled_passes_reproduce_circuit(lib, kmax, maxctl, kind):
+    """Passes with control qubits: gates diagonal on qubits outside a pass's
+    targets (above its tile) are absorbed with those qubits as controls, and
+    the pass applies the product of control value c to the amplitudes whose
+    control bits are c.  Applied that way, the plan reproduces the circuit
+    exactly; control qubits lie outside the targets and have at least 7
+    non-target qubits below them; the plan needs fewer passes."""
+    n = 15
+    if kind == "c2":
+        ops = W.c2_circuit(n=n, layers=8, seed=11)
+    else:
+        ops = [o for o in mixed_ops(n, 120, 7) if len(o[1]) <= kmax]
+    passes = make_plan(lib, n, kmax, ops, controls=maxctl)
+    plain = make_plan(lib, n, kmax, ops, controls=0)
+    rng = np.random.default_rng(5)
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    want = psi.copy()
+    if kind == "c2":
+        want = reference_from(psi, n, ops)
+    else:
+        for op in ops:
+            want = apply_matrix(want, n, list(op[1]), op[2])
+    used = 0
+    for t, cs, blocks in passes:
+        assert len(cs) <= maxctl and not set(cs) & set(t) and len(blocks) == 1 << len(cs)
+        for c in cs:
+            assert c - sum(1 for q in t if q < c) >= 7
+        if cs:
+            assert len(t) >= 4
+        used += len(cs) > 0
+        psi = apply_controlled(psi, n, t, cs, blocks)
+    assert np.max(np.abs(psi - want)) < 1e-12
+    assert used > 0 and len(passes) <= len(plain)
+    print(f"{kind} k<={kmax} controls<={maxctl}: {len(passes)} passes ({used} controlled) against {len(plain)}")
+
+
+def test_controlled_pass_count_30q(lib):
+    """The 30-qubit, 20-layer random circuit at k <= 6: with up to three
+    control qubits per pass the controlled phases of the random matching no
+    longer need both qubits in one pass (101 passes without controls)."""
+    ops = W.c2_circuit(n=30, layers=20, seed=2)
+    counts = {m: len(make_plan(lib, 30, 6, ops, controls=m)) for m in (0, 1, 3)}
+    assert counts[0] <= 105 and counts[1] <= 86 and counts[3] <= 68, counts
+    assert counts[3] < counts[1] < counts[0]
 
 
 def test_invalid_gates_rejected(lib):

@@ -228,6 +228,54 @@ def test_non_unitary_passes_keep_their_norm(gpulib, version, precision):
     L.destroy(q64)
 
 
+@pytest.mark.parametrize("kmax,version", [(6, 0), (6, 1), (6, 2), (6, 3), (6, 4), (6, 5), (5, 0), (4, 0)])
+def test_controlled_passes_match_oracle(gpulib, oracle, kmax, version, precision):
+    """Passes with control qubits (up to three, the matrix chosen per control
+    value; the CTAs of a launch split over the control values) on every
+    pipelined kernel variant (1, the direct-load kernel, takes none and maps
+    to 5): the random circuit at 20 qubits against the oracle's FP64 state."""
+    L = gpulib
+    n = 20
+    ops = W.c2_circuit(n=n, layers=8, seed=13)
+    qo = oracle.create(n)
+    W.run_ops(oracle, qo, ops)
+    ref = oracle.amps(qo).copy()
+    oracle.destroy(qo)
+    plan = L.plan(n, kmax, ops, controls=3)
+    npass = L.lib.quest_gb300_planCompile(plan)
+    ctl = sum(L.lib.quest_gb300_planPassControls(plan, i, None) > 0 for i in range(npass))
+    assert ctl > 0
+    q32 = L.lib.quest_gb300_createQuregF32(n)
+    L.lib.quest_gb300_setTensorCoreKernel(version)
+    rc = L.lib.quest_gb300_applyPlanF32(q32, plan)
+    L.lib.quest_gb300_setTensorCoreKernel(0)
+    assert rc == 0
+    got = L.amps_f32(q32, n)
+    L.lib.quest_gb300_planDestroy(plan)
+    L.lib.quest_gb300_destroyQuregF32(q32)
+    omf = 1 - abs(np.vdot(ref, got)) ** 2 / (np.vdot(ref, ref).real * np.vdot(got, got).real)
+    err = float(np.max(np.abs(got - ref)))
+    print(f"k={kmax} v{version} prec={precision}: {npass} passes ({ctl} controlled) 1-F={omf:.2e} max|d amp|={err:.2e}")
+    assert omf <= 1e-6 and err <= 1e-5
+
+
+def test_controlled_pass_needs_the_tensor_cores(gpulib):
+    """A plan compiled with control qubits refuses the SIMT applier (tensor
+    cores switched off after compiling) with an input error."""
+    L = gpulib
+    n = 20
+    plan = L.plan(n, 5, W.c2_circuit(n=n, layers=4, seed=3), controls=3)      # k <= 5: the SIMT applier takes the rest
+    q32 = L.lib.quest_gb300_createQuregF32(n)
+    L.lib.quest_gb300_setTensorCores(0)
+    rc = L.lib.quest_gb300_applyPlanF32(q32, plan)
+    L.lib.quest_gb300_setTensorCores(1)
+    errors = list(L.errors)
+    L.errors.clear()
+    L.lib.quest_gb300_planDestroy(plan)
+    L.lib.quest_gb300_destroyQuregF32(q32)
+    assert rc == -1 and any("control qubits" in e[1] for e in errors), errors
+
+
 @pytest.mark.parametrize("kmax", [4, 5, 6])
 def test_fused_matches_oracle(gpulib, oracle, kmax, precision):
     """The fused FP32 engine against the CPU oracle directly (not through
