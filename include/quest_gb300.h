@@ -49,7 +49,7 @@ int quest_gb300_planAddControlledPhaseShift(void* plan, int qubit1, int qubit2, 
 /* Sets kept per level of the pass search (1..256, default 16); wider finds
  * fewer passes on some circuits at more host time.  Returns 0 or -1. */
 int quest_gb300_planSetBeamWidth(void* plan, int width);
-/* Control qubits a pass may use (0..3; a new plan gets 3 on registers of 24
+/* Control qubits a pass may use (0..3; a new plan gets 3 on registers of 26
  * qubits or more while the tensor cores are enabled, else 0; op-stream
  * capture uses the same rule).  A pass of at least four
  * qubits may then absorb gates that also act on qubits outside its targets,

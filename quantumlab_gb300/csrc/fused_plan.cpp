@@ -360,7 +360,7 @@ void mulGate(double* __restrict Mr, double* __restrict Mi, int D, const FusedGat
 }  // namespace
 
 bool tensorCoresEnabled();   // fused_tc.cu
-int defaultMaxControls(int n) { return (n >= 24 && tensorCoresEnabled()) ? 3 : 0; }
+int defaultMaxControls(int n) { return (n >= 26 && tensorCoresEnabled()) ? 3 : 0; }
 
 bool matrixIsUnitary(const std::vector<cplx>& m, int D) {
     for (int r = 0; r < D; ++r)

@@ -57,10 +57,11 @@ struct FusedPlan {
 // SIMT applier takes up to five.
 inline int widestPass(int n) { return n >= 13 ? 6 : (n < 5 ? n : 5); }
 
-// Control qubits a new plan on n qubits may use: 3 from 24 qubits up while
-// the tensor cores are enabled (controlled passes run only there; below 24
-// qubits the extra operand images cost more host time than the passes they
-// save), else 0.
+// Control qubits a new plan on n qubits may use: 3 from 26 qubits up while
+// the tensor cores are enabled (controlled passes run only there; on a
+// 25-qubit register a captured 7,040-gate circuit took 36 ms with controls
+// against 32 without: a pass is ~90 us there, and the extra operand images
+// cost more host time than the passes they save), else 0.
 int defaultMaxControls(int n);
 
 // |m m^+ - I| <= 1e-12 entrywise for a row-major D x D matrix.
