@@ -486,6 +486,18 @@ def run_gpu(args, rank, world):
         for g in gate_roof.values():
             g["frac"] = round(g["achieved_gbs"] / peak, 4)
     achieved = pass_bytes / (dom_avg / 1e3) / 1e9
+    # the dominant kernel's tensor work: algorithmic complex MACs of a dense
+    # 2^k x 2^k pass, 8 * 2^k real flops per amplitude, and what the
+    # compensated form executes (3 MMA terms split-TF32, 4 split-BF16)
+    tensor_rates = None
+    if "kApplyTC2" in dom_name:
+        kd = int(dom_name.split("<")[1].split(",")[0])
+        alg_flops = 8.0 * (1 << kd) * (1 << n)
+        terms = 3 if prec == 0 else 4
+        tensor_rates = {"k": kd, "algorithmic_flops_per_launch": alg_flops,
+                        "algorithmic_tflops": round(alg_flops / (dom_avg / 1e3) / 1e12, 1),
+                        "executed_tflops": round(terms * alg_flops / (dom_avg / 1e3) / 1e12, 1),
+                        "executed_form": f"{terms} MMA terms ({'split-TF32' if prec == 0 else 'split-BF16'})"}
     if other:
         other["dominant_kernel_frac"] = round(pass_bytes / (other["dominant_kernel_avg_ms"] / 1e3) / 1e9 / peak, 4)
     traffic = tensor_pct = None
@@ -530,7 +542,8 @@ def run_gpu(args, rank, world):
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                      "avg_launch_ms": round(dom_avg, 4), "launches_per_circuit": dom_count,
                      "bytes_per_launch": pass_bytes,
-                     "tensor_pipe_active_pct_ncu": tensor_pct},
+                     "tensor_pipe_active_pct_ncu": tensor_pct,
+                     "tensor": tensor_rates},
         "e2e": {"value": round(world * alg_bytes / e2e_s / 1e9, 2), "unit": "GB/s (per-gate FP64 algorithmic bytes)",
                 "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes + 8,
                 "ms_per_step": round(e2e_s * 1e3, 2),
