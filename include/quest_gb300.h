@@ -112,8 +112,9 @@ int quest_gb300_getPlainArithmetic(void);
  * with every pipelined kernel variant (2: two loader groups on alternate
  * chunks + one epilogue group; 3: one + one; 4: one + two; 5: two loader
  * groups splitting each chunk + two epilogue groups) and the fastest is used
- * for that class from then on (setKernelTuning(0) returns to the fixed
- * defaults).  The table is cached as JSON ($QUEST_GB300_TUNE_CACHE, default
+ * for that class from then on, unless it beats the class's fixed default by
+ * 3 % or less (then the default stays; setKernelTuning(0) returns to the
+ * fixed defaults).  The table is cached as JSON ($QUEST_GB300_TUNE_CACHE, default
  * ~/.cache/quest_gb300_tune.json) and loaded by the first autotune call.
  * planCompileTuned compiles the plan at every width in [minK, maxK] and keeps
  * the fastest predicted one.  tunedKernel returns the chosen variant of a

@@ -1527,6 +1527,13 @@ int tunedKernel(int n, int prec, int k, int layout) {
 void setKernelTrial(int version) { g_tcTrial = (version >= 2 && version <= 5) ? version : 0; }
 void setKernelTuning(bool on) { g_tcTuning = on; }
 
+// the fixed per-class default of the pipelined kernel (measured choices,
+// listed above), by precision, width and target layout class (tuneLayout)
+int defaultTcKernel(int prec, int k, int layout) {
+    if (prec == kPrecTF32) return k == 4 ? 3 : k == 5 ? 2 : 5;
+    if (k == 4) return layout == 0 ? 2 : 5;
+    return 5;
+}
 static int tcKernelChoice(const FusedPass& pass, int n) {
     const int k = (int)pass.targets.size();
     if (g_tcVersion != 0) return g_tcVersion;
@@ -1535,11 +1542,7 @@ static int tcKernelChoice(const FusedPass& pass, int n) {
         const int v = tunedKernel(n, g_tcPrecision, k, tuneLayout(pass));
         if (v) return v;
     }
-    if (g_tcPrecision == kPrecTF32) return k == 4 ? 3 : k == 5 ? 2 : 5;
-    const bool high = pass.targets[0] >= 5;
-    if (k == 5) return 5;
-    if (k == 4) return high ? 2 : 5;
-    return 5;
+    return defaultTcKernel(g_tcPrecision, k, tuneLayout(pass));
 }
 int tcKernelFor(const FusedPass& pass, int n) {
     const int k = (int)pass.targets.size(), nc = (int)pass.controls.size();
