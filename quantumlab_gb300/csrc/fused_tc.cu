@@ -36,6 +36,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <mutex>
 #include <cstdint>
 #include <cstring>
 #include <thread>
@@ -1142,14 +1143,41 @@ bool colWords4(const TC2Params<KQ>& p) {
     return true;
 }
 
-// floats of one operand image of a k-qubit pass (one matrix block; the
-// layouts are described at buildImageBlock)
-static size_t imageFloats(int k) {
-    if (k < 4 || k > 6) return 0;
-    const size_t D = (size_t)1 << k, full = 4 * D * D;
-    const size_t bEntries = (k == 6) ? 3 * D * D : full;
-    const size_t tf32Compact = (k == 6) ? 2 * 3 * D * D : 0;
-    return (2 * full + (3 * bEntries + 1) / 2 + tf32Compact + 3) & ~(size_t)3;     // 16-byte multiple
+// Parts of an image: what the split-TF32 pipelined kernels read (the full
+// real form at k <= 5, the compact form at k = 6), what the split-BF16 ones
+// read, and the full TF32 form at every k for the direct-load kernel.
+constexpr int kPartTF32 = 1, kPartBF16 = 2, kPartDirect = 4;
+constexpr size_t kNoPart = ~(size_t)0;
+
+// Layout of the operand image of one matrix block of a k-qubit pass holding
+// `parts`: float offsets of the full TF32 real form (hi, lo), of the three
+// BF16 parts and of the compact TF32 form (hi, lo), kNoPart where absent, and
+// the block's size; every part starts on a 16-byte boundary (the kernels copy
+// them with cp.async.bulk).  The part contents are described at
+// buildImageBlock.
+struct ImageLayout {
+    size_t full = kNoPart, bf16 = kNoPart, compact = kNoPart, stride = 0;
+};
+static ImageLayout imageLayout(int k, int parts) {
+    ImageLayout L;
+    if (k < 4 || k > 6) return L;
+    const size_t D = (size_t)1 << k, fullN = 4 * D * D;
+    const size_t bEntries = (k == 6) ? 3 * D * D : fullN;
+    size_t at = 0;
+    if ((parts & kPartDirect) || ((parts & kPartTF32) && k <= 5)) {
+        L.full = at;
+        at += 2 * fullN;
+    }
+    if (parts & kPartBF16) {
+        L.bf16 = at;
+        at += ((3 * bEntries + 1) / 2 + 3) & ~(size_t)3;
+    }
+    if ((parts & kPartTF32) && k == 6) {
+        L.compact = at;
+        at += 2 * 3 * D * D;
+    }
+    L.stride = (at + 3) & ~(size_t)3;
+    return L;
 }
 
 // Launch parameters of kApplyTC2 for a pass of KQ qubits on `batch`
@@ -1258,7 +1286,6 @@ bool tc2Params(int n, const FusedPass& pass, int batch, uint64_t instStride, uin
             if (c >> j & 1u) off |= 1ull << pass.controls[j];
         p.ctrlOff[c] = off;
     }
-    p.ctrlImageStride = imageFloats(KQ);
     {
         // gridStep = ctas deposited into the qubits outside I
         uint64_t dep = 0, src = ctas;
@@ -1274,11 +1301,13 @@ bool tc2Params(int n, const FusedPass& pass, int batch, uint64_t instStride, uin
 
 // batch > 1: the same pass on `batch` registers of n qubits, instStride floats
 // apart, each with its own image, imageStride floats apart
+// `img` is the first image block of the pass, `blockStride` floats per block
+// (control value); the kernel reads its operand part at partOff.
 template <int KQ, int LG, int EG, int LS, int PR, int CV = 1, int ST = 0>
-bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, const NormLinks& nl,
-               cudaStream_t st, int batch = 1, uint64_t instStride = 0, uint64_t imageStride = 0) {
+bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* img, size_t partOff, size_t blockStride,
+               int* errFlag, const NormLinks& nl, cudaStream_t st, int batch = 1, uint64_t instStride = 0,
+               uint64_t imageStride = 0) {
     using S = TC2Shape<KQ, LG, EG, LS, PR>;
-    constexpr int K = S::K, N = S::N;
     static_assert(S::PART == ((KQ == 6) ? S::TILE / 8 : S::TILE / 4), "part layout of tc2Params");
     const size_t smem = S::smemBytes;
     TC2Params<KQ> p;
@@ -1286,12 +1315,11 @@ bool launchTC2(float* re, float* im, int n, const FusedPass& pass, const float* 
     if (!tc2Params<KQ>(n, pass, batch, instStride, imageStride, p, numTiles, grid)) return false;
     if constexpr (CV == 4) {
         if (!colWords4(p))
-            return launchTC2<KQ, LG, EG, LS, PR, 1, ST>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride);
+            return launchTC2<KQ, LG, EG, LS, PR, 1, ST>(re, im, n, pass, img, partOff, blockStride, errFlag, nl, st, batch,
+                                                        instStride, imageStride);
     }
-    // the pass image: full TF32 hi, lo (k <= 5: the split-TF32 operands), the
-    // three BF16 parts, then at k = 6 the compact TF32 hi, lo
-    if (PR == kPrecBF16) img += (size_t)2 * N * K;
-    else if (KQ == 6) img += (size_t)2 * N * K + (size_t)3 * S::GE / 2;
+    img += partOff;
+    p.ctrlImageStride = blockStride;
     static bool configured = false;
     if (!configured) {
         if (QG_CUDA(cudaFuncSetAttribute(kApplyTC2<KQ, LG, EG, LS, PR, CV, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -1316,17 +1344,19 @@ int g_tcTuned[kTuneMaxN + 1][2][7][3] = {};
 
 }  // namespace
 
-// Parts of an image: what the split-TF32 pipelined kernels read (the full
-// real form at k <= 5, the compact form at k = 6), what the split-BF16 ones
-// read, and the full TF32 form at every k for the direct-load kernel.
-constexpr int kPartTF32 = 1, kPartBF16 = 2, kPartDirect = 4;
-// the image of one matrix block of a pass (block c: control value c)
+// The image of one matrix block of a pass (block c: control value c), with
+// the parts of `parts` at the offsets of imageLayout: the full real form
+// [[Re, -Im], [Im, Re]] as TF32 hi, lo (canonical K-major, N = K = 2^(k+1));
+// its three BF16 parts (at k = 6 the compact form [-Im G; Re G; Im G], 3D
+// rows and D K columns, in 8 x 8 core blocks); the compact form as TF32 hi,
+// lo (K-major).
 static void buildImageBlock(const FusedPass& pass, int block, float* img, int parts) {
     const int k = (int)pass.targets.size();
     const int D = 1 << k, K = 2 * D, N = 2 * D;
     const cplx* const M = pass.m.data() + (size_t)block * D * D;
-    const bool full = (parts & kPartDirect) || ((parts & kPartTF32) && k <= 5);
-    const bool compact = (parts & kPartTF32) && k == 6;
+    const ImageLayout lay = imageLayout(k, parts);
+    const bool full = lay.full != kNoPart;
+    const bool compact = lay.compact != kNoPart;
     // real form [[Re, -Im], [Im, Re]] as B = Gr (rows r = output index, K index j)
     std::vector<float> hi, lo;
     if (full || compact) {
@@ -1349,13 +1379,13 @@ static void buildImageBlock(const FusedPass& pass, int block, float* img, int pa
     const int bRows = (k == 6) ? 3 * D : N, bK = (k == 6) ? D : K;
     const size_t bEntries = (size_t)bRows * bK;
     if (full) {
-        packKMajor(hi, N, K, img);
-        packKMajor(lo, N, K, img + fullN);
+        packKMajor(hi, N, K, img + lay.full);
+        packKMajor(lo, N, K, img + lay.full + fullN);
     }
-    uint16_t* bh = reinterpret_cast<uint16_t*>(img + 2 * fullN);
+    uint16_t* bh = reinterpret_cast<uint16_t*>(img + (lay.bf16 != kNoPart ? lay.bf16 : 0));
     uint16_t* bl = bh + bEntries;
     uint16_t* bll = bl + bEntries;
-    for (int r = 0; r < bRows && (parts & kPartBF16); ++r)
+    for (int r = 0; r < bRows && lay.bf16 != kNoPart; ++r)
         for (int j = 0; j < bK; ++j) {
             // k = 6: rows 0..D-1 take the (r, D + j) entries of the real form
             // (-Im), rows D..3D-1 the (r - D, j) entries (Re, then Im)
@@ -1379,15 +1409,15 @@ static void buildImageBlock(const FusedPass& pass, int block, float* img, int pa
                 ch[(size_t)r * D + j] = hi[(size_t)rr * K + jj];
                 cl[(size_t)r * D + j] = lo[(size_t)rr * K + jj];
             }
-        float* const tc = img + 2 * fullN + (3 * bEntries + 1) / 2;
+        float* const tc = img + lay.compact;
         packKMajor(ch, 3 * D, D, tc);
         packKMajor(cl, 3 * D, D, tc + (size_t)3 * D * D);
     }
 }
 
-// the images of every matrix block of a pass, imageFloats(k) floats apart
+// the images of every matrix block of a pass, one layout stride apart
 static void buildImage(const FusedPass& pass, float* img, int parts) {
-    const size_t stride = imageFloats((int)pass.targets.size());
+    const size_t stride = imageLayout((int)pass.targets.size(), parts).stride;
     for (size_t b = 0; b < ((size_t)1 << pass.controls.size()); ++b) buildImageBlock(pass, (int)b, img + b * stride, parts);
 }
 
@@ -1396,11 +1426,17 @@ static int currentParts() {
     return (g_tcPrecision == kPrecBF16 ? kPartBF16 : kPartTF32) | (g_tcVersion == 1 ? kPartDirect : 0);
 }
 
-// Operand images of every tensor-core pass: the parts the current precision
-// and kernel choice read (tcImagesFit tells when they no longer suffice),
-// built on up to 16 host threads and uploaded in one allocation and one copy.
-// A 6-qubit image holds ~300 KB; building all of its parts took ~0.4 ms of
-// host time, most of a small register's flush.
+std::mutex g_stageMutex;
+float* g_stage = nullptr;       // page-locked staging of uploadPlanTC
+size_t g_stageFloats = 0;
+
+// Operand images of every tensor-core pass (every matrix block of a pass
+// with control qubits): only the parts the current precision and kernel
+// choice read (tcImagesFit tells when they no longer suffice), laid out by
+// imageLayout, built on up to 16 host threads and uploaded in one allocation
+// and one copy.  A 6-qubit block holds 96 KB in split-TF32 (72 KB in
+// split-BF16); with every part it held 300 KB, whose building and pageable
+// copy took ~9 ms of each flush of the 30-qubit circuit.
 void* uploadPlanTC(const FusedPlan& plan) {
     DevicePlan* dp = new DevicePlan();
     dp->parts = currentParts();
@@ -1421,36 +1457,57 @@ void* uploadPlanTC(const FusedPlan& plan) {
         const int k = (int)pass.targets.size();
         dp->unitary.push_back(pass.unitary ? 1 : 0);
         const bool tc = k >= 4 && k <= 6 && plan.numQubits >= k + 7 + (int)pass.controls.size();
-        offset[i + 1] = offset[i] + (tc ? imageFloats(k) << pass.controls.size() : 0);
+        offset[i + 1] = offset[i] + (tc ? imageLayout(k, dp->parts).stride << pass.controls.size() : 0);
     }
     dp->images.assign(np, nullptr);
     if (offset[np] == 0) return dp;
-    std::vector<float> host(offset[np]);
+    if (cudaMalloc(&dp->imageBuf, offset[np] * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        dp->imageBuf = nullptr;
+        return dp;                                   // every pass then runs on the SIMT applier
+    }
+    // built in a page-locked staging buffer kept for the process (a captured
+    // 30-qubit circuit re-uploads ~50 MB at every flush), else in pageable memory
+    std::lock_guard<std::mutex> lk(g_stageMutex);
+    std::vector<float> pageable;
+    float* host = nullptr;
+    if (g_stageFloats < offset[np]) {
+        if (g_stage) cudaFreeHost(g_stage);
+        g_stage = nullptr;
+        g_stageFloats = 0;
+        if (cudaHostAlloc(reinterpret_cast<void**>(&g_stage), offset[np] * sizeof(float), cudaHostAllocDefault) ==
+            cudaSuccess)
+            g_stageFloats = offset[np];
+        else
+            cudaGetLastError();
+    }
+    if (g_stage) {
+        host = g_stage;
+    } else {
+        pageable.resize(offset[np]);
+        host = pageable.data();
+    }
     std::atomic<size_t> next{0};
     auto work = [&]() {
         for (size_t i; (i = next.fetch_add(1)) < np;)
-            if (offset[i + 1] > offset[i]) buildImage(plan.passes[i], host.data() + offset[i], dp->parts);
+            if (offset[i + 1] > offset[i]) buildImage(plan.passes[i], host + offset[i], dp->parts);
     };
     const unsigned nt = (unsigned)std::min<size_t>({(size_t)16, (size_t)std::max(1u, std::thread::hardware_concurrency()), np});
     std::vector<std::thread> pool;
     for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
     work();
     for (auto& t : pool) t.join();
-    if (cudaMalloc(&dp->imageBuf, offset[np] * sizeof(float)) != cudaSuccess) {
-        cudaGetLastError();
-        dp->imageBuf = nullptr;
-        return dp;                                   // every pass then runs on the SIMT applier
-    }
-    cudaMemcpy(dp->imageBuf, host.data(), offset[np] * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemcpy(dp->imageBuf, host, offset[np] * sizeof(float), cudaMemcpyHostToDevice);
     for (size_t i = 0; i < np; ++i)
         if (offset[i + 1] > offset[i]) dp->images[i] = dp->imageBuf + offset[i];
     return dp;
 }
 
-// The tensor-core operands of one pass, as uploadPlanTC lays them out: the
-// number of floats, and the image itself.
-size_t tcImageFloats(int k) { return imageFloats(k); }
-void tcBuildImage(const FusedPass& pass, float* img) { buildImageBlock(pass, 0, img, currentParts()); }
+// The tensor-core operands of one pass holding `parts`, as uploadPlanTC lays
+// them out: the number of floats, and the image itself (a pass without
+// control qubits).
+size_t tcImageFloats(int k, int parts) { return imageLayout(k, parts).stride; }
+void tcBuildImage(const FusedPass& pass, float* img, int parts) { buildImageBlock(pass, 0, img, parts); }
 int tcImageParts() { return currentParts(); }
 // whether a plan's images hold the parts the current precision and kernel
 // choice read (else the caller uploads the plan again)
@@ -1611,18 +1668,28 @@ int tcCheckCoverage(int n, const std::vector<int>& targets, const std::vector<in
 // Launch tensor-core kernel `version` (tcKernelFor) for a pass of k = 4..6
 // qubits on one register (batch = 1) or on a batch of registers; false if the
 // launch failed.  The direct-load kernel (version 1) takes single registers.
-static bool launchPassTC(int version, const FusedPass& pass, float* re, float* im, int n, const float* img, int* errFlag,
-                         const NormLinks& nl, cudaStream_t st, int batch, uint64_t instStride, uint64_t imageStride) {
+static bool launchPassTC(int version, const FusedPass& pass, float* re, float* im, int n, const float* img, int parts,
+                         int* errFlag, const NormLinks& nl, cudaStream_t st, int batch, uint64_t instStride,
+                         uint64_t imageStride) {
     const int k = (int)pass.targets.size();
     bool ok = false;
+    // the operand part this launch reads; a part that was not built stops the
+    // launch (its kernel would read past the image)
+    const ImageLayout lay = imageLayout(k, parts);
+    const size_t po = version < 2                        ? lay.full
+                      : g_tcPrecision == kPrecBF16 ? lay.bf16
+                      : k == 6                     ? lay.compact
+                                                   : lay.full;
+    if (po == kNoPart || lay.stride == 0) return false;
+    const size_t bs = lay.stride;
     // the default kernels, when the targets include qubits 0 and 1: the
     // variant with 16-byte column words
     bool done = false;
     if (g_tcVersion == 0 && pass.targets[0] == 0 && pass.targets[1] == 1) {
 #define QG_TC2W(KQ, LG, EG, LS, PR)                                                                                    \
     (done = true,                                                                                                       \
-     g_tcStaging ? launchTC2<KQ, LG, EG, LS, PR, 4, 1>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride) \
-                 : launchTC2<KQ, LG, EG, LS, PR, 4, 0>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride))
+     g_tcStaging ? launchTC2<KQ, LG, EG, LS, PR, 4, 1>(re, im, n, pass, img, po, bs, errFlag, nl, st, batch, instStride, imageStride) \
+                 : launchTC2<KQ, LG, EG, LS, PR, 4, 0>(re, im, n, pass, img, po, bs, errFlag, nl, st, batch, instStride, imageStride))
         const bool tf = g_tcPrecision == kPrecTF32;
         if (tf && k == 4 && version == 3) ok = QG_TC2W(4, 1, 1, 1, kPrecTF32);
         else if (tf && k == 5 && version == 2) ok = QG_TC2W(5, 2, 1, 1, kPrecTF32);
@@ -1638,10 +1705,10 @@ static bool launchPassTC(int version, const FusedPass& pass, float* re, float* i
         // + one; 4: one + two; 5: two loader groups (each half of every chunk)
         // + two epilogue groups
 #define QG_TC2S(KQ, PR, ST)                                                                                                    \
-    (version == 2   ? launchTC2<KQ, 2, 1, 1, PR, 1, ST>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride)  \
-     : version == 3 ? launchTC2<KQ, 1, 1, 1, PR, 1, ST>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride)  \
-     : version == 4 ? launchTC2<KQ, 1, 2, 1, PR, 1, ST>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride)  \
-                    : launchTC2<KQ, 2, 2, 2, PR, 1, ST>(re, im, n, pass, img, errFlag, nl, st, batch, instStride, imageStride))
+    (version == 2   ? launchTC2<KQ, 2, 1, 1, PR, 1, ST>(re, im, n, pass, img, po, bs, errFlag, nl, st, batch, instStride, imageStride)  \
+     : version == 3 ? launchTC2<KQ, 1, 1, 1, PR, 1, ST>(re, im, n, pass, img, po, bs, errFlag, nl, st, batch, instStride, imageStride)  \
+     : version == 4 ? launchTC2<KQ, 1, 2, 1, PR, 1, ST>(re, im, n, pass, img, po, bs, errFlag, nl, st, batch, instStride, imageStride)  \
+                    : launchTC2<KQ, 2, 2, 2, PR, 1, ST>(re, im, n, pass, img, po, bs, errFlag, nl, st, batch, instStride, imageStride))
 #define QG_TC2P(KQ, PR) (g_tcStaging ? QG_TC2S(KQ, PR, 1) : QG_TC2S(KQ, PR, 0))
 #define QG_TC2(KQ) (g_tcPrecision == kPrecTF32 ? QG_TC2P(KQ, kPrecTF32) : QG_TC2P(KQ, kPrecBF16))
         switch (k) {
@@ -1657,9 +1724,9 @@ static bool launchPassTC(int version, const FusedPass& pass, float* re, float* i
     }
     if (batch != 1) return false;
     switch (k) {
-        case 4: return launchTC<4>(re, im, n, pass, img, errFlag, nl, st);
-        case 5: return launchTC<5>(re, im, n, pass, img, errFlag, nl, st);
-        case 6: return launchTC<6>(re, im, n, pass, img, errFlag, nl, st);
+        case 4: return launchTC<4>(re, im, n, pass, img + po, errFlag, nl, st);
+        case 5: return launchTC<5>(re, im, n, pass, img + po, errFlag, nl, st);
+        case 6: return launchTC<6>(re, im, n, pass, img + po, errFlag, nl, st);
         default: return false;
     }
 }
@@ -1698,7 +1765,7 @@ int applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, 
         if (continues) nl.corrTarget = dp->target[dp->lastTC];
         dp->target[index] = continues ? dp->target[dp->lastTC] : dp->inNorm[index];
     }
-    const bool ok = launchPassTC(version, pass, re, im, n, dp->images[index], dp->errFlag, nl, st, 1, 0, 0);
+    const bool ok = launchPassTC(version, pass, re, im, n, dp->images[index], dp->parts, dp->errFlag, nl, st, 1, 0, 0);
     if (!ok) return -1;
     dp->lastTC = (int)index;
     dp->chain = true;
@@ -1759,11 +1826,12 @@ bool tensorCoresEnabled() { return g_tcEnabled; }
 // drift correction (the callers normalise per register).  Returns false for a
 // pass the tensor cores do not take or a failed launch.
 bool applyPassTCBatch(float* re, float* im, int n, const FusedPass& pass, const float* images, size_t imageStride,
-                      int batch, int* errFlag, cudaStream_t st) {
+                      int parts, int batch, int* errFlag, cudaStream_t st) {
     const int version = tcKernelFor(pass, n);
-    if (version < 2 || !images) return false;
+    if (version < 2 || !images || !pass.controls.empty()) return false;
     const NormLinks nl{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    return launchPassTC(version, pass, re, im, n, images, errFlag, nl, st, batch, 1ull << n, (uint64_t)imageStride);
+    return launchPassTC(version, pass, re, im, n, images, parts, errFlag, nl, st, batch, 1ull << n,
+                        (uint64_t)imageStride);
 }
 
 }  // namespace qg

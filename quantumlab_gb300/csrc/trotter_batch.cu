@@ -42,11 +42,11 @@
 
 namespace qg {
 
-size_t tcImageFloats(int k);
-void tcBuildImage(const FusedPass& pass, float* img);
+size_t tcImageFloats(int k, int parts);
+void tcBuildImage(const FusedPass& pass, float* img, int parts);
 int tcImageParts();
 bool applyPassTCBatch(float* re, float* im, int n, const FusedPass& pass, const float* images, size_t imageStride,
-                      int batch, int* errFlag, cudaStream_t st);
+                      int parts, int batch, int* errFlag, cudaStream_t st);
 
 namespace {
 
@@ -597,6 +597,8 @@ bool compileBatch(TrotterBatch* b) {
     auto planOf = [&](int c, size_t m) -> FusedPlan& { return plan[b->classes[c].members[m]]; };
     // layout: states, image offsets, result slots and rows, class after class
     size_t stateFloats = 0, imgTotal = 0;
+    // the operand image parts the current precision and kernel choice read
+    b->parts = tcImageParts();
     int pos = 0, slots = 0;
     std::vector<float> coef;                       // [class][reduction][member][kCoefs]
     for (int c = 0; c < C; ++c) {
@@ -612,7 +614,7 @@ bool compileBatch(TrotterBatch* b) {
         cl.imgStride.assign(np, 0);
         for (size_t p = 0; p < np; ++p) {
             cl.shape.push_back(widenNarrow(planOf(c, 0).passes[p], cl.n));
-            cl.imgStride[p] = tcImageFloats((int)cl.shape[p].targets.size());
+            cl.imgStride[p] = tcImageFloats((int)cl.shape[p].targets.size(), b->parts);
             cl.imgOffset[p] = imgTotal;
             imgTotal += cl.imgStride[p] * M;
         }
@@ -623,7 +625,6 @@ bool compileBatch(TrotterBatch* b) {
     }
     b->numSlots = slots;
     // operand images of every (class, pass, member), on host threads
-    b->parts = tcImageParts();
     std::vector<float> host(std::max<size_t>(imgTotal, 4));
     std::vector<std::tuple<int, int, int>> imgJobs;            // class, pass, member
     for (int c = 0; c < C; ++c)
@@ -632,7 +633,8 @@ bool compileBatch(TrotterBatch* b) {
     parallelFor(imgJobs.size(), std::min(hw, 16u), [&](size_t j) {
         const int c = std::get<0>(imgJobs[j]), p = std::get<1>(imgJobs[j]), m = std::get<2>(imgJobs[j]);
         const TrotterClass& cl = b->classes[c];
-        tcBuildImage(widenNarrow(planOf(c, m).passes[p], cl.n), host.data() + cl.imgOffset[p] + m * cl.imgStride[p]);
+        tcBuildImage(widenNarrow(planOf(c, m).passes[p], cl.n), host.data() + cl.imgOffset[p] + m * cl.imgStride[p],
+                     b->parts);
     });
     // device side
     cudaStream_t st = stream();
@@ -672,7 +674,7 @@ bool queueRun(TrotterBatch* b, cudaStream_t st) {
         kBatchClassical<<<(M + 127) / 128, 128, 0, st>>>(re, dim, b->dInit + cl.posBase, M);
         if (launchFailed(kFn)) return false;
         for (size_t p = 0; p < cl.shape.size(); ++p)
-            if (!applyPassTCBatch(re, im, cl.n, cl.shape[p], b->images + cl.imgOffset[p], cl.imgStride[p], M,
+            if (!applyPassTCBatch(re, im, cl.n, cl.shape[p], b->images + cl.imgOffset[p], cl.imgStride[p], b->parts, M,
                                   b->errFlag, st)) {
                 invalidQuESTInputError("A pass of the Trotter batch could not be launched on the tensor cores.", kFn);
                 return false;
