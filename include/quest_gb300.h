@@ -179,6 +179,11 @@ int quest_gb300_getTensorCoreStaging(void);
  * amplitude is read and written exactly once, 1 when not, -1 when the pass
  * does not fit (controls inside the tile, too few qubits). */
 int quest_gb300_checkTileCoverage(int numQubits, const int* targets, int numTargets, const int* controls, int numControls);
+/* Host check of the tensor-core operand images (no GPU): for every pass width
+ * and image layout the library builds, the part each kernel reads is present,
+ * 16-byte aligned, inside the image block and disjoint from the other parts.
+ * Returns 0 when all hold, else 1. */
+int quest_gb300_checkImageLayouts(void);
 double quest_gb300_calcTotalProbF32(void* qureg32);
 double quest_gb300_calcProbOfOutcomeF32(void* qureg32, int measureQubit, int outcome);
 /* 1 - |<ref|q>|^2 / (<ref|ref><q|q>) against an FP64 state vector; writes the

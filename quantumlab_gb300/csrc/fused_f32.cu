@@ -55,6 +55,7 @@ int tensorCorePrecision();
 bool setTensorCoreStaging(int mode);
 int tensorCoreStaging();
 int tcCheckCoverage(int n, const std::vector<int>& targets, const std::vector<int>& controls);
+int tcCheckImageLayouts();
 bool tensorCoresEnabled();
 int tcKernelFor(const FusedPass& pass, int n);
 float* f32re(QuregF32& q) { return q.re; }
@@ -554,6 +555,8 @@ void quest_gb300_setTensorCoreKernel(int version) { qg::setTensorCoreKernel(vers
 int quest_gb300_setTensorCorePrecision(int mode) { return qg::setTensorCorePrecision(mode) ? 0 : -1; }
 int quest_gb300_getTensorCorePrecision(void) { return qg::tensorCorePrecision(); }
 int quest_gb300_setTensorCoreStaging(int mode) { return qg::setTensorCoreStaging(mode) ? 0 : -1; }
+
+int quest_gb300_checkImageLayouts(void) { return qg::tcCheckImageLayouts(); }
 
 int quest_gb300_checkTileCoverage(int numQubits, const int* targets, int numTargets, const int* controls, int numControls) {
     if (!targets || numTargets < 4 || numTargets > 6 || numControls < 0 || numControls > 3 || (numControls && !controls))

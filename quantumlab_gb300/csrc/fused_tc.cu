@@ -1645,6 +1645,41 @@ int tc2Coverage(int n, const FusedPass& pass, int groups, std::vector<uint8_t>& 
     return 0;
 }
 
+// Check of imageLayout against what the kernels read (host, no GPU): for
+// k = 4..6 and every parts set the library builds (one operand form, with or
+// without the direct-load kernel's part), each part a kernel of that set
+// reads is present, starts on a 16-byte boundary, lies inside the block and
+// overlaps no other part.  0 when all hold, else 1.
+int tcCheckImageLayouts() {
+    const int sets[4] = {kPartTF32, kPartBF16, kPartTF32 | kPartDirect, kPartBF16 | kPartDirect};
+    for (int k = 4; k <= 6; ++k)
+        for (int parts : sets) {
+            const ImageLayout L = imageLayout(k, parts);
+            const size_t D = (size_t)1 << k, NK = 4 * D * D, GE = (k == 6) ? 3 * D * D : NK;
+            struct Read {
+                size_t off, floats;
+            };
+            std::vector<Read> reads;
+            if (parts & kPartTF32) reads.push_back({k == 6 ? L.compact : L.full, 2 * GE});    // hi, lo
+            if (parts & kPartBF16) reads.push_back({L.bf16, 3 * GE / 2});                       // three BF16 parts
+            if (parts & kPartDirect) reads.push_back({L.full, 2 * NK});                         // direct-load kernel
+            if (L.stride % 4) return 1;
+            for (const Read& r : reads)
+                if (r.off == kNoPart || r.off % 4 || r.off + r.floats > L.stride) return 1;
+            // the parts present do not overlap
+            std::vector<std::pair<size_t, size_t>> present;
+            if (L.full != kNoPart) present.push_back({L.full, L.full + 2 * NK});
+            if (L.bf16 != kNoPart) present.push_back({L.bf16, L.bf16 + (3 * GE + 1) / 2});
+            if (L.compact != kNoPart) present.push_back({L.compact, L.compact + 6 * D * D});
+            for (size_t a = 0; a < present.size(); ++a)
+                for (size_t b = a + 1; b < present.size(); ++b)
+                    if (present[a].first < present[b].second && present[b].first < present[a].second) return 1;
+            for (const auto& r : present)
+                if (r.second > L.stride) return 1;
+        }
+    return 0;
+}
+
 // 0 when a pass on `targets` (ascending) with `controls` reads and writes
 // every amplitude of an n-qubit register exactly once (both tile walks of
 // tc2Coverage), 1 when it does not, -1 when it does not fit or n > 26

@@ -74,3 +74,9 @@ def test_passes_of_compiled_plans(L):
             controlled += nc > 0
         lib.quest_gb300_planDestroy(p)
     assert checked > 10 and controlled > 3
+
+
+def test_operand_image_layouts(L):
+    """Every tensor-core kernel reads its operand part inside the image block
+    the library lays out for the parts it built (16-byte aligned, no overlap)."""
+    assert L.lib.quest_gb300_checkImageLayouts() == 0
