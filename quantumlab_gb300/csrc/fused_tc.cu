@@ -40,6 +40,7 @@
 #include <cstdint>
 #include <cstring>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 namespace qg {
@@ -792,63 +793,71 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
             const uint32_t aH = tmem + laneSel + b * kStageCols + p0 * JP / EPW;
             const int chq = (int)(sq % NCH);
             const float* const cb = xr + colBase;
-            float nrm = 0.f;
+            // split the chunk into TMEM; the sum of squares of what the warp
+            // reads (the pass's input norm) only when this pass measures it
+            auto splitChunk = [&](auto withNorm) -> float {
+                constexpr bool WN = decltype(withNorm)::value;
+                float nrm = 0.f;
 #pragma unroll
-            for (int c0 = 0; c0 < PPG * JP; c0 += 8 * EPW) {
-                uint32_t hi[8], lo[8];
-                if constexpr (CV == 4) {
-                    // targets on qubits 0, 1: a column's entries j .. j + 3 are one
-                    // 16-byte word (scalar reads would be a 4-way bank conflict);
-                    // four consecutive local entries stay in one part
-                    float xv[8 * EPW];
+                for (int c0 = 0; c0 < PPG * JP; c0 += 8 * EPW) {
+                    uint32_t hi[8], lo[8];
+                    if constexpr (CV == 4) {
+                        // targets on qubits 0, 1: a column's entries j .. j + 3 are one
+                        // 16-byte word (scalar reads would be a 4-way bank conflict);
+                        // four consecutive local entries stay in one part
+                        float xv[8 * EPW];
 #pragma unroll
-                    for (int v = 0; v < 2 * EPW; ++v) {
-                        const int cl = c0 + 4 * v;
-                        const int pl = cl / JP;
-                        const int j = (KQ == 6) ? 32 * S::half(chq, p0 + pl) + cl % JP : cl % JP;
-                        const float4 f = *reinterpret_cast<const float4*>(cb + pl * R + p.colJ[j]);
-                        xv[4 * v] = f.x;
-                        xv[4 * v + 1] = f.y;
-                        xv[4 * v + 2] = f.z;
-                        xv[4 * v + 3] = f.w;
-                    }
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) {
-#pragma unroll
-                        for (int h = 0; h < EPW; ++h) nrm = fmaf(xv[EPW * e + h], xv[EPW * e + h], nrm);
-                        if constexpr (BF) {
-                            splitBF16x2(xv[2 * e], xv[2 * e + 1], hi[e], lo[e]);
-                        } else {
-                            hi[e] = tf32Bits(xv[e]);
-                            lo[e] = __float_as_uint(xv[e] - __uint_as_float(hi[e]));
-                        }
-                    }
-                } else {
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) {
-                        float x[EPW];
-#pragma unroll
-                        for (int h = 0; h < EPW; ++h) {
-                            const int cl = c0 + EPW * e + h;     // local entry: buffer part cl / JP
+                        for (int v = 0; v < 2 * EPW; ++v) {
+                            const int cl = c0 + 4 * v;
                             const int pl = cl / JP;
                             const int j = (KQ == 6) ? 32 * S::half(chq, p0 + pl) + cl % JP : cl % JP;
-                            x[h] = (cb + pl * R)[p.colJ[j]];
-                            nrm = fmaf(x[h], x[h], nrm);         // the warp reads every element once
+                            const float4 f = *reinterpret_cast<const float4*>(cb + pl * R + p.colJ[j]);
+                            xv[4 * v] = f.x;
+                            xv[4 * v + 1] = f.y;
+                            xv[4 * v + 2] = f.z;
+                            xv[4 * v + 3] = f.w;
                         }
-                        if constexpr (BF) {
-                            splitBF16x2(x[0], x[EPW - 1], hi[e], lo[e]);
-                        } else {
-                            // hi = x rounded to TF32; lo = x - hi (exact), which the MMA
-                            // reads as its leading TF32 bits; lo takes both signs, so
-                            // that truncation is unbiased
-                            hi[e] = tf32Bits(x[0]);
-                            lo[e] = __float_as_uint(x[0] - __uint_as_float(hi[e]));
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) {
+#pragma unroll
+                            for (int h = 0; h < EPW; ++h)
+                                if constexpr (WN) nrm = fmaf(xv[EPW * e + h], xv[EPW * e + h], nrm);
+                            if constexpr (BF) {
+                                splitBF16x2(xv[2 * e], xv[2 * e + 1], hi[e], lo[e]);
+                            } else {
+                                hi[e] = tf32Bits(xv[e]);
+                                lo[e] = __float_as_uint(xv[e] - __uint_as_float(hi[e]));
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) {
+                            float x[EPW];
+#pragma unroll
+                            for (int h = 0; h < EPW; ++h) {
+                                const int cl = c0 + EPW * e + h;     // local entry: buffer part cl / JP
+                                const int pl = cl / JP;
+                                const int j = (KQ == 6) ? 32 * S::half(chq, p0 + pl) + cl % JP : cl % JP;
+                                x[h] = (cb + pl * R)[p.colJ[j]];
+                                if constexpr (WN) nrm = fmaf(x[h], x[h], nrm);   // the warp reads every element once
+                            }
+                            if constexpr (BF) {
+                                splitBF16x2(x[0], x[EPW - 1], hi[e], lo[e]);
+                            } else {
+                                // hi = x rounded to TF32; lo = x - hi (exact), which the MMA
+                                // reads as its leading TF32 bits; lo takes both signs, so
+                                // that truncation is unbiased
+                                hi[e] = tf32Bits(x[0]);
+                                lo[e] = __float_as_uint(x[0] - __uint_as_float(hi[e]));
+                            }
                         }
                     }
+                    tmemSt8(aH + c0 / EPW, hi);
+                    tmemSt8(aH + kStageCols / 2 + c0 / EPW, lo);
                 }
-                tmemSt8(aH + c0 / EPW, hi);
-                tmemSt8(aH + kStageCols / 2 + c0 / EPW, lo);
-            }
+                return nrm;
+            };
+            const float nrm = measure ? splitChunk(std::true_type{}) : splitChunk(std::false_type{});
             if (measure) normIn += (double)nrm;
             tmemWaitSt();
             fenceBefore();
