@@ -382,12 +382,11 @@ bool matrixIsUnitary(const std::vector<cplx>& m, int D) {
 FusedGate controlBlock(const FusedGate& g, uint64_t ctl, uint32_t val) {
     FusedGate sub;
     const int m = (int)g.qubits.size();
-    uint32_t fixedMask = 0, fixedVal = 0;
+    uint32_t fixedVal = 0;
     int keep[6], nk = 0;
     for (int b = 0; b < m; ++b) {
         const int q = g.qubits[b];
         if (ctl >> q & 1ull) {
-            fixedMask |= 1u << b;
             const int j = __builtin_popcountll(ctl & ((1ull << q) - 1ull));
             if (val >> j & 1u) fixedVal |= 1u << b;
         } else {

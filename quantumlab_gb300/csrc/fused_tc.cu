@@ -590,11 +590,14 @@ __device__ __forceinline__ bool warpWaitOrAbort(uint64_t* bar, uint32_t parity, 
 }
 
 // amplitude offset of the first amplitude of a tile: the tile index bits go,
-// in order, to the qubits outside I
+// in order, to the qubits outside I and outside the control qubits (host and
+// device: the host check of the addressing walks tiles with it)
 template <int KQ>
 __host__ __device__ __forceinline__ uint64_t tileBase(const TC2Params<KQ>& p, uint64_t tile) {
     uint64_t tb = tile << p.runBits;
+#ifdef __CUDA_ARCH__
 #pragma unroll 1
+#endif
     for (int b = p.runBits; b < p.numIns; ++b) {
         const int s = p.insI[b];
         tb = ((tb >> s) << (s + 1)) | (tb & ((1ull << s) - 1ull));
