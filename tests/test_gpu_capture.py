@@ -231,12 +231,14 @@ def test_capture_drops_queue_on_overwrite_and_off_flushes(gpulib):
 
 def test_capture_speeds_up_a_26_qubit_circuit(gpulib):
     """The 26-qubit random circuit through the QuEST API: captured (one fused
-    FP32 flush) against direct FP64 per-gate calls."""
+    FP32 flush; plans of 26 qubits and more take control qubits) against
+    direct FP64 per-gate calls, in time and in the state."""
     L = gpulib
     lib = L.lib
     n = 26
     ops = W.c2_circuit(n=n, layers=10, seed=2)
     res = {}
+    states = {}
     for mode in (0, 1):
         q = L.create(n)
         lib.quest_gb300_setCapture(q, mode)
@@ -249,10 +251,37 @@ def test_capture_speeds_up_a_26_qubit_circuit(gpulib):
         p = lib.calcTotalProb(q)
         lib.quest_gb300_eventRecord(21)
         res[mode] = (lib.quest_gb300_eventElapsedMs(20, 21), p)
+        states[mode] = L.amps(q).copy()
         L.destroy(q)
-    print(f"26q 10 layers: direct {res[0][0]:.1f} ms, captured {res[1][0]:.1f} ms")
+    a, b = states[0], states[1]
+    f = abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real)
+    err = float(np.max(np.abs(a - b)))
+    print(f"26q 10 layers: direct {res[0][0]:.1f} ms, captured {res[1][0]:.1f} ms, 1-F {1 - f:.2e}, max|d| {err:.2e}")
     assert abs(res[1][1] - 1) < 1e-5
+    assert 1 - f <= 1e-6 and err <= 1e-5
     assert res[1][0] < res[0][0] / 3
+
+
+def test_capture_density_matrix_with_control_qubits(gpulib):
+    """A 13-qubit noisy density matrix (a 26-qubit vector, so its plans take
+    control qubits): gates doubled on (t, t + N), the three channels as
+    superoperators, captured against direct FP64 calls."""
+    L = gpulib
+    lib = L.lib
+    n = 13
+    ops = W.c3_circuit(nq=n, layers=2, seed=8)
+    out = {}
+    for mode in (0, 1):
+        q = L.create(n, density=True)
+        lib.quest_gb300_setCapture(q, mode)
+        lib.initZeroState(q)
+        W.run_ops(L, q, ops)
+        out[mode] = (L.amps(q).copy(), lib.calcTotalProb(q), lib.calcPurity(q))
+        L.destroy(q)
+    (a, ta, pa), (b, tb, pb) = out[0], out[1]
+    err = float(np.max(np.abs(a - b)))
+    print(f"DM 13 qubits: max|d rho| {err:.2e}, trace {tb - ta:.1e}, purity rel. diff {abs(pb / pa - 1):.2e}")
+    assert err <= 1e-5 and abs(tb - ta) < 1e-9 and abs(pb / pa - 1) < 1e-6
 
 
 @pytest.mark.parametrize("n", [3, 5, 8, 11, 12, 13])
