@@ -131,7 +131,16 @@ static void flushRecord(Capture* c, double* re, double* im) {
     plan->maxFused = tuned && c->shape ? c->shape->maxFused : capWidest(c->n);
     plan->gates.swap(c->gates);
     const auto t0 = std::chrono::steady_clock::now();
-    const bool reused = c->shape && c->shape->maxFused == plan->maxFused && compilePlanLike(*plan, *c->shape);
+    // A new circuit shape is planned without lookahead: the search takes ~2x
+    // longer with it and saves ~2 % of the passes, a loss for a circuit run
+    // once.  When the shape comes again it is planned once more with
+    // lookahead, and the next flushes reuse that plan.
+    plan->lookahead = 0;
+    bool reused = c->shape && c->shape->maxFused == plan->maxFused && compilePlanLike(*plan, *c->shape);
+    if (reused && c->shape->lookahead == 0) {
+        reused = false;
+        plan->lookahead = 4;
+    }
     if (!reused) {
         // autotuned: the width with the lowest predicted time (the cost table
         // of this register size is measured by the first such flush)

@@ -25,7 +25,13 @@
 //     the set grows by any one live qubit.
 //   * Each level keeps the `beam` best sets, ranked by multi-qubit gates
 //     absorbed, then by gates absorbed, then by least advanced qubits first.
-//   * The best set found becomes the pass and its closure is applied.
+//   * The best set found becomes the pass and its closure is applied.  With
+//     lookahead L (default 4), the L best distinct sets of the search are
+//     each applied on a copy of the search state and followed by one more
+//     search; the set whose two passes absorb the most multi-qubit gates,
+//     then gates, becomes the pass.  On 30-qubit random circuits this saves
+//     ~2 % of the passes (65 -> 64 at seed 2; 730 -> 713 over 12 circuits of
+//     26-30 qubits); on the first-order Hubbard circuit, 58 -> 51 passes.
 // The search repeats until every gate is absorbed.  Take 30-qubit random
 // circuits of Haar one-qubit gates, random-matching controlled phases and CNOT
 // brickwork, at kmax = 6.  Merging gates into open blocks in program order
@@ -44,6 +50,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <thread>
 #include <unordered_set>
@@ -97,8 +104,9 @@ bool better(const Scored& a, const Scored& b) {
 
 class Search {
   public:
-    Search(const std::vector<FusedGate>& gates, int numQubits, int kmax, int beam, int maxCtl)
-        : nq_(numQubits), kmax_(kmax), beam_(std::max(1, beam)), maxCtl_(maxCtl), g_(gates.size()), byq_(numQubits),
+    Search(const std::vector<FusedGate>& gates, int numQubits, int kmax, int beam, int maxCtl, int look)
+        : nq_(numQubits), kmax_(kmax), beam_(std::max(1, beam)), maxCtl_(maxCtl), look_(look), g_(gates.size()),
+          byq_(numQubits),
           segStart_(numQubits), cur_(numQubits, 0), rem_(numQubits, 0), applied_(gates.size(), 0),
           stamp_(gates.size(), 0), remaining_((int)gates.size()) {
         std::vector<int> lastDiag(numQubits, 0);
@@ -133,11 +141,48 @@ class Search {
     // failure), the absorbed gates in an allowed order and the pass's
     // control qubits
     uint64_t next(std::vector<int>& absorbed, uint64_t& controls) {
+        const int look = look_;
+        std::vector<Scored> finalists;
+        Scored best;
+        bool have = search(best, look > 0 ? &finalists : nullptr);
+        if (look > 0 && have && finalists.size() > 1) {
+            std::sort(finalists.begin(), finalists.end(), better);
+            std::vector<uint64_t> uniq;
+            int bestTotal = -1, bestMulti = -1;
+            for (const Scored& f : finalists) {
+                if (std::find(uniq.begin(), uniq.end(), f.set) != uniq.end()) continue;
+                uniq.push_back(f.set);
+                if ((int)uniq.size() > look) break;
+                Search copy(*this);
+                std::vector<int> abs;
+                copy.closure(f.set, &abs, nullptr, true);
+                Scored nb;
+                const bool h2 = !copy.done() && copy.search(nb, nullptr);
+                const int tm = f.multi + (h2 ? nb.multi : 0), ta = f.all + (h2 ? nb.all : 0);
+                if (tm > bestMulti || (tm == bestMulti && ta > bestTotal)) {
+                    bestMulti = tm;
+                    bestTotal = ta;
+                    best = f;
+                }
+            }
+        }
+        uint64_t S = best.set;
+        if (!have || best.all == 0) {
+            // the earliest remaining gate can always run: every gate before it has run
+            while (applied_[first_]) ++first_;
+            S = g_[first_].mask;
+        }
+        absorbed.clear();
+        controls = closure(S, &absorbed, nullptr, true);
+        return absorbed.empty() ? 0 : S;     // 0: no progress (cannot happen, see above)
+    }
+
+    // the beam search of one pass; false when no set was scored
+    bool search(Scored& best, std::vector<Scored>* finalists) {
         std::vector<Scored> beam, cand;
         std::unordered_set<uint64_t> seen;
         for (int q = 0; q < nq_; ++q)
             if (live_ >> q & 1) cand.push_back(eval(1ull << q));
-        Scored best;
         bool have = false;
         for (int level = 1;; ++level) {
             if (cand.empty()) break;
@@ -145,6 +190,7 @@ class Search {
             std::partial_sort(cand.begin(), cand.begin() + keep, cand.end(), better);
             cand.resize(keep);
             beam.swap(cand);
+            if (finalists) finalists->insert(finalists->end(), beam.begin(), beam.end());
             if (!have || better(beam[0], best)) best = beam[0];
             have = true;
             if (level >= kmax_) break;
@@ -164,15 +210,7 @@ class Search {
                 }
             }
         }
-        uint64_t S = best.set;
-        if (!have || best.all == 0) {
-            // the earliest remaining gate can always run: every gate before it has run
-            while (applied_[first_]) ++first_;
-            S = g_[first_].mask;
-        }
-        absorbed.clear();
-        controls = closure(S, &absorbed, nullptr, true);
-        return absorbed.empty() ? 0 : S;     // 0: no progress (cannot happen, see above)
+        return have;
     }
 
   private:
@@ -295,7 +333,7 @@ class Search {
         return ctl;
     }
 
-    int nq_, kmax_, beam_, maxCtl_;
+    int nq_, kmax_, beam_, maxCtl_, look_;
     std::vector<GateInfo> g_;
     std::vector<std::vector<int>> byq_;       // gates on each qubit, program order
     std::vector<std::vector<int>> segStart_;  // per qubit: first index in byq_ of each segment, then byq_.size()
@@ -450,7 +488,7 @@ void compilePlan(FusedPlan& plan) {
     std::vector<uint64_t> sets, ctls;
     std::vector<std::vector<int>> members;
     {
-        Search search(plan.gates, plan.numQubits, plan.maxFused, plan.beamWidth, plan.maxControls);
+        Search search(plan.gates, plan.numQubits, plan.maxFused, plan.beamWidth, plan.maxControls, plan.lookahead);
         std::vector<int> absorbed;
         uint64_t ctl = 0;
         while (!search.done()) {
@@ -624,6 +662,14 @@ int quest_gb300_planSetBeamWidth(void* plan, int width) {
     FusedPlan* p = P(plan);
     if (!p || width < 1 || width > 256) return -1;
     p->beamWidth = width;
+    p->compiled = false;
+    return 0;
+}
+
+int quest_gb300_planSetLookahead(void* plan, int candidates) {
+    FusedPlan* p = P(plan);
+    if (!p || candidates < 0 || candidates > 16) return -1;
+    p->lookahead = candidates;
     p->compiled = false;
     return 0;
 }

@@ -184,6 +184,7 @@ SIGNATURES = {
     "quest_gb300_planAddControlledPhaseShift": (_I, [C.c_void_p, _I, _I, _D]),
     "quest_gb300_planSetBeamWidth": (_I, [C.c_void_p, _I]),
     "quest_gb300_planSetMaxControls": (_I, [C.c_void_p, _I]),
+    "quest_gb300_planSetLookahead": (_I, [C.c_void_p, _I]),
     "quest_gb300_planPassControls": (_I, [C.c_void_p, _I, _P(_I)]),
     "quest_gb300_planPassBlock": (_I, [C.c_void_p, _I, _I, _P(qreal), _P(qreal)]),
     "quest_gb300_setTensorCorePrecision": (_I, [_I]),

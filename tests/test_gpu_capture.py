@@ -333,9 +333,11 @@ def test_capture_small_registers(gpulib, n):
 
 
 def test_capture_stats_count_the_flushes(gpulib):
-    """quest_gb300_captureStats: -1 with capture off; after two flushes of a
-    queued circuit, the flush and gate totals, at least one fused pass per
-    flush and a non-negative planning time."""
+    """quest_gb300_captureStats: -1 with capture off; after three flushes of
+    a queued circuit, the flush and gate totals, at least one fused pass per
+    flush and a non-negative planning time.  The first flush plans the
+    circuit's shape, the second plans it again with lookahead, the third
+    reuses that plan; all three give the state to FP32 precision."""
     L = gpulib
     lib = L.lib
     n = 14
@@ -346,16 +348,15 @@ def test_capture_stats_count_the_flushes(gpulib):
     ops = W.c2_circuit(n=n, layers=2, seed=4)
     queued = 0
     states = []
-    for _ in range(2):
+    for _ in range(3):
         lib.initZeroState(q)
         W.run_ops(L, q, ops)
         queued += lib.quest_gb300_capturedGates(q)
         lib.calcTotalProb(q)
         states.append(L.amps(q).copy())
-    # the second flush takes the first one's passes (same circuit shape)
-    assert np.max(np.abs(states[0] - states[1])) < 1e-6
+    assert np.max(np.abs(states[0] - states[1])) < 1e-6 and np.max(np.abs(states[1] - states[2])) < 1e-6
     assert lib.quest_gb300_captureStats(q, C.byref(f), C.byref(g), C.byref(p), C.byref(ms)) == 0
-    assert f.value == 2 and g.value == queued == 2 * len(ops)
+    assert f.value == 3 and g.value == queued == 3 * len(ops)
     assert 2 <= p.value <= g.value and ms.value >= 0.0
     lib.quest_gb300_setCapture(q, 0)
     L.destroy(q)
