@@ -53,8 +53,7 @@ int quest_gb300_planSetBeamWidth(void* plan, int width);
  * candidates of each pass are tried with the pass that would follow them, and
  * the pair that absorbs the most gates decides (~2 % fewer passes on random
  * circuits, ~12 % on first-order Trotter circuits, for ~2x the search time).
- * 0 takes the best set at once.  Op-stream capture plans a new circuit shape
- * without lookahead and re-plans it with lookahead when the shape repeats.
+ * 0 takes the best set at once; op-stream capture plans without lookahead.
  * Returns 0 or -1. */
 int quest_gb300_planSetLookahead(void* plan, int candidates);
 /* Control qubits a pass may use (0..3; a new plan gets 3 on registers of 26

