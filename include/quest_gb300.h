@@ -49,7 +49,8 @@ int quest_gb300_planAddControlledPhaseShift(void* plan, int qubit1, int qubit2, 
 /* Sets kept per level of the pass search (1..256, default 16); wider finds
  * fewer passes on some circuits at more host time.  Returns 0 or -1. */
 int quest_gb300_planSetBeamWidth(void* plan, int width);
-/* Lookahead of the pass search (0..16 candidate sets, default 4): the best
+/* Lookahead of the pass search (0..16 candidate sets; default 4, and 8 for
+ * plans on 28 qubits or more): the best
  * candidates of each pass are tried with the pass that would follow them, and
  * the pair that absorbs the most gates decides (~2 % fewer passes on random
  * circuits, ~12 % on first-order Trotter circuits, for ~2x the search time).
