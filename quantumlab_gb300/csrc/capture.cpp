@@ -20,12 +20,14 @@
 #include "quest_gb300.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <mutex>
+#include <thread>
 #include <unordered_map>
 
 namespace qg {
@@ -43,6 +45,15 @@ struct Capture {
     // a repeated circuit, or new angles) takes its passes without a search.
     FusedPlan* shape = nullptr;
     long long shapeReuses = 0;
+    long long shapeId = 0;        // counts the shapes searched
+    // A search of the current shape with lookahead 8 on a host thread (at
+    // most one at a time; registers of 26 qubits or more): a flush plans a
+    // new shape without lookahead, which is ~2 % more passes but half the
+    // search time, and the flushes after take the better passes once found.
+    std::thread better;
+    std::atomic<bool> betterDone{false};
+    FusedPlan* betterPlan = nullptr;
+    long long betterShapeId = -1;
 };
 
 namespace {
@@ -66,6 +77,42 @@ int defaultMode() {
 Capture* find(const double* re) {
     auto it = g_caps.find(re);
     return it == g_caps.end() ? nullptr : it->second;
+}
+
+// the background search's result, if finished: taken as the shape when it
+// is of the current shape and has fewer passes, else dropped
+void adoptBetter(Capture* c) {
+    if (!c->better.joinable() || !c->betterDone.load()) return;
+    c->better.join();
+    FusedPlan* bp = c->betterPlan;
+    c->betterPlan = nullptr;
+    if (bp && bp->compiled && c->shape && c->betterShapeId == c->shapeId && bp->maxFused == c->shape->maxFused &&
+        bp->passSets.size() < c->shape->passSets.size()) {
+        quest_gb300_planDestroy(c->shape);
+        c->shape = bp;
+    } else if (bp) {
+        quest_gb300_planDestroy(bp);
+    }
+}
+
+// start the background search of the current shape (none running)
+void startBetter(Capture* c) {
+    if (c->better.joinable() || !c->shape || c->n < 26) return;
+    FusedPlan* bp = new FusedPlan();
+    bp->numQubits = c->shape->numQubits;
+    bp->maxFused = c->shape->maxFused;
+    bp->maxControls = c->shape->maxControls;
+    bp->beamWidth = c->shape->beamWidth;
+    bp->lookahead = 8;
+    bp->searchOnly = true;
+    bp->gates = c->shape->gates;
+    c->betterPlan = bp;
+    c->betterShapeId = c->shapeId;
+    c->betterDone.store(false);
+    c->better = std::thread([c, bp]() {
+        compilePlan(*bp);
+        c->betterDone.store(true);
+    });
 }
 
 // position of each touched qubit inside the gate's matrix index
@@ -136,6 +183,7 @@ static void flushRecord(Capture* c, double* re, double* im) {
     // it runs once (a captured 100-step Trotter circuit took 412 ms with it,
     // 88 ms without)
     plan->lookahead = 0;
+    adoptBetter(c);
     const bool reused = c->shape && c->shape->maxFused == plan->maxFused && compilePlanLike(*plan, *c->shape);
     if (!reused) {
         // autotuned: the width with the lowest predicted time (the cost table
@@ -167,6 +215,8 @@ static void flushRecord(Capture* c, double* re, double* im) {
         plan->passes.clear();
         if (c->shape) quest_gb300_planDestroy(c->shape);
         c->shape = plan;
+        c->shapeId += 1;
+        startBetter(c);
     }
 }
 
@@ -198,6 +248,8 @@ void captureDrop(const double* re) {
         }
     }
     if (c) {
+        if (c->better.joinable()) c->better.join();
+        if (c->betterPlan) quest_gb300_planDestroy(c->betterPlan);
         if (c->q32) quest_gb300_destroyQuregF32(c->q32);
         if (c->shape) quest_gb300_planDestroy(c->shape);
         delete c;

@@ -504,6 +504,10 @@ void compilePlan(FusedPlan& plan) {
     plan.passSets = sets;
     plan.passControls = ctls;
     plan.passMembers = members;
+    if (plan.searchOnly) {
+        plan.compiled = true;                 // a structure for compilePlanLike
+        return;
+    }
     // the pass products are independent: a few host threads share them
     const size_t np = sets.size();
     plan.passes.resize(np);

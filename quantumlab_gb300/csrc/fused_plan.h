@@ -39,6 +39,7 @@ struct FusedPlan {
     int beamWidth = 16;         // sets kept per level of the pass search
     int maxControls = 0;        // control qubits a pass may use (0..3; see FusedPass)
     int lookahead = 4;          // candidate sets tried one pass ahead (0: the best set at once)
+    bool searchOnly = false;    // compilePlan finds the passes (passSets...) without their products
     std::vector<FusedGate> gates;
     std::vector<FusedPass> passes;
     // the search's result: per pass its qubit set and the indices of the

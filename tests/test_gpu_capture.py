@@ -262,6 +262,36 @@ def test_capture_speeds_up_a_26_qubit_circuit(gpulib):
     assert res[1][0] < res[0][0] / 3
 
 
+def test_capture_takes_the_background_search(gpulib):
+    """A new circuit shape is planned without lookahead; on registers of 26
+    qubits a host thread then searches it again with lookahead, and a later
+    flush of the same shape takes those passes when fewer: the second flush
+    of the 26-qubit circuit uses no more passes than the first and gives the
+    same state to FP32 precision."""
+    import time
+    L = gpulib
+    lib = L.lib
+    n = 26
+    ops = W.c2_circuit(n=n, layers=12, seed=9)
+    q = L.create(n)
+    assert lib.quest_gb300_setCapture(q, 1) == 0
+    f, g, p, ms = C.c_longlong(), C.c_longlong(), C.c_longlong(), C.c_double()
+    passes, states = [], []
+    for _ in range(2):
+        lib.initZeroState(q)
+        W.run_ops(L, q, ops)
+        lib.calcTotalProb(q)
+        states.append(L.amps(q).copy())
+        assert lib.quest_gb300_captureStats(q, C.byref(f), C.byref(g), C.byref(p), C.byref(ms)) == 0
+        passes.append(p.value - sum(passes))
+        time.sleep(1.0)                                # the background search ends
+    lib.quest_gb300_setCapture(q, 0)
+    L.destroy(q)
+    print(f"26q: passes {passes[0]} then {passes[1]}")
+    assert passes[1] <= passes[0]
+    assert np.max(np.abs(states[0] - states[1])) < 1e-6
+
+
 def test_capture_density_matrix_with_control_qubits(gpulib):
     """A 13-qubit noisy density matrix (a 26-qubit vector, so its plans take
     control qubits): gates doubled on (t, t + N), the three channels as
