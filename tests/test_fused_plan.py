@@ -296,6 +296,22 @@ def test_lookahead_pass_counts(lib):
     assert h0 <= 60 and h4 <= 52 and h4 < h0, (h0, h4)
 
 
+def test_plan_settings_validated(lib):
+    """The plan setters accept their documented ranges and refuse the rest
+    (and a null plan) with -1."""
+    L = lib
+    L.quest_gb300_planPassControls.restype = C.c_int
+    p = L.quest_gb300_planCreate(20, 6)
+    assert L.quest_gb300_planSetLookahead(p, 0) == 0 and L.quest_gb300_planSetLookahead(p, 16) == 0
+    assert L.quest_gb300_planSetLookahead(p, -1) == -1 and L.quest_gb300_planSetLookahead(p, 17) == -1
+    assert L.quest_gb300_planSetMaxControls(p, 0) == 0 and L.quest_gb300_planSetMaxControls(p, 3) == 0
+    assert L.quest_gb300_planSetMaxControls(p, 4) == -1 and L.quest_gb300_planSetMaxControls(p, -1) == -1
+    assert L.quest_gb300_planSetBeamWidth(p, 0) == -1
+    assert L.quest_gb300_planPassControls(p, 0, None) == -1          # not compiled
+    L.quest_gb300_planDestroy(p)
+    assert L.quest_gb300_planSetLookahead(None, 4) == -1 and L.quest_gb300_planSetMaxControls(None, 1) == -1
+
+
 def test_invalid_gates_rejected(lib):
     p = lib.quest_gb300_planCreate(4, 3)
     assert lib.quest_gb300_planAddControlledNot(p, 1, 1) == -1
