@@ -109,10 +109,15 @@ void startBetter(Capture* c) {
     c->betterPlan = bp;
     c->betterShapeId = c->shapeId;
     c->betterDone.store(false);
-    c->better = std::thread([c, bp]() {
-        compilePlan(*bp);
-        c->betterDone.store(true);
-    });
+    try {
+        c->better = std::thread([c, bp]() {
+            compilePlan(*bp);
+            c->betterDone.store(true);
+        });
+    } catch (...) {                               // no thread to be had: no background search
+        c->betterPlan = nullptr;
+        quest_gb300_planDestroy(bp);
+    }
 }
 
 // position of each touched qubit inside the gate's matrix index
