@@ -518,7 +518,13 @@ void compilePlan(FusedPlan& plan) {
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     const unsigned nt = (unsigned)std::min<size_t>({(size_t)std::min(hw, 16u), np, 1 + plan.gates.size() / 64});
     std::vector<std::thread> pool;
-    for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
+    for (unsigned t = 1; t < nt; ++t) {
+        try {
+            pool.emplace_back(work);
+        } catch (...) {                     // fewer threads: the work items are shared
+            break;
+        }
+    }
     work();
     for (auto& t : pool) t.join();
     plan.compiled = true;
@@ -548,7 +554,13 @@ bool compilePlanLike(FusedPlan& plan, const FusedPlan& structure) {
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     const unsigned nt = (unsigned)std::min<size_t>({(size_t)std::min(hw, 16u), np, 1 + plan.gates.size() / 64});
     std::vector<std::thread> pool;
-    for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
+    for (unsigned t = 1; t < nt; ++t) {
+        try {
+            pool.emplace_back(work);
+        } catch (...) {                     // fewer threads: the work items are shared
+            break;
+        }
+    }
     work();
     for (auto& t : pool) t.join();
     plan.compiled = true;

@@ -1506,7 +1506,13 @@ void* uploadPlanTC(const FusedPlan& plan) {
     };
     const unsigned nt = (unsigned)std::min<size_t>({(size_t)16, (size_t)std::max(1u, std::thread::hardware_concurrency()), np});
     std::vector<std::thread> pool;
-    for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
+    for (unsigned t = 1; t < nt; ++t) {
+        try {
+            pool.emplace_back(work);
+        } catch (...) {                     // fewer threads: the work items are shared
+            break;
+        }
+    }
     work();
     for (auto& t : pool) t.join();
     cudaMemcpy(dp->imageBuf, host, offset[np] * sizeof(float), cudaMemcpyHostToDevice);

@@ -496,7 +496,13 @@ void parallelFor(size_t jobs, unsigned threads, F fn) {
     };
     const unsigned nt = (unsigned)std::max<size_t>(1, std::min<size_t>(threads, jobs));
     std::vector<std::thread> pool;
-    for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
+    for (unsigned t = 1; t < nt; ++t) {
+        try {
+            pool.emplace_back(work);
+        } catch (...) {                     // fewer threads: the work items are shared
+            break;
+        }
+    }
     work();
     for (auto& t : pool) t.join();
 }
