@@ -3,6 +3,7 @@ vectors, written in one pass, must equal initStateFromAmps of their
 Kronecker product; prepared as |0>|v>|u>, the swap-test circuit run on it
 through the QuEST API gives P(0) = (1 + |<u|v>|^2) / 2."""
 import ctypes as C
+import time
 
 import numpy as np
 import pytest
@@ -71,4 +72,35 @@ def test_product_state_rejects_bad_registers(gpulib):
     assert L.lib.quest_gb300_initProductState(q, 2, (C.c_int * 2)(4, 3), dptr(np.ones(24)), None) == -1
     assert len(L.errors) == 2
     L.errors.clear()
+    L.destroy(q)
+
+
+def test_product_state_timing_against_kron_upload(gpulib):
+    """Wall time to prepare |v>|u> on 24 qubits (two 12-qubit registers):
+    the host Kronecker product uploaded with initStateFromAmps against one
+    initProductState call; both give the same state (printed; -s)."""
+    L = gpulib
+    rng = np.random.default_rng(12)
+    d, n = 12, 24
+    u, v = rng.normal(size=1 << d), rng.normal(size=1 << d)
+    u, v = u / np.linalg.norm(u), v / np.linalg.norm(v)
+    flat = np.ascontiguousarray(np.concatenate([u, v]))
+    regs = (C.c_int * 2)(d, d)
+    q = L.create(n)
+    times = {}
+    for side in ("kron", "product", "kron", "product"):       # second round timed
+        L.lib.syncQuESTEnv(L.env)
+        t0 = time.perf_counter()
+        if side == "kron":
+            L.set_amps(q, np.kron(v, u))
+        else:
+            assert L.lib.quest_gb300_initProductState(q, 2, regs, dptr(flat), None) == 0
+        L.lib.syncQuESTEnv(L.env)
+        times[side] = (time.perf_counter() - t0) * 1e3
+        if side == "kron":
+            want = L.amps(q)
+        else:
+            assert np.max(np.abs(L.amps(q) - want)) < 1e-15
+    print(f"\n{n} qubits from two {d}-qubit vectors: kron + initStateFromAmps {times['kron']:.1f} ms, "
+          f"initProductState {times['product']:.3f} ms ({times['kron'] / times['product']:.0f}x)")
     L.destroy(q)

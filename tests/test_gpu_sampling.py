@@ -6,6 +6,7 @@ the first.  With the same seed the sampler must give the same outcome codes
 and leave the MT19937 stream at the same position.  Two measured qubits are
 certain (|0> and |1>), which QuEST resolves without a draw."""
 import ctypes as C
+import time
 
 import numpy as np
 import pytest
@@ -82,4 +83,46 @@ def test_sampler_frequencies_follow_the_outcome_probabilities(gpulib):
     freq = np.bincount(np.array(out), minlength=8) / shots
     probs = L.calcProbOfAllOutcomes(q, [0, 3, 7])
     assert np.max(np.abs(freq - probs)) < 5 * np.sqrt(0.25 / shots)
+    L.destroy(q)
+
+
+def test_sampler_timing_against_the_lab_shot_loop(gpulib):
+    """Wall time of 64 shots of 5 qubits on a 24-qubit register: the lab's
+    loop (copyStateToGPU + one measure per qubit, every shot) against one
+    sampleMeasurements call; both draw the same outcomes (printed; -s)."""
+    L = gpulib
+    lib = L.lib
+    n, shots = 24, 64
+    qubits = [0, 5, 11, 17, 23]
+    q = L.create(n)
+    lib.initZeroState(q)
+    W.run_ops(L, q, W.c2_circuit(n=n, layers=2, seed=5))
+    lib.copyStateFromGPU(q)
+    times = {}
+    codes = {}
+    for side in ("loop", "sampler"):
+        L.seed([21])
+        lib.syncQuESTEnv(L.env)
+        t0 = time.perf_counter()
+        if side == "loop":
+            got = []
+            for shot in range(shots):
+                if shot:
+                    lib.copyStateToGPU(q)
+                code = 0
+                for j, t in enumerate(qubits):
+                    code |= lib.measure(q, t) << j
+                got.append(code)
+        else:
+            out = (C.c_int * shots)()
+            qs = (C.c_int * len(qubits))(*qubits)
+            assert lib.quest_gb300_sampleMeasurements(q, qs, len(qubits), shots, out) == 0
+            got = list(out)
+        lib.syncQuESTEnv(L.env)
+        times[side] = (time.perf_counter() - t0) * 1e3
+        codes[side] = got
+        lib.copyStateToGPU(q)
+    assert codes["sampler"] == codes["loop"]
+    print(f"\n{n} qubits, {shots} shots of {len(qubits)} qubits: lab loop {times['loop']:.1f} ms, "
+          f"sampler {times['sampler']:.2f} ms ({times['loop'] / times['sampler']:.0f}x)")
     L.destroy(q)
