@@ -34,6 +34,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "fused-FP32 vs plain-FP64 gate GB/s at 30q (1-F≤1e-6); batched swap tests/s"
 FALLBACK_HBM = 6800.0
+# operand forms of the pipelined tensor-core kernel (setTensorCorePrecision)
+# and their MMA terms per product
+PREC_NAMES = {0: "split-TF32", 1: "split-BF16", 2: "split-FP16"}
+PREC_TERMS = {0: 3, 1: 4, 2: 3}
 
 
 def peaks():
@@ -243,14 +247,14 @@ def run_gpu(args, rank, world):
     L.destroy(qe)
 
     # ---- fused FP32 engine (the headline) --------------------------------
-    prec = 0 if args.precision == "tf32" else 1
-    pname = "split-TF32" if prec == 0 else "split-BF16"
+    prec = {"tf32": 0, "bf16": 1, "fp16": 2}[args.precision]
+    pname = PREC_NAMES[prec]
     lib.quest_gb300_setTensorCorePrecision(prec)
     # the autotuner: per-pass costs and the fastest tensor-core variant of
     # every (width, target layout) class, for both operand forms, then the
     # fusion width with the lowest predicted time
     t0 = time.perf_counter()
-    for pr in (1 - prec, prec):
+    for pr in ((1 - prec, prec) if prec < 2 else (prec,)):
         lib.quest_gb300_setTensorCorePrecision(pr)
         lib.quest_gb300_autotune(n)
     tune_s = time.perf_counter() - t0
@@ -392,10 +396,13 @@ def run_gpu(args, rank, world):
         L.destroy(qdf)
 
     # ---- the same plan with the pipelined kernel's other operands ---------
-    # (3-term split-TF32 is the default; 4-term split-BF16 is the other)
-    other = None
+    # (3-term split-TF32 is the default; 4-term split-BF16 and 3-term
+    # split-FP16 are the others)
+    others = {}
     dom_idx = [i for i in range(npass) if keys[i] == dom_name]
-    if lib.quest_gb300_setTensorCorePrecision(1 - prec) == 0:
+    for opr in (pr for pr in (0, 1, 2) if pr != prec):
+        if lib.quest_gb300_setTensorCorePrecision(opr) != 0:
+            continue
         fused_step()                                   # warm-up
         tf_pass = [0.0] * npass
         lib.quest_gb300_setPassEvents(1)
@@ -410,13 +417,15 @@ def run_gpu(args, rank, world):
         tf_dom = sum(tf_pass[i] for i in dom_idx) / args.steps / max(1, len(dom_idx))
         other = {"ms_per_circuit": round(tf_ms, 2), "gbs": round(alg_bytes / (tf_ms / 1e3) / 1e9, 1),
                  "dominant_kernel_avg_ms": round(tf_dom, 4),
-                 "note": "same plan; the applier choice of this precision may differ per pass"}
+                 "note": "same plan; the applier choice of this precision may differ per pass"
+                         + ("; fixed per-width kernel defaults (not tuned)" if opr == 2 else "")}
         if plain_ms:
             err = C.c_double(0)
             other["one_minus_fidelity"] = lib.quest_gb300_compareF32(q32, q64, C.byref(err))
             other["max_amp_err"] = err.value
             other["speedup_vs_plain"] = round(plain_ms / tf_ms, 2)
-        lib.quest_gb300_setTensorCorePrecision(prec)
+        others["fused_fp32_" + PREC_NAMES[opr].lower().replace("-", "_")] = other
+    lib.quest_gb300_setTensorCorePrecision(prec)
 
     # ---- the same circuit at the other fusion widths ---------------------
     # (k = 4, 5 and the headline's 6 against the per-gate FP64 engine)
@@ -493,18 +502,18 @@ def run_gpu(args, rank, world):
     if "kApplyTC2" in dom_name:
         kd = int(dom_name.split("<")[1].split(",")[0])
         alg_flops = 8.0 * (1 << kd) * (1 << n)
-        terms = 3 if prec == 0 else 4
+        terms = PREC_TERMS[prec]
         tensor_rates = {"k": kd, "algorithmic_flops_per_launch": alg_flops,
                         "algorithmic_tflops": round(alg_flops / (dom_avg / 1e3) / 1e12, 1),
                         "executed_tflops": round(terms * alg_flops / (dom_avg / 1e3) / 1e12, 1),
-                        "executed_form": f"{terms} MMA terms ({'split-TF32' if prec == 0 else 'split-BF16'})"}
-    if other:
+                        "executed_form": f"{terms} MMA terms ({pname})"}
+    for other in others.values():
         other["dominant_kernel_frac"] = round(pass_bytes / (other["dominant_kernel_avg_ms"] / 1e3) / 1e9 / peak, 4)
     traffic = tensor_pct = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         prof = json.load(open(tp))
-        kname = dom_name.split(" ")[0] + ((" tf32" if prec == 0 else " bf16") if "kApplyTC2" in dom_name else "")
+        kname = dom_name.split(" ")[0] + ((" " + ("tf32", "bf16", "fp16")[prec]) if "kApplyTC2" in dom_name else "")
         t = prof.get(kname)
         if t:
             traffic = t * (1 << n)
@@ -512,7 +521,10 @@ def run_gpu(args, rank, world):
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s (per-gate FP64 algorithmic bytes)",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": ("f32 state (3-term split-TF32 tensor-core products, FP32 accumulation; 4-term split-BF16 arm in fused_fp32_split_bf16; FP64 fusion products and reductions)" if prec == 0 else "f32 state (4-term split-BF16 tensor-core products, FP32 accumulation; 3-term split-TF32 arm in fused_fp32_split_tf32; FP64 fusion products and reductions)"),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": (f"f32 state ({PREC_TERMS[prec]}-term {pname} tensor-core products, FP32 accumulation; "
+                  + "; ".join(f"{PREC_TERMS[o]}-term {PREC_NAMES[o]} arm in fused_fp32_{PREC_NAMES[o].lower().replace('-', '_')}"
+                              for o in (0, 1, 2) if o != prec)
+                  + "; FP64 fusion products and reductions)"),
         "data": "synthetic (seeded Haar/CPhase-matching/CNOT-brickwork circuit)",
         "config": {"workload": f"{n}-qubit random circuit, {args.layers} layers: fused FP32 engine (k<={k}) vs plain FP64 per-gate engine",
                    "qubits": n, "layers": args.layers, "gates_per_circuit": len(ops), "fusion_max_qubits": k,
@@ -529,7 +541,7 @@ def run_gpu(args, rank, world):
                        "plan_compile_s": round(plan_s, 3), "one_minus_fidelity": one_minus_f,
                        "max_amp_err": max_amp_err,
                        "kernels": {name: {"passes": c, "ms_per_circuit": round(t, 2)} for name, (c, t) in groups.items()}},
-        ("fused_fp32_split_bf16" if prec == 0 else "fused_fp32_split_tf32"): other,
+        **others,
         "fused_fp32_by_width": widths or None,
         "fused_fp32_without_control_qubits": without_ctl,
         "autotune": autotune,
@@ -949,7 +961,7 @@ def main():
     ap.add_argument("--cpu-sample-ops", type=int, default=60)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fusion", type=int, default=6, help="max qubits per fused pass (1..6)")
-    ap.add_argument("--precision", default="tf32", choices=["tf32", "bf16"],
+    ap.add_argument("--precision", default="tf32", choices=["tf32", "bf16", "fp16"],
                     help="operands of the pipelined tensor-core kernel for the headline arm")
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--skip-widths", action="store_true", help="skip the k = 4 and k = 5 fused arms")

@@ -168,7 +168,13 @@ void quest_gb300_setTensorCoreKernel(int version);
 /* Operands of the pipelined tensor-core kernel: 0 = 3-term split-TF32
  * (X, G in two TF32 parts; Xh.Gh + Xl.Gh + Xh.Gl), the default; 1 = 4-term
  * split-BF16 (X in two BF16 parts, G in three; Xh.Gh + Xl.Gh + Xh.Gl +
- * Xh.Gll).  Both accumulate in FP32.  Returns 0, or -1 for another mode. */
+ * Xh.Gll); 2 = 3-term split-FP16 (as split-TF32, with FP16 parts of the same
+ * 11-bit precision at twice the MMA rate; X and each matrix block are scaled
+ * by powers of two before the split, X's from the norm the previous pass of
+ * a plan application measured, else 2^14, so the first tensor-core pass of
+ * an application needs amplitudes of modulus below 3.99: a non-finite output
+ * is reported as an error, the state is then lost).  All accumulate in FP32.
+ * Returns 0, or -1 for another mode. */
 int quest_gb300_setTensorCorePrecision(int mode);
 int quest_gb300_getTensorCorePrecision(void);
 /* How the pipelined tensor-core kernels stage state tiles in shared memory:
@@ -192,6 +198,10 @@ int quest_gb300_checkTileCoverage(int numQubits, const int* targets, int numTarg
  * 16-byte aligned, inside the image block and disjoint from the other parts.
  * Returns 0 when all hold, else 1. */
 int quest_gb300_checkImageLayouts(void);
+/* The host rounding that builds split-FP16 operand images: each value to the
+ * nearest IEEE binary16 (ties to even; infinity beyond 65504), as bit
+ * patterns.  Returns 0, or -1 for a negative count or a missing array. */
+int quest_gb300_roundHalf(const double* values, unsigned short* out, int count);
 double quest_gb300_calcTotalProbF32(void* qureg32);
 double quest_gb300_calcProbOfOutcomeF32(void* qureg32, int measureQubit, int outcome);
 /* 1 - |<ref|q>|^2 / (<ref|ref><q|q>) against an FP64 state vector; writes the

@@ -73,7 +73,7 @@ void loadCache() {
         int n = 0, prec = 0, k = 0, lay = 0, chars = 0;
         double v = 0;
         if (sscanf(key.c_str(), "n%d_p%d_k%d_l%d%n", &n, &prec, &k, &lay, &chars) == 4 && k >= 1 && k <= 6 &&
-            lay >= 0 && lay < 3 && (prec == 0 || prec == 1) && sscanf(s.c_str() + end + 1, " : %lf", &v) == 1 && v > 0) {
+            lay >= 0 && lay < 3 && prec >= 0 && prec <= 2 && sscanf(s.c_str() + end + 1, " : %lf", &v) == 1 && v > 0) {
             CostTable& t = g_tables[{n, prec}];
             if (key.compare(chars, std::string::npos, "_v") == 0) {
                 t.ver[k][lay] = (int)v;

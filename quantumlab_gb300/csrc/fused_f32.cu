@@ -56,6 +56,7 @@ bool setTensorCoreStaging(int mode);
 int tensorCoreStaging();
 int tcCheckCoverage(int n, const std::vector<int>& targets, const std::vector<int>& controls);
 int tcCheckImageLayouts();
+void tcRoundHalf(const double* v, uint16_t* out, int count);
 bool tensorCoresEnabled();
 int tcKernelFor(const FusedPass& pass, int n);
 float* f32re(QuregF32& q) { return q.re; }
@@ -519,13 +520,16 @@ int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPas
         if (e) {
             // codes: 1 copy of G (direct-load kernel), 2 its MMAs; pipelined
             // kernel: 3 loaders waiting for a free stage, 4 epilogue waiting for
-            // an accumulator, 5 MMA issuer waiting for operands or a free accumulator
+            // an accumulator, 5 MMA issuer waiting for operands or a free
+            // accumulator, 6 a non-finite split-FP16 output
             static const char* const what[] = {
                 "", "tensor-core applier: operand staging timed out", "tensor-core applier: MMA completion timed out",
                 "tensor-core applier: loaders timed out waiting for a free operand stage",
                 "tensor-core applier: epilogue timed out waiting for an accumulator",
-                "tensor-core applier: MMA issue timed out waiting for operands or an accumulator"};
-            invalidQuESTInputError(e >= 1 && e <= 5 ? what[e] : "tensor-core applier: timed out", "applyPlanF32");
+                "tensor-core applier: MMA issue timed out waiting for operands or an accumulator",
+                "tensor-core applier: split-FP16 operands out of range (an amplitude of modulus 3.99 or more, or a "
+                "non-finite state); use split-TF32"};
+            invalidQuESTInputError(e >= 1 && e <= 6 ? what[e] : "tensor-core applier: timed out", "applyPlanF32");
             return -1;
         }
     }
@@ -557,6 +561,12 @@ int quest_gb300_getTensorCorePrecision(void) { return qg::tensorCorePrecision();
 int quest_gb300_setTensorCoreStaging(int mode) { return qg::setTensorCoreStaging(mode) ? 0 : -1; }
 
 int quest_gb300_checkImageLayouts(void) { return qg::tcCheckImageLayouts(); }
+
+int quest_gb300_roundHalf(const double* values, unsigned short* out, int count) {
+    if (count < 0 || (count > 0 && (!values || !out))) return -1;
+    qg::tcRoundHalf(values, reinterpret_cast<uint16_t*>(out), count);
+    return 0;
+}
 
 int quest_gb300_checkTileCoverage(int numQubits, const int* targets, int numTargets, const int* controls, int numControls) {
     if (!targets || numTargets < 4 || numTargets > 6 || numControls < 0 || numControls > 3 || (numControls && !controls))

@@ -21,6 +21,15 @@
 //         Gr = Gh + Gl + Gll (three BF16 parts, ~2^-24), Out = Xh.Gh + Xl.Gh
 //         + Xh.Gl + Xh.Gll accumulated in FP32 by kind::f16 MMAs, which run
 //         at twice the TF32 rate;
+//       - 3-term split-FP16: the split-TF32 scheme with FP16 parts (the same
+//         11-bit significands, so the same ~2^-22 precision) on kind::f16
+//         MMAs at twice the TF32 rate.  FP16's exponent range is met by
+//         power-of-two scales: X is multiplied by 2^e before the split, with
+//         e from the input's norm where a previous pass of the chain measured
+//         it, else 14 (amplitudes of modulus below ~3.99 fit), and each
+//         matrix block by the 2^s its operand image records (|G| * 2^s <=
+//         2^14); the epilogue multiplies by 2^-(e + s), all exact.  A
+//         non-finite output (an amplitude out of range) sets error code 6;
 //   * kApplyTC (setTensorCoreKernel(1)): the direct-load kernel, split-TF32.
 //     Each thread owns one tile column and loads its 2D values straight from
 //     global memory (the 32 lanes of a warp read 32 consecutive amplitudes),
@@ -33,9 +42,11 @@
 #include "qg_internal.h"
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <mutex>
 #include <cstdint>
 #include <cstring>
@@ -56,6 +67,13 @@ constexpr int kTile = 128;              // groups per tile = MMA M = TMEM lanes
 constexpr int kThreadsTC = 128;         // 4 warps: one TMEM lane quarter each
 // every wait gives up after this much wall-clock time (read from %globaltimer)
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;   // 1 s
+
+// Operand precision of kApplyTC2: 3-term split-TF32, 4-term split-BF16 or
+// 3-term split-FP16.  Split-FP16 scales X by 2^kF16XExp before its split
+// unless the input's norm is known (f16XExp).
+constexpr int kPrecTF32 = 0, kPrecBF16 = 1, kPrecF16 = 2;
+constexpr int kF16XExp = 14;
+constexpr int kF16GMaxExp = 14;        // the largest |G| entry * 2^s stays <= 2^14
 
 __device__ __forceinline__ unsigned long long globalTimerNs() {
     unsigned long long t;
@@ -163,9 +181,10 @@ __device__ __forceinline__ void mmaTF32(uint32_t dT, uint32_t aT, uint64_t bDesc
         "r"(aT), "l"(bDesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
-// D[tmem] (+)= A[tmem] * B[smem desc], A and B bf16 (two per 32-bit TMEM
-// column, the lower K index in the low half), D f32
-__device__ __forceinline__ void mmaBF16(uint32_t dT, uint32_t aT, uint64_t bDesc, uint32_t idesc, uint32_t accumulate) {
+// D[tmem] (+)= A[tmem] * B[smem desc], kind::f16: A and B both bf16 or both
+// f16, as the instruction descriptor says (two per 32-bit TMEM column, the
+// lower K index in the low half), D f32
+__device__ __forceinline__ void mma16(uint32_t dT, uint32_t aT, uint64_t bDesc, uint32_t idesc, uint32_t accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
         " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}" ::"r"(dT),
@@ -192,6 +211,23 @@ __host__ __device__ constexpr uint32_t idescTF32(int M, int N) {
 // instruction descriptor, kind::f16: D f32, A/B bf16, both K-major
 __host__ __device__ constexpr uint32_t idescBF16(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// instruction descriptor, kind::f16: D f32, A/B f16, both K-major
+__host__ __device__ constexpr uint32_t idescF16(int M, int N) {
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Split-FP16 of two consecutive K elements (already scaled into FP16's
+// range): hi = both rounded to the nearest FP16 (packed, the first in the low
+// half), lo = the exact remainders rounded to the nearest FP16.  x = hi + lo
+// to ~2^-22 relative, unbiased, or to 2^-25 absolute below FP16's normal range.
+__device__ __forceinline__ void splitF16x2(float x0, float x1, uint32_t& hi, uint32_t& lo) {
+    const __half2 h = __floats2half2_rn(x0, x1);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn(x0 - hf.x, x1 - hf.y);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
 // Split-BF16 of two consecutive K elements: hi = both rounded to the nearest
@@ -235,7 +271,10 @@ __device__ __forceinline__ void splitTF32(float x, uint32_t& hi, uint32_t& lo) {
 //            f = out / (in * scale^2) predicts this pass's own (the drift of
 //            the tensor cores' accumulation is systematic);
 //   corrTarget  when this pass continues a chain of unitary passes, the input
-//            norm T of the chain's first pass, else null.
+//            norm T of the chain's first pass, else null;
+//   boundSq  sum |x|^2 of this pass's input when a previous tensor-core pass
+//            of the chain measured it (its output), else null: it bounds every
+//            |x|, and split-FP16 takes the scale of X from it.
 // The scale makes this pass's output norm T (chained: its input norm is the
 // previous output, so scale^2 = T / (out * f)) or, unchained, its own input
 // norm (scale^2 = 1 / f).  With a constant drift every output after the first
@@ -248,6 +287,7 @@ struct NormLinks {
     const double* corrOut;
     const double* corrScaleSq;
     const double* corrTarget;
+    const double* boundSq;
 };
 // the scale minus one (kept exact to FP32 relative precision)
 __device__ __forceinline__ float driftCorrection(const NormLinks& nl) {
@@ -259,6 +299,18 @@ __device__ __forceinline__ float driftCorrection(const NormLinks& nl) {
 // written once per launch, by the calling thread when `writer`
 __device__ __forceinline__ void recordScale(const NormLinks& nl, float sm1, bool writer) {
     if (nl.scaleSq && writer) *nl.scaleSq = (1.0 + (double)sm1) * (1.0 + (double)sm1);
+}
+// Split-FP16: the exponent e of X's scale 2^e.  With a bound B on every |x|,
+// the largest e with B * 2^e <= 2^15 (all of FP16's 11 bits for the lo parts
+// of the smallest amplitudes; the tensor cores take no FP16 subnormals),
+// else kF16XExp (|x| below ~3.99).
+__device__ __forceinline__ int f16XExp(const NormLinks& nl) {
+    if (!nl.boundSq) return kF16XExp;
+    const double b = *nl.boundSq;
+    if (!(b > 0.0) || !(b < 1.0e300)) return kF16XExp;
+    int e = 0;
+    frexp(sqrt(b), &e);                                  // sqrt(b) < 2^e
+    return min(40, max(-40, 15 - e));
 }
 
 __device__ __forceinline__ double warpSumD(double v) {
@@ -507,31 +559,30 @@ struct TC2Params {
     uint64_t ctrlImageStride;
 };
 
-// Operand precision of kApplyTC2: 3-term split-TF32 or 4-term split-BF16.
-constexpr int kPrecTF32 = 0, kPrecBF16 = 1;
 
 // Layout of kApplyTC2<KQ, LG, EG, LS, PR>, used by the kernel and its
 // launcher.  Shared memory: the parts of G (split-TF32: Gh, Gl in FP32 words,
-// G to ~2^-22; split-BF16: Gh, Gl, Gll in BF16, G to ~2^-24), the loader row
+// G to ~2^-22; split-BF16: Gh, Gl, Gll in BF16, G to ~2^-24; split-FP16: Gh,
+// Gl in FP16, G to ~2^-22), the loader row
 // stages and the epilogue buffers.  At k = 6, G is the compact real form
 // [-Im G; Re G; Im G] (192 rows x 64 K).  The B operand of the K-chunk of the
 // real parts of X is rows 64..191 ([Re; Im]).  That of the imaginary parts is
 // rows 0..127 ([-Im; Re]).  Loader row buffers: XST stages per loader warp
 // (three at k = 4, two at k >= 5).  TMEM: NST operand stages (Xh then Xl; one
-// TF32 or two BF16 per column), then two accumulators of N columns.
+// TF32 or two 16-bit values per column), then two accumulators of N columns.
 template <int KQ, int LG, int EG, int LS, int PR>
 struct TC2Shape {
     static constexpr int D = 1 << KQ, K = 2 * D, N = 2 * D;
     static constexpr int TILE = 1 << (KQ + kTileBitsC);       // amplitudes per plane per tile
-    static constexpr int ESZ = (PR == kPrecBF16) ? 2 : 4;     // bytes per operand entry
-    // K chunks per tile: chunks of <= 64 (BF16) or <= 32 (TF32) K entries,
+    static constexpr int ESZ = (PR != kPrecTF32) ? 2 : 4;     // bytes per operand entry
+    // K chunks per tile: chunks of <= 64 (BF16, FP16) or <= 32 (TF32) K entries,
     // so that four operand stages fit beside the two accumulators
-    static constexpr int NCH = (PR == kPrecBF16) ? ((KQ == 6) ? 2 : 1) : ((KQ == 6) ? 4 : (KQ == 5) ? 2 : 1);
+    static constexpr int NCH = (PR != kPrecTF32) ? ((KQ == 6) ? 2 : 1) : ((KQ == 6) ? 4 : (KQ == 5) ? 2 : 1);
     static constexpr int KC = K / NCH;                        // K entries per chunk
     // Parts: the positions a warp stages at once (<= 1024).  k <= 5: the two
     // planes; k = 6: the halves of a plane by the top target bit.  A chunk is
     // one part (a plane at k = 5 in TF32; a plane half at k = 6 in TF32) or
-    // two (both planes at k <= 5; both halves of a plane at k = 6 in BF16).
+    // two (both planes at k <= 5; both halves of a plane at k = 6 in BF16 or FP16).
     static constexpr int PART = (KQ == 6) ? TILE / 8 : TILE / 4;   // positions per warp per part (<= 1024)
     static constexpr int PPC = ((KQ == 6) ? (NCH == 2) : (NCH == 1)) ? 2 : 1;   // parts per chunk
     static constexpr int JPP = KC / PPC;                      // K entries (matrix indices) per part
@@ -636,7 +687,10 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                                                                   int* __restrict__ errFlag, const NormLinks nl,
                                                                   const __grid_constant__ TC2Params<KQ> p) {
     using S = TC2Shape<KQ, LG, EG, LS, PR>;
-    constexpr bool BF = (PR == kPrecBF16);
+    constexpr bool BF = (PR == kPrecBF16), F16 = (PR == kPrecF16), H16 = BF || F16;
+    // split-FP16: X's scale 2^xe before the split (the epilogue undoes it)
+    const int xe = F16 ? f16XExp(nl) : 0;
+    const float kXs = __int_as_float((127 + xe) << 23);
     // this CTA's register of a batch and control value, and its place among
     // the CTAs of that pair
     const uint32_t cta = blockIdx.x % p.ctasPerInst, ncta = p.ctasPerInst;
@@ -659,7 +713,7 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
     constexpr uint32_t kCols = kUsed <= 64 ? 64 : (kUsed <= 128 ? 128 : (kUsed <= 256 ? 256 : 512));
     static_assert(kUsed <= 512, "TMEM");
     constexpr uint32_t kLBO = 128;
-    constexpr uint32_t idesc = BF ? idescBF16(kTile, N) : idescTF32(kTile, N);
+    constexpr uint32_t idesc = BF ? idescBF16(kTile, N) : F16 ? idescF16(kTile, N) : idescTF32(kTile, N);
     constexpr int kEpiWarp0 = 4 * LG, kMmaWarp = 4 * (LG + EG);
     // loader groups split every chunk (S::SPLIT) or take alternate chunks
     static_assert(LS == 1 || LG == 2, "part-split loading needs two loader groups");
@@ -792,7 +846,7 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                 __syncwarp();                                    // ... and every lane's
             }
             // this group's K entries of the stage: [p0 JP, (p0 + PPG) JP); EPW per column
-            constexpr int EPW = BF ? 2 : 1;
+            constexpr int EPW = H16 ? 2 : 1;
             const uint32_t aH = tmem + laneSel + b * kStageCols + p0 * JP / EPW;
             const int chq = (int)(sq % NCH);
             const float* const cb = xr + colBase;
@@ -827,6 +881,8 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                                 if constexpr (WN) nrm = fmaf(xv[EPW * e + h], xv[EPW * e + h], nrm);
                             if constexpr (BF) {
                                 splitBF16x2(xv[2 * e], xv[2 * e + 1], hi[e], lo[e]);
+                            } else if constexpr (F16) {
+                                splitF16x2(xv[2 * e] * kXs, xv[2 * e + 1] * kXs, hi[e], lo[e]);
                             } else {
                                 hi[e] = tf32Bits(xv[e]);
                                 lo[e] = __float_as_uint(xv[e] - __uint_as_float(hi[e]));
@@ -846,6 +902,8 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                             }
                             if constexpr (BF) {
                                 splitBF16x2(x[0], x[EPW - 1], hi[e], lo[e]);
+                            } else if constexpr (F16) {
+                                splitF16x2(x[0] * kXs, x[EPW - 1] * kXs, hi[e], lo[e]);
                             } else {
                                 // hi = x rounded to TF32; lo = x - hi (exact), which the MMA
                                 // reads as its leading TF32 bits; lo takes both signs, so
@@ -900,6 +958,9 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
         bool ok = true;
         const float sm1 = driftCorrection(nl);
         recordScale(nl, sm1, blockIdx.x == 0 && et == 0);
+        // split-FP16: 2^-(xe + s), s the scale of this CTA's matrix block (its
+        // image records 2^-(14 + s) after the two parts)
+        const float unscale = F16 ? __ldg(gImage + 2 * kGW) * __int_as_float((127 + kF16XExp - xe) << 23) : 1.f;
         uint32_t tl = eg;
         double normOut = 0.0;
         TileWalker<KQ> walk;
@@ -936,7 +997,7 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
 #pragma unroll
                     for (int e = 0; e < JP; ++e) {
                         uint32_t& w = e < 16 ? va[e] : vb[e - 16];
-                        const float y0 = __uint_as_float(w);
+                        const float y0 = F16 ? __uint_as_float(w) * unscale : __uint_as_float(w);
                         const float y = fmaf(y0, sm1, y0);
                         nrmTile = fmaf(y, y, nrmTile);
                         w = __float_as_uint(y);
@@ -948,7 +1009,8 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                 } else {
 #pragma unroll
                     for (int e = 0; e < JP; ++e) {
-                        const float y0 = __uint_as_float(e < 16 ? va[e] : vb[e - 16]);
+                        const float y0 = F16 ? __uint_as_float(e < 16 ? va[e] : vb[e - 16]) * unscale
+                                             : __uint_as_float(e < 16 ? va[e] : vb[e - 16]);
                         const float y = fmaf(y0, sm1, y0);
                         nrmTile = fmaf(y, y, nrmTile);
                         cb[p.colJ[h * 32 + e]] = y;
@@ -970,6 +1032,9 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
             if (lane == 0) atomicExch(errFlag, 4);
             abortF = 1;
         }
+        // split-FP16: an input beyond FP16's range after scaling gave a
+        // non-finite output
+        if (F16 && !(normOut <= 1.0e300)) atomicExch(errFlag, 6);
         normOut = warpSumD(normOut);
         if (lane == 0 && nl.out) atomicAdd(nl.out, normOut);
     } else if (lane == 0) {
@@ -1016,13 +1081,22 @@ __global__ void __launch_bounds__((4 * (LG + EG) + 1) * 32, 1) kApplyTC2(float* 
                     // on the state); the dropped Xl.Gl is unbiased
 #pragma unroll
                     for (int ks = 0; ks < KC / 16; ++ks)
-                        mmaBF16(dT, aH + 8 * ks, dH + 16u * ks, idesc, (ch | ks) != 0);
+                        mma16(dT, aH + 8 * ks, dH + 16u * ks, idesc, (ch | ks) != 0);
 #pragma unroll
-                    for (int ks = 0; ks < KC / 16; ++ks) mmaBF16(dT, aL + 8 * ks, dH + 16u * ks, idesc, 1);
+                    for (int ks = 0; ks < KC / 16; ++ks) mma16(dT, aL + 8 * ks, dH + 16u * ks, idesc, 1);
 #pragma unroll
-                    for (int ks = 0; ks < KC / 16; ++ks) mmaBF16(dT, aH + 8 * ks, dL + 16u * ks, idesc, 1);
+                    for (int ks = 0; ks < KC / 16; ++ks) mma16(dT, aH + 8 * ks, dL + 16u * ks, idesc, 1);
 #pragma unroll
-                    for (int ks = 0; ks < KC / 16; ++ks) mmaBF16(dT, aH + 8 * ks, dLL + 16u * ks, idesc, 1);
+                    for (int ks = 0; ks < KC / 16; ++ks) mma16(dT, aH + 8 * ks, dLL + 16u * ks, idesc, 1);
+                } else if constexpr (F16) {
+                    // Xh.Gh + Xl.Gh + Xh.Gl (K = 16 per MMA), as split-TF32
+#pragma unroll
+                    for (int ks = 0; ks < KC / 16; ++ks)
+                        mma16(dT, aH + 8 * ks, dH + 16u * ks, idesc, (ch | ks) != 0);
+#pragma unroll
+                    for (int ks = 0; ks < KC / 16; ++ks) mma16(dT, aL + 8 * ks, dH + 16u * ks, idesc, 1);
+#pragma unroll
+                    for (int ks = 0; ks < KC / 16; ++ks) mma16(dT, aH + 8 * ks, dL + 16u * ks, idesc, 1);
                 } else {
                     // Xh.Gh + Xl.Gh + Xh.Gl (K = 8 per MMA)
 #pragma unroll
@@ -1108,6 +1182,34 @@ float bf16Value(uint16_t h) {
     return y;
 }
 
+// Nearest IEEE binary16 value (ties to even) of a double, rounded once:
+// below 2^-14 on the subnormal grid of 2^-24, else to 11 significant bits;
+// beyond the largest finite value (65504) ties and above give infinity.
+uint16_t hostF16RN(double v) {
+    const uint16_t sign = std::signbit(v) ? 0x8000u : 0u;
+    const double a = std::fabs(v);
+    if (std::isnan(v)) return 0x7E00u;
+    if (a >= 65520.0) return sign | 0x7C00u;
+    int e = 0;
+    std::frexp(a, &e);                                   // a in [2^(e-1), 2^e)
+    const int qe = std::max(e - 11, -24);                // exponent of the quantum
+    const double m = std::nearbyint(std::ldexp(a, -qe));   // a / quantum, exact, then rounded (ties even)
+    const double r = std::ldexp(m, qe);
+    if (r == 0.0) return sign;
+    if (r < 0x1p-14) return sign | (uint16_t)m;          // subnormal: the count of 2^-24
+    int re = 0;
+    std::frexp(r, &re);                                  // r in [2^(re-1), 2^re)
+    const int E = re - 1;                                // r = 2^E (1 + f / 1024)
+    const uint32_t f = (uint32_t)(std::ldexp(r, 10 - E) - 1024.0);
+    return sign | (uint16_t)(((E + 15) << 10) | f);
+}
+double f16Value(uint16_t h) {
+    const int ex = (h >> 10) & 31, man = h & 1023;
+    const double s = (h & 0x8000u) ? -1.0 : 1.0;
+    if (ex == 31) return man ? std::nan("") : s * INFINITY;
+    return s * (ex == 0 ? std::ldexp((double)man, -24) : std::ldexp((double)(1024 + man), ex - 25));
+}
+
 template <int KQ>
 bool launchTC(float* re, float* im, int n, const FusedPass& pass, const float* img, int* errFlag, const NormLinks& nl,
               cudaStream_t st) {
@@ -1157,18 +1259,19 @@ bool colWords4(const TC2Params<KQ>& p) {
 
 // Parts of an image: what the split-TF32 pipelined kernels read (the full
 // real form at k <= 5, the compact form at k = 6), what the split-BF16 ones
-// read, and the full TF32 form at every k for the direct-load kernel.
-constexpr int kPartTF32 = 1, kPartBF16 = 2, kPartDirect = 4;
+// read, the full TF32 form at every k for the direct-load kernel, and what the
+// split-FP16 ones read.
+constexpr int kPartTF32 = 1, kPartBF16 = 2, kPartDirect = 4, kPartF16 = 8;
 constexpr size_t kNoPart = ~(size_t)0;
 
 // Layout of the operand image of one matrix block of a k-qubit pass holding
 // `parts`: float offsets of the full TF32 real form (hi, lo), of the three
-// BF16 parts and of the compact TF32 form (hi, lo), kNoPart where absent, and
-// the block's size; every part starts on a 16-byte boundary (the kernels copy
-// them with cp.async.bulk).  The part contents are described at
-// buildImageBlock.
+// BF16 parts, of the compact TF32 form (hi, lo) and of the two FP16 parts
+// with their scale, kNoPart where absent, and the block's size; every part
+// starts on a 16-byte boundary (the kernels copy them with cp.async.bulk).
+// The part contents are described at buildImageBlock.
 struct ImageLayout {
-    size_t full = kNoPart, bf16 = kNoPart, compact = kNoPart, stride = 0;
+    size_t full = kNoPart, bf16 = kNoPart, compact = kNoPart, f16 = kNoPart, stride = 0;
 };
 static ImageLayout imageLayout(int k, int parts) {
     ImageLayout L;
@@ -1187,6 +1290,10 @@ static ImageLayout imageLayout(int k, int parts) {
     if ((parts & kPartTF32) && k == 6) {
         L.compact = at;
         at += 2 * 3 * D * D;
+    }
+    if (parts & kPartF16) {
+        L.f16 = at;
+        at += bEntries + 4;                              // two FP16 parts, then 16 bytes: the unscale factor
     }
     L.stride = (at + 3) & ~(size_t)3;
     return L;
@@ -1352,7 +1459,7 @@ int g_tcStaging = 0;      // loader staging of the pipelined kernels: 0 cp.async
 // tuned pipelined variant (2..5, 0 = none) by register size, precision,
 // width k and target layout (tuneLayout)
 constexpr int kTuneMaxN = 40;
-int g_tcTuned[kTuneMaxN + 1][2][7][3] = {};
+int g_tcTuned[kTuneMaxN + 1][3][7][3] = {};
 
 }  // namespace
 
@@ -1361,7 +1468,9 @@ int g_tcTuned[kTuneMaxN + 1][2][7][3] = {};
 // [[Re, -Im], [Im, Re]] as TF32 hi, lo (canonical K-major, N = K = 2^(k+1));
 // its three BF16 parts (at k = 6 the compact form [-Im G; Re G; Im G], 3D
 // rows and D K columns, in 8 x 8 core blocks); the compact form as TF32 hi,
-// lo (K-major).
+// lo (K-major); the two FP16 parts of 2^s times the BF16 parts' form, with
+// 2^s the largest power of two for which every |entry| * 2^s <= 2^14, and
+// after them the float 2^-(14 + s) the split-FP16 epilogue multiplies by.
 static void buildImageBlock(const FusedPass& pass, int block, float* img, int parts) {
     const int k = (int)pass.targets.size();
     const int D = 1 << k, K = 2 * D, N = 2 * D;
@@ -1412,6 +1521,32 @@ static void buildImageBlock(const FusedPass& pass, int block, float* img, int pa
             bl[at] = l;
             bll[at] = hostBF16RN((float)(r1 - (double)bf16Value(l)));
         }
+    if (lay.f16 != kNoPart) {
+        double mx = 0.0;
+        for (size_t e = 0; e < (size_t)D * D; ++e) mx = std::max(mx, std::max(std::fabs(M[e].real()), std::fabs(M[e].imag())));
+        int sc = 24;                                     // all-zero block: any scale
+        if (mx > 0.0) {
+            int e2 = 0;
+            std::frexp(mx, &e2);                         // mx in [2^(e2-1), 2^e2)
+            sc = std::min(24, std::max(-24, kF16GMaxExp - e2));
+        }
+        uint16_t* fh = reinterpret_cast<uint16_t*>(img + lay.f16);
+        uint16_t* fl = fh + bEntries;
+        for (int r = 0; r < bRows; ++r)
+            for (int j = 0; j < bK; ++j) {
+                const int rr = (k == 6 && r >= D) ? r - D : r, jj = (k == 6 && r < D) ? D + j : j;
+                const cplx g = M[(size_t)(rr % D) * D + (jj % D)];
+                const double v = (rr < D) ? ((jj < D) ? g.real() : -g.imag()) : ((jj < D) ? g.imag() : g.real());
+                const double vs = std::ldexp(v, sc);             // exact
+                const uint16_t h = hostF16RN(vs);
+                const size_t at = (size_t)(r / 8) * (bK / 8) * 64 + (size_t)(j / 8) * 64 + (r % 8) * 8 + (j % 8);
+                fh[at] = h;
+                fl[at] = hostF16RN(vs - f16Value(h));
+            }
+        float* const tail = img + lay.f16 + bEntries;
+        tail[0] = std::ldexp(1.0f, -(kF16XExp + sc));
+        tail[1] = tail[2] = tail[3] = 0.f;
+    }
     if (compact) {
         // the compact TF32 form for the split-TF32 pipelined kernel
         std::vector<float> ch((size_t)3 * D * D), cl((size_t)3 * D * D);
@@ -1435,7 +1570,8 @@ static void buildImage(const FusedPass& pass, float* img, int parts) {
 
 // the image parts the kernels of the current precision and kernel choice read
 static int currentParts() {
-    return (g_tcPrecision == kPrecBF16 ? kPartBF16 : kPartTF32) | (g_tcVersion == 1 ? kPartDirect : 0);
+    const int form = g_tcPrecision == kPrecBF16 ? kPartBF16 : g_tcPrecision == kPrecF16 ? kPartF16 : kPartTF32;
+    return form | (g_tcVersion == 1 ? kPartDirect : 0);
 }
 
 std::mutex g_stageMutex;
@@ -1527,6 +1663,10 @@ void* uploadPlanTC(const FusedPlan& plan) {
 size_t tcImageFloats(int k, int parts) { return imageLayout(k, parts).stride; }
 void tcBuildImage(const FusedPass& pass, float* img, int parts) { buildImageBlock(pass, 0, img, parts); }
 int tcImageParts() { return currentParts(); }
+// the host's FP16 rounding of split-FP16 operand images (nearest, ties to even)
+void tcRoundHalf(const double* v, uint16_t* out, int count) {
+    for (int i = 0; i < count; ++i) out[i] = hostF16RN(v[i]);
+}
 // whether a plan's images hold the parts the current precision and kernel
 // choice read (else the caller uploads the plan again)
 bool tcImagesFit(const void* devPlan) {
@@ -1577,7 +1717,7 @@ void tcNoteSimtPass(void* devPlan, size_t index) {
 //   * 4 qubits: kernel 3 (2.8-3.0, against 2.8-3.1 for kernel 2, 3.1-3.2 SIMT);
 //   * 5 qubits: kernel 2 (2.5-2.9, against 2.8-3.0 for kernel 5);
 //   * 6 qubits: kernel 5 (2.6-3.0, against 2.8-3.1 for kernel 2).
-// Split-BF16 operands:
+// Split-BF16 operands (split-FP16 takes the same choices):
 //   * 4 qubits, high targets: kernel 2 (2.6-2.8, against SIMT 3.1-3.2);
 //   * 4 qubits, other targets: kernel 5 (2.7-3.0);
 //   * 5 qubits: kernel 5 (2.7-3.0, against 2.9-3.1 for kernel 2);
@@ -1592,11 +1732,11 @@ int tuneLayout(const FusedPass& pass) {
     return pass.targets[0] < 5 ? 1 : 0;
 }
 void setTunedKernel(int n, int prec, int k, int layout, int version) {
-    if (n >= 0 && n <= kTuneMaxN && (prec == 0 || prec == 1) && k >= 4 && k <= 6 && layout >= 0 && layout < 3)
+    if (n >= 0 && n <= kTuneMaxN && prec >= 0 && prec <= 2 && k >= 4 && k <= 6 && layout >= 0 && layout < 3)
         g_tcTuned[n][prec][k][layout] = (version >= 2 && version <= 5) ? version : 0;
 }
 int tunedKernel(int n, int prec, int k, int layout) {
-    if (n < 0 || n > kTuneMaxN || (prec != 0 && prec != 1) || k < 4 || k > 6 || layout < 0 || layout > 2) return 0;
+    if (n < 0 || n > kTuneMaxN || prec < 0 || prec > 2 || k < 4 || k > 6 || layout < 0 || layout > 2) return 0;
     return g_tcTuned[n][prec][k][layout];
 }
 void setKernelTrial(int version) { g_tcTrial = (version >= 2 && version <= 5) ? version : 0; }
@@ -1669,7 +1809,8 @@ int tc2Coverage(int n, const FusedPass& pass, int groups, std::vector<uint8_t>& 
 // reads is present, starts on a 16-byte boundary, lies inside the block and
 // overlaps no other part.  0 when all hold, else 1.
 int tcCheckImageLayouts() {
-    const int sets[4] = {kPartTF32, kPartBF16, kPartTF32 | kPartDirect, kPartBF16 | kPartDirect};
+    const int sets[6] = {kPartTF32, kPartBF16, kPartF16, kPartTF32 | kPartDirect, kPartBF16 | kPartDirect,
+                         kPartF16 | kPartDirect};
     for (int k = 4; k <= 6; ++k)
         for (int parts : sets) {
             const ImageLayout L = imageLayout(k, parts);
@@ -1681,6 +1822,7 @@ int tcCheckImageLayouts() {
             if (parts & kPartTF32) reads.push_back({k == 6 ? L.compact : L.full, 2 * GE});    // hi, lo
             if (parts & kPartBF16) reads.push_back({L.bf16, 3 * GE / 2});                       // three BF16 parts
             if (parts & kPartDirect) reads.push_back({L.full, 2 * NK});                         // direct-load kernel
+            if (parts & kPartF16) reads.push_back({L.f16, GE + 1});                             // two FP16 parts, the factor
             if (L.stride % 4) return 1;
             for (const Read& r : reads)
                 if (r.off == kNoPart || r.off % 4 || r.off + r.floats > L.stride) return 1;
@@ -1689,6 +1831,7 @@ int tcCheckImageLayouts() {
             if (L.full != kNoPart) present.push_back({L.full, L.full + 2 * NK});
             if (L.bf16 != kNoPart) present.push_back({L.bf16, L.bf16 + (3 * GE + 1) / 2});
             if (L.compact != kNoPart) present.push_back({L.compact, L.compact + 6 * D * D});
+            if (L.f16 != kNoPart) present.push_back({L.f16, L.f16 + GE + 4});
             for (size_t a = 0; a < present.size(); ++a)
                 for (size_t b = a + 1; b < present.size(); ++b)
                     if (present[a].first < present[b].second && present[b].first < present[a].second) return 1;
@@ -1731,6 +1874,7 @@ static bool launchPassTC(int version, const FusedPass& pass, float* re, float* i
     const ImageLayout lay = imageLayout(k, parts);
     const size_t po = version < 2                        ? lay.full
                       : g_tcPrecision == kPrecBF16 ? lay.bf16
+                      : g_tcPrecision == kPrecF16  ? lay.f16
                       : k == 6                     ? lay.compact
                                                    : lay.full;
     if (po == kNoPart || lay.stride == 0) return false;
@@ -1743,14 +1887,21 @@ static bool launchPassTC(int version, const FusedPass& pass, float* re, float* i
     (done = true,                                                                                                       \
      g_tcStaging ? launchTC2<KQ, LG, EG, LS, PR, 4, 1>(re, im, n, pass, img, po, bs, errFlag, nl, st, batch, instStride, imageStride) \
                  : launchTC2<KQ, LG, EG, LS, PR, 4, 0>(re, im, n, pass, img, po, bs, errFlag, nl, st, batch, instStride, imageStride))
-        const bool tf = g_tcPrecision == kPrecTF32;
+// split-FP16 kernels stage with cp.async only
+#define QG_TC2F(KQ) \
+    (done = true, launchTC2<KQ, 2, 2, 2, kPrecF16, 4, 0>(re, im, n, pass, img, po, bs, errFlag, nl, st, batch, instStride, imageStride))
+        const bool tf = g_tcPrecision == kPrecTF32, bf = g_tcPrecision == kPrecBF16;
         if (tf && k == 4 && version == 3) ok = QG_TC2W(4, 1, 1, 1, kPrecTF32);
         else if (tf && k == 5 && version == 2) ok = QG_TC2W(5, 2, 1, 1, kPrecTF32);
         else if (tf && k == 6 && version == 5) ok = QG_TC2W(6, 2, 2, 2, kPrecTF32);
-        else if (!tf && k == 4 && version == 5) ok = QG_TC2W(4, 2, 2, 2, kPrecBF16);
-        else if (!tf && k == 5 && version == 5) ok = QG_TC2W(5, 2, 2, 2, kPrecBF16);
-        else if (!tf && k == 6 && version == 5) ok = QG_TC2W(6, 2, 2, 2, kPrecBF16);
+        else if (bf && k == 4 && version == 5) ok = QG_TC2W(4, 2, 2, 2, kPrecBF16);
+        else if (bf && k == 5 && version == 5) ok = QG_TC2W(5, 2, 2, 2, kPrecBF16);
+        else if (bf && k == 6 && version == 5) ok = QG_TC2W(6, 2, 2, 2, kPrecBF16);
+        else if (!tf && !bf && k == 4 && version == 5) ok = QG_TC2F(4);
+        else if (!tf && !bf && k == 5 && version == 5) ok = QG_TC2F(5);
+        else if (!tf && !bf && k == 6 && version == 5) ok = QG_TC2F(6);
 #undef QG_TC2W
+#undef QG_TC2F
     }
     if (done) return ok;
     if (version >= 2) {
@@ -1763,7 +1914,10 @@ static bool launchPassTC(int version, const FusedPass& pass, float* re, float* i
      : version == 4 ? launchTC2<KQ, 1, 2, 1, PR, 1, ST>(re, im, n, pass, img, po, bs, errFlag, nl, st, batch, instStride, imageStride)  \
                     : launchTC2<KQ, 2, 2, 2, PR, 1, ST>(re, im, n, pass, img, po, bs, errFlag, nl, st, batch, instStride, imageStride))
 #define QG_TC2P(KQ, PR) (g_tcStaging ? QG_TC2S(KQ, PR, 1) : QG_TC2S(KQ, PR, 0))
-#define QG_TC2(KQ) (g_tcPrecision == kPrecTF32 ? QG_TC2P(KQ, kPrecTF32) : QG_TC2P(KQ, kPrecBF16))
+#define QG_TC2(KQ)                                                                     \
+    (g_tcPrecision == kPrecTF32   ? QG_TC2P(KQ, kPrecTF32)                               \
+     : g_tcPrecision == kPrecBF16 ? QG_TC2P(KQ, kPrecBF16)                               \
+                                  : QG_TC2S(KQ, kPrecF16, 0))
         switch (k) {
             case 4: ok = QG_TC2(4); break;
             case 5: ok = QG_TC2(5); break;
@@ -1796,7 +1950,7 @@ int applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, 
     const int n = f32n(q);
     const int version = tcKernelFor(pass, n);
     if (version == 0) return 0;
-    NormLinks nl{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    NormLinks nl{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     if (dp->norms) {
         if (dp->inNorm.size() != dp->images.size()) dp->inNorm.assign(dp->images.size(), nullptr);
         if (dp->target.size() != dp->images.size()) dp->target.assign(dp->images.size(), nullptr);
@@ -1807,6 +1961,7 @@ int applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, 
         const bool chained = dp->chain && dp->lastTC >= 0;
         nl.in = chained ? nullptr : mine;
         dp->inNorm[index] = chained ? dp->norms + 3 * dp->lastTC + 1 : mine;
+        if (chained) nl.boundSq = dp->norms + 3 * dp->lastTC + 1;
         const bool prevUnitary = dp->lastTC >= 0 && dp->unitary[dp->lastTC];
         if (prevUnitary) {
             nl.corrIn = dp->inNorm[dp->lastTC];
@@ -1831,6 +1986,7 @@ int tcErrorFlag(const void* devPlan) {
     int v = 0;
     cudaMemcpyAsync(&v, dp->errFlag, sizeof(int), cudaMemcpyDeviceToHost, stream());
     cudaStreamSynchronize(stream());
+    if (v) cudaMemsetAsync(dp->errFlag, 0, sizeof(int), stream());   // reported once
     return v;
 }
 
@@ -1859,7 +2015,7 @@ bool tcFinalNorms(const void* devPlan, const double** target, const double** out
 
 void setTensorCoresEnabled(bool on) { g_tcEnabled = on; }
 bool setTensorCorePrecision(int mode) {
-    if (mode != kPrecTF32 && mode != kPrecBF16) return false;
+    if (mode != kPrecTF32 && mode != kPrecBF16 && mode != kPrecF16) return false;
     g_tcPrecision = mode;
     return true;
 }
@@ -1882,7 +2038,7 @@ bool applyPassTCBatch(float* re, float* im, int n, const FusedPass& pass, const 
                       int parts, int batch, int* errFlag, cudaStream_t st) {
     const int version = tcKernelFor(pass, n);
     if (version < 2 || !images || !pass.controls.empty()) return false;
-    const NormLinks nl{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    const NormLinks nl{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     return launchPassTC(version, pass, re, im, n, images, parts, errFlag, nl, st, batch, 1ull << n,
                         (uint64_t)imageStride);
 }

@@ -853,7 +853,9 @@ int quest_gb300_trotterBatchRun(void* batch, double* energies) {
     int err = 0;
     if (QG_CUDA(cudaMemcpy(&err, b->errFlag, sizeof(int), cudaMemcpyDeviceToHost), fn)) return -1;
     if (err) {
-        invalidQuESTInputError("A tensor-core pass of the Trotter batch timed out waiting on its pipeline.", fn);
+        invalidQuESTInputError(err == 6 ? "A split-FP16 tensor-core pass of the Trotter batch gave a non-finite output."
+                                        : "A tensor-core pass of the Trotter batch timed out waiting on its pipeline.",
+                               fn);
         return -1;
     }
     if (energies)

@@ -113,10 +113,10 @@ def _single_gate_plan(L, n, targets, seed):
     return p, u
 
 
-@pytest.fixture(params=[0, 1], ids=["tf32", "bf16"])
+@pytest.fixture(params=[0, 1, 2], ids=["tf32", "bf16", "fp16"])
 def precision(request, gpulib):
     """Operands of the pipelined kernel: 0 = 3-term split-TF32 (default),
-    1 = 4-term split-BF16."""
+    1 = 4-term split-BF16, 2 = 3-term split-FP16."""
     assert gpulib.lib.quest_gb300_setTensorCorePrecision(request.param) == 0
     yield request.param
     gpulib.lib.quest_gb300_setTensorCorePrecision(0)
@@ -418,3 +418,93 @@ def test_pass_events_time_every_pass(gpulib):
         lib.quest_gb300_setPassEvents(0)
     lib.quest_gb300_destroyQuregF32(q32)
     lib.quest_gb300_planDestroy(p)
+
+
+@pytest.fixture
+def split_fp16(gpulib):
+    assert gpulib.lib.quest_gb300_setTensorCorePrecision(2) == 0
+    assert gpulib.lib.quest_gb300_getTensorCorePrecision() == 2
+    yield
+    gpulib.lib.quest_gb300_setTensorCorePrecision(0)
+
+
+def _dense_plan(L, n, gates):
+    p = L.lib.quest_gb300_planCreate(n, 6)
+    for ts, m in gates:
+        re, im = np.ascontiguousarray(m.real.ravel()), np.ascontiguousarray(m.imag.ravel())
+        assert L.lib.quest_gb300_planAddGate(p, (C.c_int * len(ts))(*ts), len(ts),
+                                             re.ctypes.data_as(C.POINTER(C.c_double)),
+                                             im.ctypes.data_as(C.POINTER(C.c_double))) == 0
+    assert L.lib.quest_gb300_planCompile(p) == len(gates)
+    return p
+
+
+@pytest.mark.parametrize("version", [0, 2, 5])
+def test_split_fp16_scales_each_matrix_block(gpulib, split_fp16, version):
+    """Split-FP16 with matrices far from unit size: a 5-qubit matrix of
+    entries up to ~30 (60 x a unitary), then 6-qubit ones scaled by 1/60,
+    1e-3 and 1e3, on a normalised 18-qubit state (the state's norm goes 60,
+    1, 1e-3, 1).  Each operand block carries its own power-of-two scale, so
+    every pass keeps FP16's 11-bit precision: the result matches the FP64
+    engine as closely as unit-size passes do."""
+    L = gpulib
+    n = 18
+    rng = np.random.default_rng(23)
+
+    def haar(k):
+        return np.linalg.qr(rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k)))[0]
+
+    gates = [([0, 4, 7, 11, 16], 60.0 * haar(5)), ([1, 2, 3, 5, 6, 8], haar(6) / 60.0),
+             ([9, 10, 12, 13, 14, 15], 1e-3 * haar(6)), ([0, 1, 4, 9, 16, 17], 1e3 * haar(6))]
+    p = _dense_plan(L, n, gates)
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    psi /= np.linalg.norm(psi)
+    q64 = L.create(n)
+    L.set_amps(q64, psi)
+    q32 = L.lib.quest_gb300_createQuregF32(n)
+    L.lib.quest_gb300_copyFromQureg(q32, q64)
+    L.lib.quest_gb300_setTensorCoreKernel(version)
+    rc = L.lib.quest_gb300_applyPlanF32(q32, p)
+    L.lib.quest_gb300_setTensorCoreKernel(0)
+    assert rc == 0
+    assert all(L.lib.quest_gb300_planPassUsesTensorCores(p, i) >= 2 for i in range(len(gates)))
+    for ts, m in gates:
+        L.applyMatrixN(q64, ts, m)
+    ref, got = L.amps(q64), L.amps_f32(q32, n)
+    omf = 1 - abs(np.vdot(ref, got)) ** 2 / (np.vdot(ref, ref).real * np.vdot(got, got).real)
+    err = float(np.max(np.abs(got - ref)))
+    p64, p32 = np.vdot(ref, ref).real, np.vdot(got, got).real
+    print(f"split-FP16 scaled blocks v{version}: norm {p64:.6e} vs {p32:.6e}, 1-F={omf:.2e}, max|d amp|={err:.2e}")
+    assert abs(p32 / p64 - 1) < 1e-5 and omf < 1e-10 and err < 1e-7
+    L.lib.quest_gb300_planDestroy(p)
+    L.lib.quest_gb300_destroyQuregF32(q32)
+    L.destroy(q64)
+
+
+def test_split_fp16_reports_out_of_range_amplitudes(gpulib, split_fp16):
+    """An amplitude of modulus 5 exceeds split-FP16's range (3.99 after the
+    2^14 scale): the pass's non-finite output is reported as an input error
+    naming split-FP16 (the state is lost); split-TF32 takes the same state."""
+    L = gpulib
+    n = 14
+    psi = np.zeros(1 << n, dtype=np.complex128)
+    psi[3], psi[900] = 5.0, 0.5j
+    q64 = L.create(n)
+    L.set_amps(q64, psi)
+    plan, u = _single_gate_plan(L, n, [0, 1, 2, 3, 4, 5], 5)
+    q32 = L.lib.quest_gb300_createQuregF32(n)
+    L.lib.quest_gb300_copyFromQureg(q32, q64)
+    rc = L.lib.quest_gb300_applyPlanF32(q32, plan)
+    errors = list(L.errors)
+    L.errors.clear()
+    assert rc == -1 and any("split-FP16" in e[1] for e in errors), errors
+    L.lib.quest_gb300_setTensorCorePrecision(0)
+    L.lib.quest_gb300_copyFromQureg(q32, q64)
+    assert L.lib.quest_gb300_applyPlanF32(q32, plan) == 0
+    L.multiQubitUnitary(q64, [0, 1, 2, 3, 4, 5], u)
+    err = C.c_double(0)
+    omf = L.lib.quest_gb300_compareF32(q32, q64, C.byref(err))
+    assert omf < 1e-9
+    L.lib.quest_gb300_planDestroy(plan)
+    L.lib.quest_gb300_destroyQuregF32(q32)
+    L.destroy(q64)

@@ -181,7 +181,7 @@ def test_batch_checks_and_precision_switch(gpulib, library_errors):
     before = lib.quest_gb300_getTensorCorePrecision()
     e = (C.c_double * 2)()
     try:
-        for prec in (0, 1, 0):
+        for prec in (0, 1, 2, 0):
             assert lib.quest_gb300_setTensorCorePrecision(prec) == 0
             assert lib.quest_gb300_trotterBatchRun(b, e) == 0, list(library_errors)
             for i, order in enumerate((1, 2)):

@@ -80,3 +80,26 @@ def test_operand_image_layouts(L):
     """Every tensor-core kernel reads its operand part inside the image block
     the library lays out for the parts it built (16-byte aligned, no overlap)."""
     assert L.lib.quest_gb300_checkImageLayouts() == 0
+
+
+def test_host_half_rounding_matches_ieee(L):
+    """The host rounding that builds split-FP16 operand images equals IEEE
+    binary16 round-to-nearest-even (numpy's float64 -> float16, one rounding):
+    random values over FP16's whole range, its subnormals, exact ties at
+    both ends of a binade, and values past the largest finite one."""
+    rng = np.random.default_rng(7)
+    vals = [rng.normal(size=4000) * np.exp2(rng.integers(-30, 17, size=4000)),
+            rng.uniform(-1, 1, size=2000) * 2.0 ** -14,                           # subnormal range
+            (np.arange(1, 2049) + 0.5) * 2.0 ** -24,                             # ties on the subnormal grid
+            (1024 + np.arange(0, 1024) + 0.5) * 2.0 ** -10,                      # ties in [1, 2)
+            np.array([0.0, -0.0, 65504.0, 65519.99, 65520.0, 1e6, -1e6, 2.0 ** -25, 2.0 ** -25 * 1.0000001,
+                      6.103515625e-05, 5.960464477539063e-08])]
+    v = np.ascontiguousarray(np.concatenate(vals))
+    out = np.zeros(v.size, dtype=np.uint16)
+    assert L.lib.quest_gb300_roundHalf(v.ctypes.data_as(C.POINTER(C.c_double)),
+                                       out.ctypes.data_as(C.POINTER(C.c_ushort)), v.size) == 0
+    with np.errstate(over="ignore"):
+        want = v.astype(np.float16).view(np.uint16)
+    bad = np.nonzero(out != want)[0]
+    assert bad.size == 0, [(v[i], hex(out[i]), hex(want[i])) for i in bad[:8]]
+    assert L.lib.quest_gb300_roundHalf(None, None, -1) == -1
