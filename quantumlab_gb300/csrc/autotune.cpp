@@ -19,6 +19,7 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <complex>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -115,14 +116,32 @@ void saveCache() {
 
 std::once_flag g_loaded;
 
-// time one synthetic pass of width k on targets `t` (median of 3)
+// time one synthetic pass of width k on targets `t` (median of 3).  The
+// matrix is a random unitary (Gram-Schmidt on complex Gaussian columns), so
+// the register keeps its norm over the hundreds of timed passes: split-FP16
+// operands take amplitudes of modulus below ~3.99 at a plan's first pass.
 double timePass(void* q32, int n, const std::vector<int>& t) {
     const int k = (int)t.size(), D = 1 << k;
     std::mt19937_64 rng(1234 + k);
     std::normal_distribution<double> g;
+    std::vector<std::complex<double>> m((size_t)D * D);     // row-major
+    for (auto& v : m) v = {g(rng), g(rng)};
+    for (int c = 0; c < D; ++c) {
+        for (int pc = 0; pc < c; ++pc) {
+            std::complex<double> dot = 0;
+            for (int r = 0; r < D; ++r) dot += std::conj(m[(size_t)r * D + pc]) * m[(size_t)r * D + c];
+            for (int r = 0; r < D; ++r) m[(size_t)r * D + c] -= dot * m[(size_t)r * D + pc];
+        }
+        double nrm = 0;
+        for (int r = 0; r < D; ++r) nrm += std::norm(m[(size_t)r * D + c]);
+        nrm = std::sqrt(nrm);
+        for (int r = 0; r < D; ++r) m[(size_t)r * D + c] /= nrm;
+    }
     std::vector<double> re((size_t)D * D), im((size_t)D * D);
-    for (auto& v : re) v = g(rng) / std::sqrt((double)D);
-    for (auto& v : im) v = g(rng) / std::sqrt((double)D);
+    for (size_t e = 0; e < m.size(); ++e) {
+        re[e] = m[e].real();
+        im[e] = m[e].imag();
+    }
     void* p = quest_gb300_planCreate(n, k);
     if (!p) return 0;
     quest_gb300_planAddGate(p, t.data(), k, re.data(), im.data());
