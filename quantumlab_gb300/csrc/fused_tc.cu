@@ -221,7 +221,9 @@ __host__ __device__ constexpr uint32_t idescF16(int M, int N) {
 // Split-FP16 of two consecutive K elements (already scaled into FP16's
 // range): hi = both rounded to the nearest FP16 (packed, the first in the low
 // half), lo = the exact remainders rounded to the nearest FP16.  x = hi + lo
-// to ~2^-22 relative, unbiased, or to 2^-25 absolute below FP16's normal range.
+// to ~2^-22 relative, unbiased, while lo is a normal FP16 number (|x| >= 2^-3);
+// below that the measured precision is hi's alone, as if the MMA read
+// subnormal parts as zero (f16XExp keeps the amplitudes above it).
 __device__ __forceinline__ void splitF16x2(float x0, float x1, uint32_t& hi, uint32_t& lo) {
     const __half2 h = __floats2half2_rn(x0, x1);
     hi = *reinterpret_cast<const uint32_t*>(&h);
@@ -301,9 +303,9 @@ __device__ __forceinline__ void recordScale(const NormLinks& nl, float sm1, bool
     if (nl.scaleSq && writer) *nl.scaleSq = (1.0 + (double)sm1) * (1.0 + (double)sm1);
 }
 // Split-FP16: the exponent e of X's scale 2^e.  With a bound B on every |x|,
-// the largest e with B * 2^e <= 2^15 (all of FP16's 11 bits for the lo parts
-// of the smallest amplitudes; the tensor cores take no FP16 subnormals),
-// else kF16XExp (|x| below ~3.99).
+// the largest e with B * 2^e <= 2^15, which keeps the lo parts of small
+// amplitudes normal FP16 numbers (splitF16x2), else kF16XExp (|x| below
+// ~3.99).
 __device__ __forceinline__ int f16XExp(const NormLinks& nl) {
     if (!nl.boundSq) return kF16XExp;
     const double b = *nl.boundSq;
@@ -558,7 +560,6 @@ struct TC2Params {
     uint64_t ctrlOff[8];
     uint64_t ctrlImageStride;
 };
-
 
 // Layout of kApplyTC2<KQ, LG, EG, LS, PR>, used by the kernel and its
 // launcher.  Shared memory: the parts of G (split-TF32: Gh, Gl in FP32 words,
