@@ -103,3 +103,19 @@ def test_host_half_rounding_matches_ieee(L):
     bad = np.nonzero(out != want)[0]
     assert bad.size == 0, [(v[i], hex(out[i]), hex(want[i])) for i in bad[:8]]
     assert L.lib.quest_gb300_roundHalf(None, None, -1) == -1
+
+
+def test_tensor_core_precision_modes(L):
+    """setTensorCorePrecision takes 0 (split-TF32), 1 (split-BF16) and 2
+    (split-FP16) and refuses other modes (host state only, no GPU)."""
+    lib = L.lib
+    before = lib.quest_gb300_getTensorCorePrecision()
+    try:
+        for mode in (0, 1, 2):
+            assert lib.quest_gb300_setTensorCorePrecision(mode) == 0
+            assert lib.quest_gb300_getTensorCorePrecision() == mode
+        for bad in (-1, 3):
+            assert lib.quest_gb300_setTensorCorePrecision(bad) == -1
+            assert lib.quest_gb300_getTensorCorePrecision() == 2
+    finally:
+        lib.quest_gb300_setTensorCorePrecision(before)
