@@ -251,8 +251,9 @@ def run_gpu(args, rank, world):
     pname = PREC_NAMES[prec]
     lib.quest_gb300_setTensorCorePrecision(prec)
     # the autotuner: per-pass costs and the fastest tensor-core variant of
-    # every (width, target layout) class, for both operand forms, then the
-    # fusion width with the lowest predicted time
+    # every (width, target layout) class, for split-TF32 and split-BF16 (or
+    # split-FP16 alone when it is the headline form), then the fusion width
+    # with the lowest predicted time
     t0 = time.perf_counter()
     for pr in ((1 - prec, prec) if prec < 2 else (prec,)):
         lib.quest_gb300_setTensorCorePrecision(pr)

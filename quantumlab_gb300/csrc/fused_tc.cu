@@ -13,7 +13,7 @@
 //
 // Two kernels:
 //   * kApplyTC2 (the default; "pipelined kernel" below): warp-specialised and
-//     persistent, with one of two operand forms (setTensorCorePrecision):
+//     persistent, with one of three operand forms (setTensorCorePrecision):
 //       - 3-term split-TF32, the default: X = Xh + Xl and Gr = Gh + Gl in
 //         TF32 parts, Out = Xh.Gh + Xl.Gh + Xh.Gl accumulated in FP32 by
 //         kind::tf32 MMAs;
