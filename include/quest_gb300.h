@@ -171,9 +171,11 @@ void quest_gb300_setTensorCoreKernel(int version);
  * Xh.Gll); 2 = 3-term split-FP16 (as split-TF32, with FP16 parts of the same
  * 11-bit precision at twice the MMA rate; X and each matrix block are scaled
  * by powers of two before the split, X's from the norm the previous pass of
- * a plan application measured, else 2^14, so the first tensor-core pass of
- * an application needs amplitudes of modulus below 3.99: a non-finite output
- * is reported as an error, the state is then lost).  All accumulate in FP32.
+ * a plan application measured, or, at the first pass, the norm a capture
+ * flush sums while converting the state, else 2^14: so the first tensor-core
+ * pass of quest_gb300_applyPlanF32 needs amplitudes of modulus below 3.99; a
+ * non-finite output is reported as an error, the state is then lost).  All
+ * accumulate in FP32.
  * Returns 0, or -1 for another mode. */
 int quest_gb300_setTensorCorePrecision(int mode);
 int quest_gb300_getTensorCorePrecision(void);

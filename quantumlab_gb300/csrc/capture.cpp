@@ -174,8 +174,12 @@ static void flushRecord(Capture* c, double* re, double* im) {
     const bool keepTrace = c->dmQubits > 0 && c->tracePreserving;
     c->tracePreserving = true;
     if (keepTrace) traceBeforePlan(re, c->dmQubits);
-    // the FP64 -> FP32 conversion runs on the device while the host plans
-    quest_gb300_copyFromQureg(c->q32, view);
+    // the FP64 -> FP32 conversion runs on the device while the host plans;
+    // with split-FP16 operands it also sums |x|^2, from which the first
+    // tensor-core pass takes its scale (any state then fits FP16's range)
+    const double* entryNorm = nullptr;
+    if (quest_gb300_getTensorCorePrecision() == 2) entryNorm = copyFromQuregNorm(c->q32, view);
+    else quest_gb300_copyFromQureg(c->q32, view);
     FusedPlan* plan = new FusedPlan();
     plan->numQubits = c->n;
     plan->maxControls = defaultMaxControls(c->n);
@@ -204,7 +208,8 @@ static void flushRecord(Capture* c, double* re, double* im) {
         delete plan;
         return;
     }
-    quest_gb300_applyPlanF32(c->q32, plan);
+    if (entryNorm) applyPlanF32Entry(c->q32, plan, entryNorm);
+    else quest_gb300_applyPlanF32(c->q32, plan);
     if (keepTrace) copyToQuregTraceKept(c->q32, view, c->dmQubits);
     else copyToQuregAfterPlan(c->q32, view, plan);
     c->gatesApplied += (long long)plan->gates.size();

@@ -46,7 +46,7 @@ int tcErrorFlag(const void* devPlan);
 int tcPassNorms(const void* devPlan, size_t index, double* out3);
 bool tcFinalNorms(const void* devPlan, const double** target, const double** out);
 void tcBeginPlan(void* devPlan, size_t numPasses);
-void tcBeginRange(void* devPlan);
+void tcBeginRange(void* devPlan, const double* entryBound);
 void tcNoteSimtPass(void* devPlan, size_t index);
 void setTensorCoresEnabled(bool on);
 void setTensorCoreKernel(int version);
@@ -169,6 +169,48 @@ __global__ void kF64toF32(const double* __restrict__ sr, const double* __restric
             dr[j] = (float)sr[j];
             di[j] = (float)si[j];
         }
+    }
+}
+// FP64 -> FP32 as kF64toF32, also adding sum |x|^2 of the FP32 values into
+// *normSq (FP32 sums of each thread's 8 values, FP64 across its groups, one
+// FP64 atomic per block; grid-stride over one wave of blocks)
+__global__ void kF64toF32Norm(const double* __restrict__ sr, const double* __restrict__ si, float* __restrict__ dr,
+                              float* __restrict__ di, uint64_t n, double* __restrict__ normSq) {
+    double acc = 0.0;
+    const uint64_t groups = n / 4;
+    for (uint64_t g = (uint64_t)blockIdx.x * kConvThreads + threadIdx.x; g < groups;
+         g += (uint64_t)gridDim.x * kConvThreads) {
+        const uint64_t i = 4 * g;
+        const double2 r0 = *reinterpret_cast<const double2*>(sr + i), r1 = *reinterpret_cast<const double2*>(sr + i + 2);
+        const double2 m0 = *reinterpret_cast<const double2*>(si + i), m1 = *reinterpret_cast<const double2*>(si + i + 2);
+        const float4 fr = make_float4((float)r0.x, (float)r0.y, (float)r1.x, (float)r1.y);
+        const float4 fi = make_float4((float)m0.x, (float)m0.y, (float)m1.x, (float)m1.y);
+        *reinterpret_cast<float4*>(dr + i) = fr;
+        *reinterpret_cast<float4*>(di + i) = fi;
+        float s = fr.x * fr.x;
+        s = fmaf(fr.y, fr.y, s);
+        s = fmaf(fr.z, fr.z, s);
+        s = fmaf(fr.w, fr.w, s);
+        s = fmaf(fi.x, fi.x, s);
+        s = fmaf(fi.y, fi.y, s);
+        s = fmaf(fi.z, fi.z, s);
+        s = fmaf(fi.w, fi.w, s);
+        acc += (double)s;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        for (uint64_t j = 4 * groups; j < n; ++j) {
+            dr[j] = (float)sr[j];
+            di[j] = (float)si[j];
+            acc += (double)dr[j] * dr[j] + (double)di[j] * di[j];
+        }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    __shared__ double ws[kConvThreads / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < (int)(kConvThreads / 32); ++w) b += ws[w];
+        atomicAdd(normSq, b);
     }
 }
 // FP32 -> FP64, each amplitude times *scale when scale is given
@@ -453,7 +495,9 @@ extern "C" int quest_gb300_passTimesMs(double* out, int maxPasses) {
     return n;
 }
 
-int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPasses) {
+// applyPlanF32Range with, when entryBound is given, sum |x|^2 of the
+// register's state on the device (the first tensor-core pass's bound)
+static int applyRange(void* h, void* plan, int firstPass, int numPasses, const double* entryBound) {
     QuregF32* q = qg::Q(h);
     qg::FusedPlan* p = reinterpret_cast<qg::FusedPlan*>(plan);
     if (!q || !p || p->numQubits != q->n) {
@@ -481,7 +525,7 @@ int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPas
     const int last = std::min(total, firstPass + numPasses);
     cudaStream_t st = qg::stream();
     if (firstPass == 0) qg::tcBeginPlan(p->device, p->passes.size());
-    qg::tcBeginRange(p->device);
+    qg::tcBeginRange(p->device, entryBound);
     bool usedTC = false;
     if (g_passEvents) {
         while ((int)g_passEv.size() < 2 * total) {
@@ -534,6 +578,10 @@ int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPas
         }
     }
     return 0;
+}
+
+int quest_gb300_applyPlanF32Range(void* h, void* plan, int firstPass, int numPasses) {
+    return applyRange(h, plan, firstPass, numPasses, nullptr);
 }
 
 int quest_gb300_applyPlanF32(void* h, void* plan) { return quest_gb300_applyPlanF32Range(h, plan, 0, 1 << 30); }
@@ -656,6 +704,28 @@ void copyToQuregTraceKept(void* h, Qureg& dst, int N) {
                                                            dst.deviceStateVec.imag, n, scale);
     launchFailed("copyToQureg");
 }
+
+// FP64 Qureg -> FP32 register, also summing |x|^2 of the converted state on
+// the device; returns where the sum is (in the register's scratch, valid
+// until the register changes), or null when the conversion failed
+const double* copyFromQuregNorm(void* h, const Qureg& src) {
+    QuregF32* q = Q(h);
+    const uint64_t n = 1ull << q->n;
+    if (src.numAmpsTotal != (long long)n) {
+        invalidQuESTInputError("Dimensions of the qubit registers don't match.", "copyFromQureg");
+        return nullptr;
+    }
+    double* slot = q->scratch + 2 * kMaxReduceBlocks + 40;
+    if (QG_CUDA(cudaMemsetAsync(slot, 0, sizeof(double), stream()), "copyFromQureg")) return nullptr;
+    const unsigned blocks = (unsigned)std::min<uint64_t>(convBlocks(n), 8ull * (uint64_t)numSMs());
+    kF64toF32Norm<<<blocks, kConvThreads, 0, stream()>>>(src.deviceStateVec.real, src.deviceStateVec.imag, q->re, q->im,
+                                                        n, slot);
+    return launchFailed("copyFromQureg") ? nullptr : slot;
+}
+
+// the whole plan on the register, whose state has sum |x|^2 = *entryBound
+// (device), from copyFromQuregNorm
+int applyPlanF32Entry(void* h, void* plan, const double* entryBound) { return applyRange(h, plan, 0, 1 << 30, entryBound); }
 
 // FP32 register -> FP64 Qureg after a plan: when the plan ended in a chain of
 // unitary passes, the conversion also removes the norm residue of its last

@@ -25,8 +25,9 @@
 //         11-bit significands, so the same ~2^-22 precision) on kind::f16
 //         MMAs at twice the TF32 rate.  FP16's exponent range is met by
 //         power-of-two scales: X is multiplied by 2^e before the split, with
-//         e from the input's norm where a previous pass of the chain measured
-//         it, else 14 (amplitudes of modulus below ~3.99 fit), and each
+//         e from the input's norm where a previous pass of the chain or the
+//         caller (a capture flush's conversion) measured it, else 14
+//         (amplitudes of modulus below ~3.99 fit), and each
 //         matrix block by the 2^s its operand image records (|G| * 2^s <=
 //         2^14); the epilogue multiplies by 2^-(e + s), all exact.  A
 //         non-finite output (an amplitude out of range) sets error code 6;
@@ -275,8 +276,9 @@ __device__ __forceinline__ void splitTF32(float x, uint32_t& hi, uint32_t& lo) {
 //   corrTarget  when this pass continues a chain of unitary passes, the input
 //            norm T of the chain's first pass, else null;
 //   boundSq  sum |x|^2 of this pass's input when a previous tensor-core pass
-//            of the chain measured it (its output), else null: it bounds every
-//            |x|, and split-FP16 takes the scale of X from it.
+//            of the chain measured it (its output) or the caller did (the
+//            first pass), else null: it bounds every |x|, and split-FP16
+//            takes the scale of X from it.
 // The scale makes this pass's output norm T (chained: its input norm is the
 // previous output, so scale^2 = T / (out * f)) or, unchained, its own input
 // norm (scale^2 = 1 / f).  With a constant drift every output after the first
@@ -1143,6 +1145,10 @@ struct DevicePlan {
     std::vector<const double*> target;
     int lastTC = -1;        // last tensor-core pass applied (its drift is corrected next)
     bool chain = false;     // the state is still lastTC's output up to unitary SIMT passes
+    // sum |x|^2 of the state this range started from, when the caller measured
+    // it (device; until a non-unitary SIMT pass): the bound of the first
+    // tensor-core pass's split-FP16 scale
+    const double* entryBound = nullptr;
     // per pass: 1 if its matrix is unitary to 1e-10.  Only the drift of a
     // unitary pass is corrected; a non-unitary pass changes the norm on purpose.
     std::vector<char> unitary;
@@ -1696,16 +1702,22 @@ void tcBeginPlan(void* devPlan, size_t numPasses) {
 }
 
 // start of every applyPlanF32Range call: the caller may have changed the
-// state since the last call, so the next tensor-core pass measures its input
-void tcBeginRange(void* devPlan) {
+// state since the last call, so the next tensor-core pass measures its input;
+// entryBound: sum |x|^2 of the state now, on the device, or null
+void tcBeginRange(void* devPlan, const double* entryBound) {
     DevicePlan* dp = reinterpret_cast<DevicePlan*>(devPlan);
-    if (dp) dp->chain = false;
+    if (!dp) return;
+    dp->chain = false;
+    dp->entryBound = entryBound;
 }
 
 // a pass ran on the SIMT applier: a non-unitary one changes the norm
 void tcNoteSimtPass(void* devPlan, size_t index) {
     DevicePlan* dp = reinterpret_cast<DevicePlan*>(devPlan);
-    if (dp && (index >= dp->unitary.size() || !dp->unitary[index])) dp->chain = false;
+    if (dp && (index >= dp->unitary.size() || !dp->unitary[index])) {
+        dp->chain = false;
+        dp->entryBound = nullptr;
+    }
 }
 
 // Which applier runs a pass on registers of n qubits: 0 = the FP32 SIMT
@@ -1963,6 +1975,7 @@ int applyPassTCIndexed(QuregF32& q, const FusedPass& pass, const void* devPlan, 
         nl.in = chained ? nullptr : mine;
         dp->inNorm[index] = chained ? dp->norms + 3 * dp->lastTC + 1 : mine;
         if (chained) nl.boundSq = dp->norms + 3 * dp->lastTC + 1;
+        else if (dp->entryBound) nl.boundSq = dp->entryBound;
         const bool prevUnitary = dp->lastTC >= 0 && dp->unitary[dp->lastTC];
         if (prevUnitary) {
             nl.corrIn = dp->inNorm[dp->lastTC];

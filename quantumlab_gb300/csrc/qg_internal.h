@@ -64,6 +64,11 @@ void copyToQuregAfterPlan(void* qureg32, Qureg& dst, void* plan);
 // trace recorded by traceBeforePlan is restored (fused_f32.cu)
 void traceBeforePlan(const double* re, int N);
 void copyToQuregTraceKept(void* qureg32, Qureg& dst, int N);
+// FP64 Qureg -> FP32 register with sum |x|^2 of the result summed on the
+// device (returned; null on failure), and a whole plan applied to a register
+// whose sum |x|^2 the device holds at entryBound (fused_f32.cu)
+const double* copyFromQuregNorm(void* qureg32, const Qureg& src);
+int applyPlanF32Entry(void* qureg32, void* plan, const double* entryBound);
 void captureDiscard(const double* re);            // drop the queued gates (the state is overwritten next)
 void captureDrop(const double* re);               // at destruction
 // launcher hooks: queue the gate and return true, or return false (after a

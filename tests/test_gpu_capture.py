@@ -389,3 +389,40 @@ def test_capture_stats_count_the_flushes(gpulib):
     assert 2 <= p.value <= g.value and ms.value >= 0.0
     lib.quest_gb300_setCapture(q, 0)
     L.destroy(q)
+
+
+def test_capture_split_fp16_takes_any_norm(gpulib):
+    """With split-FP16 operands a flush's FP64 -> FP32 conversion also sums
+    |x|^2, and the first tensor-core pass takes its operand scale from that
+    sum (later passes from the previous pass's): a state of norm ~40 with an
+    amplitude of 5 (beyond the fixed scale's 3.99) and one of norm 1e-4 both
+    match the same calls run directly in FP64."""
+    L = gpulib
+    lib = L.lib
+    n = 15
+    before = lib.quest_gb300_getTensorCorePrecision()
+    assert lib.quest_gb300_setTensorCorePrecision(2) == 0
+    try:
+        for scale in (40.0, 1e-4):
+            rng = np.random.default_rng(5)
+            psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+            psi *= scale / np.linalg.norm(psi)
+            if scale > 1:
+                psi[7] = 5.0
+            direct = L.create(n)
+            L.set_amps(direct, psi)
+            mixed_circuit(L, direct, n, 3)
+            cap = L.create(n)
+            assert lib.quest_gb300_setCapture(cap, 1) == 0
+            L.set_amps(cap, psi)
+            mixed_circuit(L, cap, n, 3)
+            assert lib.quest_gb300_capturedGates(cap) > 0
+            a, b = L.amps(direct), L.amps(cap)
+            f = abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real)
+            err = float(np.max(np.abs(a - b)))
+            print(f"norm {np.linalg.norm(psi):.3g}: 1-F={1 - f:.2e}, max|d|={err:.2e} (max|amp| {np.abs(a).max():.3g})")
+            assert 1 - f <= 1e-9 and err <= 1e-6 * np.abs(a).max()
+            L.destroy(direct)
+            L.destroy(cap)
+    finally:
+        lib.quest_gb300_setTensorCorePrecision(before)
