@@ -200,6 +200,12 @@ int quest_gb300_checkTileCoverage(int numQubits, const int* targets, int numTarg
  * 16-byte aligned, inside the image block and disjoint from the other parts.
  * Returns 0 when all hold, else 1. */
 int quest_gb300_checkImageLayouts(void);
+/* Host check of the split-FP16 operand images (no GPU): for pass widths 4..6
+ * and random matrix blocks from zero to 1e4 in size, the two FP16 parts of
+ * every entry, times the factor stored after them, give the entry to 2^-21
+ * of the block's largest, with every scaled entry at most 2^14.  Returns 0
+ * when all hold, else 1. */
+int quest_gb300_checkHalfImages(void);
 /* The host rounding that builds split-FP16 operand images: each value to the
  * nearest IEEE binary16 (ties to even; infinity beyond 65504), as bit
  * patterns.  Returns 0, or -1 for a negative count or a missing array. */

@@ -57,6 +57,7 @@ int tensorCoreStaging();
 int tcCheckCoverage(int n, const std::vector<int>& targets, const std::vector<int>& controls);
 int tcCheckImageLayouts();
 void tcRoundHalf(const double* v, uint16_t* out, int count);
+int tcCheckHalfImages();
 bool tensorCoresEnabled();
 int tcKernelFor(const FusedPass& pass, int n);
 float* f32re(QuregF32& q) { return q.re; }
@@ -609,6 +610,8 @@ int quest_gb300_getTensorCorePrecision(void) { return qg::tensorCorePrecision();
 int quest_gb300_setTensorCoreStaging(int mode) { return qg::setTensorCoreStaging(mode) ? 0 : -1; }
 
 int quest_gb300_checkImageLayouts(void) { return qg::tcCheckImageLayouts(); }
+
+int quest_gb300_checkHalfImages(void) { return qg::tcCheckHalfImages(); }
 
 int quest_gb300_roundHalf(const double* values, unsigned short* out, int count) {
     if (count < 0 || (count > 0 && (!values || !out))) return -1;

@@ -1674,6 +1674,53 @@ int tcImageParts() { return currentParts(); }
 void tcRoundHalf(const double* v, uint16_t* out, int count) {
     for (int i = 0; i < count; ++i) out[i] = hostF16RN(v[i]);
 }
+
+// Check of the split-FP16 operand images (host, no GPU): for k = 4..6 and
+// random matrix blocks scaled by 1e-6 .. 1e4 (one all zero), decode the two
+// FP16 parts of every entry of the image's form with the factor after them
+// (G = (hi + lo) * 2^-s, 2^-s = factor * 2^14) and compare with the real form
+// of G: every entry within 2^-21 of the block's largest, and the largest
+// scaled entry at most 2^14.  0 when all hold, else 1.
+int tcCheckHalfImages() {
+    uint64_t x = 0x9E3779B97F4A7C15ull;
+    auto uni = [&x]() {                                  // xorshift64*, uniform in (-1, 1)
+        x ^= x >> 12;
+        x ^= x << 25;
+        x ^= x >> 27;
+        return (double)((x * 0x2545F4914F6CDD1Dull) >> 11) * 0x1p-52 - 1.0;
+    };
+    const double scales[7] = {0.0, 1e-6, 1e-3, 1.0, 7.5, 60.0, 1e4};
+    for (int k = 4; k <= 6; ++k)
+        for (double sc : scales) {
+            const int D = 1 << k;
+            FusedPass pass;
+            for (int b = 0; b < k; ++b) pass.targets.push_back(b);
+            pass.m.resize((size_t)D * D);
+            for (auto& g : pass.m) g = cplx(sc * uni(), sc * uni());
+            const ImageLayout lay = imageLayout(k, kPartF16);
+            std::vector<float> img(lay.stride, 0.f);
+            buildImageBlock(pass, 0, img.data(), kPartF16);
+            const int bRows = (k == 6) ? 3 * D : 2 * D, bK = (k == 6) ? D : 2 * D;
+            const size_t bEntries = (size_t)bRows * bK;
+            const uint16_t* fh = reinterpret_cast<const uint16_t*>(img.data() + lay.f16);
+            const uint16_t* fl = fh + bEntries;
+            const double unscale = (double)img[lay.f16 + bEntries] * std::ldexp(1.0, kF16XExp);
+            if (!(unscale > 0.0)) return 1;
+            double mx = 0.0;
+            for (const cplx& g : pass.m) mx = std::max(mx, std::max(std::fabs(g.real()), std::fabs(g.imag())));
+            for (int r = 0; r < bRows; ++r)
+                for (int j = 0; j < bK; ++j) {
+                    const int rr = (k == 6 && r >= D) ? r - D : r, jj = (k == 6 && r < D) ? D + j : j;
+                    const cplx g = pass.m[(size_t)(rr % D) * D + (jj % D)];
+                    const double v = (rr < D) ? ((jj < D) ? g.real() : -g.imag()) : ((jj < D) ? g.imag() : g.real());
+                    const size_t at = (size_t)(r / 8) * (bK / 8) * 64 + (size_t)(j / 8) * 64 + (r % 8) * 8 + (j % 8);
+                    const double hi = f16Value(fh[at]), lo = f16Value(fl[at]);
+                    if (std::fabs(hi) > 16384.0) return 1;
+                    if (std::fabs((hi + lo) * unscale - v) > std::ldexp(mx, -21)) return 1;
+                }
+        }
+    return 0;
+}
 // whether a plan's images hold the parts the current precision and kernel
 // choice read (else the caller uploads the plan again)
 bool tcImagesFit(const void* devPlan) {

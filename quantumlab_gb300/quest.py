@@ -194,6 +194,7 @@ SIGNATURES = {
     "quest_gb300_checkTileCoverage": (_I, [_I, _P(_I), _I, _P(_I), _I]),
     "quest_gb300_checkImageLayouts": (_I, []),
     "quest_gb300_roundHalf": (_I, [_P(qreal), _P(C.c_ushort), _I]),
+    "quest_gb300_checkHalfImages": (_I, []),
     "quest_gb300_planPassNorms": (_I, [C.c_void_p, _I, C.POINTER(C.c_double)]),
     "quest_gb300_planCompile": (_I, [C.c_void_p]),
     "quest_gb300_planNumGates": (_I, [C.c_void_p]),

@@ -119,3 +119,10 @@ def test_tensor_core_precision_modes(L):
             assert lib.quest_gb300_getTensorCorePrecision() == 2
     finally:
         lib.quest_gb300_setTensorCorePrecision(before)
+
+
+def test_split_fp16_images_encode_their_blocks(L):
+    """The split-FP16 operand images (two FP16 parts of 2^s G and the factor
+    2^-(14 + s) after them) give every entry of matrix blocks from zero to
+    1e4 in size back to 2^-21 of the block's largest entry."""
+    assert L.lib.quest_gb300_checkHalfImages() == 0
