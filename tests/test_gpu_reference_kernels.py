@@ -61,7 +61,7 @@ class RefKernels:
             raise RuntimeError(f"{what}: CUDA driver error {rc}")
 
     def _launch(self, name, num_tasks, args):
-        # each argument is a ctypes object; the driver copies it by value
+        # each argument is a ctypes object; cuLaunchKernel copies it by value
         params = (C.c_void_p * len(args))(*[C.addressof(a) for a in args])
         blocks = (num_tasks + THREADS - 1) // THREADS
         self._check(self.cu.cuLaunchKernel(self.fn[name], blocks, 1, 1, THREADS, 1, 1, 0, None, params, None), name)
